@@ -1,0 +1,84 @@
+"""The host-side case layer (geometry, plan, project JSON) against the reference.
+
+Fixtures in tests/golden/geometry.json were produced by the reference's own
+numpy code (tests/golden/make_golden.py): plans, normalised polygons, solid
+flags and Bouzidi fractions.  Flags, link sets and fractions are compared for
+exact equality, as the engine must reproduce them bit for bit.
+"""
+import json
+
+import numpy as np
+import pytest
+
+from aerokinetic_gb300.config import Flow, Grid, Plan
+from aerokinetic_gb300.geometry import Contour, Section, naca4
+from aerokinetic_gb300.project import Project
+
+O = pytest.importorskip("oracle.oracle")
+
+CASES = ["kat272", "uniform_c1", "failure_capture_n16", "two_element"]
+
+
+def rebuild(fixture):
+    s = fixture["section"]
+    elements = tuple(Contour(np.array(xy), name) for xy, name in zip(s["elements"], s["names"]))
+    section = Section(elements, s["chord"], tuple(s["moment_reference"]))
+    flow, grid = Flow(**fixture["flow"]), Grid(**fixture["grid"])
+    return section, flow, grid
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_plan_and_normalised_polygon_bit_exact(golden, name):
+    fixture = golden["geometry"][name]
+    section, flow, grid = rebuild(fixture)
+    plan = Plan.create(section, flow, grid)
+    ref = fixture["plan"]
+    assert list(plan.shape) == ref["shape"]
+    assert list(plan.origin) == ref["origin"]
+    for key in ("dx", "span", "viscosity", "relaxation_rate", "dt_convective"):
+        assert getattr(plan, key) == ref[key], key
+    for mine, theirs in zip(section.normalized(flow.alpha_deg), fixture["normalized"]):
+        assert np.array_equal(mine.xy, np.array(theirs))
+
+
+def test_naca_points_match_reference_project(golden):
+    """The project files of the reference embed naca4 polygons verbatim."""
+    record = golden["histories"]["characteristic_down3"]["project"]
+    xy = np.array(record["geometry"]["elements"][0]["xy"])
+    assert np.array_equal(naca4("0012", 81).xy, xy)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_flags_and_fractions_bit_exact(golden, name):
+    fixture = golden["geometry"][name]
+    plan = fixture["plan"]
+    nx, ny, _ = plan["shape"]
+    contours = [np.array(c) for c in fixture["normalized"]]
+    cx = (np.arange(nx) + 0.5) * plan["dx"] + plan["origin"][0]
+    cy = (np.arange(ny) + 0.5) * plan["dx"] + plan["origin"][1]
+    flags = np.zeros((nx, ny), np.int64)
+    for k, c in enumerate(contours):
+        flags[O.contains(c, cx[:, None], cy[None, :])] = k + 1
+    assert np.array_equal(flags, np.array(fixture["solid_xy"]))
+    # oracle link set and fractions, through its own lattice set-up at nz=1 rows
+    case = O.AirfoilCase(contours, (nx, ny, 8), plan["origin"], plan["dx"], plan["span"],
+                         plan["relaxation_rate"], 0.04, 32, "legacy", 0.0, 31, (0.0, 0.0), 1)
+    rows = case.wall_links()
+    mine = {(int(r[0]), int(r[1]), int(r[3]), int(r[4])): r[6] for r in rows if r[2] == 0 and r[5] == 0}
+    theirs = {(r[1], r[2], r[3], r[4]): r[5] for r in fixture["wall_links_2d"]}
+    assert mine.keys() == theirs.keys()
+    for key, q in theirs.items():
+        assert mine[key] == q, key
+
+
+def test_project_round_trip_and_fingerprint(golden, tmp_path):
+    record = golden["histories"]["characteristic_down3"]["project"]
+    project = Project.from_dict(record)
+    assert project.as_dict()["geometry"]["elements"][0]["xy"] == record["geometry"]["elements"][0]["xy"]
+    path = tmp_path / "p.json"
+    project.save(path)
+    again = Project.load(path)
+    assert again.case_fingerprint == project.case_fingerprint
+    assert json.loads(path.read_text())["format"] == "aerokinetic_project"
+    with pytest.raises(ValueError):
+        Project.from_dict({"format": "other"})
