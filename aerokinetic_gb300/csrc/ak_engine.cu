@@ -1,0 +1,774 @@
+// ak_engine.cu -- host side of the C ABI declared in include/aerokinetic_gb300.h.
+//
+// Owns the device memory of each case, builds its boundary description on the
+// GPU (flags, cut links, Bouzidi q) and on the host (the thin outer ring of
+// links, O(surface)), and issues the per-step kernels on the case's stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/aerokinetic_gb300.h"
+#include "ak_geometry.cuh"
+
+using namespace ak;
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string &msg) {
+    g_error = msg;
+    return code;
+}
+
+#define AK_CUDA(call)                                                                              \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return fail(e_ == cudaErrorMemoryAllocation ? AK_ERR_NOMEM : AK_ERR_CUDA,              \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                       \
+    } while (0)
+
+#define AK_TRY(call)              \
+    do {                          \
+        int r_ = (call);          \
+        if (r_ != AK_OK) return r_; \
+    } while (0)
+
+long long blocks_for(long long n, int threads) { return (n + threads - 1) / threads; }
+
+}  // namespace
+
+struct ak_case {
+    // description
+    int nx = 0, ny = 0, nz = 0;
+    double origin_x = 0, origin_y = 0, dx = 0, omega_s = 0, omega_b = 1, speed = 0;
+    double ox = 0, oy = 0;  // origin / dx, the lever-arm offset of solver.py:239-240
+    int farfield = 0, storage = 0, n_elements = 0;
+    std::vector<int> poly_start, poly_count;
+    std::vector<double> poly_xy;
+    Grid G{};
+    size_t esize = 8;
+    // device memory
+    void *pdf[2] = {nullptr, nullptr};
+    int cur = 0;
+    uint8_t *flags = nullptr;
+    double *d_poly = nullptr;
+    int *d_start = nullptr, *d_count = nullptr;
+    WallKey *keys = nullptr;
+    double *wall_q = nullptr;
+    long long nkeys = 0, fallback = 0;
+    // outer ring
+    int *ox_ = nullptr, *oy_ = nullptr, *oz_ = nullptr;
+    signed char *od = nullptr, *oobj = nullptr, *oedge = nullptr;
+    long long nouter = 0;
+    int *sel_ubb = nullptr, *sel_out = nullptr;
+    long long n_ubb = 0, n_out = 0;
+    double *out_state = nullptr;
+    double *ff_in = nullptr, *ff_der = nullptr;
+    long long *ff_clock = nullptr;
+    double *ff_lo = nullptr, *ff_hi = nullptr;
+    FarfieldParams ff{};
+    // reductions
+    double *partials = nullptr, *reduced = nullptr;
+    long long partial_doubles = 0;
+    // staging for host transfers
+    double *staging = nullptr;
+    size_t staging_doubles = 0;
+    long long fluid_cells = 0;
+    long long steps = 0;
+    long long launches = 0;  // kernels issued by stepping since creation
+    bool prepared = false;
+    // optional per-kernel timing: events recorded around each kernel group
+    std::vector<cudaEvent_t> *timing = nullptr;
+    cudaStream_t stream = nullptr;
+    size_t device_bytes = 0;
+
+    OuterLinks outer() const { return OuterLinks{ox_, oy_, oz_, od, oobj, oedge, nouter}; }
+};
+
+namespace {
+
+template <typename T>
+int dalloc(ak_case *c, T **p, size_t count) {
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    if (e != cudaSuccess)
+        return fail(e == cudaErrorMemoryAllocation ? AK_ERR_NOMEM : AK_ERR_CUDA,
+                    std::string("device allocation of ") + std::to_string(count * sizeof(T)) +
+                        " bytes failed: " + cudaGetErrorString(e));
+    c->device_bytes += count * sizeof(T);
+    return AK_OK;
+}
+
+template <typename T>
+int upload(ak_case *c, T **p, const std::vector<T> &v) {
+    AK_TRY(dalloc(c, p, v.size()));
+    if (!v.empty()) AK_CUDA(cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+    return AK_OK;
+}
+
+void release(ak_case *c) {
+    void *ptrs[] = {c->pdf[0], c->pdf[1], c->flags, c->d_poly, c->d_start, c->d_count, c->keys, c->wall_q,
+                    c->ox_, c->oy_, c->oz_, c->od, c->oobj, c->oedge, c->sel_ubb, c->sel_out, c->out_state,
+                    c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, c->partials, c->reduced, c->staging};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (c->stream) cudaStreamDestroy(c->stream);
+}
+
+int ensure_staging(ak_case *c, size_t doubles) {
+    if (c->staging_doubles >= doubles) return AK_OK;
+    if (c->staging) {
+        cudaFree(c->staging);
+        c->device_bytes -= c->staging_doubles * sizeof(double);
+        c->staging = nullptr;
+    }
+    AK_TRY(dalloc(c, &c->staging, doubles));
+    c->staging_doubles = doubles;
+    return AK_OK;
+}
+
+int ensure_partials(ak_case *c, long long doubles) {
+    if (c->partial_doubles >= doubles) return AK_OK;
+    if (c->partials) {
+        cudaFree(c->partials);
+        c->device_bytes -= c->partial_doubles * sizeof(double);
+        c->partials = nullptr;
+    }
+    AK_TRY(dalloc(c, &c->partials, (size_t)doubles));
+    c->partial_doubles = doubles;
+    return AK_OK;
+}
+
+// ---- dispatch on the storage type
+template <typename F>
+int with_storage(ak_case *c, F &&f) {
+    switch (c->storage) {
+    case AK_STORAGE_F64: return f((double *)nullptr);
+    case AK_STORAGE_F32: return f((float *)nullptr);
+    case AK_STORAGE_F16: return f((__half *)nullptr);
+    }
+    return fail(AK_ERR_INVALID, "unknown storage");
+}
+
+// ---- characteristic farfield objects, farfield.py:34-47 and 209-224
+void build_farfield_objects(ak_case *c) {
+    FarfieldParams &P = c->ff;
+    P.nobj = 0;
+    const double vel[3] = {c->speed, 0.0, 0.0};
+    for (int nx_ = -1; nx_ <= 1; ++nx_)
+        for (int ny_ = -1; ny_ <= 1; ++ny_) {
+            if (nx_ == 0 && ny_ == 0) continue;
+            FarfieldObject &o = P.obj[P.nobj++];
+            o.normal[0] = nx_;
+            o.normal[1] = ny_;
+            o.normal[2] = 0;
+            const double len = std::sqrt((double)(nx_ * nx_ + ny_ * ny_));
+            o.nh[0] = nx_ / len;
+            o.nh[1] = ny_ / len;
+            o.nh[2] = 0.0;
+            o.density = 1.0;
+            for (int a = 0; a < 3; ++a) o.vel[a] = vel[a];
+            const double nu = nx_ * vel[0] + ny_ * vel[1];
+            const bool any = vel[0] != 0 || vel[1] != 0 || vel[2] != 0;
+            const bool evolve = nu >= 0 && any;
+            const bool glancing = evolve && nu == 0;
+            o.mode = glancing ? 2 : (evolve ? 1 : 0);
+            o.un_inf = o.nh[0] * vel[0] + o.nh[1] * vel[1] + o.nh[2] * vel[2];
+            for (int a = 0; a < 3; ++a) {
+                o.ut_inf[a] = vel[a] - o.un_inf * o.nh[a];
+                bool row = false;
+                for (int b = 0; b < 3; ++b) {
+                    o.P[a][b] = (a == b ? 1.0 : 0.0) - o.nh[a] * o.nh[b];
+                    row |= o.P[a][b] != 0.0;
+                }
+                o.active[a] = !(o.ut_inf[a] == 0.0 && !row);
+            }
+        }
+}
+
+int farfield_object_of(const ak_case *c, int gx, int gy) {
+    // ghost cell (gx, gy) in interior coordinates -> index of its normal in
+    // the order built above
+    const int nx_ = gx < 0 ? -1 : (gx >= c->nx ? 1 : 0);
+    const int ny_ = gy < 0 ? -1 : (gy >= c->ny ? 1 : 0);
+    for (int k = 0; k < c->ff.nobj; ++k)
+        if (c->ff.obj[k].normal[0] == nx_ && c->ff.obj[k].normal[1] == ny_) return k;
+    return -1;
+}
+
+// ---- outer ring links (pystencils index-list semantics: interior fluid cells
+// with a neighbour in the ghost ring), built on the host: O(surface)
+int build_outer(ak_case *c, const std::vector<uint8_t> &hflags) {
+    std::vector<int> X, Y, Z;
+    std::vector<signed char> D, OBJ, EDGE;
+    std::vector<int> sel_ubb, sel_out;
+    const int nx = c->nx, ny = c->ny, nz = c->nz, nxp = nx + 2;
+    auto push = [&](int x, int y) {  // interior coordinates
+        if (hflags[(size_t)(y + 1) * nxp + (x + 1)] != FLAG_FLUID) return;
+        for (int d = 1; d < Q; ++d) {
+            const int gx = x + cx(d), gy = y + cy(d);
+            if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) continue;
+            for (int z = 0; z < nz; ++z) {
+                const long long idx = (long long)X.size();
+                X.push_back(x + 1);
+                Y.push_back(y + 1);
+                Z.push_back(z);
+                D.push_back((signed char)d);
+                if (c->farfield == AK_FARFIELD_LEGACY) {
+                    // UBB owns x<0, y<0, y>ny; the outflow (set later) owns x>nx
+                    const bool outflow = gx >= nx;
+                    OBJ.push_back(outflow ? 1 : 0);
+                    (outflow ? sel_out : sel_ubb).push_back((int)idx);
+                    EDGE.push_back(0);
+                    EDGE.push_back(0);
+                } else {
+                    const int k = farfield_object_of(c, gx, gy);
+                    OBJ.push_back((signed char)k);
+                    const FarfieldObject &o = c->ff.obj[k];
+                    const int fx = x + cx(d) - o.normal[0], fy = y + cy(d) - o.normal[1];
+                    if (fx < 0 || fx >= nx || fy < 0 || fy >= ny) return;  // checked below
+                    EDGE.push_back((signed char)(fx == 0 ? -1 : (fx == nx - 1 ? 1 : 0)));
+                    EDGE.push_back((signed char)(fy == 0 ? -1 : (fy == ny - 1 ? 1 : 0)));
+                }
+            }
+        }
+    };
+    for (int x = 0; x < nx; ++x) {
+        push(x, 0);
+        if (ny > 1) push(x, ny - 1);
+    }
+    for (int y = 1; y < ny - 1; ++y) {
+        push(0, y);
+        if (nx > 1) push(nx - 1, y);
+    }
+    if (c->farfield == AK_FARFIELD_CHARACTERISTIC && EDGE.size() != 2 * X.size())
+        return fail(AK_ERR_INVALID, "farfield foot cell outside the domain; the lattice is too small");
+    c->nouter = (long long)X.size();
+    AK_TRY(upload(c, &c->ox_, X));
+    AK_TRY(upload(c, &c->oy_, Y));
+    AK_TRY(upload(c, &c->oz_, Z));
+    AK_TRY(upload(c, &c->od, D));
+    AK_TRY(upload(c, &c->oobj, OBJ));
+    AK_TRY(upload(c, &c->oedge, EDGE));
+    if (c->farfield == AK_FARFIELD_LEGACY) {
+        c->n_ubb = (long long)sel_ubb.size();
+        c->n_out = (long long)sel_out.size();
+        AK_TRY(upload(c, &c->sel_ubb, sel_ubb));
+        AK_TRY(upload(c, &c->sel_out, sel_out));
+        AK_TRY(dalloc(c, &c->out_state, (size_t)(2 * c->n_out)));
+    } else {
+        AK_TRY(dalloc(c, &c->ff_in, (size_t)c->nouter));
+        AK_TRY(dalloc(c, &c->ff_der, (size_t)c->nouter));
+        AK_TRY(dalloc(c, &c->ff_clock, (size_t)c->nouter));
+        AK_TRY(dalloc(c, &c->ff_lo, (size_t)nx * nz));
+        AK_TRY(dalloc(c, &c->ff_hi, (size_t)nx * nz));
+    }
+    return AK_OK;
+}
+
+int build_geometry(ak_case *c, std::vector<uint8_t> &hflags) {
+    const int nx = c->nx, ny = c->ny, nxp = nx + 2, nyp = ny + 2;
+    AK_TRY(upload(c, &c->d_poly, c->poly_xy));
+    AK_TRY(upload(c, &c->d_start, c->poly_start));
+    AK_TRY(upload(c, &c->d_count, c->poly_count));
+    Polygons P{c->d_poly, c->d_start, c->d_count, c->n_elements};
+    AK_TRY(dalloc(c, &c->flags, (size_t)nxp * nyp));
+    k_flags<<<dim3((unsigned)blocks_for(nxp, 128), nyp), 128, 0, c->stream>>>(c->flags, nx, ny, P, c->dx, c->origin_x,
+                                                                               c->origin_y);
+    AK_CUDA(cudaGetLastError());
+    hflags.assign((size_t)nxp * nyp, 0);
+    AK_CUDA(cudaMemcpyAsync(hflags.data(), c->flags, hflags.size(), cudaMemcpyDeviceToHost, c->stream));
+    AK_CUDA(cudaStreamSynchronize(c->stream));
+    std::vector<long long> per_element(c->n_elements, 0);
+    long long fluid_columns = 0;
+    for (int y = 0; y < nyp; ++y)
+        for (int x = 0; x < nxp; ++x) {
+            const uint8_t f = hflags[(size_t)y * nxp + x];
+            const bool ghost = x == 0 || y == 0 || x == nx + 1 || y == ny + 1;
+            if (ghost && f != FLAG_OUTER)
+                return fail(AK_ERR_INVALID, "an element reaches the outer boundary; enlarge the domain");
+            if (!ghost && f == FLAG_FLUID) ++fluid_columns;
+            if (!ghost && f >= 1 && f <= c->n_elements) ++per_element[f - 1];
+        }
+    for (int e = 0; e < c->n_elements; ++e)
+        if (per_element[e] == 0)
+            return fail(AK_ERR_INVALID, "Element " + std::to_string(e) + " has no solid cells; increase resolution");
+    c->fluid_cells = fluid_columns * c->nz;
+    // compacted wall keys in (x, y, direction) order: every fluid column and
+    // planar direction whose neighbour column is solid (pystencils index-list
+    // semantics, deduplicated over z and c_z as solver.py:102-109 does)
+    static const int planar[8] = {1, 2, 3, 4, 7, 8, 9, 10};
+    std::vector<WallKey> keys;
+    for (int x = 1; x <= nx; ++x)
+        for (int y = 1; y <= ny; ++y) {
+            if (hflags[(size_t)y * nxp + x] != FLAG_FLUID) continue;
+            for (int k = 0; k < 8; ++k) {
+                const int d = planar[k];
+                const uint8_t nb = hflags[(size_t)(y + cy(d)) * nxp + x + cx(d)];
+                if (nb >= 1 && nb <= c->n_elements) keys.push_back(WallKey{x, y, d, nb - 1});
+            }
+        }
+    c->nkeys = (long long)keys.size();
+    AK_TRY(upload(c, &c->keys, keys));
+    AK_TRY(dalloc(c, &c->wall_q, (size_t)c->nkeys));
+    int *status = nullptr;
+    AK_TRY(dalloc(c, &status, (size_t)c->nkeys));
+    if (c->nkeys) {
+        k_wall_fractions<<<(unsigned)blocks_for(c->nkeys, 128), 128, 0, c->stream>>>(
+            c->keys, c->nkeys, P, c->dx, c->origin_x, c->origin_y, c->wall_q, status);
+        AK_CUDA(cudaGetLastError());
+    }
+    std::vector<int> hstatus((size_t)c->nkeys);
+    std::vector<double> hq((size_t)c->nkeys);
+    if (c->nkeys) {
+        AK_CUDA(cudaMemcpyAsync(hstatus.data(), status, hstatus.size() * sizeof(int), cudaMemcpyDeviceToHost,
+                                c->stream));
+        AK_CUDA(cudaMemcpyAsync(hq.data(), c->wall_q, hq.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    }
+    AK_CUDA(cudaStreamSynchronize(c->stream));
+    cudaFree(status);
+    c->device_bytes -= std::max<size_t>(1, (size_t)c->nkeys) * sizeof(int);
+    c->fallback = 0;
+    for (long long k = 0; k < c->nkeys; ++k) {
+        if (hstatus[k]) return fail(AK_ERR_GEOMETRY, "A fluid-to-solid link has no geometric intersection");
+        if (hq[k] == -1.0) c->fallback += 3LL * c->nz;
+    }
+    return AK_OK;
+}
+
+template <typename S>
+int allocate_populations(ak_case *c) {
+    const size_t n = (size_t)Q * c->G.qs;
+    for (int k = 0; k < 2; ++k) {
+        S *p = nullptr;
+        AK_TRY(dalloc(c, &p, n));
+        AK_CUDA(cudaMemsetAsync(p, 0, n * sizeof(S), c->stream));
+        c->pdf[k] = p;
+    }
+    return AK_OK;
+}
+
+template <typename S>
+S *src_of(ak_case *c) { return (S *)c->pdf[c->cur]; }
+template <typename S>
+S *dst_of(ak_case *c) { return (S *)c->pdf[1 - c->cur]; }
+
+template <typename S>
+int prepare_boundaries(ak_case *c) {
+    S *src = src_of<S>(c);
+    const int T = 256;
+    if (c->farfield == AK_FARFIELD_LEGACY) {
+        if (c->n_out) {
+            k_outflow_prepare<S><<<(unsigned)blocks_for(c->n_out, T), T, 0, c->stream>>>(
+                src, c->G, c->outer(), c->sel_out, c->n_out, c->out_state, 1, 0, 0, 1.0, c->speed, 0.0, 0.0);
+            AK_CUDA(cudaGetLastError());
+        }
+    } else {
+        if (c->nouter) {
+            k_farfield<S><<<(unsigned)blocks_for(c->nouter, T), T, 0, c->stream>>>(
+                src, c->G, c->outer(), c->ff, c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, 1);
+            AK_CUDA(cudaGetLastError());
+        }
+        k_glancing_rows<S><<<(unsigned)blocks_for((long long)c->nx * c->nz, T), T, 0, c->stream>>>(src, c->G, c->ff,
+                                                                                                  c->ff_lo, c->ff_hi);
+        AK_CUDA(cudaGetLastError());
+    }
+    c->prepared = true;
+    return AK_OK;
+}
+
+void mark(ak_case *c) {
+    if (!c->timing) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, c->stream);
+    c->timing->push_back(e);
+}
+
+template <typename S>
+int one_step(ak_case *c, bool sample) {
+    using T = typename Store<S>::T;
+    if (!c->prepared) AK_TRY(prepare_boundaries<S>(c));
+    S *src = src_of<S>(c);
+    const int TB = 256;
+    mark(c);
+    // outer boundary: the reference applies its boundary objects in
+    // installation order; the outflow reads ghost values the UBB just wrote
+    if (c->farfield == AK_FARFIELD_LEGACY) {
+        if (c->n_ubb) {
+            k_ubb<S><<<(unsigned)blocks_for(c->n_ubb, TB), TB, 0, c->stream>>>(src, c->G, c->outer(), c->sel_ubb,
+                                                                               c->n_ubb, c->speed, 0.0, 0.0);
+            AK_CUDA(cudaGetLastError());
+            ++c->launches;
+        }
+        if (c->n_out) {
+            k_outflow<S><<<(unsigned)blocks_for(c->n_out, TB), TB, 0, c->stream>>>(src, c->G, c->outer(), c->sel_out,
+                                                                                   c->n_out, c->out_state, 1, 0, 0);
+            AK_CUDA(cudaGetLastError());
+            ++c->launches;
+        }
+    } else if (c->nouter) {
+        k_farfield<S><<<(unsigned)blocks_for(c->nouter, TB), TB, 0, c->stream>>>(
+            src, c->G, c->outer(), c->ff, c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, 0);
+        AK_CUDA(cudaGetLastError());
+        ++c->launches;
+    }
+    mark(c);
+    // walls and loads
+    const long long nlinks = c->nkeys * c->nz * 3;
+    if (nlinks) {
+        const long long nb = blocks_for(nlinks, 256);
+        if (sample) AK_TRY(ensure_partials(c, nb * 5 * c->n_elements));
+        k_walls<S><<<(unsigned)nb, 256, 0, c->stream>>>(src, c->G, c->keys, c->wall_q, c->nkeys, sample ? 1 : 0,
+                                                        c->n_elements, c->ox, c->oy, c->partials);
+        AK_CUDA(cudaGetLastError());
+        ++c->launches;
+        if (sample) {
+            k_sum_partials<<<1, 64, 0, c->stream>>>(c->partials, (int)nb, 5 * c->n_elements, c->reduced);
+            AK_CUDA(cudaGetLastError());
+            ++c->launches;
+        }
+    } else if (sample) {
+        AK_CUDA(cudaMemsetAsync(c->reduced, 0, sizeof(double) * 5 * c->n_elements, c->stream));
+    }
+    // bulk
+    mark(c);
+    dim3 grid((unsigned)blocks_for(c->nx, 128), (unsigned)c->ny, (unsigned)c->nz);
+    k_stream_collide<S><<<grid, 128, 0, c->stream>>>(src, dst_of<S>(c), c->flags, c->G, (T)c->omega_s,
+                                                     (T)c->omega_b);
+    AK_CUDA(cudaGetLastError());
+    ++c->launches;
+    mark(c);
+    c->cur = 1 - c->cur;
+    c->steps += 1;
+    return AK_OK;
+}
+
+int check_case(const ak_case *c) {
+    if (!c) return fail(AK_ERR_INVALID, "null case");
+    return AK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *ak_last_error(void) { return g_error.c_str(); }
+
+const char *ak_version(void) { return "aerokinetic_gb300 1.0 sm_103a"; }
+
+int ak_case_create(const ak_case_desc *desc, ak_case **out) {
+    g_error.clear();
+    if (!desc || !out) return fail(AK_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (desc->nx < 4 || desc->ny < 4 || desc->nz < 1) return fail(AK_ERR_INVALID, "lattice needs nx, ny >= 4 and nz >= 1");
+    if ((long long)desc->nx + 2 > 32767 || (long long)desc->ny + 2 > 65535 || desc->nz > 65535)
+        return fail(AK_ERR_INVALID, "lattice extent too large for one case");
+    if (!(desc->dx > 0) || !std::isfinite(desc->dx)) return fail(AK_ERR_INVALID, "dx must be positive");
+    if (!(desc->omega_shear > 0 && desc->omega_shear < 2) || !(desc->omega_bulk > 0 && desc->omega_bulk < 2))
+        return fail(AK_ERR_INVALID, "relaxation rates must lie in (0, 2)");
+    if (!std::isfinite(desc->speed) || std::fabs(desc->speed) >= 1.0 / std::sqrt(3.0))
+        return fail(AK_ERR_INVALID, "freestream speed must be subsonic");
+    if (desc->farfield != AK_FARFIELD_LEGACY && desc->farfield != AK_FARFIELD_CHARACTERISTIC)
+        return fail(AK_ERR_INVALID, "unknown farfield");
+    if (desc->storage < AK_STORAGE_F64 || desc->storage > AK_STORAGE_F16) return fail(AK_ERR_INVALID, "unknown storage");
+    if (desc->n_elements < 1 || desc->n_elements > MAX_ELEMENTS || !desc->element_sizes || !desc->polygon_xy)
+        return fail(AK_ERR_INVALID, "between 1 and 8 polygons are required");
+    ak_case *c = new ak_case();
+    c->nx = desc->nx;
+    c->ny = desc->ny;
+    c->nz = desc->nz;
+    c->origin_x = desc->origin_x;
+    c->origin_y = desc->origin_y;
+    c->dx = desc->dx;
+    c->ox = desc->origin_x / desc->dx;
+    c->oy = desc->origin_y / desc->dx;
+    c->omega_s = desc->omega_shear;
+    c->omega_b = desc->omega_bulk;
+    c->speed = desc->speed;
+    c->farfield = desc->farfield;
+    c->storage = desc->storage;
+    c->n_elements = desc->n_elements;
+    int total = 0;
+    for (int e = 0; e < desc->n_elements; ++e) {
+        if (desc->element_sizes[e] < 3) {
+            delete c;
+            return fail(AK_ERR_INVALID, "a polygon needs at least three vertices");
+        }
+        c->poly_start.push_back(total);
+        c->poly_count.push_back(desc->element_sizes[e]);
+        total += desc->element_sizes[e];
+    }
+    c->poly_xy.assign(desc->polygon_xy, desc->polygon_xy + 2 * (size_t)total);
+    for (double v : c->poly_xy)
+        if (!std::isfinite(v)) {
+            delete c;
+            return fail(AK_ERR_INVALID, "polygon vertices must be finite");
+        }
+    c->esize = c->storage == AK_STORAGE_F64 ? 8 : (c->storage == AK_STORAGE_F32 ? 4 : 2);
+    Grid &G = c->G;
+    G.nx = c->nx;
+    G.ny = c->ny;
+    G.nz = c->nz;
+    G.nxp = c->nx + 2;
+    G.nyp = c->ny + 2;
+    G.sx = (G.nxp + 31) / 32 * 32;
+    G.plane = (long long)G.nyp * G.sx;
+    G.qs = (long long)G.nz * G.plane;
+    int r = AK_OK;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        r = fail(AK_ERR_CUDA, "stream creation failed (no CUDA device?)");
+    }
+    std::vector<uint8_t> hflags;
+    if (r == AK_OK && c->farfield == AK_FARFIELD_CHARACTERISTIC) build_farfield_objects(c);
+    if (r == AK_OK) r = build_geometry(c, hflags);
+    if (r == AK_OK) r = build_outer(c, hflags);
+    if (r == AK_OK) r = dalloc(c, &c->reduced, 64);
+    if (r == AK_OK) r = with_storage(c, [&](auto *tag) { return allocate_populations<std::remove_pointer_t<decltype(tag)>>(c); });
+    if (r == AK_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) r = fail(AK_ERR_CUDA, "case set-up failed");
+    if (r != AK_OK) {
+        std::string keep = g_error;
+        release(c);
+        delete c;
+        g_error = keep;
+        return r;
+    }
+    *out = c;
+    return AK_OK;
+}
+
+int ak_case_destroy(ak_case *c) {
+    if (!c) return AK_OK;
+    cudaStreamSynchronize(c->stream);
+    release(c);
+    delete c;
+    return AK_OK;
+}
+
+int ak_case_get_info(const ak_case *c, ak_case_info *info) {
+    AK_TRY(check_case(c));
+    if (!info) return fail(AK_ERR_INVALID, "null info");
+    info->cells = (int64_t)c->nx * c->ny * c->nz;
+    info->fluid_cells = c->fluid_cells;
+    info->wall_keys = c->nkeys;
+    info->wall_links = c->nkeys * c->nz * 3;
+    info->outer_links = c->nouter;
+    info->fallback_links = c->fallback;
+    info->device_bytes = (int64_t)c->device_bytes;
+    info->row_pitch = c->G.sx;
+    info->storage = c->storage;
+    return AK_OK;
+}
+
+int ak_init_perturbed(ak_case *c, double amp, double phase_y, double phase_z, double lead_x, double lead_y,
+                      double span) {
+    AK_TRY(check_case(c));
+    if (!(span > 0)) return fail(AK_ERR_INVALID, "span must be positive");
+    const double ky = 2 * M_PI / (c->ny * c->dx);
+    const double kz = 2 * M_PI / span;
+    const long long n = (long long)c->nx * c->ny * c->nz;
+    AK_TRY(with_storage(c, [&](auto *tag) {
+        using S = std::remove_pointer_t<decltype(tag)>;
+        k_init_perturbed<S><<<(unsigned)blocks_for(n, 256), 256, 0, c->stream>>>(
+            src_of<S>(c), c->G, c->flags, c->speed, amp, phase_y, phase_z, lead_x, lead_y, c->origin_x, c->origin_y,
+            c->dx, ky, kz);
+        AK_CUDA(cudaGetLastError());
+        return AK_OK;
+    }));
+    AK_CUDA(cudaStreamSynchronize(c->stream));
+    c->prepared = false;
+    return AK_OK;
+}
+
+int ak_init_fields(ak_case *c, const double *rho, const double *u) {
+    AK_TRY(check_case(c));
+    if (!rho || !u) return fail(AK_ERR_INVALID, "null field");
+    const long long n = (long long)c->nx * c->ny * c->nz;
+    AK_TRY(ensure_staging(c, (size_t)n * 4));
+    AK_CUDA(cudaMemcpyAsync(c->staging, rho, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    AK_CUDA(cudaMemcpyAsync(c->staging + n, u, 3 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    AK_TRY(with_storage(c, [&](auto *tag) {
+        using S = std::remove_pointer_t<decltype(tag)>;
+        k_init_fields<S><<<(unsigned)blocks_for(n, 256), 256, 0, c->stream>>>(src_of<S>(c), c->G, c->staging,
+                                                                               c->staging + n);
+        AK_CUDA(cudaGetLastError());
+        return AK_OK;
+    }));
+    AK_CUDA(cudaStreamSynchronize(c->stream));
+    c->prepared = false;
+    return AK_OK;
+}
+
+int ak_step(ak_case *c, int32_t nsteps, double *loads) {
+    AK_TRY(check_case(c));
+    if (nsteps < 1) return fail(AK_ERR_INVALID, "nsteps must be >= 1");
+    for (int s = 0; s < nsteps; ++s) {
+        const bool sample = loads != nullptr && s == nsteps - 1;
+        AK_TRY(with_storage(c, [&](auto *tag) { return one_step<std::remove_pointer_t<decltype(tag)>>(c, sample); }));
+    }
+    if (loads) {
+        AK_CUDA(cudaMemcpyAsync(loads, c->reduced, sizeof(double) * 5 * c->n_elements, cudaMemcpyDeviceToHost,
+                                c->stream));
+        AK_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    return AK_OK;
+}
+
+int64_t ak_steps_done(const ak_case *c) { return c ? c->steps : -1; }
+
+int64_t ak_kernel_launches(const ak_case *c) { return c ? c->launches : -1; }
+
+void *ak_case_stream(const ak_case *c) { return c ? (void *)c->stream : nullptr; }
+
+int ak_step_timed(ak_case *c, int32_t nsteps, double *ms) {
+    AK_TRY(check_case(c));
+    if (nsteps < 1 || !ms) return fail(AK_ERR_INVALID, "nsteps >= 1 and an output array are required");
+    if (!c->prepared) AK_TRY(with_storage(c, [&](auto *tag) { return prepare_boundaries<std::remove_pointer_t<decltype(tag)>>(c); }));
+    std::vector<cudaEvent_t> events;
+    events.reserve((size_t)4 * nsteps);
+    c->timing = &events;
+    int r = AK_OK;
+    for (int s = 0; s < nsteps && r == AK_OK; ++s)
+        r = with_storage(c, [&](auto *tag) { return one_step<std::remove_pointer_t<decltype(tag)>>(c, false); });
+    c->timing = nullptr;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    for (int k = 0; k < 4; ++k) ms[k] = 0.0;
+    if (r == AK_OK && e == cudaSuccess && events.size() == (size_t)4 * nsteps) {
+        float t = 0.0f;
+        cudaEventElapsedTime(&t, events.front(), events.back());
+        ms[0] = t;
+        for (int s = 0; s < nsteps; ++s) {
+            cudaEvent_t *ev = events.data() + 4 * s;
+            cudaEventElapsedTime(&t, ev[0], ev[1]);  // outer boundary
+            ms[3] += t;
+            cudaEventElapsedTime(&t, ev[1], ev[2]);  // walls
+            ms[2] += t;
+            cudaEventElapsedTime(&t, ev[2], ev[3]);  // stream-collide
+            ms[1] += t;
+        }
+    }
+    for (cudaEvent_t ev : events) cudaEventDestroy(ev);
+    if (r != AK_OK) return r;
+    AK_CUDA(e);
+    return AK_OK;
+}
+
+int ak_diagnostics(ak_case *c, double *diag) {
+    AK_TRY(check_case(c));
+    if (!diag) return fail(AK_ERR_INVALID, "null output");
+    const int nb = 152 * 4;
+    AK_TRY(ensure_partials(c, (long long)nb * 6));
+    AK_TRY(with_storage(c, [&](auto *tag) {
+        using S = std::remove_pointer_t<decltype(tag)>;
+        k_diagnostics<S><<<nb, 256, 0, c->stream>>>(src_of<S>(c), c->G, c->flags, c->partials);
+        AK_CUDA(cudaGetLastError());
+        return AK_OK;
+    }));
+    k_diagnostics_final<<<1, 32, 0, c->stream>>>(c->partials, nb, c->reduced);
+    AK_CUDA(cudaGetLastError());
+    double r[6];
+    AK_CUDA(cudaMemcpyAsync(r, c->reduced, sizeof r, cudaMemcpyDeviceToHost, c->stream));
+    AK_CUDA(cudaStreamSynchronize(c->stream));
+    diag[0] = std::sqrt(3.0) * std::sqrt(r[0]);
+    diag[1] = r[5] > 0 ? r[3] / r[5] : NAN;
+    diag[2] = r[1];
+    diag[3] = -r[2];
+    diag[4] = (r[4] == 0 && r[5] > 0) ? 1.0 : 0.0;
+    if (diag[4] != 1.0) return fail(AK_ERR_NONFINITE, "Non-finite fluid state; the run is invalid");
+    if (diag[0] > 0.3 || diag[2] > 0.1 || diag[3] <= 0) {
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "Low-Mach validity check failed: local Ma=%.3g, |rho-1|max=%.3g", diag[0],
+                      diag[2]);
+        return fail(AK_ERR_GUARD, buf);
+    }
+    return AK_OK;
+}
+
+int ak_macros(ak_case *c, double *rho, double *u) {
+    AK_TRY(check_case(c));
+    if (!rho || !u) return fail(AK_ERR_INVALID, "null output");
+    const long long n = (long long)c->nx * c->ny * c->nz;
+    AK_TRY(ensure_staging(c, (size_t)n * 4));
+    AK_TRY(with_storage(c, [&](auto *tag) {
+        using S = std::remove_pointer_t<decltype(tag)>;
+        k_macros<S><<<(unsigned)blocks_for(n, 256), 256, 0, c->stream>>>(src_of<S>(c), c->G, c->staging,
+                                                                          c->staging + n);
+        AK_CUDA(cudaGetLastError());
+        return AK_OK;
+    }));
+    AK_CUDA(cudaMemcpyAsync(rho, c->staging, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    AK_CUDA(cudaMemcpyAsync(u, c->staging + n, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    AK_CUDA(cudaStreamSynchronize(c->stream));
+    return AK_OK;
+}
+
+int ak_get_pdf(ak_case *c, double *pdf) {
+    AK_TRY(check_case(c));
+    if (!pdf) return fail(AK_ERR_INVALID, "null output");
+    const long long n = (long long)c->nx * c->ny * c->nz;
+    AK_TRY(ensure_staging(c, (size_t)n * Q));
+    AK_TRY(with_storage(c, [&](auto *tag) {
+        using S = std::remove_pointer_t<decltype(tag)>;
+        k_export<S><<<(unsigned)blocks_for(n, 256), 256, 0, c->stream>>>(src_of<S>(c), c->G, c->staging);
+        AK_CUDA(cudaGetLastError());
+        return AK_OK;
+    }));
+    AK_CUDA(cudaMemcpyAsync(pdf, c->staging, n * Q * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    AK_CUDA(cudaStreamSynchronize(c->stream));
+    return AK_OK;
+}
+
+int ak_set_pdf(ak_case *c, const double *pdf) {
+    AK_TRY(check_case(c));
+    if (!pdf) return fail(AK_ERR_INVALID, "null input");
+    const long long n = (long long)c->nx * c->ny * c->nz;
+    AK_TRY(ensure_staging(c, (size_t)n * Q));
+    AK_CUDA(cudaMemcpyAsync(c->staging, pdf, n * Q * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    AK_TRY(with_storage(c, [&](auto *tag) {
+        using S = std::remove_pointer_t<decltype(tag)>;
+        k_import<S><<<(unsigned)blocks_for(n, 256), 256, 0, c->stream>>>(src_of<S>(c), c->G, c->staging);
+        AK_CUDA(cudaGetLastError());
+        return AK_OK;
+    }));
+    AK_CUDA(cudaStreamSynchronize(c->stream));
+    return AK_OK;
+}
+
+int ak_get_flags(ak_case *c, uint8_t *flags) {
+    AK_TRY(check_case(c));
+    if (!flags) return fail(AK_ERR_INVALID, "null output");
+    const int nxp = c->nx + 2;
+    std::vector<uint8_t> h((size_t)nxp * (c->ny + 2));
+    AK_CUDA(cudaMemcpyAsync(h.data(), c->flags, h.size(), cudaMemcpyDeviceToHost, c->stream));
+    AK_CUDA(cudaStreamSynchronize(c->stream));
+    for (int x = 0; x < c->nx; ++x)
+        for (int y = 0; y < c->ny; ++y) flags[(size_t)x * c->ny + y] = h[(size_t)(y + 1) * nxp + (x + 1)];
+    return AK_OK;
+}
+
+int ak_get_wall_links(ak_case *c, int32_t *rows, double *q) {
+    AK_TRY(check_case(c));
+    if ((!rows || !q) && c->nkeys) return fail(AK_ERR_INVALID, "null output");
+    std::vector<WallKey> keys((size_t)c->nkeys);
+    if (c->nkeys) {
+        AK_CUDA(cudaMemcpyAsync(keys.data(), c->keys, keys.size() * sizeof(WallKey), cudaMemcpyDeviceToHost, c->stream));
+        AK_CUDA(cudaMemcpyAsync(q, c->wall_q, c->nkeys * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    }
+    AK_CUDA(cudaStreamSynchronize(c->stream));
+    for (long long k = 0; k < c->nkeys; ++k) {
+        rows[4 * k] = keys[k].element;
+        rows[4 * k + 1] = keys[k].x - 1;
+        rows[4 * k + 2] = keys[k].y - 1;
+        rows[4 * k + 3] = keys[k].d2;
+    }
+    return AK_OK;
+}
+
+}  // extern "C"

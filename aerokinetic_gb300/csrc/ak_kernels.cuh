@@ -1,0 +1,556 @@
+// ak_kernels.cuh -- sm_103a kernels of the uniform engine.
+//
+// HBM layout of one case (all device-resident for the life of the case):
+//   populations  two copies (A/B), structure of arrays pdf[q][z][y][x]; x and
+//                y carry one ghost layer (x, y in 0..n+1), z is periodic and
+//                wraps in the index arithmetic; rows are padded to a multiple
+//                of 32 elements.  Storage double, float or half.
+//   flags        one byte per padded (x, y) column: 0 fluid, k+1 wall element
+//                k, 255 outer ghost.  The geometry is extruded, so a column
+//                flag covers the whole span and stays in L2.
+//   wall keys    compacted (x, y, planar direction, element) + Bouzidi q;
+//                one key stands for nz * 3 links (all z and all c_z).
+//   outer links  (x, y, z, d, boundary object) of the links into the ghost
+//                ring, with the per-link state of the legacy outflow or the
+//                characteristic farfield.
+//
+// One step (the reference's solver.py:256-261) is, on the case's stream:
+//   outer boundary kernels -> wall kernel (Bouzidi into solid cells, loads)
+//   -> stream_collide (pull from A, collide, write B) -> swap A/B.
+#pragma once
+#include "ak_lattice.cuh"
+
+namespace ak {
+
+constexpr uint8_t FLAG_FLUID = 0;
+constexpr uint8_t FLAG_OUTER = 255;
+constexpr double CS = 0.57735026918962576451;
+constexpr double ONE_MINUS_CS = 0.42264973081037423549;
+
+struct Grid {
+    int nx, ny, nz;   // interior
+    int nxp, nyp;     // padded columns
+    int sx;           // row pitch (elements)
+    long long plane;  // nyp * sx
+    long long qs;     // nz * plane, stride between populations
+    __host__ __device__ long long cell(int x, int y, int z) const { return (long long)z * plane + (long long)y * sx + x; }
+    __device__ int wrapz(int z) const { return z < 0 ? z + nz : (z >= nz ? z - nz : z); }
+};
+
+template <typename S>
+__device__ __forceinline__ double load_g(const S *pdf, const Grid &G, int q, int x, int y, int z) {
+    return (double)Store<S>::load(pdf + q * G.qs + G.cell(x, y, z), q);
+}
+template <typename S>
+__device__ __forceinline__ void store_g(S *pdf, const Grid &G, int q, int x, int y, int z, double v) {
+    Store<S>::store(pdf + q * G.qs + G.cell(x, y, z), q, (typename Store<S>::T)v);
+}
+
+// ------------------------------------------------------------ bulk step
+template <typename S>
+__global__ void __launch_bounds__(128) k_stream_collide(const S *__restrict__ src, S *__restrict__ dst,
+                                                        const uint8_t *__restrict__ flags, Grid G,
+                                                        typename Store<S>::T omega_s,
+                                                        typename Store<S>::T omega_b) {
+    using T = typename Store<S>::T;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int y = blockIdx.y + 1;
+    const int z = blockIdx.z;
+    if (x > G.nx) return;
+    if (__ldg(flags + y * G.nxp + x) != FLAG_FLUID) return;
+    T g[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const int zs = G.wrapz(z - cz(q));
+        g[q] = Store<S>::load(src + q * G.qs + G.cell(x - cx(q), y - cy(q), zs), q);
+    }
+    collide<T>(g, omega_s, omega_b);
+    const long long c = G.cell(x, y, z);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) Store<S>::store(dst + q * G.qs + c, q, g[q]);
+}
+
+// ------------------------------------------------------------ walls
+struct WallKey {
+    int x, y;      // padded coordinates of the fluid column
+    int d2;        // direction index of (cx, cy, 0)
+    int element;
+};
+
+// Block reduction of nv doubles per thread into shared partials; thread 0 of
+// the block writes them to out[blockIdx.x * nv ...] in a fixed order.
+template <int NV>
+__device__ void block_sum_store(double (&v)[NV], double *out) {
+    __shared__ double red[32][NV];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) red[warp][k] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        for (int k = 0; k < NV; ++k) {
+            double s = 0.0;
+            for (int w = 0; w < nw; ++w) s += red[w][k];
+            out[(long long)blockIdx.x * NV + k] = s;
+        }
+    }
+}
+
+// NoSlipLinearBouzidi (solver.py:139-143) over all links of the compacted keys,
+// written into the solid cells of pdf; optionally the per-element loads of
+// solver.py:217-243: F = sum c_d (g_out + g_in), Mz = sum rx Fy - ry Fx,
+// mass = sum g_in - g_out.  Partials: [block][element][5].
+constexpr int MAX_ELEMENTS = 8;
+template <typename S>
+__global__ void __launch_bounds__(256) k_walls(S *__restrict__ pdf, Grid G, const WallKey *__restrict__ keys,
+                                               const double *__restrict__ qs, long long nkeys, int sample,
+                                               int n_elements, double ox, double oy,
+                                               double *__restrict__ partials) {
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nlinks = nkeys * G.nz * 3;
+    double acc[5] = {0, 0, 0, 0, 0};
+    int element = -1;
+    if (tid < nlinks) {
+        const long long k = tid / (3LL * G.nz);
+        const int rem = (int)(tid - k * 3LL * G.nz);
+        const int z = rem / 3, icz = rem - 3 * (rem / 3);
+        const WallKey key = keys[k];
+        const int ex = cx(key.d2), ey = cy(key.d2), ez = icz - 1;
+        const int d = qof(ex + 1, ey + 1, icz), di = inv(d);
+        const double q = qs[k];
+        const double f_xf = load_g(pdf, G, d, key.x, key.y, z);
+        const double f_xf_inv = load_g(pdf, G, di, key.x, key.y, z);
+        double v;
+        if (q >= 0.5) {
+            v = (0.5 * (f_xf + f_xf_inv * (2.0 * q - 1.0))) / q;
+        } else if (q > 0.0) {
+            const double d_x2f = load_g(pdf, G, d, key.x - ex, key.y - ey, G.wrapz(z - ez));
+            v = 2.0 * q * f_xf + (1.0 - 2.0 * q) * d_x2f;
+        } else {
+            v = f_xf;
+        }
+        store_g(pdf, G, di, key.x + ex, key.y + ey, G.wrapz(z + ez), v);
+        if (sample) {
+            // the stored value is what the fluid will pull; use it as g_in
+            const double gin = load_g(pdf, G, di, key.x + ex, key.y + ey, G.wrapz(z + ez));
+            const double s = f_xf + gin;
+            const double fx = ex * s, fy = ey * s, fz = ez * s;
+            const double rx = (double)(key.x - 1) + 0.5 + ox, ry = (double)(key.y - 1) + 0.5 + oy;
+            acc[0] = fx;
+            acc[1] = fy;
+            acc[2] = fz;
+            acc[3] = rx * fy - ry * fx;
+            acc[4] = gin - f_xf;
+            element = key.element;
+        }
+    }
+    if (!sample) return;
+    for (int e = 0; e < n_elements; ++e) {
+        double v[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) v[k] = element == e ? acc[k] : 0.0;
+        block_sum_store<5>(v, partials + (long long)e * 5 * gridDim.x);
+        __syncthreads();
+    }
+}
+
+// partials laid out [element][block][5]; one thread per (element, component)
+__global__ void k_sum_partials(const double *__restrict__ partials, int nblocks, int nvalues,
+                               double *__restrict__ out) {
+    const int t = threadIdx.x;
+    if (t >= nvalues) return;
+    const int e = t / 5, k = t - 5 * (t / 5);
+    double s = 0.0;
+    for (int b = 0; b < nblocks; ++b) s += partials[((long long)e * nblocks + b) * 5 + k];
+    out[t] = s;
+}
+
+// ------------------------------------------------------------ outer ring
+struct OuterLinks {
+    const int *x, *y, *z;     // padded x, y; interior z
+    const signed char *d;     // direction from the fluid cell into the ghost ring
+    const signed char *obj;   // boundary object (farfield: normal index)
+    const signed char *edge;  // farfield: edge flag of the foot in x and y (2 per link)
+    long long n;
+};
+
+// compressible UBB (solver.py:131): g_inv(x+c) = g_d(x) - 6 (c.U) w_d rho(x)
+template <typename S>
+__global__ void k_ubb(S *__restrict__ pdf, Grid G, OuterLinks L, const int *__restrict__ selected, long long n,
+                      double ux, double uy, double uz) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int li = selected[i];
+    const int x = L.x[li], y = L.y[li], z = L.z[li], d = L.d[li];
+    double drho = 0.0;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) drho += load_g(pdf, G, q, x, y, z);
+    const double rho = drho + 1.0;
+    const double term = 6.0 * (cx(d) * ux + cy(d) * uy + cz(d) * uz) * weight(d);
+    const double gd = load_g(pdf, G, d, x, y, z);
+    store_g(pdf, G, inv(d), x + cx(d), y + cy(d), G.wrapz(z + cz(d)), gd - term * rho);
+}
+
+// ExtrapolationOutflow (Geier et al. 2015 eq. F.1, normal +x): first-order
+// upwind advection at c_s of the incoming population on the boundary cell.
+// state[2i] = neighbour value of the previous step, state[2i+1] = boundary
+// value of the previous step.
+template <typename S>
+__global__ void k_outflow(S *__restrict__ pdf, Grid G, OuterLinks L, const int *__restrict__ selected, long long n,
+                          double *__restrict__ state, int nx_, int ny_, int nz_) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int li = selected[i];
+    const int x = L.x[li], y = L.y[li], z = L.z[li], d = L.d[li], di = inv(d);
+    const double nb = load_g(pdf, G, di, x + cx(d) - nx_, y + cy(d) - ny_, G.wrapz(z + cz(d) - nz_));
+    const double v = CS * state[2 * i] + ONE_MINUS_CS * state[2 * i + 1];
+    state[2 * i] = nb;
+    state[2 * i + 1] = v;
+    store_g(pdf, G, di, x + cx(d), y + cy(d), G.wrapz(z + cz(d)), v);
+}
+
+// first application: neighbour value from the initial populations, boundary
+// value from the zero-centred equilibrium of the initial freestream
+template <typename S>
+__global__ void k_outflow_prepare(const S *__restrict__ pdf, Grid G, OuterLinks L, const int *__restrict__ selected,
+                                  long long n, double *__restrict__ state, int nx_, int ny_, int nz_, double rho0,
+                                  double ux, double uy, double uz) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int li = selected[i];
+    const int x = L.x[li], y = L.y[li], z = L.z[li], d = L.d[li], di = inv(d);
+    state[2 * i] = load_g(pdf, G, di, x + cx(d) - nx_, y + cy(d) - ny_, G.wrapz(z + cz(d) - nz_));
+    const double u[3] = {ux, uy, uz};
+    const int c[3] = {cx(di), cy(di), cz(di)};
+    double p = rho0;
+    for (int a = 0; a < 3; ++a) p *= c[a] == 0 ? 2.0 / 3.0 - u[a] * u[a] : 0.5 * (1.0 / 3.0 + u[a] * u[a] + c[a] * u[a]);
+    state[2 * i + 1] = p - weight(di);
+}
+
+// characteristic farfield, farfield.py:144-206
+struct FarfieldObject {
+    int normal[3];
+    int mode;            // 0 inflow (fixed invariant), 1 evolving outflow, 2 glancing
+    double nh[3];        // unit normal
+    double un_inf;       // n.U
+    double ut_inf[3];    // U - un_inf n
+    double P[3][3];      // I - n n^T
+    int active[3];       // axes carrying a transverse term
+    double density;
+    double vel[3];
+};
+struct FarfieldParams {
+    FarfieldObject obj[8];
+    int nobj;
+};
+
+template <typename S>
+__device__ __forceinline__ void macro_at(const S *pdf, const Grid &G, int x, int y, int z, double &rho, double u[3]) {
+    double d = 0.0, j[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const double g = load_g(pdf, G, q, x, y, z);
+        d += g;
+        j[0] += cx(q) * g;
+        j[1] += cy(q) * g;
+        j[2] += cz(q) * g;
+    }
+    rho = 1.0 + d;
+    for (int a = 0; a < 3; ++a) u[a] = j[a] / rho;
+}
+
+// transverse term F of the evolving outflow invariant (farfield.py:162-180)
+template <typename S>
+__device__ double farfield_transverse(const S *pdf, const Grid &G, const FarfieldObject &o, const int foot[3],
+                                      const signed char edge[3], const double u[3], double rm) {
+    double F = 0.0;
+    for (int a = 0; a < 3; ++a) {
+        if (!o.active[a]) continue;
+        const int e = edge[a];
+        const int off1 = e == -1 ? 1 : -1;
+        const int off2 = e == 0 ? 1 : -2 * e;
+        const double c0 = 1.5 * e;
+        const double c1 = e == 0 ? -0.5 : -2.0 * e;
+        const double c2 = e == 0 ? 0.5 : 0.5 * e;
+        int s1[3] = {foot[0], foot[1], foot[2]}, s2[3] = {foot[0], foot[1], foot[2]};
+        s1[a] += off1;
+        s2[a] += off2;
+        s1[2] = G.wrapz(s1[2]);
+        s2[2] = G.wrapz(s2[2]);
+        double r1, v1[3], r2, v2[3];
+        macro_at(pdf, G, s1[0], s1[1], s1[2], r1, v1);
+        macro_at(pdf, G, s2[0], s2[1], s2[2], r2, v2);
+        double du[3];
+        for (int b = 0; b < 3; ++b) du[b] = c0 * u[b] + c1 * v1[b] + c2 * v2[b];
+        const double rm1 = o.nh[0] * v1[0] + o.nh[1] * v1[1] + o.nh[2] * v1[2] - CS * log(r1 / o.density);
+        const double rm2 = o.nh[0] * v2[0] + o.nh[1] * v2[1] + o.nh[2] * v2[2] - CS * log(r2 / o.density);
+        F += o.un_inf * (o.P[a][0] * du[0] + o.P[a][1] * du[1] + o.P[a][2] * du[2]) -
+             o.ut_inf[a] * (c0 * rm + c1 * rm1 + c2 * rm2);
+    }
+    return F;
+}
+
+__device__ __forceinline__ double feq_dir(double r, const double v[3], int q) {
+    const int c[3] = {cx(q), cy(q), cz(q)};
+    double p = r;
+    for (int a = 0; a < 3; ++a) {
+        const double cc = (double)c[a], w = v[a];
+        p *= 2.0 / 3.0 - w * w + (1.5 * w * w - 0.5) * cc * cc + cc * w / 2.0;
+    }
+    return p;
+}
+
+template <typename S>
+__global__ void k_farfield(S *__restrict__ pdf, Grid G, OuterLinks L, FarfieldParams P, double *__restrict__ incoming,
+                           double *__restrict__ derivative, long long *__restrict__ clock,
+                           const double *__restrict__ init_lo, const double *__restrict__ init_hi, int prepare) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= L.n) return;
+    const int x = L.x[i], y = L.y[i], z = L.z[i], d = L.d[i], di = inv(d);
+    const FarfieldObject &o = P.obj[L.obj[i]];
+    // foot = x + c_d - n: a fluid cell next to the ghost cell, wrapped in z
+    const int foot[3] = {x + cx(d) - o.normal[0], y + cy(d) - o.normal[1], G.wrapz(z + cz(d) - o.normal[2])};
+    const signed char edge[3] = {L.edge[2 * i], L.edge[2 * i + 1], 0};
+    double rho, u[3];
+    macro_at(pdf, G, foot[0], foot[1], foot[2], rho, u);
+    const double un = o.nh[0] * u[0] + o.nh[1] * u[1] + o.nh[2] * u[2];
+    const double lr = log(rho / o.density);
+    const double rm = un - CS * lr, rp = un + CS * lr;
+    if (prepare) {
+        // farfield.py:84-113: seed the trapezoid so the first update returns
+        // the actual initial invariant
+        if (o.mode == 1) {
+            const double F = farfield_transverse(pdf, G, o, foot, edge, u, rm);
+            incoming[i] = rm - F;
+            derivative[i] = F;
+        } else if (o.mode == 2) {
+            clock[i] = 0;
+        } else {
+            incoming[i] = o.un_inf;
+            derivative[i] = 0.0;
+        }
+        return;
+    }
+    double value, F = 0.0;
+    if (o.mode == 1) {
+        F = farfield_transverse(pdf, G, o, foot, edge, u, rm);
+        value = incoming[i] + (F + derivative[i]) / 2.0;
+    } else if (o.mode == 2) {
+        // one linear interpolation of the saved initial invariant at the shift
+        // U * clock along x (the only axis with U != 0), zero outside
+        const double target = (double)(foot[0] - 1) - o.vel[0] * (double)clock[i];
+        const int lower = (int)floor(target);
+        const double frac = target - lower;
+        const double *row = o.normal[1] < 0 ? init_lo : init_hi;
+        double sum = 0.0;
+        for (int bit = 0; bit < 2; ++bit) {
+            const int k = lower + bit;
+            const double w = bit ? frac : 1.0 - frac;
+            const int kc = k < 0 ? 0 : (k > G.nx - 1 ? G.nx - 1 : k);
+            const double sample = row[(long long)kc * G.nz + foot[2]];
+            sum += w * ((k >= 0 && k < G.nx) ? sample : 0.0);
+        }
+        value = o.un_inf + sum;
+    } else {
+        value = o.un_inf;
+    }
+    const double unb = (rp + value) / 2.0;
+    const double rhob = o.density * exp((rp - value) / (2.0 * CS));
+    double ub[3];
+    for (int a = 0; a < 3; ++a) {
+        const double tangential = unb >= 0.0 ? u[a] - o.nh[a] * un : o.vel[a] - o.nh[a] * o.un_inf;
+        ub[a] = o.nh[a] * unb + tangential;
+    }
+    const double ghost = load_g(pdf, G, di, foot[0], foot[1], foot[2]) + feq_dir(rhob, ub, di) - feq_dir(rho, u, di);
+    store_g(pdf, G, di, x + cx(d), y + cy(d), G.wrapz(z + cz(d)), ghost);
+    if (o.mode == 1) {
+        incoming[i] = value;
+        derivative[i] = F;
+    } else if (o.mode == 2) {
+        clock[i] += 1;
+    }
+}
+
+// glancing faces: initial invariant u.n - cs ln(rho/rho_inf) - un_inf on the
+// fluid row next to the face (the only row the transport reads)
+template <typename S>
+__global__ void k_glancing_rows(const S *__restrict__ pdf, Grid G, FarfieldParams P, double *__restrict__ lo,
+                                double *__restrict__ hi) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)G.nx * G.nz) return;
+    const int x = (int)(i / G.nz) + 1, z = (int)(i - (i / G.nz) * G.nz);
+    for (int k = 0; k < P.nobj; ++k) {
+        const FarfieldObject &o = P.obj[k];
+        if (o.mode != 2) continue;
+        const int y = o.normal[1] < 0 ? 1 : G.ny;
+        double rho, u[3];
+        macro_at(pdf, G, x, y, z, rho, u);
+        const double v = o.nh[0] * u[0] + o.nh[1] * u[1] + o.nh[2] * u[2] - CS * log(rho / o.density) - o.un_inf;
+        (o.normal[1] < 0 ? lo : hi)[i] = v;
+    }
+}
+
+// ------------------------------------------------------------ fields
+__device__ __forceinline__ void equilibrium_g(double rho, const double u[3], double g[Q]) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const int c[3] = {cx(q), cy(q), cz(q)};
+        double p = rho;
+        for (int a = 0; a < 3; ++a)
+            p *= c[a] == 0 ? 2.0 / 3.0 - u[a] * u[a] : 0.5 * (1.0 / 3.0 + u[a] * u[a] + c[a] * u[a]);
+        g[q] = p - weight(q);
+    }
+}
+
+// solver.py:157-202 on the device: freestream plus the divergence-free seed
+template <typename S>
+__global__ void k_init_perturbed(S *__restrict__ pdf, Grid G, const uint8_t *__restrict__ flags, double speed,
+                                 double amp, double phase_y, double phase_z, double lead_x, double lead_y,
+                                 double origin_x, double origin_y, double dx, double ky, double kz) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)G.nx * G.ny * G.nz) return;
+    const int z = (int)(i % G.nz);
+    const long long xy = i / G.nz;
+    const int y = (int)(xy % G.ny), x = (int)(xy / G.ny);
+    double u[3] = {speed, 0.0, 0.0};
+    const double xm = x + 0.5, ym = y + 0.5, zm = z + 0.5;
+    const double rel_x = (xm * dx + origin_x) - lead_x, rel_y = (ym * dx + origin_y) - lead_y;
+    const double zz = zm * dx;
+    const double t = (rel_x - 0.5) / 0.75;
+    const double env = exp(-(t * t));
+    u[1] = amp * sin(ky * rel_y + phase_y) * cos(kz * zz + phase_z) * env;
+    u[2] = -amp * ky / kz * cos(ky * rel_y + phase_y) * sin(kz * zz + phase_z) * env;
+    if (flags[(y + 1) * G.nxp + (x + 1)] != FLAG_FLUID) u[0] = u[1] = u[2] = 0.0;
+    double g[Q];
+    equilibrium_g(1.0, u, g);
+    for (int q = 0; q < Q; ++q) store_g(pdf, G, q, x + 1, y + 1, z, g[q]);
+}
+
+// rho/u given per interior cell in (x, y, z) order
+template <typename S>
+__global__ void k_init_fields(S *__restrict__ pdf, Grid G, const double *__restrict__ rho,
+                              const double *__restrict__ vel) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)G.nx * G.ny * G.nz) return;
+    const int z = (int)(i % G.nz);
+    const long long xy = i / G.nz;
+    const int y = (int)(xy % G.ny), x = (int)(xy / G.ny);
+    const double u[3] = {vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]};
+    double g[Q];
+    equilibrium_g(rho[i], u, g);
+    for (int q = 0; q < Q; ++q) store_g(pdf, G, q, x + 1, y + 1, z, g[q]);
+}
+
+// (x, y, z, 27) doubles <-> device layout
+template <typename S>
+__global__ void k_export(const S *__restrict__ pdf, Grid G, double *__restrict__ out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)G.nx * G.ny * G.nz) return;
+    const int z = (int)(i % G.nz);
+    const long long xy = i / G.nz;
+    const int y = (int)(xy % G.ny), x = (int)(xy / G.ny);
+    for (int q = 0; q < Q; ++q) out[i * Q + q] = load_g(pdf, G, q, x + 1, y + 1, z);
+}
+template <typename S>
+__global__ void k_import(S *__restrict__ pdf, Grid G, const double *__restrict__ in) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)G.nx * G.ny * G.nz) return;
+    const int z = (int)(i % G.nz);
+    const long long xy = i / G.nz;
+    const int y = (int)(xy % G.ny), x = (int)(xy / G.ny);
+    for (int q = 0; q < Q; ++q) store_g(pdf, G, q, x + 1, y + 1, z, in[i * Q + q]);
+}
+
+template <typename S>
+__global__ void k_macros(const S *__restrict__ pdf, Grid G, double *__restrict__ rho, double *__restrict__ vel) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)G.nx * G.ny * G.nz) return;
+    const int z = (int)(i % G.nz);
+    const long long xy = i / G.nz;
+    const int y = (int)(xy % G.ny), x = (int)(xy / G.ny);
+    double r, u[3];
+    macro_at(pdf, G, x + 1, y + 1, z, r, u);
+    rho[i] = r;
+    vel[3 * i] = u[0];
+    vel[3 * i + 1] = u[1];
+    vel[3 * i + 2] = u[2];
+}
+
+// validity reduction over fluid cells (solver.py:281-297):
+// partial[block] = (max |u|^2, max |rho-1|, min rho (as -max -rho), sum rho, count non-finite)
+template <typename S>
+__global__ void __launch_bounds__(256) k_diagnostics(const S *__restrict__ pdf, Grid G,
+                                                     const uint8_t *__restrict__ flags, double *__restrict__ partials) {
+    const long long n = (long long)G.nx * G.ny * G.nz;
+    double mx_u2 = 0.0, mx_dr = 0.0, mx_neg = -1e300, sum = 0.0, bad = 0.0, cnt = 0.0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % G.nx);
+        const long long yz = i / G.nx;
+        const int y = (int)(yz % G.ny), z = (int)(yz / G.ny);
+        if (flags[(y + 1) * G.nxp + (x + 1)] != FLAG_FLUID) continue;
+        double r, u[3];
+        macro_at(pdf, G, x + 1, y + 1, z, r, u);
+        const double u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+        if (!isfinite(r) || !isfinite(u2)) {
+            bad += 1.0;
+            continue;
+        }
+        mx_u2 = fmax(mx_u2, u2);
+        mx_dr = fmax(mx_dr, fabs(r - 1.0));
+        mx_neg = fmax(mx_neg, -r);
+        sum += r;
+        cnt += 1.0;
+    }
+    __shared__ double red[32][6];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        mx_u2 = fmax(mx_u2, __shfl_down_sync(0xffffffffu, mx_u2, o));
+        mx_dr = fmax(mx_dr, __shfl_down_sync(0xffffffffu, mx_dr, o));
+        mx_neg = fmax(mx_neg, __shfl_down_sync(0xffffffffu, mx_neg, o));
+        sum += __shfl_down_sync(0xffffffffu, sum, o);
+        bad += __shfl_down_sync(0xffffffffu, bad, o);
+        cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    }
+    if (lane == 0) {
+        red[warp][0] = mx_u2;
+        red[warp][1] = mx_dr;
+        red[warp][2] = mx_neg;
+        red[warp][3] = sum;
+        red[warp][4] = bad;
+        red[warp][5] = cnt;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int nw = blockDim.x >> 5;
+        double a[6] = {red[0][0], red[0][1], red[0][2], red[0][3], red[0][4], red[0][5]};
+        for (int w = 1; w < nw; ++w) {
+            a[0] = fmax(a[0], red[w][0]);
+            a[1] = fmax(a[1], red[w][1]);
+            a[2] = fmax(a[2], red[w][2]);
+            a[3] += red[w][3];
+            a[4] += red[w][4];
+            a[5] += red[w][5];
+        }
+        for (int k = 0; k < 6; ++k) partials[blockIdx.x * 6 + k] = a[k];
+    }
+}
+
+__global__ void k_diagnostics_final(const double *__restrict__ partials, int nblocks, double *__restrict__ out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double a[6] = {partials[0], partials[1], partials[2], partials[3], partials[4], partials[5]};
+    for (int b = 1; b < nblocks; ++b) {
+        a[0] = fmax(a[0], partials[6 * b]);
+        a[1] = fmax(a[1], partials[6 * b + 1]);
+        a[2] = fmax(a[2], partials[6 * b + 2]);
+        a[3] += partials[6 * b + 3];
+        a[4] += partials[6 * b + 4];
+        a[5] += partials[6 * b + 5];
+    }
+    for (int k = 0; k < 6; ++k) out[k] = a[k];
+}
+
+}  // namespace ak

@@ -1,0 +1,182 @@
+// ak_lattice.cuh -- D3Q27 stencil, population storage and the cumulant
+// collision used by every sm_103a kernel of the engine.
+//
+// Directions follow lbmpy's D3Q27 order (the reference's pdf[..., d] index).
+// The collision is the compressible cumulant operator the reference configures
+// (src/aerokinetic/solver.py:75-77, interface.py:124-128): the five deviatoric
+// second-order cumulants relax with omega_shear, their trace with omega_bulk,
+// and every cumulant of order >= 3 with rate 1 to its zero equilibrium
+// (Geier et al. 2015, doi:10.1016/j.camwa.2015.05.001).
+//
+// With all higher cumulants at zero, the post-collision state is determined by
+// rho, u and the relaxed covariance S (= second-order central moments / rho):
+// its central moments are Gaussian pairings of S.  Applying the per-axis
+// central-moment -> population map (the three-point transform of Geier's
+// chimera scheme) to that pairing sum gives eleven separable terms,
+//
+//   f*(cx,cy,cz)/rho = A(cx,cy) phi_z(cz) + B(cx,cy) psi_z(cz) + C(cx,cy) chi(cz)
+//   A = phi_x phi_y + s_xy psi_x psi_y + 2 s_xy^2 chi chi
+//   B = s_xz psi_x phi_y + s_yz phi_x psi_y + 2 s_xy (s_xz chi psi_y + s_yz psi_x chi)
+//   C = 2 s_xz^2 chi phi_y + 2 s_yz^2 phi_x chi + 2 s_xz s_yz psi_x psi_y + 8 s_xy s_xz s_yz chi chi
+//
+// with phi_a(c) the 1-D population of mean u_a and variance s_aa, psi_a(c) =
+// (u-1/2, -2u, u+1/2) and chi = (1/2, -1, 1/2).  Everything is evaluated as a
+// deviation from the rest weights (g = f - w, rho = 1 + drho, s_aa = 1/3 +
+// sigma_a), so single precision keeps its relative accuracy on the small
+// quantities it stores.
+#pragma once
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+namespace ak {
+
+constexpr int Q = 27;
+
+// lbmpy D3Q27 order
+__host__ __device__ constexpr int cx(int q) {
+    constexpr int8_t t[Q] = {0, 0, 0, -1, 1, 0, 0, -1, 1, -1, 1, 0, 0, -1, 1, 0, 0, -1, 1, 1, -1, 1, -1, 1, -1, 1, -1};
+    return t[q];
+}
+__host__ __device__ constexpr int cy(int q) {
+    constexpr int8_t t[Q] = {0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, -1, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1};
+    return t[q];
+}
+__host__ __device__ constexpr int cz(int q) {
+    constexpr int8_t t[Q] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, 1, 1, -1, -1, -1, -1, 1, 1, 1, 1, -1, -1, -1, -1};
+    return t[q];
+}
+// direction index of (cx, cy, cz) given as (ix, iy, iz) = c + 1
+__host__ __device__ constexpr int qof(int ix, int iy, int iz) {
+    constexpr int8_t t[27] = {26, 9, 22, 17, 3, 13, 24, 7, 20,   // cx = -1
+                              16, 2, 12, 6, 0, 5, 15, 1, 11,     // cx = 0
+                              25, 10, 21, 18, 4, 14, 23, 8, 19}; // cx = +1
+    return t[(ix * 3 + iy) * 3 + iz];
+}
+__host__ __device__ constexpr int inv(int q) {
+    constexpr int8_t t[Q] = {0, 2, 1, 4, 3, 6, 5, 10, 9, 8, 7, 16, 15, 18, 17, 12, 11, 14, 13, 26, 25, 24, 23, 22, 21, 20, 19};
+    return t[q];
+}
+__host__ __device__ constexpr double w1(int i) { return i == 1 ? 2.0 / 3.0 : 1.0 / 6.0; }  // i = c + 1
+__host__ __device__ constexpr double weight(int q) {
+    return w1(cx(q) + 1) * w1(cy(q) + 1) * w1(cz(q) + 1);
+}
+
+// ---------------------------------------------------------------- storage
+// Populations are stored as g = f - w.  F16 stores g / w (rescaled back in
+// FP32 arithmetic) so that the small deviations use the normal range of the
+// format.
+template <typename S> struct Store;
+template <> struct Store<double> {
+    using T = double;
+    __device__ static __forceinline__ double load(const double *p, int) { return __ldg(p); }
+    __device__ static __forceinline__ void store(double *p, int, double v) { *p = v; }
+    __host__ __device__ static double to_g(double v, int) { return v; }
+};
+template <> struct Store<float> {
+    using T = float;
+    __device__ static __forceinline__ float load(const float *p, int) { return __ldg(p); }
+    __device__ static __forceinline__ void store(float *p, int, float v) { *p = v; }
+    __host__ __device__ static double to_g(float v, int) { return v; }
+};
+template <> struct Store<__half> {
+    using T = float;
+    __device__ static __forceinline__ float load(const __half *p, int q) {
+        return __half2float(__ldg(p)) * (float)weight(q);
+    }
+    __device__ static __forceinline__ void store(__half *p, int q, float v) {
+        *p = __float2half_rn(v * (float)(1.0 / weight(q)));
+    }
+};
+
+// ---------------------------------------------------------------- collision
+template <typename T>
+__device__ __forceinline__ void collide(T g[Q], T omega_s, T omega_b) {
+    // raw moments of g up to second order through partial line sums
+    T Z0[3][3], Z1[3][3], Z2[3][3];
+#pragma unroll
+    for (int ix = 0; ix < 3; ++ix)
+#pragma unroll
+        for (int iy = 0; iy < 3; ++iy) {
+            const T a = g[qof(ix, iy, 0)], b = g[qof(ix, iy, 1)], c = g[qof(ix, iy, 2)];
+            Z1[ix][iy] = c - a;
+            Z2[ix][iy] = c + a;
+            Z0[ix][iy] = Z2[ix][iy] + b;
+        }
+    T Y00[3], Y01[3], Y02[3], Y10[3], Y11[3], Y20[3];
+#pragma unroll
+    for (int ix = 0; ix < 3; ++ix) {
+        Y01[ix] = Z0[ix][2] - Z0[ix][0];
+        Y02[ix] = Z0[ix][2] + Z0[ix][0];
+        Y00[ix] = Y02[ix] + Z0[ix][1];
+        Y11[ix] = Z1[ix][2] - Z1[ix][0];
+        Y10[ix] = Z1[ix][0] + Z1[ix][1] + Z1[ix][2];
+        Y20[ix] = Z2[ix][0] + Z2[ix][1] + Z2[ix][2];
+    }
+    const T M200 = Y00[2] + Y00[0];
+    const T drho = M200 + Y00[1];
+    const T jx = Y00[2] - Y00[0];
+    const T jy = Y01[0] + Y01[1] + Y01[2];
+    const T M110 = Y01[2] - Y01[0];
+    const T M020 = Y02[0] + Y02[1] + Y02[2];
+    const T jz = Y10[0] + Y10[1] + Y10[2];
+    const T M101 = Y10[2] - Y10[0];
+    const T M011 = Y11[0] + Y11[1] + Y11[2];
+    const T M002 = Y20[0] + Y20[1] + Y20[2];
+
+    const T rho = T(1) + drho;
+    const T rinv = T(1) / rho;
+    const T ux = jx * rinv, uy = jy * rinv, uz = jz * rinv;
+    // second-order central moments minus their rest value 1/3
+    const T kdx = M200 - jx * ux, kdy = M020 - jy * uy, kdz = M002 - jz * uz;
+    const T kxy = M110 - jx * uy, kxz = M101 - jx * uz, kyz = M011 - jy * uz;
+    const T om1 = T(1) - omega_s;
+    const T P1 = om1 * (kdx - kdy), P2 = om1 * (kdx - kdz);
+    const T S = kdx + kdy + kdz;
+    const T tr = S + omega_b * (drho - S);
+    const T third = T(1) / T(3);
+    const T kx = (P1 + P2 + tr) * third;
+    const T ky = kx - P1, kz = kx - P2;
+    const T d3 = drho * third;
+    const T sig[3] = {(kx - d3) * rinv, (ky - d3) * rinv, (kz - d3) * rinv};
+    const T sxy = om1 * kxy * rinv, sxz = om1 * kxz * rinv, syz = om1 * kyz * rinv;
+    const T u[3] = {ux, uy, uz};
+
+    T dphi[3][3], phi[3][3], psi[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const T t = u[a] * u[a] + sig[a];
+        const T h = T(0.5) * t, hu = T(0.5) * u[a];
+        dphi[a][0] = h - hu;
+        dphi[a][1] = -t;
+        dphi[a][2] = h + hu;
+        phi[a][0] = T(1.0 / 6.0) + dphi[a][0];
+        phi[a][1] = T(2.0 / 3.0) + dphi[a][1];
+        phi[a][2] = T(1.0 / 6.0) + dphi[a][2];
+        psi[a][0] = u[a] - T(0.5);
+        psi[a][1] = T(-2) * u[a];
+        psi[a][2] = u[a] + T(0.5);
+    }
+    const T chi[3] = {T(0.5), T(-1), T(0.5)};
+    const T sxy2 = T(2) * sxy * sxy, sxz2 = T(2) * sxz * sxz, syz2 = T(2) * syz * syz;
+    const T bxz = T(2) * sxy * sxz, byz = T(2) * sxy * syz, cxz = T(2) * sxz * syz;
+    const T c8 = T(4) * bxz * syz;  // 8 s_xy s_xz s_yz
+#pragma unroll
+    for (int ix = 0; ix < 3; ++ix)
+#pragma unroll
+        for (int iy = 0; iy < 3; ++iy) {
+            const T A0 = T(w1(ix) * w1(iy));
+            const T dA = dphi[0][ix] * phi[1][iy] + T(w1(ix)) * dphi[1][iy] + sxy * psi[0][ix] * psi[1][iy] +
+                         sxy2 * (chi[ix] * chi[iy]);
+            const T B = sxz * psi[0][ix] * phi[1][iy] + syz * phi[0][ix] * psi[1][iy] +
+                        bxz * chi[ix] * psi[1][iy] + byz * psi[0][ix] * chi[iy];
+            const T C = sxz2 * chi[ix] * phi[1][iy] + syz2 * phi[0][ix] * chi[iy] + cxz * psi[0][ix] * psi[1][iy] +
+                        c8 * (chi[ix] * chi[iy]);
+            const T rA = rho * dA, rB = rho * B, rC = rho * C, rA0 = rho * A0, dA0 = drho * A0;
+#pragma unroll
+            for (int iz = 0; iz < 3; ++iz)
+                g[qof(ix, iy, iz)] = dA0 * T(w1(iz)) + rA0 * dphi[2][iz] + rA * phi[2][iz] + rB * psi[2][iz] +
+                                     rC * chi[iz];
+        }
+}
+
+}  // namespace ak

@@ -1,0 +1,146 @@
+/*
+ * aerokinetic_gb300.h -- C ABI of the GB300 engine for AeroKinetic's uniform
+ * D3Q27 cumulant lattice-Boltzmann step.
+ *
+ * The reference (Bulbulator72/Aerokinetic 0.5.3, Python) drives a lbmpy
+ * LatticeBoltzmannStep through a handful of private calls; each entry point
+ * below replaces one of them (reference paths are relative to that project):
+ *
+ *   ak_case_create      LatticeBoltzmannStep construction and boundary set-up,
+ *                       src/aerokinetic/solver.py:58-91 and 124-155 (solid
+ *                       flags, cut links, Bouzidi q with the half-way fallback,
+ *                       UBB/ExtrapolationOutflow or the characteristic farfield
+ *                       of src/aerokinetic/farfield.py:209-224)
+ *   ak_init_perturbed   Solver._initialize, solver.py:157-202
+ *   ak_init_fields      LatticeBoltzmannStep.set_pdf_fields_from_macroscopic_values
+ *                       with caller-supplied rho/u (solver.py:202)
+ *   ak_step             the step body, solver.py:256-261 (_sync_src,
+ *                       boundary_handling, run_kernel(stream_collide), swap),
+ *                       with the loads of Solver._loads, solver.py:204-250
+ *   ak_diagnostics      Solver.diagnostics, solver.py:281-297
+ *   ak_macros           LatticeBoltzmannStep.post_run + gather_array of the
+ *                       density/velocity fields (solver.py:283-286, 318-319)
+ *   ak_get_pdf /        data_handling.cpu_arrays[pdf] reads and writes used by
+ *   ak_set_pdf          the checkpoint module (checkpoint.py:20-68)
+ *   ak_get_wall_links   boundary_handling index lists of the walls
+ *                       (walls.py:51-66, solver.py:218-226)
+ *
+ * Conventions.  All functions return 0 (AK_OK) or an AK_ERR_* code and leave
+ * a message for ak_last_error.  Populations cross the ABI as double, in the
+ * reference's layout: (nx, ny, nz, 27) C order, interior cells only,
+ * zero-centred g = f - w, lbmpy's D3Q27 direction order.  Device memory is
+ * allocated and owned by the case; every call on one case is stream-ordered on
+ * the case's own CUDA stream and returns after its results are on the host.
+ * One case may be used by one host thread at a time.
+ */
+#ifndef AEROKINETIC_GB300_H
+#define AEROKINETIC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AK_OK 0
+#define AK_ERR_INVALID 1     /* bad argument; maps to ValueError */
+#define AK_ERR_CUDA 2        /* CUDA runtime failure */
+#define AK_ERR_NOMEM 3       /* device allocation failed; maps to MemoryError */
+#define AK_ERR_NONFINITE 4   /* non-finite state; maps to NumericalFailure */
+#define AK_ERR_GUARD 5       /* local Mach or density guard; maps to NumericalFailure */
+#define AK_ERR_GEOMETRY 6    /* a cut link without a polygon crossing */
+
+#define AK_FARFIELD_LEGACY 0          /* UBB + ExtrapolationOutflow (solver.py:130-135) */
+#define AK_FARFIELD_CHARACTERISTIC 1  /* characteristic_transport_v1 (farfield.py) */
+
+#define AK_STORAGE_F64 0  /* plain form: FP64 storage and arithmetic */
+#define AK_STORAGE_F32 1  /* FP32 arithmetic, FP32 (f - w) storage */
+#define AK_STORAGE_F16 2  /* FP32 arithmetic, FP16 (f - w)/w storage */
+
+typedef struct ak_case ak_case;
+
+typedef struct {
+    int32_t nx, ny, nz;          /* interior lattice; z is periodic */
+    double origin_x, origin_y;   /* plan origin (chord units), solver.py:39-40 */
+    double dx;                   /* plan dx = 1 / cells_per_chord */
+    double omega_shear;          /* plan relaxation rate */
+    double omega_bulk;           /* 1.0 for the uniform solver */
+    double speed;                /* freestream lattice speed along +x */
+    int32_t farfield;            /* AK_FARFIELD_* */
+    int32_t storage;             /* AK_STORAGE_* */
+    int32_t n_elements;          /* number of polygons (wall elements) */
+    const int32_t *element_sizes;/* vertices per polygon */
+    const double *polygon_xy;    /* all vertices, (x, y) pairs, normalised frame */
+} ak_case_desc;
+
+typedef struct {
+    int64_t cells;          /* nx * ny * nz */
+    int64_t fluid_cells;
+    int64_t wall_keys;      /* distinct (column, planar direction) cut links */
+    int64_t wall_links;     /* wall_keys * nz * 3 */
+    int64_t outer_links;    /* links into the outer ghost ring */
+    int64_t fallback_links; /* 3-D links using the half-way fallback */
+    int64_t device_bytes;   /* bytes of device memory held by the case */
+    int32_t row_pitch;      /* elements between consecutive x rows */
+    int32_t storage;
+} ak_case_info;
+
+/* solver.py:58-155.  Builds the case on the current CUDA device. */
+int ak_case_create(const ak_case_desc *desc, ak_case **out);
+int ak_case_destroy(ak_case *c);
+int ak_case_get_info(const ak_case *c, ak_case_info *info);
+
+/* solver.py:157-202: rho = 1, u = (U, u_y, u_z) with the divergence-free
+ * perturbation of amplitude amp (= perturbation * U), phases phase_y/phase_z,
+ * Gaussian envelope about the rotated leading edge (lead_x, lead_y), span in
+ * chord units; solid cells at rest. */
+int ak_init_perturbed(ak_case *c, double amp, double phase_y, double phase_z, double lead_x,
+                      double lead_y, double span);
+/* set_pdf_fields_from_macroscopic_values with host rho (nx*ny*nz) and u (*3). */
+int ak_init_fields(ak_case *c, const double *rho, const double *u);
+
+/* Advance nsteps steps.  If loads != NULL the last step samples the
+ * momentum-exchange loads before streaming (solver.py:258-259) into
+ * loads[n_elements * 5] = (Fx, Fy, Fz, Mz, incoming-minus-outgoing mass) per
+ * element, in lattice units, Mz about the normalised frame's origin. */
+int ak_step(ak_case *c, int32_t nsteps, double *loads);
+int64_t ak_steps_done(const ak_case *c);
+/* Kernels the case has issued while stepping (for launch accounting). */
+int64_t ak_kernel_launches(const ak_case *c);
+/* The case's CUDA stream (cudaStream_t), for callers that order their own work
+ * after the case's or time it with their own events. */
+void *ak_case_stream(const ak_case *c);
+/* ak_step without loads, timed with CUDA events on the case's stream:
+ * ms[0] whole interval, ms[1] stream-collide kernels, ms[2] wall kernels,
+ * ms[3] outer-boundary kernels (milliseconds, summed over the steps).  No
+ * counterpart in the reference; it exists for measurement. */
+int ak_step_timed(ak_case *c, int32_t nsteps, double *ms);
+
+/* diag[0] = local Mach max over fluid cells, diag[1] = mean density of fluid
+ * cells, diag[2] = max |rho - 1|, diag[3] = min rho, diag[4] = 1 if every
+ * fluid value is finite.  Returns AK_ERR_NONFINITE / AK_ERR_GUARD like
+ * solver.py:289-294 after filling diag. */
+int ak_diagnostics(ak_case *c, double *diag);
+
+/* rho (nx*ny*nz) and u (nx*ny*nz*3) of the current state, to host memory. */
+int ak_macros(ak_case *c, double *rho, double *u);
+int ak_get_pdf(ak_case *c, double *pdf);
+int ak_set_pdf(ak_case *c, const double *pdf);
+
+/* Solid flags of the interior columns (nx*ny, x-major like the reference's
+ * _solid_xy): 0 fluid, k+1 inside element k. */
+int ak_get_flags(ak_case *c, uint8_t *flags);
+/* Distinct wall keys: rows[4k..4k+3] = (element, x, y, direction index of the
+ * planar link), q[k] the Bouzidi fraction (-1 = half-way fallback). */
+int ak_get_wall_links(ak_case *c, int32_t *rows, double *q);
+
+/* Message of the last failure on this thread ("" if none). */
+const char *ak_last_error(void);
+/* Library build identification, e.g. "aerokinetic_gb300 sm_103a". */
+const char *ak_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

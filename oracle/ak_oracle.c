@@ -51,38 +51,7 @@ static double W[Q];
 static int INV[Q];
 static int LINE[3][3][3]; /* (cx+1, cy+1, cz+1) -> direction index */
 
-/* Post-collision central moments of order 4 and 6 follow from the second-order
- * ones by Isserlis' pairing theorem when every cumulant of order >= 3 is zero.
- * PAIRS[e] lists, for each multi-index e = (a,b,c), its perfect matchings as
- * index pairs into the 6 second-order moments (xx,yy,zz,xy,xz,yz). */
-#define MAXM 15
-static int NMATCH[27];
-static int MATCH[27][MAXM][3];
 static int initialised = 0;
-
-static int second_index(int p, int q) {
-    if (p > q) { int t = p; p = q; q = t; }
-    if (p == q) return p;          /* xx=0 yy=1 zz=2 */
-    if (p == 0 && q == 1) return 3; /* xy */
-    if (p == 0 && q == 2) return 4; /* xz */
-    return 5;                      /* yz */
-}
-
-static void enumerate_matchings(const int *axes, int n, int used, int *cur, int depth, int e) {
-    int first = -1;
-    for (int i = 0; i < n; ++i)
-        if (!(used & (1 << i))) { first = i; break; }
-    if (first < 0) {
-        int k = NMATCH[e]++;
-        for (int m = 0; m < 3; ++m) MATCH[e][k][m] = m < depth ? cur[m] : -1;
-        return;
-    }
-    for (int j = first + 1; j < n; ++j) {
-        if (used & (1 << j)) continue;
-        cur[depth] = second_index(axes[first], axes[j]);
-        enumerate_matchings(axes, n, used | (1 << first) | (1 << j), cur, depth + 1, e);
-    }
-}
 
 static void init_tables(void) {
     if (initialised) return;
@@ -100,16 +69,6 @@ static void init_tables(void) {
     for (int q = 0; q < Q; ++q)
         for (int p = 0; p < Q; ++p)
             if (CV[p][0] == -CV[q][0] && CV[p][1] == -CV[q][1] && CV[p][2] == -CV[q][2]) INV[q] = p;
-    for (int a = 0; a < 3; ++a)
-        for (int b = 0; b < 3; ++b)
-            for (int c = 0; c < 3; ++c) {
-                int e = (a * 3 + b) * 3 + c, axes[6], n = 0, cur[3];
-                for (int i = 0; i < a; ++i) axes[n++] = 0;
-                for (int i = 0; i < b; ++i) axes[n++] = 1;
-                for (int i = 0; i < c; ++i) axes[n++] = 2;
-                NMATCH[e] = 0;
-                if (n % 2 == 0 && n > 0) enumerate_matchings(axes, n, 0, cur, 0, e);
-            }
     initialised = 1;
 }
 
@@ -185,22 +144,26 @@ static void collide_cell(double *g, double omega_s, double omega_b) {
     s[4] = (1.0 - omega_s) * K[1][0][1];
     s[5] = (1.0 - omega_s) * K[0][1][1];
     /* all higher cumulants relax to their zero equilibrium with rate 1, so the
-     * post-collision central moments are sums over pairings of second-order ones */
-    double cov[6];
-    for (int i = 0; i < 6; ++i) cov[i] = s[i] / rho;
-    for (int a = 0; a < 3; ++a)
-        for (int b = 0; b < 3; ++b)
-            for (int c = 0; c < 3; ++c) {
-                int e = (a * 3 + b) * 3 + c;
-                double v = 0.0;
-                if (e == 0) v = 1.0;
-                for (int k = 0; k < NMATCH[e]; ++k) {
-                    double p = 1.0;
-                    for (int m = 0; m < 3 && MATCH[e][k][m] >= 0; ++m) p *= cov[MATCH[e][k][m]];
-                    v += p;
-                }
-                K[a][b][c] = rho * v;
-            }
+     * post-collision central moments are Gaussian (Isserlis) pairings of the
+     * normalised second-order ones; odd orders vanish */
+    double sxx = s[0] / rho, syy = s[1] / rho, szz = s[2] / rho;
+    double sxy = s[3] / rho, sxz = s[4] / rho, syz = s[5] / rho;
+    memset(K, 0, sizeof K);
+    K[0][0][0] = rho;
+    K[2][0][0] = s[0];
+    K[0][2][0] = s[1];
+    K[0][0][2] = s[2];
+    K[1][1][0] = s[3];
+    K[1][0][1] = s[4];
+    K[0][1][1] = s[5];
+    K[2][2][0] = rho * (sxx * syy + 2.0 * sxy * sxy);
+    K[2][0][2] = rho * (sxx * szz + 2.0 * sxz * sxz);
+    K[0][2][2] = rho * (syy * szz + 2.0 * syz * syz);
+    K[2][1][1] = rho * (sxx * syz + 2.0 * sxy * sxz);
+    K[1][2][1] = rho * (syy * sxz + 2.0 * sxy * syz);
+    K[1][1][2] = rho * (szz * sxy + 2.0 * sxz * syz);
+    K[2][2][2] = rho * (sxx * syy * szz + 2.0 * (sxx * syz * syz + syy * sxz * sxz + szz * sxy * sxy) +
+                        8.0 * sxy * sxz * syz);
     /* central moments -> populations: x lines, then y, then z */
     for (int b = 0; b < 3; ++b)
         for (int c = 0; c < 3; ++c) {

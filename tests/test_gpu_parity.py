@@ -1,0 +1,203 @@
+"""Parity of the sm_103a engine with the CPU oracle and the reference's records.
+
+Bars (the reference's own implementation gates, tools/research_tests/
+study_protocol.json:37-40): populations within 2e-12 per step and loads within
+2e-10 over tens of steps; flags, cut links and Bouzidi fractions bit-exact.
+The reduced-precision forms are compared with the FP64 engine and their
+errors bounded explicitly.
+"""
+import numpy as np
+import pytest
+
+from aerokinetic_gb300.config import Flow, Grid, Plan
+from aerokinetic_gb300.geometry import Contour, Section, naca0012
+from aerokinetic_gb300.project import Project
+from tests.conftest import oracle_threads
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+O = pytest.importorskip("oracle.oracle")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _needs_device():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def solver_for(project, storage="f64"):
+    from aerokinetic_gb300.solver import Solver
+    return Solver(project.section, project.flow, project.grid, storage=storage)
+
+
+def oracle_for(project):
+    plan = Plan.create(project.section, project.flow, project.grid)
+    contours = [c.xy for c in project.section.normalized(project.flow.alpha_deg)]
+    lead = O.leading_edge([e.xy for e in project.section.elements], project.section.moment_reference,
+                          project.section.chord, project.flow.alpha_deg)
+    return O.AirfoilCase(contours, plan.shape, plan.origin, plan.dx, plan.span, plan.relaxation_rate,
+                         project.flow.lattice_speed, project.grid.cells_per_chord, project.grid.farfield,
+                         project.flow.perturbation, project.flow.seed, lead, oracle_threads())
+
+
+def kat_project(farfield="legacy"):
+    return Project(Section((naca0012(81),), 1., (.25, 0)), Flow(reynolds=30000, alpha_deg=4, physical_chord_m=.15),
+                   Grid(cells_per_chord=32, upstream_chords=1.5, downstream_chords=3, transverse_chords=1.5,
+                        span_chords=.5, memory_limit_gib=2, farfield=farfield))
+
+
+def geometry_project(fixture):
+    s = fixture["section"]
+    elements = tuple(Contour(np.array(xy), name) for xy, name in zip(s["elements"], s["names"]))
+    return Project(Section(elements, s["chord"], tuple(s["moment_reference"])), Flow(**fixture["flow"]),
+                   Grid(**fixture["grid"]))
+
+
+@pytest.mark.parametrize("name", ["kat272", "uniform_c1", "failure_capture_n16", "two_element"])
+def test_flags_links_and_fractions_bit_exact(golden, name):
+    fixture = golden["geometry"][name]
+    solver = solver_for(geometry_project(fixture))
+    try:
+        assert list(solver.plan.shape) == fixture["plan"]["shape"]
+        flags = solver._solid_xy.astype(int)
+        ref = (np.array(fixture["solid_xy"]) != 0).astype(int)
+        assert np.array_equal(flags, ref)
+        rows, q = solver.wall_links()
+        c = O.stencil()[0]
+        mine = {(int(e), int(x), int(y), int(c[d][0]), int(c[d][1])): qq for (e, x, y, d), qq in zip(rows, q)}
+        theirs = {tuple(r[:5]): r[5] for r in fixture["wall_links_2d"]}
+        assert mine.keys() == theirs.keys()
+        assert all(mine[k] == theirs[k] for k in theirs)  # exact equality of doubles
+        assert solver.wall_fallback_links == 3 * solver.plan.shape[2] * fixture["wall_fallback_links_2d"]
+    finally:
+        solver.close()
+
+
+def compare_run(project, steps, sample_every, pdf_tol=2e-12, load_tol=2e-10):
+    solver, oracle = solver_for(project), oracle_for(project)
+    try:
+        np.testing.assert_allclose(solver.pdf(), oracle.lattice.interior(), rtol=0, atol=1e-15)
+        fluid = oracle.lattice.fluid
+        worst = 0.0
+        for s in range(1, steps + 1):
+            sample = s % sample_every == 0
+            mine = solver.step(sample)
+            theirs = oracle.step(sample)
+            if sample:
+                for k in ("cl", "cd", "cm"):
+                    assert mine[k] == pytest.approx(theirs[k], abs=load_tol), (s, k)
+                np.testing.assert_allclose(mine["element_lattice_loads"], theirs["element_lattice_loads"][:, :4],
+                                           rtol=0, atol=load_tol)
+            if s % max(1, steps // 4) == 0 or s == steps:
+                diff = np.abs(solver.pdf() - oracle.lattice.interior())[fluid].max()
+                worst = max(worst, diff)
+                assert diff <= pdf_tol * s, (s, diff)
+        return worst
+    finally:
+        solver.close()
+
+
+def test_legacy_case_matches_oracle():
+    compare_run(kat_project("legacy"), steps=40, sample_every=8)
+
+
+def test_characteristic_case_matches_oracle():
+    compare_run(kat_project("characteristic_transport_v1"), steps=40, sample_every=8)
+
+
+def test_known_answer_272_steps_on_gpu(golden):
+    kat = golden["kat272"]
+    solver = solver_for(kat_project("legacy"))
+    try:
+        solver.advance(kat["steps"] - 1)
+        loads = solver.step(sample=True)
+        for k, v in kat["last_sample"].items():
+            assert loads[k] == pytest.approx(v, rel=2e-12)
+    finally:
+        solver.close()
+
+
+def test_characteristic_history_on_gpu(golden):
+    record = golden["histories"]["characteristic_down3"]
+    solver = solver_for(Project.from_dict(record["project"]))
+    try:
+        for row in record["history"][:40]:
+            loads = solver.advance(row["step"] - solver.steps, sample_last=True)
+            for k in ("cl", "cd", "cm"):
+                assert loads[k] == pytest.approx(row[k], abs=2e-12)
+            diag = solver.diagnostics()
+            assert diag["local_mach_max"] == pytest.approx(row["local_mach_max"], rel=1e-12)
+            assert diag["density_error_max"] == pytest.approx(row["density_error_max"], rel=1e-12)
+    finally:
+        solver.close()
+
+
+def test_failure_capture_guard_and_loads(golden):
+    """docs/verification_failure_capture_20261107: colliding density pulses; the
+    engine reproduces loads and guards, then raises like the reference."""
+    from aerokinetic_gb300.solver import NumericalFailure
+    record = golden["histories"]["failure_capture_n16"]
+    solver = solver_for(Project.from_dict(record["project"]))
+    try:
+        nx, ny, nz = solver.plan.shape
+        y = np.arange(ny) + 0.5
+        a = .085 * np.exp(-.5 * ((y - 5.5) / 1.5) ** 2)
+        b = .085 * np.exp(-.5 * ((y - 12.5) / 1.5) ** 2)
+        u = np.zeros((nx, ny, nz, 3))
+        u[..., 0] = solver.flow.lattice_speed
+        u[..., 1] = (np.sqrt(1 / 3) * (a - b))[None, :, None]
+        u[solver._solid_xy] = 0.0
+        solver.set_fields(np.broadcast_to((1 + a + b)[None, :, None], solver.plan.shape), u)
+        for row in record["history"]:
+            loads = solver.step(sample=True)
+            diag = solver.diagnostics()
+            for k in ("cl", "cd", "cm"):
+                assert loads[k] == pytest.approx(row[k], rel=1e-12, abs=1e-13)
+            assert diag["local_mach_max"] == pytest.approx(row["local_mach_max"], rel=1e-12)
+        with pytest.raises(NumericalFailure):
+            for _ in range(20):
+                solver.step()
+                solver.diagnostics()
+    finally:
+        solver.close()
+
+
+def test_full_size_uniform_case_matches_oracle(golden):
+    """384x256x8 characteristic-farfield case at lattice Mach 0.1 (the bench workload)."""
+    compare_run(geometry_project(golden["geometry"]["uniform_c1"]), steps=12, sample_every=4)
+
+
+def test_non_finite_state_is_reported(golden):
+    """A host-made fault: NaN populations written through the ABI."""
+    from aerokinetic_gb300.solver import NumericalFailure
+    solver = solver_for(kat_project("legacy"))
+    try:
+        pdf = solver.pdf()
+        pdf[40, 40, 3, 5] = np.nan
+        solver.set_pdf(pdf)
+        with pytest.raises(NumericalFailure):
+            solver.diagnostics()
+    finally:
+        solver.close()
+
+
+@pytest.mark.parametrize("storage,tol", [("f32", 5e-4), ("f16", 5e-3)])
+def test_precision_forms_track_fp64(storage, tol):
+    """FP32 arithmetic with FP32 / FP16 shifted storage against the FP64 form:
+    Cl, Cd, Cm after 200 steps within the stated relative bound of max|C|."""
+    project = kat_project("characteristic_transport_v1")
+    ref, low = solver_for(project, "f64"), solver_for(project, storage)
+    try:
+        a = ref.advance(200, sample_last=True)
+        b = low.advance(200, sample_last=True)
+        scale = max(abs(a["cl"]), abs(a["cd"]), abs(a["cm"]))
+        for k in ("cl", "cd", "cm"):
+            assert abs(a[k] - b[k]) <= tol * scale, (k, a[k], b[k])
+        ra, ua = ref.macros()
+        rb, ub = low.macros()
+        fluid = ~ref._solid_xy
+        assert np.abs(ra - rb)[fluid].max() < 50 * tol * 1e-2
+    finally:
+        ref.close()
+        low.close()
