@@ -365,11 +365,10 @@ int prepare_boundaries(ak_case *c) {
     S *src = src_of<S>(c);
     const int T = 256;
     if (c->farfield == AK_FARFIELD_LEGACY) {
-        if (c->n_out) {
-            k_outflow_prepare<S><<<(unsigned)blocks_for(c->n_out, T), T, 0, c->stream>>>(
-                src, c->G, c->outer(), c->sel_out, c->n_out, c->out_state, 1, 0, 0, 1.0, c->speed, 0.0, 0.0);
-            AK_CUDA(cudaGetLastError());
-        }
+        // the outflow state is seeded inside the first step, after the UBB
+        // kernel (one_step): its corner links read ghost values the UBB writes
+        c->prepared = true;
+        return AK_OK;
     } else {
         if (c->nouter) {
             k_farfield<S><<<(unsigned)blocks_for(c->nouter, T), T, 0, c->stream>>>(
@@ -395,7 +394,8 @@ void mark(ak_case *c) {
 template <typename S>
 int one_step(ak_case *c, bool sample) {
     using T = typename Store<S>::T;
-    if (!c->prepared) AK_TRY(prepare_boundaries<S>(c));
+    const bool first = !c->prepared;
+    if (first) AK_TRY(prepare_boundaries<S>(c));
     S *src = src_of<S>(c);
     const int TB = 256;
     mark(c);
@@ -405,6 +405,16 @@ int one_step(ak_case *c, bool sample) {
         if (c->n_ubb) {
             k_ubb<S><<<(unsigned)blocks_for(c->n_ubb, TB), TB, 0, c->stream>>>(src, c->G, c->outer(), c->sel_ubb,
                                                                                c->n_ubb, c->speed, 0.0, 0.0);
+            AK_CUDA(cudaGetLastError());
+            ++c->launches;
+        }
+        if (c->n_out && first) {
+            // ExtrapolationOutflow's initial history: the neighbour value as it
+            // stands after the UBB of this step, matching the reference's
+            // recorded legacy histories (docs/verification_farfield_20261107/
+            // airfoil/legacy_down6) to 2e-13 over 960 steps
+            k_outflow_prepare<S><<<(unsigned)blocks_for(c->n_out, TB), TB, 0, c->stream>>>(
+                src, c->G, c->outer(), c->sel_out, c->n_out, c->out_state, 1, 0, 0, 1.0, c->speed, 0.0, 0.0);
             AK_CUDA(cudaGetLastError());
             ++c->launches;
         }
@@ -630,7 +640,6 @@ void *ak_case_stream(const ak_case *c) { return c ? (void *)c->stream : nullptr;
 int ak_step_timed(ak_case *c, int32_t nsteps, double *ms) {
     AK_TRY(check_case(c));
     if (nsteps < 1 || !ms) return fail(AK_ERR_INVALID, "nsteps >= 1 and an output array are required");
-    if (!c->prepared) AK_TRY(with_storage(c, [&](auto *tag) { return prepare_boundaries<std::remove_pointer_t<decltype(tag)>>(c); }));
     std::vector<cudaEvent_t> events;
     events.reserve((size_t)4 * nsteps);
     c->timing = &events;

@@ -112,7 +112,7 @@ def test_known_answer_272_steps(golden):
         assert loads[k] == pytest.approx(v, rel=2e-12)
 
 
-@pytest.mark.parametrize("name,samples", [("characteristic_down3", 40), ("legacy_corrected32", 40)])
+@pytest.mark.parametrize("name,samples", [("characteristic_down3", 40), ("legacy_corrected32", 60)])
 def test_history_first_samples(golden, name, samples):
     record = golden["histories"][name]
     project = Project.from_dict(record["project"])
