@@ -532,6 +532,15 @@ int ak_case_create(const ak_case_desc *desc, ak_case **out) {
     G.sx = (G.nxp + 31) / 32 * 32;
     G.plane = (long long)G.nyp * G.sx;
     G.qs = (long long)G.nz * G.plane;
+    for (int q = 0; q < Q; ++q) {
+        // zero-centred equilibrium of the freestream (1, (U, 0, 0)), the FP16 shift
+        const double u[3] = {c->speed, 0.0, 0.0};
+        const int e[3] = {cx(q), cy(q), cz(q)};
+        double p = 1.0;
+        for (int a = 0; a < 3; ++a)
+            p *= e[a] == 0 ? 2.0 / 3.0 - u[a] * u[a] : 0.5 * (1.0 / 3.0 + u[a] * u[a] + e[a] * u[a]);
+        G.shift[q] = c->storage == AK_STORAGE_F16 ? (float)(p - weight(q)) : 0.0f;
+    }
     int r = AK_OK;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         r = fail(AK_ERR_CUDA, "stream creation failed (no CUDA device?)");

@@ -33,17 +33,18 @@ struct Grid {
     int sx;           // row pitch (elements)
     long long plane;  // nyp * sx
     long long qs;     // nz * plane, stride between populations
+    float shift[27];  // FP16 storage: zero-centred freestream equilibrium per direction
     __host__ __device__ long long cell(int x, int y, int z) const { return (long long)z * plane + (long long)y * sx + x; }
     __device__ int wrapz(int z) const { return z < 0 ? z + nz : (z >= nz ? z - nz : z); }
 };
 
 template <typename S>
 __device__ __forceinline__ double load_g(const S *pdf, const Grid &G, int q, int x, int y, int z) {
-    return (double)Store<S>::load(pdf + q * G.qs + G.cell(x, y, z), q);
+    return (double)Store<S>::load(pdf + q * G.qs + G.cell(x, y, z), q, G.shift);
 }
 template <typename S>
 __device__ __forceinline__ void store_g(S *pdf, const Grid &G, int q, int x, int y, int z, double v) {
-    Store<S>::store(pdf + q * G.qs + G.cell(x, y, z), q, (typename Store<S>::T)v);
+    Store<S>::store(pdf + q * G.qs + G.cell(x, y, z), q, (typename Store<S>::T)v, G.shift);
 }
 
 // ------------------------------------------------------------ bulk step
@@ -62,12 +63,12 @@ __global__ void __launch_bounds__(128) k_stream_collide(const S *__restrict__ sr
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         const int zs = G.wrapz(z - cz(q));
-        g[q] = Store<S>::load(src + q * G.qs + G.cell(x - cx(q), y - cy(q), zs), q);
+        g[q] = Store<S>::load(src + q * G.qs + G.cell(x - cx(q), y - cy(q), zs), q, G.shift);
     }
     collide<T>(g, omega_s, omega_b);
     const long long c = G.cell(x, y, z);
 #pragma unroll
-    for (int q = 0; q < Q; ++q) Store<S>::store(dst + q * G.qs + c, q, g[q]);
+    for (int q = 0; q < Q; ++q) Store<S>::store(dst + q * G.qs + c, q, g[q], G.shift);
 }
 
 // ------------------------------------------------------------ walls

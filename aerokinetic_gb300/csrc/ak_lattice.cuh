@@ -62,29 +62,31 @@ __host__ __device__ constexpr double weight(int q) {
 }
 
 // ---------------------------------------------------------------- storage
-// Populations are stored as g = f - w.  F16 stores g / w (rescaled back in
-// FP32 arithmetic) so that the small deviations use the normal range of the
-// format.
+// Populations are stored shifted, as g = f - w (zero-centred, the reference's
+// own representation).  The FP16 form stores (g - a_q) / w_q, where a_q is
+// the zero-centred equilibrium of the freestream: a per-direction constant
+// shift that makes the stored numbers small deviations from the farfield
+// state (so the format's 11-bit significand is spent on the flow's
+// departures from it) and scaled by 1/w_q into the same range for every
+// direction.  With a zero freestream a_q = 0 and the shift is plain f - w.
 template <typename S> struct Store;
 template <> struct Store<double> {
     using T = double;
-    __device__ static __forceinline__ double load(const double *p, int) { return __ldg(p); }
-    __device__ static __forceinline__ void store(double *p, int, double v) { *p = v; }
-    __host__ __device__ static double to_g(double v, int) { return v; }
+    __device__ static __forceinline__ double load(const double *p, int, const float *) { return __ldg(p); }
+    __device__ static __forceinline__ void store(double *p, int, double v, const float *) { *p = v; }
 };
 template <> struct Store<float> {
     using T = float;
-    __device__ static __forceinline__ float load(const float *p, int) { return __ldg(p); }
-    __device__ static __forceinline__ void store(float *p, int, float v) { *p = v; }
-    __host__ __device__ static double to_g(float v, int) { return v; }
+    __device__ static __forceinline__ float load(const float *p, int, const float *) { return __ldg(p); }
+    __device__ static __forceinline__ void store(float *p, int, float v, const float *) { *p = v; }
 };
 template <> struct Store<__half> {
     using T = float;
-    __device__ static __forceinline__ float load(const __half *p, int q) {
-        return __half2float(__ldg(p)) * (float)weight(q);
+    __device__ static __forceinline__ float load(const __half *p, int q, const float *shift) {
+        return fmaf(__half2float(__ldg(p)), (float)weight(q), shift[q]);
     }
-    __device__ static __forceinline__ void store(__half *p, int q, float v) {
-        *p = __float2half_rn(v * (float)(1.0 / weight(q)));
+    __device__ static __forceinline__ void store(__half *p, int q, float v, const float *shift) {
+        *p = __float2half_rn((v - shift[q]) * (float)(1.0 / weight(q)));
     }
 };
 

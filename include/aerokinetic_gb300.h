@@ -56,7 +56,7 @@ extern "C" {
 
 #define AK_STORAGE_F64 0  /* plain form: FP64 storage and arithmetic */
 #define AK_STORAGE_F32 1  /* FP32 arithmetic, FP32 (f - w) storage */
-#define AK_STORAGE_F16 2  /* FP32 arithmetic, FP16 (f - w)/w storage */
+#define AK_STORAGE_F16 2  /* FP32 arithmetic, FP16 storage of (f - f_eq(1, U)) / w */
 
 typedef struct ak_case ak_case;
 
