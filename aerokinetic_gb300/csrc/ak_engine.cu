@@ -73,7 +73,11 @@ struct ak_case {
     double *ff_in = nullptr, *ff_der = nullptr;
     long long *ff_clock = nullptr;
     double *ff_lo = nullptr, *ff_hi = nullptr;
-    FarfieldParams ff{};
+    FarfieldObject ff_host[8];
+    int ff_count = 0;
+    FarfieldObject *d_ff = nullptr;
+    float *d_shift = nullptr;
+    FarfieldParams ff() const { return FarfieldParams{d_ff, ff_count}; }
     // reductions
     double *partials = nullptr, *reduced = nullptr;
     long long partial_doubles = 0;
@@ -116,7 +120,8 @@ int upload(ak_case *c, T **p, const std::vector<T> &v) {
 void release(ak_case *c) {
     void *ptrs[] = {c->pdf[0], c->pdf[1], c->flags, c->d_poly, c->d_start, c->d_count, c->keys, c->wall_q,
                     c->ox_, c->oy_, c->oz_, c->od, c->oobj, c->oedge, c->sel_ubb, c->sel_out, c->out_state,
-                    c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, c->partials, c->reduced, c->staging};
+                    c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, c->partials, c->reduced, c->staging,
+                    c->d_ff, c->d_shift};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -159,13 +164,12 @@ int with_storage(ak_case *c, F &&f) {
 
 // ---- characteristic farfield objects, farfield.py:34-47 and 209-224
 void build_farfield_objects(ak_case *c) {
-    FarfieldParams &P = c->ff;
-    P.nobj = 0;
+    c->ff_count = 0;
     const double vel[3] = {c->speed, 0.0, 0.0};
     for (int nx_ = -1; nx_ <= 1; ++nx_)
         for (int ny_ = -1; ny_ <= 1; ++ny_) {
             if (nx_ == 0 && ny_ == 0) continue;
-            FarfieldObject &o = P.obj[P.nobj++];
+            FarfieldObject &o = c->ff_host[c->ff_count++];
             o.normal[0] = nx_;
             o.normal[1] = ny_;
             o.normal[2] = 0;
@@ -198,8 +202,8 @@ int farfield_object_of(const ak_case *c, int gx, int gy) {
     // the order built above
     const int nx_ = gx < 0 ? -1 : (gx >= c->nx ? 1 : 0);
     const int ny_ = gy < 0 ? -1 : (gy >= c->ny ? 1 : 0);
-    for (int k = 0; k < c->ff.nobj; ++k)
-        if (c->ff.obj[k].normal[0] == nx_ && c->ff.obj[k].normal[1] == ny_) return k;
+    for (int k = 0; k < c->ff_count; ++k)
+        if (c->ff_host[k].normal[0] == nx_ && c->ff_host[k].normal[1] == ny_) return k;
     return -1;
 }
 
@@ -231,7 +235,7 @@ int build_outer(ak_case *c, const std::vector<uint8_t> &hflags) {
                 } else {
                     const int k = farfield_object_of(c, gx, gy);
                     OBJ.push_back((signed char)k);
-                    const FarfieldObject &o = c->ff.obj[k];
+                    const FarfieldObject &o = c->ff_host[k];
                     const int fx = x + cx(d) - o.normal[0], fy = y + cy(d) - o.normal[1];
                     if (fx < 0 || fx >= nx || fy < 0 || fy >= ny) return;  // checked below
                     EDGE.push_back((signed char)(fx == 0 ? -1 : (fx == nx - 1 ? 1 : 0)));
@@ -264,6 +268,7 @@ int build_outer(ak_case *c, const std::vector<uint8_t> &hflags) {
         AK_TRY(upload(c, &c->sel_out, sel_out));
         AK_TRY(dalloc(c, &c->out_state, (size_t)(2 * c->n_out)));
     } else {
+        AK_TRY(upload(c, &c->d_ff, std::vector<FarfieldObject>(c->ff_host, c->ff_host + c->ff_count)));
         AK_TRY(dalloc(c, &c->ff_in, (size_t)c->nouter));
         AK_TRY(dalloc(c, &c->ff_der, (size_t)c->nouter));
         AK_TRY(dalloc(c, &c->ff_clock, (size_t)c->nouter));
@@ -372,10 +377,10 @@ int prepare_boundaries(ak_case *c) {
     } else {
         if (c->nouter) {
             k_farfield<S><<<(unsigned)blocks_for(c->nouter, T), T, 0, c->stream>>>(
-                src, c->G, c->outer(), c->ff, c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, 1);
+                src, c->G, c->outer(), c->ff(), c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, 1);
             AK_CUDA(cudaGetLastError());
         }
-        k_glancing_rows<S><<<(unsigned)blocks_for((long long)c->nx * c->nz, T), T, 0, c->stream>>>(src, c->G, c->ff,
+        k_glancing_rows<S><<<(unsigned)blocks_for((long long)c->nx * c->nz, T), T, 0, c->stream>>>(src, c->G, c->ff(),
                                                                                                   c->ff_lo, c->ff_hi);
         AK_CUDA(cudaGetLastError());
     }
@@ -426,7 +431,7 @@ int one_step(ak_case *c, bool sample) {
         }
     } else if (c->nouter) {
         k_farfield<S><<<(unsigned)blocks_for(c->nouter, TB), TB, 0, c->stream>>>(
-            src, c->G, c->outer(), c->ff, c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, 0);
+            src, c->G, c->outer(), c->ff(), c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, 0);
         AK_CUDA(cudaGetLastError());
         ++c->launches;
     }
@@ -472,7 +477,23 @@ extern "C" {
 
 const char *ak_last_error(void) { return g_error.c_str(); }
 
-const char *ak_version(void) { return "aerokinetic_gb300 1.0 sm_103a"; }
+const char *ak_version(void) {
+#ifdef AK_CHECKED
+    return "aerokinetic_gb300 1.0 sm_103a checked";
+#else
+    return "aerokinetic_gb300 1.0 sm_103a";
+#endif
+}
+
+#ifdef AK_CHECKED
+unsigned long long ak_debug_status(void) {
+    unsigned long long v = 0, zero = 0;
+    cudaDeviceSynchronize();
+    cudaMemcpyFromSymbol(&v, ak_debug_word, sizeof v);
+    cudaMemcpyToSymbol(ak_debug_word, &zero, sizeof zero);
+    return v;
+}
+#endif
 
 int ak_case_create(const ak_case_desc *desc, ak_case **out) {
     g_error.clear();
@@ -532,6 +553,7 @@ int ak_case_create(const ak_case_desc *desc, ak_case **out) {
     G.sx = (G.nxp + 31) / 32 * 32;
     G.plane = (long long)G.nyp * G.sx;
     G.qs = (long long)G.nz * G.plane;
+    std::vector<float> shift(Q);
     for (int q = 0; q < Q; ++q) {
         // zero-centred equilibrium of the freestream (1, (U, 0, 0)), the FP16 shift
         const double u[3] = {c->speed, 0.0, 0.0};
@@ -539,12 +561,14 @@ int ak_case_create(const ak_case_desc *desc, ak_case **out) {
         double p = 1.0;
         for (int a = 0; a < 3; ++a)
             p *= e[a] == 0 ? 2.0 / 3.0 - u[a] * u[a] : 0.5 * (1.0 / 3.0 + u[a] * u[a] + e[a] * u[a]);
-        G.shift[q] = c->storage == AK_STORAGE_F16 ? (float)(p - weight(q)) : 0.0f;
+        shift[q] = c->storage == AK_STORAGE_F16 ? (float)(p - weight(q)) : 0.0f;
     }
     int r = AK_OK;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         r = fail(AK_ERR_CUDA, "stream creation failed (no CUDA device?)");
     }
+    if (r == AK_OK) r = upload(c, &c->d_shift, shift);
+    G.shift = c->d_shift;
     std::vector<uint8_t> hflags;
     if (r == AK_OK && c->farfield == AK_FARFIELD_CHARACTERISTIC) build_farfield_objects(c);
     if (r == AK_OK) r = build_geometry(c, hflags);

@@ -33,17 +33,37 @@ struct Grid {
     int sx;           // row pitch (elements)
     long long plane;  // nyp * sx
     long long qs;     // nz * plane, stride between populations
-    float shift[27];  // FP16 storage: zero-centred freestream equilibrium per direction
+    const float *shift;  // FP16 storage: zero-centred freestream equilibrium per direction (device)
     __host__ __device__ long long cell(int x, int y, int z) const { return (long long)z * plane + (long long)y * sx + x; }
     __device__ int wrapz(int z) const { return z < 0 ? z + nz : (z >= nz ? z - nz : z); }
 };
 
+#ifdef AK_CHECKED
+// Debug builds check every population index against the padded lattice and
+// record the first offending access (kernel tag, q, x, y, z) instead of
+// performing it.
+__device__ unsigned long long ak_debug_word;
+__device__ __forceinline__ bool ak_in_range(const Grid &G, int q, int x, int y, int z, int tag) {
+    if (q >= 0 && q < Q && x >= 0 && x < G.nxp && y >= 0 && y < G.nyp && z >= 0 && z < G.nz) return true;
+    const unsigned long long code = 1ULL << 63 | (unsigned long long)(tag & 0xff) << 48 |
+                                    (unsigned long long)(q & 0xff) << 40 | (unsigned long long)(x & 0xfff) << 28 |
+                                    (unsigned long long)(y & 0xfff) << 16 | (unsigned long long)(z & 0xffff);
+    atomicCAS(&ak_debug_word, 0ULL, code);
+    return false;
+}
+#define AK_CHECK(G, q, x, y, z, tag) ak_in_range(G, q, x, y, z, tag)
+#else
+#define AK_CHECK(G, q, x, y, z, tag) true
+#endif
+
 template <typename S>
 __device__ __forceinline__ double load_g(const S *pdf, const Grid &G, int q, int x, int y, int z) {
+    if (!AK_CHECK(G, q, x, y, z, 1)) return 0.0;
     return (double)Store<S>::load(pdf + q * G.qs + G.cell(x, y, z), q, G.shift);
 }
 template <typename S>
 __device__ __forceinline__ void store_g(S *pdf, const Grid &G, int q, int x, int y, int z, double v) {
+    if (!AK_CHECK(G, q, x, y, z, 2)) return;
     Store<S>::store(pdf + q * G.qs + G.cell(x, y, z), q, (typename Store<S>::T)v, G.shift);
 }
 
@@ -63,7 +83,9 @@ __global__ void __launch_bounds__(128) k_stream_collide(const S *__restrict__ sr
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         const int zs = G.wrapz(z - cz(q));
-        g[q] = Store<S>::load(src + q * G.qs + G.cell(x - cx(q), y - cy(q), zs), q, G.shift);
+        g[q] = AK_CHECK(G, q, x - cx(q), y - cy(q), zs, 3)
+                   ? Store<S>::load(src + q * G.qs + G.cell(x - cx(q), y - cy(q), zs), q, G.shift)
+                   : T(0);
     }
     collide<T>(g, omega_s, omega_b);
     const long long c = G.cell(x, y, z);
@@ -244,8 +266,9 @@ struct FarfieldObject {
     double density;
     double vel[3];
 };
+// the eight objects live in device memory (indexed per link at run time)
 struct FarfieldParams {
-    FarfieldObject obj[8];
+    const FarfieldObject *obj;
     int nobj;
 };
 
@@ -312,6 +335,12 @@ __global__ void k_farfield(S *__restrict__ pdf, Grid G, OuterLinks L, FarfieldPa
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= L.n) return;
     const int x = L.x[i], y = L.y[i], z = L.z[i], d = L.d[i], di = inv(d);
+#ifdef AK_CHECKED
+    if (L.obj[i] < 0 || L.obj[i] >= P.nobj) {
+        AK_CHECK(G, -1, x, y, z, 4);
+        return;
+    }
+#endif
     const FarfieldObject &o = P.obj[L.obj[i]];
     // foot = x + c_d - n: a fluid cell next to the ghost cell, wrapped in z
     const int foot[3] = {x + cx(d) - o.normal[0], y + cy(d) - o.normal[1], G.wrapz(z + cz(d) - o.normal[2])};

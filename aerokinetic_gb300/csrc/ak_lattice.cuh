@@ -83,10 +83,10 @@ template <> struct Store<float> {
 template <> struct Store<__half> {
     using T = float;
     __device__ static __forceinline__ float load(const __half *p, int q, const float *shift) {
-        return fmaf(__half2float(__ldg(p)), (float)weight(q), shift[q]);
+        return fmaf(__half2float(__ldg(p)), (float)weight(q), __ldg(shift + q));
     }
     __device__ static __forceinline__ void store(__half *p, int q, float v, const float *shift) {
-        *p = __float2half_rn((v - shift[q]) * (float)(1.0 / weight(q)));
+        *p = __float2half_rn((v - __ldg(shift + q)) * (float)(1.0 / weight(q)));
     }
 };
 
