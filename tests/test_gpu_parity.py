@@ -182,22 +182,29 @@ def test_non_finite_state_is_reported(golden):
         solver.close()
 
 
-@pytest.mark.parametrize("storage,tol", [("f32", 5e-4), ("f16", 5e-3)])
-def test_precision_forms_track_fp64(storage, tol):
-    """FP32 arithmetic with FP32 / FP16 shifted storage against the FP64 form:
-    Cl, Cd, Cm after 200 steps within the stated relative bound of max|C|."""
+@pytest.mark.parametrize("storage,inst_tol,mean_tol", [("f32", 5e-4, 5e-4), ("f16", 1e-2, 5e-3)])
+def test_precision_forms_track_fp64(storage, inst_tol, mean_tol):
+    """FP32 arithmetic with FP32 / FP16 shifted storage against the FP64 form on
+    the impulsive start (steps 20..200, every 20): the largest instantaneous
+    Cl/Cd/Cm difference relative to max|C| stays below inst_tol, the
+    difference of the sample means below mean_tol."""
     project = kat_project("characteristic_transport_v1")
     ref, low = solver_for(project, "f64"), solver_for(project, storage)
     try:
-        a = ref.advance(200, sample_last=True)
-        b = low.advance(200, sample_last=True)
-        scale = max(abs(a["cl"]), abs(a["cd"]), abs(a["cm"]))
-        for k in ("cl", "cd", "cm"):
-            assert abs(a[k] - b[k]) <= tol * scale, (k, a[k], b[k])
-        ra, ua = ref.macros()
-        rb, ub = low.macros()
+        a, b = [], []
+        for _ in range(10):
+            ra = ref.advance(20, sample_last=True)
+            rb = low.advance(20, sample_last=True)
+            a.append([ra["cl"], ra["cd"], ra["cm"]])
+            b.append([rb["cl"], rb["cd"], rb["cm"]])
+        a, b = np.array(a), np.array(b)
+        scale = np.abs(a).max()
+        assert np.abs(a - b).max() <= inst_tol * scale, np.abs(a - b).max() / scale
+        assert np.abs(a.mean(axis=0) - b.mean(axis=0)).max() <= mean_tol * scale
+        rho_a, _ = ref.macros()
+        rho_b, _ = low.macros()
         fluid = ~ref._solid_xy
-        assert np.abs(ra - rb)[fluid].max() < 50 * tol * 1e-2
+        assert np.abs(rho_a - rho_b)[fluid].max() < 10 * inst_tol * np.abs(rho_a - 1)[fluid].max()
     finally:
         ref.close()
         low.close()
