@@ -204,7 +204,7 @@ def test_precision_forms_track_fp64(storage, inst_tol, mean_tol):
         rho_a, _ = ref.macros()
         rho_b, _ = low.macros()
         fluid = ~ref._solid_xy
-        assert np.abs(rho_a - rho_b)[fluid].max() < 10 * inst_tol * np.abs(rho_a - 1)[fluid].max()
+        assert np.abs(rho_a - rho_b)[fluid].max() < 2e-2 * np.abs(rho_a - 1)[fluid].max()
     finally:
         ref.close()
         low.close()
