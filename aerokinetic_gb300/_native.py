@@ -80,6 +80,7 @@ SIGNATURES = {
     "ak_init_perturbed": ([_P, _D, _D, _D, _D, _D, _D], ctypes.c_int),
     "ak_init_fields": ([_P, _P, _P], ctypes.c_int),
     "ak_step": ([_P, ctypes.c_int32, _P], ctypes.c_int),
+    "ak_step_loads_static": ([_P, ctypes.c_int32, _P], ctypes.c_int),
     "ak_steps_done": ([_P], ctypes.c_int64),
     "ak_kernel_launches": ([_P], ctypes.c_int64),
     "ak_case_stream": ([_P], _P),

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -88,6 +89,7 @@ struct ak_case {
     long long steps = 0;
     long long launches = 0;  // kernels issued by stepping since creation
     bool prepared = false;
+    int device = 0;  // CUDA device current when the case was created
     // optional per-kernel timing: events recorded around each kernel group
     std::vector<cudaEvent_t> *timing = nullptr;
     cudaStream_t stream = nullptr;
@@ -397,7 +399,7 @@ void mark(ak_case *c) {
 }
 
 template <typename S>
-int one_step(ak_case *c, bool sample) {
+int one_step(ak_case *c, bool sample, double *fixed_partials = nullptr, long long fixed_capacity = 0) {
     using T = typename Store<S>::T;
     const bool first = !c->prepared;
     if (first) AK_TRY(prepare_boundaries<S>(c));
@@ -440,13 +442,23 @@ int one_step(ak_case *c, bool sample) {
     const long long nlinks = c->nkeys * c->nz * 3;
     if (nlinks) {
         const long long nb = blocks_for(nlinks, 256);
-        if (sample) AK_TRY(ensure_partials(c, nb * 5 * c->n_elements));
+        double *partials = c->partials;
+        if (sample && fixed_partials) {
+            if (nb * 5 * c->n_elements > fixed_capacity)
+                return fail(AK_ERR_INVALID, "wall links need " + std::to_string(nb * 5 * c->n_elements) +
+                                                " partial sums; the static scratch holds " +
+                                                std::to_string(fixed_capacity));
+            partials = fixed_partials;
+        } else if (sample) {
+            AK_TRY(ensure_partials(c, nb * 5 * c->n_elements));
+            partials = c->partials;
+        }
         k_walls<S><<<(unsigned)nb, 256, 0, c->stream>>>(src, c->G, c->keys, c->wall_q, c->nkeys, sample ? 1 : 0,
-                                                        c->n_elements, c->ox, c->oy, c->partials);
+                                                        c->n_elements, c->ox, c->oy, partials);
         AK_CUDA(cudaGetLastError());
         ++c->launches;
         if (sample) {
-            k_sum_partials<<<1, 64, 0, c->stream>>>(c->partials, (int)nb, 5 * c->n_elements, c->reduced);
+            k_sum_partials<<<1, 64, 0, c->stream>>>(partials, (int)nb, 5 * c->n_elements, c->reduced);
             AK_CUDA(cudaGetLastError());
             ++c->launches;
         }
@@ -564,7 +576,8 @@ int ak_case_create(const ak_case_desc *desc, ak_case **out) {
         shift[q] = c->storage == AK_STORAGE_F16 ? (float)(p - weight(q)) : 0.0f;
     }
     int r = AK_OK;
-    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaGetDevice(&c->device) != cudaSuccess) r = fail(AK_ERR_CUDA, "no current CUDA device");
+    if (r == AK_OK && cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         r = fail(AK_ERR_CUDA, "stream creation failed (no CUDA device?)");
     }
     if (r == AK_OK) r = upload(c, &c->d_shift, shift);
@@ -661,6 +674,68 @@ int ak_step(ak_case *c, int32_t nsteps, double *loads) {
                                 c->stream));
         AK_CUDA(cudaStreamSynchronize(c->stream));
     }
+    return AK_OK;
+}
+
+}  // extern "C"
+
+// ---- allocation-free loads
+// Callers that run where device allocation is not allowed or not wanted (a
+// host thread inside CUDA stream capture, a real-time control loop on a
+// pre-sized device budget, a plugin host that forbids driver allocations
+// after start-up) cannot use ak_step's loads path, which allocates its
+// per-block partial sums on the first sampled step.  ak_step_loads_static
+// keeps those partial sums in this file-scope array instead: 131072 doubles
+// (1 MiB) that every GPU loading the library holds until the process exits.
+namespace {
+constexpr long long STATIC_LOADS_DOUBLES = 131072;
+constexpr int STATIC_MAX_DEVICES = 64;
+std::mutex g_static_mutex;
+double *g_static_address[STATIC_MAX_DEVICES] = {nullptr};
+}  // namespace
+static __device__ __align__(256) double g_static_loads[STATIC_LOADS_DOUBLES];
+
+namespace {
+// Device address of the scratch array for the current device, looked up once
+// per device (the host-side symbol is only a stand-in, never a device address).
+int static_loads_scratch(double **out) {
+    int dev = 0;
+    AK_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= STATIC_MAX_DEVICES) return fail(AK_ERR_INVALID, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_static_mutex);
+    if (!g_static_address[dev]) {
+        void *ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_static_loads);
+        if (e != cudaSuccess)
+            return fail(AK_ERR_CUDA, std::string("cudaGetSymbolAddress of the static scratch failed: ") +
+                                         cudaGetErrorString(e));
+        g_static_address[dev] = (double *)ptr;
+    }
+    *out = g_static_address[dev];
+    return AK_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int ak_step_loads_static(ak_case *c, int32_t nsteps, double *loads) {
+    AK_TRY(check_case(c));
+    if (nsteps < 1 || !loads) return fail(AK_ERR_INVALID, "nsteps >= 1 and a loads array are required");
+    int dev = 0;
+    AK_CUDA(cudaGetDevice(&dev));
+    if (dev != c->device)
+        return fail(AK_ERR_INVALID, "make the case's device current before ak_step_loads_static");
+    double *scratch = nullptr;
+    AK_TRY(static_loads_scratch(&scratch));
+    for (int s = 0; s < nsteps; ++s) {
+        const bool sample = s == nsteps - 1;
+        AK_TRY(with_storage(c, [&](auto *tag) {
+            return one_step<std::remove_pointer_t<decltype(tag)>>(c, sample, scratch, STATIC_LOADS_DOUBLES);
+        }));
+    }
+    AK_CUDA(cudaMemcpyAsync(loads, c->reduced, sizeof(double) * 5 * c->n_elements, cudaMemcpyDeviceToHost,
+                            c->stream));
+    AK_CUDA(cudaStreamSynchronize(c->stream));
     return AK_OK;
 }
 

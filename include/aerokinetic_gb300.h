@@ -105,6 +105,16 @@ int ak_init_fields(ak_case *c, const double *rho, const double *u);
  * loads[n_elements * 5] = (Fx, Fy, Fz, Mz, incoming-minus-outgoing mass) per
  * element, in lattice units, Mz about the normalised frame's origin. */
 int ak_step(ak_case *c, int32_t nsteps, double *loads);
+/* ak_step with loads that allocates no device memory, for callers that
+ * cannot allocate (inside stream capture, on a fixed device-memory budget):
+ * the per-block partial sums of the loads live in a static device array of
+ * 131072 doubles (1 MiB, held by every GPU that loads the library).  No
+ * counterpart in the reference.  The first call on a device looks up the
+ * array's device address, so make that first call before any stream capture,
+ * with the case's device current.  Cases whose wall links need more partial
+ * sums than the array holds get AK_ERR_INVALID.  All calls share the array:
+ * calls that overlap on the GPU (other cases on other streams) race. */
+int ak_step_loads_static(ak_case *c, int32_t nsteps, double *loads);
 int64_t ak_steps_done(const ak_case *c);
 /* Kernels the case has issued while stepping (for launch accounting). */
 int64_t ak_kernel_launches(const ak_case *c);
