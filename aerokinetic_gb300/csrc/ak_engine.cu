@@ -74,6 +74,10 @@ struct ak_case {
     double *ff_in = nullptr, *ff_der = nullptr;
     long long *ff_clock = nullptr;
     double *ff_lo = nullptr, *ff_hi = nullptr;
+    Macro4 *ring_ru = nullptr;
+    double *ring_lr = nullptr;
+    long long ring_n = 0;
+    Ring ring() const { return Ring{ring_ru, ring_lr, ring_n}; }
     FarfieldObject ff_host[8];
     int ff_count = 0;
     FarfieldObject *d_ff = nullptr;
@@ -123,7 +127,7 @@ void release(ak_case *c) {
     void *ptrs[] = {c->pdf[0], c->pdf[1], c->flags, c->d_poly, c->d_start, c->d_count, c->keys, c->wall_q,
                     c->ox_, c->oy_, c->oz_, c->od, c->oobj, c->oedge, c->sel_ubb, c->sel_out, c->out_state,
                     c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, c->partials, c->reduced, c->staging,
-                    c->d_ff, c->d_shift};
+                    c->d_ff, c->d_shift, c->ring_ru, c->ring_lr};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -276,6 +280,9 @@ int build_outer(ak_case *c, const std::vector<uint8_t> &hflags) {
         AK_TRY(dalloc(c, &c->ff_clock, (size_t)c->nouter));
         AK_TRY(dalloc(c, &c->ff_lo, (size_t)nx * nz));
         AK_TRY(dalloc(c, &c->ff_hi, (size_t)nx * nz));
+        c->ring_n = 2LL * nx + 2LL * (ny - 2);
+        AK_TRY(dalloc(c, &c->ring_ru, (size_t)(c->ring_n * nz)));
+        AK_TRY(dalloc(c, &c->ring_lr, (size_t)(c->ring_n * nz)));
     }
     return AK_OK;
 }
@@ -377,13 +384,15 @@ int prepare_boundaries(ak_case *c) {
         c->prepared = true;
         return AK_OK;
     } else {
+        k_ring_macros<S><<<(unsigned)blocks_for(c->ring_n * c->nz, T), T, 0, c->stream>>>(src, c->G, c->ring());
+        AK_CUDA(cudaGetLastError());
         if (c->nouter) {
             k_farfield<S><<<(unsigned)blocks_for(c->nouter, T), T, 0, c->stream>>>(
-                src, c->G, c->outer(), c->ff(), c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, 1);
+                src, c->G, c->outer(), c->ff(), c->ring(), c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, 1);
             AK_CUDA(cudaGetLastError());
         }
-        k_glancing_rows<S><<<(unsigned)blocks_for((long long)c->nx * c->nz, T), T, 0, c->stream>>>(src, c->G, c->ff(),
-                                                                                                  c->ff_lo, c->ff_hi);
+        k_glancing_rows<<<(unsigned)blocks_for((long long)c->nx * c->nz, T), T, 0, c->stream>>>(c->G, c->ff(), c->ring(),
+                                                                                               c->ff_lo, c->ff_hi);
         AK_CUDA(cudaGetLastError());
     }
     c->prepared = true;
@@ -432,10 +441,12 @@ int one_step(ak_case *c, bool sample, double *fixed_partials = nullptr, long lon
             ++c->launches;
         }
     } else if (c->nouter) {
-        k_farfield<S><<<(unsigned)blocks_for(c->nouter, TB), TB, 0, c->stream>>>(
-            src, c->G, c->outer(), c->ff(), c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, 0);
+        k_ring_macros<S><<<(unsigned)blocks_for(c->ring_n * c->nz, TB), TB, 0, c->stream>>>(src, c->G, c->ring());
         AK_CUDA(cudaGetLastError());
-        ++c->launches;
+        k_farfield<S><<<(unsigned)blocks_for(c->nouter, TB), TB, 0, c->stream>>>(
+            src, c->G, c->outer(), c->ff(), c->ring(), c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, 0);
+        AK_CUDA(cudaGetLastError());
+        c->launches += 2;
     }
     mark(c);
     // walls and loads

@@ -87,7 +87,10 @@ __global__ void __launch_bounds__(128) k_stream_collide(const S *__restrict__ sr
                    ? Store<S>::load(src + q * G.qs + G.cell(x - cx(q), y - cy(q), zs), q, G.shift)
                    : T(0);
     }
-    collide<T>(g, omega_s, omega_b);
+    if constexpr (sizeof(T) == 8)
+        collide_full<T>(g, T(1) - omega_s, omega_b);
+    else
+        collide<T>(g, omega_s, omega_b);
     const long long c = G.cell(x, y, z);
 #pragma unroll
     for (int q = 0; q < Q; ++q) Store<S>::store(dst + q * G.qs + c, q, g[q], G.shift);
@@ -287,9 +290,61 @@ __device__ __forceinline__ void macro_at(const S *pdf, const Grid &G, int x, int
     for (int a = 0; a < 3; ++a) u[a] = j[a] / rho;
 }
 
-// transverse term F of the evolving outflow invariant (farfield.py:162-180)
+// The farfield reads density, velocity and ln(rho) of the fluid cells next to
+// the ghost ring only (the feet of its links and their neighbours along the
+// boundary).  They are computed once per step for that one-cell-wide band
+// ("ring": interior cells with x in {0, nx-1} or y in {0, ny-1}) and looked up
+// by the links, instead of being recomputed by every link that touches them.
+struct alignas(32) Macro4 {
+    double rho, ux, uy, uz;
+};
+struct Ring {
+    Macro4 *ru;   // (rho, ux, uy, uz) per ring cell and z
+    double *lr;   // ln(rho)
+    long long n;  // ring cells per z-plane: 2 nx + 2 (ny - 2)
+};
+__device__ __forceinline__ long long ring_index(const Grid &G, int x, int y) {  // interior coordinates
+    if (y == 0) return x;
+    if (y == G.ny - 1) return G.nx + x;
+    if (x == 0) return 2LL * G.nx + (y - 1);
+    return 2LL * G.nx + (G.ny - 2) + (y - 1);  // x == nx - 1
+}
+__device__ __forceinline__ void ring_cell(const Grid &G, long long r, int &x, int &y) {
+    if (r < G.nx) { x = (int)r; y = 0; return; }
+    if (r < 2LL * G.nx) { x = (int)(r - G.nx); y = G.ny - 1; return; }
+    const long long k = r - 2LL * G.nx;
+    if (k < G.ny - 2) { x = 0; y = (int)k + 1; return; }
+    x = G.nx - 1;
+    y = (int)(k - (G.ny - 2)) + 1;
+}
+
 template <typename S>
-__device__ double farfield_transverse(const S *pdf, const Grid &G, const FarfieldObject &o, const int foot[3],
+__global__ void k_ring_macros(const S *__restrict__ pdf, Grid G, Ring R) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= R.n * G.nz) return;
+    const long long r = i / G.nz;
+    const int z = (int)(i - r * G.nz);
+    int x, y;
+    ring_cell(G, r, x, y);
+    double rho, u[3];
+    macro_at(pdf, G, x + 1, y + 1, z, rho, u);
+    R.ru[i] = Macro4{rho, u[0], u[1], u[2]};
+    R.lr[i] = log(rho);
+}
+
+__device__ __forceinline__ void ring_get(const Grid &G, const Ring &R, int px, int py, int z, double &rho,
+                                         double u[3], double &lr) {  // padded x, y
+    const long long i = ring_index(G, px - 1, py - 1) * G.nz + z;
+    const Macro4 v = R.ru[i];
+    rho = v.rho;
+    u[0] = v.ux;
+    u[1] = v.uy;
+    u[2] = v.uz;
+    lr = R.lr[i];
+}
+
+// transverse term F of the evolving outflow invariant (farfield.py:162-180)
+__device__ double farfield_transverse(const Grid &G, const Ring &R, const FarfieldObject &o, const int foot[3],
                                       const signed char edge[3], const double u[3], double rm) {
     double F = 0.0;
     for (int a = 0; a < 3; ++a) {
@@ -305,13 +360,14 @@ __device__ double farfield_transverse(const S *pdf, const Grid &G, const Farfiel
         s2[a] += off2;
         s1[2] = G.wrapz(s1[2]);
         s2[2] = G.wrapz(s2[2]);
-        double r1, v1[3], r2, v2[3];
-        macro_at(pdf, G, s1[0], s1[1], s1[2], r1, v1);
-        macro_at(pdf, G, s2[0], s2[1], s2[2], r2, v2);
+        double r1, v1[3], l1, r2, v2[3], l2;
+        ring_get(G, R, s1[0], s1[1], s1[2], r1, v1, l1);
+        ring_get(G, R, s2[0], s2[1], s2[2], r2, v2, l2);
         double du[3];
         for (int b = 0; b < 3; ++b) du[b] = c0 * u[b] + c1 * v1[b] + c2 * v2[b];
-        const double rm1 = o.nh[0] * v1[0] + o.nh[1] * v1[1] + o.nh[2] * v1[2] - CS * log(r1 / o.density);
-        const double rm2 = o.nh[0] * v2[0] + o.nh[1] * v2[1] + o.nh[2] * v2[2] - CS * log(r2 / o.density);
+        // ln(rho / density) with density 1 for every object
+        const double rm1 = o.nh[0] * v1[0] + o.nh[1] * v1[1] + o.nh[2] * v1[2] - CS * l1;
+        const double rm2 = o.nh[0] * v2[0] + o.nh[1] * v2[1] + o.nh[2] * v2[2] - CS * l2;
         F += o.un_inf * (o.P[a][0] * du[0] + o.P[a][1] * du[1] + o.P[a][2] * du[2]) -
              o.ut_inf[a] * (c0 * rm + c1 * rm1 + c2 * rm2);
     }
@@ -329,9 +385,10 @@ __device__ __forceinline__ double feq_dir(double r, const double v[3], int q) {
 }
 
 template <typename S>
-__global__ void k_farfield(S *__restrict__ pdf, Grid G, OuterLinks L, FarfieldParams P, double *__restrict__ incoming,
-                           double *__restrict__ derivative, long long *__restrict__ clock,
-                           const double *__restrict__ init_lo, const double *__restrict__ init_hi, int prepare) {
+__global__ void __launch_bounds__(256) k_farfield(S *__restrict__ pdf, Grid G, OuterLinks L, FarfieldParams P, Ring R,
+                                                  double *__restrict__ incoming, double *__restrict__ derivative,
+                                                  long long *__restrict__ clock, const double *__restrict__ init_lo,
+                                                  const double *__restrict__ init_hi, int prepare) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= L.n) return;
     const int x = L.x[i], y = L.y[i], z = L.z[i], d = L.d[i], di = inv(d);
@@ -345,16 +402,15 @@ __global__ void k_farfield(S *__restrict__ pdf, Grid G, OuterLinks L, FarfieldPa
     // foot = x + c_d - n: a fluid cell next to the ghost cell, wrapped in z
     const int foot[3] = {x + cx(d) - o.normal[0], y + cy(d) - o.normal[1], G.wrapz(z + cz(d) - o.normal[2])};
     const signed char edge[3] = {L.edge[2 * i], L.edge[2 * i + 1], 0};
-    double rho, u[3];
-    macro_at(pdf, G, foot[0], foot[1], foot[2], rho, u);
+    double rho, u[3], lr;
+    ring_get(G, R, foot[0], foot[1], foot[2], rho, u, lr);
     const double un = o.nh[0] * u[0] + o.nh[1] * u[1] + o.nh[2] * u[2];
-    const double lr = log(rho / o.density);
     const double rm = un - CS * lr, rp = un + CS * lr;
     if (prepare) {
         // farfield.py:84-113: seed the trapezoid so the first update returns
         // the actual initial invariant
         if (o.mode == 1) {
-            const double F = farfield_transverse(pdf, G, o, foot, edge, u, rm);
+            const double F = farfield_transverse(G, R, o, foot, edge, u, rm);
             incoming[i] = rm - F;
             derivative[i] = F;
         } else if (o.mode == 2) {
@@ -367,7 +423,7 @@ __global__ void k_farfield(S *__restrict__ pdf, Grid G, OuterLinks L, FarfieldPa
     }
     double value, F = 0.0;
     if (o.mode == 1) {
-        F = farfield_transverse(pdf, G, o, foot, edge, u, rm);
+        F = farfield_transverse(G, R, o, foot, edge, u, rm);
         value = incoming[i] + (F + derivative[i]) / 2.0;
     } else if (o.mode == 2) {
         // one linear interpolation of the saved initial invariant at the shift
@@ -407,9 +463,7 @@ __global__ void k_farfield(S *__restrict__ pdf, Grid G, OuterLinks L, FarfieldPa
 
 // glancing faces: initial invariant u.n - cs ln(rho/rho_inf) - un_inf on the
 // fluid row next to the face (the only row the transport reads)
-template <typename S>
-__global__ void k_glancing_rows(const S *__restrict__ pdf, Grid G, FarfieldParams P, double *__restrict__ lo,
-                                double *__restrict__ hi) {
+__global__ void k_glancing_rows(Grid G, FarfieldParams P, Ring R, double *__restrict__ lo, double *__restrict__ hi) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (long long)G.nx * G.nz) return;
     const int x = (int)(i / G.nz) + 1, z = (int)(i - (i / G.nz) * G.nz);
@@ -417,9 +471,9 @@ __global__ void k_glancing_rows(const S *__restrict__ pdf, Grid G, FarfieldParam
         const FarfieldObject &o = P.obj[k];
         if (o.mode != 2) continue;
         const int y = o.normal[1] < 0 ? 1 : G.ny;
-        double rho, u[3];
-        macro_at(pdf, G, x, y, z, rho, u);
-        const double v = o.nh[0] * u[0] + o.nh[1] * u[1] + o.nh[2] * u[2] - CS * log(rho / o.density) - o.un_inf;
+        double rho, u[3], lr;
+        ring_get(G, R, x, y, z, rho, u, lr);
+        const double v = o.nh[0] * u[0] + o.nh[1] * u[1] + o.nh[2] * u[2] - CS * lr - o.un_inf;
         (o.normal[1] < 0 ? lo : hi)[i] = v;
     }
 }

@@ -92,7 +92,7 @@ template <> struct Store<__half> {
 
 // ---------------------------------------------------------------- collision
 template <typename T>
-__device__ __forceinline__ void collide(T g[Q], T omega_s, T omega_b) {
+__host__ __device__ __forceinline__ void collide(T g[Q], T omega_s, T omega_b) {
     // raw moments of g up to second order through partial line sums
     T Z0[3][3], Z1[3][3], Z2[3][3];
 #pragma unroll
@@ -179,6 +179,110 @@ __device__ __forceinline__ void collide(T g[Q], T omega_s, T omega_b) {
                 g[qof(ix, iy, iz)] = dA0 * T(w1(iz)) + rA0 * dphi[2][iz] + rA * phi[2][iz] + rB * psi[2][iz] +
                                      rC * chi[iz];
         }
+}
+
+// Plain FP64 form.  The same operator with the fewest double-precision
+// operations (the FP64 pipe bounds this kernel on GB300): populations f = g + w
+// are formed directly, and the three per-axis expansions are factored as
+// chimera passes that share their coefficients,
+//   X(+-) = E_X +- D_X,  X(0) = (1 - t) X_phi - 2u X_psi - X_chi,
+// first along x for A, B, C of every c_y, then along z with rho folded into
+// the z-functions.  About 370 FP64 operations per cell.
+template <typename T>
+__host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b) {
+    T Z0[3][3], Z1[3][3], Z2[3][3];
+#pragma unroll
+    for (int ix = 0; ix < 3; ++ix)
+#pragma unroll
+        for (int iy = 0; iy < 3; ++iy) {
+            const T a = g[qof(ix, iy, 0)], b = g[qof(ix, iy, 1)], c = g[qof(ix, iy, 2)];
+            Z1[ix][iy] = c - a;
+            Z2[ix][iy] = c + a;
+            Z0[ix][iy] = Z2[ix][iy] + b;
+        }
+    T Y00[3], Y01[3], Y02[3], Y10[3], Y11[3], Y20[3];
+#pragma unroll
+    for (int ix = 0; ix < 3; ++ix) {
+        Y01[ix] = Z0[ix][2] - Z0[ix][0];
+        Y02[ix] = Z0[ix][2] + Z0[ix][0];
+        Y00[ix] = Y02[ix] + Z0[ix][1];
+        Y11[ix] = Z1[ix][2] - Z1[ix][0];
+        Y10[ix] = Z1[ix][0] + Z1[ix][1] + Z1[ix][2];
+        Y20[ix] = Z2[ix][0] + Z2[ix][1] + Z2[ix][2];
+    }
+    const T M200 = Y00[2] + Y00[0];
+    const T drho = M200 + Y00[1];
+    const T jx = Y00[2] - Y00[0];
+    const T jy = Y01[0] + Y01[1] + Y01[2];
+    const T M110 = Y01[2] - Y01[0];
+    const T M020 = Y02[0] + Y02[1] + Y02[2];
+    const T jz = Y10[0] + Y10[1] + Y10[2];
+    const T M101 = Y10[2] - Y10[0];
+    const T M011 = Y11[0] + Y11[1] + Y11[2];
+    const T M002 = Y20[0] + Y20[1] + Y20[2];
+
+    const T rho = T(1) + drho;
+    const T rinv = T(1) / rho;
+    const T ux = jx * rinv, uy = jy * rinv, uz = jz * rinv;
+    // second-order central moments minus 1/3, relaxed
+    const T kdx = M200 - jx * ux, kdy = M020 - jy * uy, kdz = M002 - jz * uz;
+    const T P1 = om1 * (kdx - kdy), P2 = om1 * (kdx - kdz);
+    const T S = kdx + kdy + kdz;
+    const T third = T(1) / T(3);
+    const T kx = (P1 + P2 + (S + omega_b * (drho - S))) * third;
+    // normalised covariance: s_aa = (1/3 + k_a) / rho; t_a = u_a^2 + s_aa
+    const T r3 = third * rinv;
+    const T tx = ux * ux + (r3 + kx * rinv);
+    const T ty = uy * uy + (r3 + (kx - P1) * rinv);
+    const T tz = uz * uz + (r3 + (kx - P2) * rinv);
+    const T omr = om1 * rinv;
+    const T sxy = (M110 - jx * uy) * omr, sxz = (M101 - jx * uz) * omr, syz = (M011 - jy * uz) * omr;
+    // coefficient products
+    const T s2xy = T(2) * sxy, s2xz = T(2) * sxz, s2yz = T(2) * syz;
+    const T kAchi = s2xy * sxy;        // 2 sxy^2
+    const T kBpsi = s2xy * syz;        // 2 sxy syz
+    const T kBchi = s2xy * sxz;        // 2 sxy sxz
+    const T kCphi = s2yz * syz;        // 2 syz^2
+    const T kCpsi = s2xz * syz;        // 2 sxz syz
+    const T kCchi = s2xz * sxz;        // 2 sxz^2
+    const T k8 = T(4) * kBchi * syz;   // 8 sxy sxz syz
+    // y-functions
+    const T phy[3] = {T(0.5) * (ty - uy), T(1) - ty, T(0.5) * (ty + uy)};
+    const T psy[3] = {uy - T(0.5), T(-2) * uy, uy + T(0.5)};
+    const T chy[3] = {T(0.5), T(-1), T(0.5)};
+    // x-functions in the E/D split
+    const T htx = T(0.5) * tx, hux = T(0.5) * ux, omtx = T(1) - tx, m2ux = T(-2) * ux;
+    // rho-scaled z-functions in the E/D split
+    const T rhtz = T(0.5) * rho * tz, rhuz = T(0.5) * rho * uz, rh = T(0.5) * rho;
+    const T r0z = rho * (T(1) - tz), rm2uz = T(-2) * rho * uz, ruz = rho * uz;
+#pragma unroll
+    for (int iy = 0; iy < 3; ++iy) {
+        // coefficients of phi_x, psi_x, chi_x in A, B, C for this c_y
+        const T Ap = phy[iy], As = sxy * psy[iy], Ac = kAchi * chy[iy];
+        const T Bp = syz * psy[iy], Bs = sxz * phy[iy] + kBpsi * chy[iy], Bc = kBchi * psy[iy];
+        const T Cp = kCphi * chy[iy], Cs = kCpsi * psy[iy], Cc = kCchi * phy[iy] + k8 * chy[iy];
+        T A[3], B[3], C[3];
+        {
+            const T E = htx * Ap + ux * As + T(0.5) * Ac, D = hux * Ap + T(0.5) * As;
+            A[2] = E + D; A[0] = E - D; A[1] = omtx * Ap + m2ux * As - Ac;
+        }
+        {
+            const T E = htx * Bp + ux * Bs + T(0.5) * Bc, D = hux * Bp + T(0.5) * Bs;
+            B[2] = E + D; B[0] = E - D; B[1] = omtx * Bp + m2ux * Bs - Bc;
+        }
+        {
+            const T E = htx * Cp + ux * Cs + T(0.5) * Cc, D = hux * Cp + T(0.5) * Cs;
+            C[2] = E + D; C[0] = E - D; C[1] = omtx * Cp + m2ux * Cs - Cc;
+        }
+#pragma unroll
+        for (int ix = 0; ix < 3; ++ix) {
+            const T E = A[ix] * rhtz + B[ix] * ruz + C[ix] * rh;
+            const T D = A[ix] * rhuz + B[ix] * rh;
+            g[qof(ix, iy, 2)] = (E + D) - T(weight(qof(ix, iy, 2)));
+            g[qof(ix, iy, 0)] = (E - D) - T(weight(qof(ix, iy, 0)));
+            g[qof(ix, iy, 1)] = (A[ix] * r0z + B[ix] * rm2uz - C[ix] * rho) - T(weight(qof(ix, iy, 1)));
+        }
+    }
 }
 
 }  // namespace ak
