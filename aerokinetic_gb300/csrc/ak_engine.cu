@@ -82,6 +82,7 @@ struct ak_case {
     int ff_count = 0;
     FarfieldObject *d_ff = nullptr;
     float *d_shift = nullptr;
+    Shift27 shift_host{};
     FarfieldParams ff() const { return FarfieldParams{d_ff, ff_count}; }
     // reductions
     double *partials = nullptr, *reduced = nullptr;
@@ -479,8 +480,8 @@ int one_step(ak_case *c, bool sample, double *fixed_partials = nullptr, long lon
     // bulk
     mark(c);
     dim3 grid((unsigned)blocks_for(c->nx, 128), (unsigned)c->ny, (unsigned)c->nz);
-    k_stream_collide<S><<<grid, 128, 0, c->stream>>>(src, dst_of<S>(c), c->flags, c->G, (T)c->omega_s,
-                                                     (T)c->omega_b);
+    k_stream_collide<S><<<grid, 128, 0, c->stream>>>(src, dst_of<S>(c), c->flags, c->G, c->shift_host,
+                                                     (T)c->omega_s, (T)c->omega_b);
     AK_CUDA(cudaGetLastError());
     ++c->launches;
     mark(c);
@@ -585,6 +586,7 @@ int ak_case_create(const ak_case_desc *desc, ak_case **out) {
         for (int a = 0; a < 3; ++a)
             p *= e[a] == 0 ? 2.0 / 3.0 - u[a] * u[a] : 0.5 * (1.0 / 3.0 + u[a] * u[a] + e[a] * u[a]);
         shift[q] = c->storage == AK_STORAGE_F16 ? (float)(p - weight(q)) : 0.0f;
+        c->shift_host.v[q] = shift[q];
     }
     int r = AK_OK;
     if (cudaGetDevice(&c->device) != cudaSuccess) r = fail(AK_ERR_CUDA, "no current CUDA device");

@@ -59,41 +59,42 @@ __device__ __forceinline__ bool ak_in_range(const Grid &G, int q, int x, int y, 
 template <typename S>
 __device__ __forceinline__ double load_g(const S *pdf, const Grid &G, int q, int x, int y, int z) {
     if (!AK_CHECK(G, q, x, y, z, 1)) return 0.0;
-    return (double)Store<S>::load(pdf + q * G.qs + G.cell(x, y, z), q, G.shift);
+    return (double)Store<S>::load(pdf + q * G.qs + G.cell(x, y, z), q, G.shift[q]);
 }
 template <typename S>
 __device__ __forceinline__ void store_g(S *pdf, const Grid &G, int q, int x, int y, int z, double v) {
     if (!AK_CHECK(G, q, x, y, z, 2)) return;
-    Store<S>::store(pdf + q * G.qs + G.cell(x, y, z), q, (typename Store<S>::T)v, G.shift);
+    Store<S>::store(pdf + q * G.qs + G.cell(x, y, z), q, (typename Store<S>::T)v, G.shift[q]);
 }
 
 // ------------------------------------------------------------ bulk step
 template <typename S>
-__global__ void __launch_bounds__(128) k_stream_collide(const S *__restrict__ src, S *__restrict__ dst,
-                                                        const uint8_t *__restrict__ flags, Grid G,
-                                                        typename Store<S>::T omega_s,
-                                                        typename Store<S>::T omega_b) {
+__global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
+    k_stream_collide(const S *__restrict__ src, S *__restrict__ dst, const uint8_t *__restrict__ flags, Grid G,
+                     Shift27 shift, typename Store<S>::T omega_s, typename Store<S>::T omega_b) {
     using T = typename Store<S>::T;
     const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int y = blockIdx.y + 1;
     const int z = blockIdx.z;
     if (x > G.nx) return;
-    if (__ldg(flags + y * G.nxp + x) != FLAG_FLUID) return;
+    // the column flag only gates the stores, so the 27 loads issue at once
+    const bool fluid = __ldg(flags + y * G.nxp + x) == FLAG_FLUID;
     T g[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         const int zs = G.wrapz(z - cz(q));
         g[q] = AK_CHECK(G, q, x - cx(q), y - cy(q), zs, 3)
-                   ? Store<S>::load(src + q * G.qs + G.cell(x - cx(q), y - cy(q), zs), q, G.shift)
+                   ? Store<S>::load(src + q * G.qs + G.cell(x - cx(q), y - cy(q), zs), q, shift.v[q])
                    : T(0);
     }
     if constexpr (sizeof(T) == 8)
         collide_full<T>(g, T(1) - omega_s, omega_b);
     else
         collide<T>(g, omega_s, omega_b);
+    if (!fluid) return;
     const long long c = G.cell(x, y, z);
 #pragma unroll
-    for (int q = 0; q < Q; ++q) Store<S>::store(dst + q * G.qs + c, q, g[q], G.shift);
+    for (int q = 0; q < Q; ++q) Store<S>::store(dst + q * G.qs + c, q, g[q], shift.v[q]);
 }
 
 // ------------------------------------------------------------ walls
@@ -347,6 +348,7 @@ __device__ __forceinline__ void ring_get(const Grid &G, const Ring &R, int px, i
 __device__ double farfield_transverse(const Grid &G, const Ring &R, const FarfieldObject &o, const int foot[3],
                                       const signed char edge[3], const double u[3], double rm) {
     double F = 0.0;
+#pragma unroll
     for (int a = 0; a < 3; ++a) {
         if (!o.active[a]) continue;
         const int e = edge[a];
@@ -447,6 +449,7 @@ __global__ void __launch_bounds__(256) k_farfield(S *__restrict__ pdf, Grid G, O
     const double unb = (rp + value) / 2.0;
     const double rhob = o.density * exp((rp - value) / (2.0 * CS));
     double ub[3];
+#pragma unroll
     for (int a = 0; a < 3; ++a) {
         const double tangential = unb >= 0.0 ? u[a] - o.nh[a] * un : o.vel[a] - o.nh[a] * o.un_inf;
         ub[a] = o.nh[a] * unb + tangential;

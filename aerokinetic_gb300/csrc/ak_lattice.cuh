@@ -72,22 +72,29 @@ __host__ __device__ constexpr double weight(int q) {
 template <typename S> struct Store;
 template <> struct Store<double> {
     using T = double;
-    __device__ static __forceinline__ double load(const double *p, int, const float *) { return __ldg(p); }
-    __device__ static __forceinline__ void store(double *p, int, double v, const float *) { *p = v; }
+    static constexpr int MIN_BLOCKS = 4;
+    __device__ static __forceinline__ double load(const double *p, int, float) { return __ldg(p); }
+    __device__ static __forceinline__ void store(double *p, int, double v, float) { *p = v; }
 };
 template <> struct Store<float> {
     using T = float;
-    __device__ static __forceinline__ float load(const float *p, int, const float *) { return __ldg(p); }
-    __device__ static __forceinline__ void store(float *p, int, float v, const float *) { *p = v; }
+    static constexpr int MIN_BLOCKS = 8;
+    __device__ static __forceinline__ float load(const float *p, int, float) { return __ldg(p); }
+    __device__ static __forceinline__ void store(float *p, int, float v, float) { *p = v; }
 };
 template <> struct Store<__half> {
     using T = float;
-    __device__ static __forceinline__ float load(const __half *p, int q, const float *shift) {
-        return fmaf(__half2float(__ldg(p)), (float)weight(q), __ldg(shift + q));
+    static constexpr int MIN_BLOCKS = 8;
+    __device__ static __forceinline__ float load(const __half *p, int q, float shift) {
+        return fmaf(__half2float(__ldg(p)), (float)weight(q), shift);
     }
-    __device__ static __forceinline__ void store(__half *p, int q, float v, const float *shift) {
-        *p = __float2half_rn((v - __ldg(shift + q)) * (float)(1.0 / weight(q)));
+    __device__ static __forceinline__ void store(__half *p, int q, float v, float shift) {
+        *p = __float2half_rn((v - shift) * (float)(1.0 / weight(q)));
     }
+};
+// the FP16 shift by value, for kernels that index it with compile-time q
+struct Shift27 {
+    float v[27];
 };
 
 // ---------------------------------------------------------------- collision
