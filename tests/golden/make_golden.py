@@ -170,6 +170,14 @@ def main():
         project = json.loads((base / "project.json").read_text())
         histories[name] = {"project": project, "history": read_history(base / "history.csv", limit),
                            "source": path}
+    for name, (path, limit) in {"refined_startup": ("docs/verification_040", 12)}.items():
+        base = ref / path
+        project = json.loads((base / "startup_project.json").read_text())
+        with open(base / "startup_history.csv", newline="", encoding="utf-8") as handle:
+            rows = list(csv.DictReader(handle))[:limit]
+        histories[name] = {"project": project, "source": path,
+                           "history": [{k: (int(r[k]) if k == "step" else float(r[k]))
+                                        for k in ("step", "cl", "cd", "cm")} for r in rows]}
     (HERE / "histories.json").write_text(json.dumps(histories) + "\n")
 
     profile = json.loads((ref / "docs/verification_stage1_20261106/profile_threads1.json").read_text())

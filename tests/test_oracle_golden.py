@@ -223,3 +223,24 @@ def test_collision_matches_generic_cumulant_route():
         np.testing.assert_allclose(fast, slow, rtol=0, atol=5e-15)
         # mass and momentum are collision invariants
         assert abs(fast.sum() - g.sum()) < 1e-15
+
+
+def test_refined_startup_history(golden):
+    """Two-level start-up (docs/verification_040/startup_*): 2:1 box, fine walls,
+    donors, reflux and restriction; the first three samples (12 coarse steps)."""
+    from aerokinetic_gb300.refined_plan import RefinedPlan, load_refined_project
+    from oracle.refined import RefinedCase
+    record = golden["histories"]["refined_startup"]
+    project, refinement = load_refined_project(record["project"])
+    plan = RefinedPlan.create(project, refinement)
+    sec, flow = project.section, project.flow
+    lead = O.leading_edge([e.xy for e in sec.elements], sec.moment_reference, sec.chord, flow.alpha_deg)
+    case = RefinedCase([c.xy for c in sec.normalized(flow.alpha_deg)], plan.shape, plan.origin, plan.coarse_level.dx,
+                       plan.coarse_level.dt, plan.coarse_level.tau_shear, plan.coarse_level.tau_bulk,
+                       plan.box.lower, plan.box.upper, flow.lattice_speed, flow.perturbation, flow.seed, lead,
+                       plan.span, oracle_threads())
+    for row in record["history"][:3]:
+        while case.steps < row["step"]:
+            loads = case.step()
+        for k in ("cl", "cd", "cm"):
+            assert loads[k] == pytest.approx(row[k], abs=1e-12)
