@@ -64,6 +64,12 @@ class CaseDesc(ctypes.Structure):
                 ("element_sizes", ctypes.POINTER(ctypes.c_int32)), ("polygon_xy", ctypes.POINTER(ctypes.c_double))]
 
 
+class RefinedDesc(ctypes.Structure):
+    _fields_ = [("coarse", CaseDesc), ("tau_shear", ctypes.c_double), ("tau_bulk", ctypes.c_double),
+                ("dt_coarse", ctypes.c_double), ("span", ctypes.c_double),
+                ("box_lower", ctypes.c_int32 * 3), ("box_upper", ctypes.c_int32 * 3)]
+
+
 class CaseInfo(ctypes.Structure):
     _fields_ = [("cells", ctypes.c_int64), ("fluid_cells", ctypes.c_int64), ("wall_keys", ctypes.c_int64),
                 ("wall_links", ctypes.c_int64), ("outer_links", ctypes.c_int64),
@@ -91,6 +97,12 @@ SIGNATURES = {
     "ak_set_pdf": ([_P, _P], ctypes.c_int),
     "ak_get_flags": ([_P, _P], ctypes.c_int),
     "ak_get_wall_links": ([_P, _P, _P], ctypes.c_int),
+    "ak_refined_create": ([ctypes.POINTER(RefinedDesc), ctypes.POINTER(_P)], ctypes.c_int),
+    "ak_refined_destroy": ([_P], ctypes.c_int),
+    "ak_refined_init_perturbed": ([_P, _D, _D, _D, _D, _D], ctypes.c_int),
+    "ak_refined_step": ([_P, ctypes.c_int32, _P], ctypes.c_int),
+    "ak_refined_steps_done": ([_P], ctypes.c_int64),
+    "ak_refined_level": ([_P, ctypes.c_int32], _P),
     "ak_last_error": ([], ctypes.c_char_p),
     "ak_version": ([], ctypes.c_char_p),
 }

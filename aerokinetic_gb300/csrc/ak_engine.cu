@@ -15,6 +15,7 @@
 
 #include "../../include/aerokinetic_gb300.h"
 #include "ak_geometry.cuh"
+#include "ak_transfer.cuh"
 
 using namespace ak;
 
@@ -95,6 +96,7 @@ struct ak_case {
     long long launches = 0;  // kernels issued by stepping since creation
     bool prepared = false;
     int device = 0;  // CUDA device current when the case was created
+    bool periodic_xy = false;  // the padded fine block of a refined case wraps in x and y
     // optional per-kernel timing: events recorded around each kernel group
     std::vector<cudaEvent_t> *timing = nullptr;
     cudaStream_t stream = nullptr;
@@ -519,23 +521,13 @@ unsigned long long ak_debug_status(void) {
 }
 #endif
 
-int ak_case_create(const ak_case_desc *desc, ak_case **out) {
-    g_error.clear();
-    if (!desc || !out) return fail(AK_ERR_INVALID, "null argument");
+}  // extern "C"
+
+namespace {
+// Builds a lattice from a validated description.  farfield -1 = no outer
+// boundary (the refined fine block), periodic_xy wraps x and y.
+int create_lattice(const ak_case_desc *desc, int farfield, bool periodic_xy, ak_case **out) {
     *out = nullptr;
-    if (desc->nx < 4 || desc->ny < 4 || desc->nz < 1) return fail(AK_ERR_INVALID, "lattice needs nx, ny >= 4 and nz >= 1");
-    if ((long long)desc->nx + 2 > 32767 || (long long)desc->ny + 2 > 65535 || desc->nz > 65535)
-        return fail(AK_ERR_INVALID, "lattice extent too large for one case");
-    if (!(desc->dx > 0) || !std::isfinite(desc->dx)) return fail(AK_ERR_INVALID, "dx must be positive");
-    if (!(desc->omega_shear > 0 && desc->omega_shear < 2) || !(desc->omega_bulk > 0 && desc->omega_bulk < 2))
-        return fail(AK_ERR_INVALID, "relaxation rates must lie in (0, 2)");
-    if (!std::isfinite(desc->speed) || std::fabs(desc->speed) >= 1.0 / std::sqrt(3.0))
-        return fail(AK_ERR_INVALID, "freestream speed must be subsonic");
-    if (desc->farfield != AK_FARFIELD_LEGACY && desc->farfield != AK_FARFIELD_CHARACTERISTIC)
-        return fail(AK_ERR_INVALID, "unknown farfield");
-    if (desc->storage < AK_STORAGE_F64 || desc->storage > AK_STORAGE_F16) return fail(AK_ERR_INVALID, "unknown storage");
-    if (desc->n_elements < 1 || desc->n_elements > MAX_ELEMENTS || !desc->element_sizes || !desc->polygon_xy)
-        return fail(AK_ERR_INVALID, "between 1 and 8 polygons are required");
     ak_case *c = new ak_case();
     c->nx = desc->nx;
     c->ny = desc->ny;
@@ -548,7 +540,8 @@ int ak_case_create(const ak_case_desc *desc, ak_case **out) {
     c->omega_s = desc->omega_shear;
     c->omega_b = desc->omega_bulk;
     c->speed = desc->speed;
-    c->farfield = desc->farfield;
+    c->farfield = farfield;
+    c->periodic_xy = periodic_xy;
     c->storage = desc->storage;
     c->n_elements = desc->n_elements;
     int total = 0;
@@ -561,7 +554,7 @@ int ak_case_create(const ak_case_desc *desc, ak_case **out) {
         c->poly_count.push_back(desc->element_sizes[e]);
         total += desc->element_sizes[e];
     }
-    c->poly_xy.assign(desc->polygon_xy, desc->polygon_xy + 2 * (size_t)total);
+    if (total) c->poly_xy.assign(desc->polygon_xy, desc->polygon_xy + 2 * (size_t)total);
     for (double v : c->poly_xy)
         if (!std::isfinite(v)) {
             delete c;
@@ -598,7 +591,7 @@ int ak_case_create(const ak_case_desc *desc, ak_case **out) {
     std::vector<uint8_t> hflags;
     if (r == AK_OK && c->farfield == AK_FARFIELD_CHARACTERISTIC) build_farfield_objects(c);
     if (r == AK_OK) r = build_geometry(c, hflags);
-    if (r == AK_OK) r = build_outer(c, hflags);
+    if (r == AK_OK && c->farfield >= 0) r = build_outer(c, hflags);
     if (r == AK_OK) r = dalloc(c, &c->reduced, 64);
     if (r == AK_OK) r = with_storage(c, [&](auto *tag) { return allocate_populations<std::remove_pointer_t<decltype(tag)>>(c); });
     if (r == AK_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) r = fail(AK_ERR_CUDA, "case set-up failed");
@@ -611,6 +604,35 @@ int ak_case_create(const ak_case_desc *desc, ak_case **out) {
     }
     *out = c;
     return AK_OK;
+}
+
+int validate_desc(const ak_case_desc *desc, bool need_elements) {
+    if (desc->nx < 4 || desc->ny < 4 || desc->nz < 1) return fail(AK_ERR_INVALID, "lattice needs nx, ny >= 4 and nz >= 1");
+    if ((long long)desc->nx + 2 > 32767 || (long long)desc->ny + 2 > 65535 || desc->nz > 65535)
+        return fail(AK_ERR_INVALID, "lattice extent too large for one case");
+    if (!(desc->dx > 0) || !std::isfinite(desc->dx)) return fail(AK_ERR_INVALID, "dx must be positive");
+    if (!(desc->omega_shear > 0 && desc->omega_shear < 2) || !(desc->omega_bulk > 0 && desc->omega_bulk < 2))
+        return fail(AK_ERR_INVALID, "relaxation rates must lie in (0, 2)");
+    if (!std::isfinite(desc->speed) || std::fabs(desc->speed) >= 1.0 / std::sqrt(3.0))
+        return fail(AK_ERR_INVALID, "freestream speed must be subsonic");
+    if (desc->farfield != AK_FARFIELD_LEGACY && desc->farfield != AK_FARFIELD_CHARACTERISTIC)
+        return fail(AK_ERR_INVALID, "unknown farfield");
+    if (desc->storage < AK_STORAGE_F64 || desc->storage > AK_STORAGE_F16) return fail(AK_ERR_INVALID, "unknown storage");
+    if ((need_elements && desc->n_elements < 1) || desc->n_elements > MAX_ELEMENTS ||
+        (desc->n_elements && (!desc->element_sizes || !desc->polygon_xy)))
+        return fail(AK_ERR_INVALID, "between 1 and 8 polygons are required");
+    return AK_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int ak_case_create(const ak_case_desc *desc, ak_case **out) {
+    g_error.clear();
+    if (!desc || !out) return fail(AK_ERR_INVALID, "null argument");
+    *out = nullptr;
+    AK_TRY(validate_desc(desc, true));
+    return create_lattice(desc, desc->farfield, false, out);
 }
 
 int ak_case_destroy(ak_case *c) {
@@ -900,5 +922,391 @@ int ak_get_wall_links(ak_case *c, int32_t *rows, double *q) {
     }
     return AK_OK;
 }
+
+}  // extern "C"
+
+// ==================================================================== refined
+// Two-level 2:1 case (refined_solver.py:115-345, interface.py:133-352): a
+// coarse lattice with the legacy outer boundary and a padded fine block with
+// the walls, advanced as one coarse step + two fine steps per call, with
+// time-interpolated donors, face-flux reflux and restriction.  Every kernel
+// of a refined case runs on the coarse lattice's stream.
+struct ak_refined {
+    ak_case *coarse = nullptr, *fine = nullptr;
+    BoxSpec B{};
+    int pad = 2;
+    double dx_c = 0, dt_c = 0, dx_f = 0, dt_f = 0, span = 0, speed = 0;
+    double tau_s_c = 0, tau_b_c = 0, tau_s_f = 0, tau_b_f = 0;
+    double free_g[Q];
+    double *d_free = nullptr;
+    double *mom_old = nullptr, *mom_new = nullptr;
+    Face faces[4];
+    int nfaces = 0;
+    long long offs[4] = {0, 0, 0, 0};
+    long long reg_doubles = 0, max_face = 0;
+    Face *d_faces = nullptr;
+    long long *d_offs = nullptr;
+    double *reg_c = nullptr, *reg_f = nullptr;
+    FluxTerm *d_terms[2] = {nullptr, nullptr};
+    int nterms = 0;
+    int *d_flag = nullptr;
+    double *d_loads = nullptr;
+    long long steps = 0;
+    std::vector<void *> owned;  // device buffers of the driver
+};
+
+namespace {
+
+template <typename T>
+int ralloc(ak_refined *R, T **p, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess)
+        return fail(e == cudaErrorMemoryAllocation ? AK_ERR_NOMEM : AK_ERR_CUDA,
+                    std::string("device allocation failed: ") + cudaGetErrorString(e));
+    R->owned.push_back(*p);
+    return AK_OK;
+}
+
+void refined_release(ak_refined *R) {
+    if (R->coarse) cudaStreamSynchronize(R->coarse->stream);
+    for (void *p : R->owned) cudaFree(p);
+    if (R->coarse) {
+        release(R->coarse);
+        delete R->coarse;
+    }
+    if (R->fine) {
+        release(R->fine);
+        delete R->fine;
+    }
+}
+
+// zero-centred populations of (rho = 1, u = (U, 0, 0)) with zero stress
+void free_populations(double speed, double g[Q]) {
+    for (int q = 0; q < Q; ++q) {
+        const int c[3] = {cx(q), cy(q), cz(q)};
+        const double u[3] = {speed, 0.0, 0.0};
+        double eq = 1.0;
+        for (int a = 0; a < 3; ++a)
+            eq *= c[a] == 0 ? 2.0 / 3.0 - u[a] * u[a] : (1.0 / 3.0 + u[a] * u[a] + c[a] * u[a]) / 2.0;
+        g[q] = eq - weight(q);
+    }
+}
+
+// face-flux terms of one normal axis (interface.py:73-94)
+std::vector<FluxTerm> flux_terms(int axis) {
+    std::vector<FluxTerm> out;
+    for (int d = 0; d < Q; ++d) {
+        const int c[3] = {cx(d), cy(d), cz(d)};
+        const int normal = c[axis];
+        if (normal == 0) continue;
+        std::vector<int> moving;
+        for (int a = 0; a < 3; ++a)
+            if (a != axis && c[a] != 0) moving.push_back(a);
+        const int m = (int)moving.size();
+        auto fact = [](int n) { double f = 1; for (int k = 2; k <= n; ++k) f *= k; return f; };
+        for (int count = 0; count <= m; ++count) {
+            const double weight_ = fact(count) * fact(m - count) / fact(m + 1);
+            for (int mask = 0; mask < (1 << m); ++mask) {
+                if (__builtin_popcount(mask) != count) continue;
+                FluxTerm t{};
+                t.d = d;
+                for (int k = 0; k < m; ++k)
+                    if (mask & (1 << k)) t.shift[moving[k]] = -c[moving[k]];
+                t.coef[0] = weight_ * normal;
+                for (int a = 0; a < 3; ++a) t.coef[a + 1] = weight_ * normal * c[a];
+                out.push_back(t);
+            }
+        }
+    }
+    return out;
+}
+
+long long blocks3(long long n) { return (n + 255) / 256; }
+
+template <typename S>
+int refined_init(ak_refined *R, double amp, double phase_y, double phase_z, double lead_x, double lead_y) {
+    ak_case *C = R->coarse, *F = R->fine;
+    cudaStream_t st = C->stream;
+    for (ak_case *L : {C, F})
+        for (int k = 0; k < 2; ++k) {
+            k_fill<S><<<(unsigned)blocks3(L->G.qs), 256, 0, st>>>((S *)L->pdf[k], L->G, R->d_free);
+            AK_CUDA(cudaGetLastError());
+        }
+    const double ky = 2 * M_PI / (C->ny * R->dx_c), kz = 2 * M_PI / R->span;
+    for (ak_case *L : {C, F}) {
+        const long long n = (long long)L->nx * L->ny * L->nz;
+        k_init_perturbed<S><<<(unsigned)blocks3(n), 256, 0, st>>>(src_of<S>(L), L->G, L->flags, R->speed, amp,
+                                                                   phase_y, phase_z, lead_x, lead_y, L->origin_x,
+                                                                   L->origin_y, L->dx, ky, kz);
+        AK_CUDA(cudaGetLastError());
+    }
+    const Rescale f2c{R->tau_s_c * R->dt_c / (R->tau_s_f * R->dt_f), R->tau_b_c * R->dt_c / (R->tau_b_f * R->dt_f)};
+    AK_CUDA(cudaMemsetAsync(R->d_flag, 0, sizeof(int), st));
+    k_restrict<S, S><<<(unsigned)blocks3((long long)R->B.bx * R->B.by * R->B.bz), 256, 0, st>>>(
+        src_of<S>(C), C->G, src_of<S>(F), F->G, R->B, R->pad, R->d_free, f2c, R->d_flag);
+    AK_CUDA(cudaGetLastError());
+    // boundary data from the initial state, ghosts still holding the free
+    // stream (refined_solver.py:224-262)
+    if (C->n_out) {
+        k_outflow_prepare<S><<<(unsigned)blocks3(C->n_out), 256, 0, st>>>(
+            src_of<S>(C), C->G, C->outer(), C->sel_out, C->n_out, C->out_state, 1, 0, 0, 1.0, C->speed, 0.0, 0.0);
+        AK_CUDA(cudaGetLastError());
+    }
+    C->prepared = F->prepared = true;
+    R->steps = 0;
+    AK_CUDA(cudaStreamSynchronize(st));
+    int flag = 0;
+    AK_CUDA(cudaMemcpy(&flag, R->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) return fail(AK_ERR_NONFINITE, "initial restriction produced an invalid state");
+    return AK_OK;
+}
+
+template <typename S>
+int refined_step(ak_refined *R) {
+    using T = typename Store<S>::T;
+    ak_case *C = R->coarse, *F = R->fine;
+    cudaStream_t st = C->stream;
+    const BoxSpec &B = R->B;
+    const long long nblock = (long long)B.dnx * B.dny * C->nz;
+    dim3 gc((unsigned)blocks_for(C->nx, 128), (unsigned)C->ny, (unsigned)C->nz);
+    dim3 gf((unsigned)blocks_for(F->nx, 128), (unsigned)F->ny, (unsigned)F->nz);
+    const Rescale c2f{R->tau_s_f * R->dt_f / (R->tau_s_c * R->dt_c), R->tau_b_f * R->dt_f / (R->tau_b_c * R->dt_c)};
+    const Rescale f2c{R->tau_s_c * R->dt_c / (R->tau_s_f * R->dt_f), R->tau_b_c * R->dt_c / (R->tau_b_f * R->dt_f)};
+    // donors before the coarse step
+    k_block_moments<S><<<(unsigned)blocks3(nblock), 256, 0, st>>>(src_of<S>(C), C->G, B, R->d_free, R->mom_old,
+                                                                   R->d_flag);
+    k_collide<S><<<gc, 128, 0, st>>>(src_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s, (T)C->omega_b);
+    k_face_flux_coarse<S><<<dim3((unsigned)blocks3(R->max_face), R->nfaces), 256, 0, st>>>(
+        src_of<S>(C), C->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs,
+        R->dx_c * R->dx_c * R->dx_c, R->reg_c);
+    if (C->n_ubb)
+        k_ubb<S><<<(unsigned)blocks3(C->n_ubb), 256, 0, st>>>(src_of<S>(C), C->G, C->outer(), C->sel_ubb, C->n_ubb,
+                                                              C->speed, 0.0, 0.0);
+    if (C->n_out)
+        k_outflow<S><<<(unsigned)blocks3(C->n_out), 256, 0, st>>>(src_of<S>(C), C->G, C->outer(), C->sel_out,
+                                                                  C->n_out, C->out_state, 1, 0, 0);
+    k_stream<S><<<gc, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, 0);
+    AK_CUDA(cudaGetLastError());
+    C->cur = 1 - C->cur;
+    // donors after the coarse step
+    k_block_moments<S><<<(unsigned)blocks3(nblock), 256, 0, st>>>(src_of<S>(C), C->G, B, R->d_free, R->mom_new,
+                                                                   R->d_flag);
+    AK_CUDA(cudaMemsetAsync(R->reg_f, 0, sizeof(double) * R->reg_doubles, st));
+    const long long nfine = (long long)F->nx * F->ny * F->nz;
+    const long long nlinks = F->nkeys * F->nz * 3;
+    const long long nb = blocks_for(nlinks, 256);
+    for (int sub = 0; sub < 2; ++sub) {
+        k_donors<S><<<(unsigned)blocks3(nfine), 256, 0, st>>>(src_of<S>(F), F->G, B, C->nz, R->mom_old, R->mom_new,
+                                                              sub / 2.0, c2f, R->pad, R->d_flag);
+        k_collide<S><<<gf, 128, 0, st>>>(src_of<S>(F), F->flags, F->G, F->shift_host, (T)F->omega_s, (T)F->omega_b);
+        k_face_flux_fine<S><<<dim3((unsigned)blocks3(R->max_face), R->nfaces), 256, 0, st>>>(
+            src_of<S>(F), F->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs, R->pad,
+            R->dx_f * R->dx_f * R->dx_f, R->reg_f);
+        if (nlinks) {
+            k_walls<S><<<(unsigned)nb, 256, 0, st>>>(src_of<S>(F), F->G, F->keys, F->wall_q, F->nkeys, 1,
+                                                     F->n_elements, F->ox, F->oy, F->partials);
+            k_sum_partials<<<1, 64, 0, st>>>(F->partials, (int)nb, 5 * F->n_elements, R->d_loads + sub * 5 * F->n_elements);
+        }
+        k_stream<S><<<gf, 128, 0, st>>>(src_of<S>(F), dst_of<S>(F), F->flags, F->G, 1);
+        AK_CUDA(cudaGetLastError());
+        F->cur = 1 - F->cur;
+    }
+    k_reflux<S><<<dim3((unsigned)blocks3(R->max_face), R->nfaces), 256, 0, st>>>(
+        src_of<S>(C), C->G, R->d_faces, R->nfaces, R->d_offs, R->reg_c, R->reg_f,
+        1.0 / (R->dx_c * R->dx_c * R->dx_c), R->d_flag);
+    k_restrict<S, S><<<(unsigned)blocks3((long long)B.bx * B.by * B.bz), 256, 0, st>>>(
+        src_of<S>(C), C->G, src_of<S>(F), F->G, B, R->pad, R->d_free, f2c, R->d_flag);
+    AK_CUDA(cudaGetLastError());
+    C->steps += 1;
+    F->steps += 2;
+    R->steps += 1;
+    return AK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
+    g_error.clear();
+    if (!desc || !out) return fail(AK_ERR_INVALID, "null argument");
+    *out = nullptr;
+    const ak_case_desc &cd = desc->coarse;
+    AK_TRY(validate_desc(&cd, true));
+    if (cd.farfield != AK_FARFIELD_LEGACY) return fail(AK_ERR_INVALID, "the refined solver uses the legacy outer boundary");
+    for (int a = 0; a < 3; ++a)
+        if (desc->box_lower[a] < 0 || desc->box_upper[a] <= desc->box_lower[a])
+            return fail(AK_ERR_INVALID, "fine-box bounds must have 0 <= lower < upper");
+    if (desc->box_lower[2] != 0 || desc->box_upper[2] != cd.nz)
+        return fail(AK_ERR_INVALID, "the fine box must span the whole periodic z axis");
+    if (desc->box_lower[0] < 1 || desc->box_lower[1] < 1 || desc->box_upper[0] > cd.nx - 1 || desc->box_upper[1] > cd.ny - 1)
+        return fail(AK_ERR_INVALID, "the refined box must fit strictly inside the external x/y domain");
+    if (!(desc->tau_shear > 0.5) || !(desc->tau_bulk > 0.5) || !(desc->dt_coarse > 0) || !(desc->span > 0))
+        return fail(AK_ERR_INVALID, "relaxation times must exceed 0.5 and dt, span be positive");
+    ak_refined *R = new ak_refined();
+    R->dx_c = cd.dx;
+    R->dt_c = desc->dt_coarse;
+    R->dx_f = cd.dx / 2;
+    R->dt_f = desc->dt_coarse / 2;
+    R->tau_s_c = desc->tau_shear;
+    R->tau_b_c = desc->tau_bulk;
+    R->tau_s_f = 0.5 + 2 * (desc->tau_shear - 0.5);
+    R->tau_b_f = 0.5 + 2 * (desc->tau_bulk - 0.5);
+    R->span = desc->span;
+    R->speed = cd.speed;
+    BoxSpec &B = R->B;
+    for (int a = 0; a < 3; ++a) {
+        B.lo[a] = desc->box_lower[a];
+        B.hi[a] = desc->box_upper[a];
+    }
+    B.bx = B.hi[0] - B.lo[0];
+    B.by = B.hi[1] - B.lo[1];
+    B.bz = B.hi[2] - B.lo[2];
+    B.dx0 = B.lo[0] - 3;
+    B.dy0 = B.lo[1] - 3;
+    B.dnx = B.bx + 6;
+    B.dny = B.by + 6;
+    int r = AK_OK;
+    // coarse lattice: no walls (they live on the fine level)
+    ak_case_desc coarse = cd;
+    coarse.omega_shear = 1.0 / R->tau_s_c;
+    coarse.omega_bulk = 1.0 / R->tau_b_c;
+    coarse.n_elements = 0;
+    r = create_lattice(&coarse, AK_FARFIELD_LEGACY, false, &R->coarse);
+    // fine block: two donor cells around the box in x and y, wraps everywhere
+    ak_case_desc fine = cd;
+    fine.nx = 2 * B.bx + 2 * R->pad;
+    fine.ny = 2 * B.by + 2 * R->pad;
+    fine.nz = 2 * B.bz;
+    fine.dx = R->dx_f;
+    fine.origin_x = cd.origin_x + B.lo[0] * cd.dx - R->pad * R->dx_f;
+    fine.origin_y = cd.origin_y + B.lo[1] * cd.dx - R->pad * R->dx_f;
+    fine.omega_shear = 1.0 / R->tau_s_f;
+    fine.omega_bulk = 1.0 / R->tau_b_f;
+    if (r == AK_OK) r = create_lattice(&fine, -1, true, &R->fine);
+    if (r == AK_OK) {
+        // every wall link must belong to the physical fine box, and the
+        // donor band must be fluid
+        ak_case *F = R->fine;
+        std::vector<WallKey> keys((size_t)F->nkeys);
+        if (F->nkeys)
+            cudaMemcpy(keys.data(), F->keys, keys.size() * sizeof(WallKey), cudaMemcpyDeviceToHost);
+        for (const WallKey &k : keys)
+            if (k.x - 1 < R->pad + 6 || k.x - 1 >= F->nx - R->pad - 6 || k.y - 1 < R->pad + 6 ||
+                k.y - 1 >= F->ny - R->pad - 6)
+                r = fail(AK_ERR_INVALID, "A solid intersects the fluid donor band");
+    }
+    if (r == AK_OK) {
+        free_populations(R->speed, R->free_g);
+        r = ralloc(R, &R->d_free, Q);
+        if (r == AK_OK) r = cudaMemcpy(R->d_free, R->free_g, sizeof R->free_g, cudaMemcpyHostToDevice) == cudaSuccess
+                                ? AK_OK : fail(AK_ERR_CUDA, "upload failed");
+    }
+    const long long nblock = (long long)B.dnx * B.dny * cd.nz;
+    if (r == AK_OK) r = ralloc(R, &R->mom_old, (size_t)nblock * 10);
+    if (r == AK_OK) r = ralloc(R, &R->mom_new, (size_t)nblock * 10);
+    if (r == AK_OK) {
+        R->nfaces = 0;
+        long long off = 0;
+        for (int axis = 0; axis < 2; ++axis)
+            for (int side = -1; side <= 1; side += 2) {
+                Face f{};
+                f.axis = axis;
+                f.side = side;
+                const int b = axis == 0 ? B.bx : B.by;
+                f.coarse_index = side < 0 ? B.lo[axis] - 1 : B.hi[axis] - 1;
+                f.fine_index = side < 0 ? R->pad - 1 : R->pad + 2 * b - 1;
+                f.lo1 = axis == 0 ? B.lo[1] : B.lo[0];
+                f.n1 = axis == 0 ? B.by : B.bx;
+                f.lo2 = 0;
+                f.n2 = cd.nz;
+                R->faces[R->nfaces] = f;
+                R->offs[R->nfaces] = off;
+                off += 4LL * f.n1 * f.n2;
+                R->max_face = std::max<long long>(R->max_face, (long long)f.n1 * f.n2);
+                ++R->nfaces;
+            }
+        R->reg_doubles = off;
+        r = ralloc(R, &R->reg_c, (size_t)off);
+        if (r == AK_OK) r = ralloc(R, &R->reg_f, (size_t)off);
+        if (r == AK_OK) r = ralloc(R, &R->d_faces, 4);
+        if (r == AK_OK) r = ralloc(R, &R->d_offs, 4);
+        if (r == AK_OK) {
+            cudaMemcpy(R->d_faces, R->faces, sizeof R->faces, cudaMemcpyHostToDevice);
+            cudaMemcpy(R->d_offs, R->offs, sizeof R->offs, cudaMemcpyHostToDevice);
+        }
+        for (int axis = 0; axis < 2 && r == AK_OK; ++axis) {
+            std::vector<FluxTerm> t = flux_terms(axis);
+            R->nterms = (int)t.size();
+            r = ralloc(R, &R->d_terms[axis], t.size());
+            if (r == AK_OK) cudaMemcpy(R->d_terms[axis], t.data(), t.size() * sizeof(FluxTerm), cudaMemcpyHostToDevice);
+        }
+    }
+    if (r == AK_OK) r = ralloc(R, &R->d_flag, 1);
+    if (r == AK_OK) r = ralloc(R, &R->d_loads, (size_t)2 * 5 * std::max(1, cd.n_elements));
+    if (r == AK_OK) {
+        ak_case *F = R->fine;
+        const long long nb = blocks_for(F->nkeys * F->nz * 3, 256);
+        r = ensure_partials(F, std::max<long long>(1, nb * 5 * F->n_elements));
+    }
+    if (r == AK_OK && cudaMemset(R->d_loads, 0, sizeof(double) * 2 * 5 * std::max(1, cd.n_elements)) != cudaSuccess)
+        r = fail(AK_ERR_CUDA, "memset failed");
+    if (r == AK_OK && cudaDeviceSynchronize() != cudaSuccess) r = fail(AK_ERR_CUDA, "refined set-up failed");
+    if (r != AK_OK) {
+        std::string keep = g_error;
+        refined_release(R);
+        delete R;
+        g_error = keep;
+        return r;
+    }
+    *out = R;
+    return AK_OK;
+}
+
+int ak_refined_destroy(ak_refined *R) {
+    if (!R) return AK_OK;
+    refined_release(R);
+    delete R;
+    return AK_OK;
+}
+
+ak_case *ak_refined_level(ak_refined *R, int32_t level) {
+    if (!R) return nullptr;
+    return level == 0 ? R->coarse : (level == 1 ? R->fine : nullptr);
+}
+
+int ak_refined_init_perturbed(ak_refined *R, double amp, double phase_y, double phase_z, double lead_x,
+                              double lead_y) {
+    if (!R) return fail(AK_ERR_INVALID, "null case");
+    return with_storage(R->coarse, [&](auto *tag) {
+        return refined_init<std::remove_pointer_t<decltype(tag)>>(R, amp, phase_y, phase_z, lead_x, lead_y);
+    });
+}
+
+int ak_refined_step(ak_refined *R, int32_t nsteps, double *loads) {
+    if (!R) return fail(AK_ERR_INVALID, "null case");
+    if (nsteps < 1) return fail(AK_ERR_INVALID, "nsteps must be >= 1");
+    cudaStream_t st = R->coarse->stream;
+    AK_CUDA(cudaMemsetAsync(R->d_flag, 0, sizeof(int), st));
+    for (int s = 0; s < nsteps; ++s)
+        AK_TRY(with_storage(R->coarse, [&](auto *tag) { return refined_step<std::remove_pointer_t<decltype(tag)>>(R); }));
+    int flag = 0;
+    AK_CUDA(cudaMemcpyAsync(&flag, R->d_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    const int n = R->fine->n_elements;
+    std::vector<double> two((size_t)10 * std::max(1, n));
+    if (loads) AK_CUDA(cudaMemcpyAsync(two.data(), R->d_loads, sizeof(double) * 10 * n, cudaMemcpyDeviceToHost, st));
+    AK_CUDA(cudaStreamSynchronize(st));
+    if (flag) {
+        std::string why = (flag & XF_NEGATIVE) ? "negative physical populations" :
+                          (flag & XF_MACH) ? "local lattice Mach above 0.3" : "nonpositive density";
+        return fail(AK_ERR_GUARD, "Refined transfer failed: " + why);
+    }
+    if (loads)
+        for (int k = 0; k < 5 * n; ++k) loads[k] = two[k] + two[5 * n + k];
+    return AK_OK;
+}
+
+int64_t ak_refined_steps_done(const ak_refined *R) { return R ? R->steps : -1; }
 
 }  // extern "C"

@@ -145,6 +145,39 @@ int ak_get_flags(ak_case *c, uint8_t *flags);
  * planar link), q[k] the Bouzidi fraction (-1 = half-way fallback). */
 int ak_get_wall_links(ak_case *c, int32_t *rows, double *q);
 
+/* ---- two-level (2:1) refined case: refined_solver.py:115-345 and
+ * interface.py:133-352.  One coarse lattice with the legacy outer boundary
+ * and a fine block (2x resolution, walls on the fine level) over the box;
+ * each coarse step runs two fine steps with time-interpolated donors,
+ * face-flux reflux and restriction. */
+typedef struct ak_refined ak_refined;
+
+typedef struct {
+    ak_case_desc coarse;         /* the uniform plan of the coarse level (legacy farfield) */
+    double tau_shear, tau_bulk;  /* coarse relaxation times (refined_solver.py:77-78) */
+    double dt_coarse;            /* coarse time step in convective units */
+    double span;                 /* periodic span in chord units */
+    int32_t box_lower[3], box_upper[3];  /* fine box in coarse cells; z spans the whole span */
+} ak_refined_desc;
+
+/* RefinedSolver construction (refined_solver.py:116-162). */
+int ak_refined_create(const ak_refined_desc *desc, ak_refined **out);
+int ak_refined_destroy(ak_refined *r);
+/* initialize_flow (refined_solver.py:224-269): free stream everywhere, the
+ * seeded perturbation on both levels, covered coarse cells restricted from
+ * the fine level, outflow history from that state. */
+int ak_refined_init_perturbed(ak_refined *r, double amp, double phase_y, double phase_z, double lead_x,
+                              double lead_y);
+/* nsteps coarse steps (PeriodicRefinedBox._step_once, interface.py:311-352);
+ * loads[n_elements * 5] = fine-lattice (Fx, Fy, Fz, Mz, mass) of the last
+ * coarse step summed over its two fine steps (walls.py:68-95), Mz about the
+ * normalised frame's origin in fine lattice units. */
+int ak_refined_step(ak_refined *r, int32_t nsteps, double *loads);
+int64_t ak_refined_steps_done(const ak_refined *r);
+/* The level's lattice (0 coarse, 1 fine block) for ak_get_pdf / ak_macros /
+ * ak_get_wall_links; owned by the refined case. */
+ak_case *ak_refined_level(ak_refined *r, int32_t level);
+
 /* Message of the last failure on this thread ("" if none). */
 const char *ak_last_error(void);
 /* Library build identification, e.g. "aerokinetic_gb300 sm_103a". */

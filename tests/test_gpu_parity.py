@@ -208,3 +208,54 @@ def test_precision_forms_track_fp64(storage, inst_tol, mean_tol):
     finally:
         ref.close()
         low.close()
+
+
+# ---------------------------------------------------------------- two levels
+def refined_pair(record, steps_needed=0):
+    from aerokinetic_gb300.refined import RefinedSolver
+    from aerokinetic_gb300.refined_plan import load_refined_project
+    from oracle.refined import RefinedCase
+    project, refinement = load_refined_project(record["project"])
+    solver = RefinedSolver(project, refinement)
+    plan = solver.plan
+    sec, flow = project.section, project.flow
+    lead = O.leading_edge([e.xy for e in sec.elements], sec.moment_reference, sec.chord, flow.alpha_deg)
+    oracle = RefinedCase([c.xy for c in sec.normalized(flow.alpha_deg)], plan.shape, plan.origin,
+                         plan.coarse_level.dx, plan.coarse_level.dt, plan.coarse_level.tau_shear,
+                         plan.coarse_level.tau_bulk, plan.box.lower, plan.box.upper, flow.lattice_speed,
+                         flow.perturbation, flow.seed, lead, plan.span, oracle_threads())
+    return solver, oracle
+
+
+def test_refined_levels_match_oracle(golden):
+    """Both levels' populations and the loads after each of 3 coarse steps."""
+    solver, oracle = refined_pair(golden["histories"]["refined_startup"])
+    try:
+        pad = oracle.pad
+        coarse, fine = solver.states()
+        np.testing.assert_allclose(coarse, oracle.coarse.interior(), rtol=0, atol=1e-14)
+        np.testing.assert_allclose(fine, oracle.fine.interior()[oracle.fine_slices], rtol=0, atol=1e-14)
+        for s in range(1, 4):
+            mine, theirs = solver.step(), oracle.step()
+            for k in ("cl", "cd", "cm"):
+                assert mine[k] == pytest.approx(theirs[k], abs=2e-10), (s, k)
+            coarse, fine = solver.states()
+            assert np.abs(coarse - oracle.coarse.interior()).max() <= 2e-12 * s
+            assert np.abs(fine - oracle.fine.interior()[oracle.fine_slices]).max() <= 2e-12 * s
+    finally:
+        solver.close()
+
+
+def test_refined_startup_history_on_gpu(golden):
+    from aerokinetic_gb300.refined import RefinedSolver
+    from aerokinetic_gb300.refined_plan import load_refined_project
+    record = golden["histories"]["refined_startup"]
+    project, refinement = load_refined_project(record["project"])
+    solver = RefinedSolver(project, refinement)
+    try:
+        for row in record["history"]:
+            loads = solver.advance(row["step"] - solver.steps)
+            for k in ("cl", "cd", "cm"):
+                assert loads[k] == pytest.approx(row[k], abs=1e-11), (row["step"], k)
+    finally:
+        solver.close()
