@@ -241,7 +241,9 @@ def test_refined_levels_match_oracle(golden):
                 assert mine[k] == pytest.approx(theirs[k], abs=2e-10), (s, k)
             coarse, fine = solver.states()
             assert np.abs(coarse - oracle.coarse.interior()).max() <= 2e-12 * s
-            assert np.abs(fine - oracle.fine.interior()[oracle.fine_slices]).max() <= 2e-12 * s
+            # solid cells hold no state the fluid reads (the engine leaves them unstreamed)
+            fluid = (oracle.fine.flags[1:-1, 1:-1, 1:-1] == 0)[oracle.fine_slices]
+            assert np.abs(fine - oracle.fine.interior()[oracle.fine_slices])[fluid].max() <= 2e-12 * s
     finally:
         solver.close()
 
