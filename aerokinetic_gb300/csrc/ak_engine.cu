@@ -1073,10 +1073,13 @@ int refined_step(ak_refined *R) {
     dim3 gf((unsigned)blocks_for(F->nx, 128), (unsigned)F->ny, (unsigned)F->nz);
     const Rescale c2f{R->tau_s_f * R->dt_f / (R->tau_s_c * R->dt_c), R->tau_b_f * R->dt_f / (R->tau_b_c * R->dt_c)};
     const Rescale f2c{R->tau_s_c * R->dt_c / (R->tau_s_f * R->dt_f), R->tau_b_c * R->dt_c / (R->tau_b_f * R->dt_f)};
+    mark(C);  // step start
     // donors before the coarse step
     k_block_moments<S><<<(unsigned)blocks3(nblock), 256, 0, st>>>(src_of<S>(C), C->G, B, R->d_free, R->mom_old,
                                                                    R->d_flag);
+    mark(C);
     k_collide<S><<<gc, 128, 0, st>>>(src_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s, (T)C->omega_b);
+    mark(C);
     k_face_flux_coarse<S><<<dim3((unsigned)blocks3(R->max_face), R->nfaces), 256, 0, st>>>(
         src_of<S>(C), C->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs,
         R->dx_c * R->dx_c * R->dx_c, R->reg_c);
@@ -1086,7 +1089,9 @@ int refined_step(ak_refined *R) {
     if (C->n_out)
         k_outflow<S><<<(unsigned)blocks3(C->n_out), 256, 0, st>>>(src_of<S>(C), C->G, C->outer(), C->sel_out,
                                                                   C->n_out, C->out_state, 1, 0, 0);
+    mark(C);
     k_stream<S><<<gc, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, 0);
+    mark(C);
     AK_CUDA(cudaGetLastError());
     C->cur = 1 - C->cur;
     // donors after the coarse step
@@ -1099,7 +1104,9 @@ int refined_step(ak_refined *R) {
     for (int sub = 0; sub < 2; ++sub) {
         k_donors<S><<<(unsigned)blocks3(nfine), 256, 0, st>>>(src_of<S>(F), F->G, B, C->nz, R->mom_old, R->mom_new,
                                                               sub / 2.0, c2f, R->pad, R->d_flag);
+        mark(C);
         k_collide<S><<<gf, 128, 0, st>>>(src_of<S>(F), F->flags, F->G, F->shift_host, (T)F->omega_s, (T)F->omega_b);
+        mark(C);
         k_face_flux_fine<S><<<dim3((unsigned)blocks3(R->max_face), R->nfaces), 256, 0, st>>>(
             src_of<S>(F), F->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs, R->pad,
             R->dx_f * R->dx_f * R->dx_f, R->reg_f);
@@ -1108,7 +1115,9 @@ int refined_step(ak_refined *R) {
                                                      F->n_elements, F->ox, F->oy, F->partials);
             k_sum_partials<<<1, 64, 0, st>>>(F->partials, (int)nb, 5 * F->n_elements, R->d_loads + sub * 5 * F->n_elements);
         }
+        mark(C);
         k_stream<S><<<gf, 128, 0, st>>>(src_of<S>(F), dst_of<S>(F), F->flags, F->G, 1);
+        mark(C);
         AK_CUDA(cudaGetLastError());
         F->cur = 1 - F->cur;
     }
@@ -1118,6 +1127,8 @@ int refined_step(ak_refined *R) {
     k_restrict<S, S><<<(unsigned)blocks3((long long)B.bx * B.by * B.bz), 256, 0, st>>>(
         src_of<S>(C), C->G, src_of<S>(F), F->G, B, R->pad, R->d_free, f2c, R->d_flag);
     AK_CUDA(cudaGetLastError());
+    mark(C);  // step end
+    C->launches += 6 + 6 * 2 + (C->n_ubb ? 1 : 0) + (C->n_out ? 1 : 0) + (nlinks ? 0 : -4) + 1;
     C->steps += 1;
     F->steps += 2;
     R->steps += 1;
@@ -1308,5 +1319,42 @@ int ak_refined_step(ak_refined *R, int32_t nsteps, double *loads) {
 }
 
 int64_t ak_refined_steps_done(const ak_refined *R) { return R ? R->steps : -1; }
+
+int ak_refined_step_timed(ak_refined *R, int32_t nsteps, double *ms) {
+    if (!R || nsteps < 1 || !ms) return fail(AK_ERR_INVALID, "a case, nsteps >= 1 and an output array are required");
+    ak_case *C = R->coarse;
+    std::vector<cudaEvent_t> events;
+    C->timing = &events;
+    int r = AK_OK;
+    for (int s = 0; s < nsteps && r == AK_OK; ++s)
+        r = with_storage(C, [&](auto *tag) { return refined_step<std::remove_pointer_t<decltype(tag)>>(R); });
+    C->timing = nullptr;
+    const cudaError_t e = cudaStreamSynchronize(C->stream);
+    for (int k = 0; k < 6; ++k) ms[k] = 0.0;
+    // per step: start, cc0, cc1, cs0, cs1, (fc0, fc1, fs0, fs1) x 2, end = 14 marks
+    if (r == AK_OK && e == cudaSuccess && events.size() == (size_t)14 * nsteps) {
+        float t = 0.0f;
+        for (int s = 0; s < nsteps; ++s) {
+            cudaEvent_t *ev = events.data() + 14 * s;
+            cudaEventElapsedTime(&t, ev[0], ev[13]);
+            ms[0] += t;
+            cudaEventElapsedTime(&t, ev[1], ev[2]);
+            ms[1] += t;  // coarse collide
+            cudaEventElapsedTime(&t, ev[3], ev[4]);
+            ms[2] += t;  // coarse stream
+            for (int sub = 0; sub < 2; ++sub) {
+                cudaEventElapsedTime(&t, ev[5 + 4 * sub], ev[6 + 4 * sub]);
+                ms[3] += t;  // fine collide
+                cudaEventElapsedTime(&t, ev[7 + 4 * sub], ev[8 + 4 * sub]);
+                ms[4] += t;  // fine stream
+            }
+        }
+        ms[5] = ms[0] - ms[1] - ms[2] - ms[3] - ms[4];  // transfers, fluxes, boundaries, walls
+    }
+    for (cudaEvent_t ev : events) cudaEventDestroy(ev);
+    if (r != AK_OK) return r;
+    AK_CUDA(e);
+    return AK_OK;
+}
 
 }  // extern "C"

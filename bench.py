@@ -1,12 +1,17 @@
 """Benchmark: D3Q27 cumulant step throughput (MLUPS) and its HBM roofline.
 
-Workload: the uniform lattice-Mach-0.1 NACA0012 case (384 x 256 x 8 cells, 12 x 8
-chords, leading edge at (128, 128), chord 32 cells, AoA 4 deg, Re 30000,
-characteristic farfield on all x/y faces, seeded 1e-4 perturbation, z periodic).
-The reference's own minimum span is 8 cells, used here so the same case runs
-in both arms.  Inputs are larger than L2 for the FP64 form (2 x 185 MB of
-populations); the reduced-storage forms are timed step by step with an L2
-flush (a 512 MB device write) between steps.
+Headline workload (the two-level case): NACA0012 at AoA 8 deg, Re 30000,
+lattice Mach 0.1; coarse level 512 x 384 x 8 cells (16 x 12 chords, chord 32
+coarse cells), fine level at twice the resolution (chord 64) over
+x in [-0.5c, 2c], y in [-0.6c, 0.6c] around the section: 160 x 76 x 16 fine
+cells.  Legacy outer boundary (the reference's refined solver accepts no
+other), FP64 (the reference's dtype).  MLUPS counts coarse cells + 2 x fine
+cells per coarse step, as the reference does for two-level runs.  Inputs are
+larger than L2 (2 x 686 MB of coarse populations).
+
+Also reported: the reduced-precision forms (FP32 arithmetic with FP32 or FP16
+shifted storage) of the same case, and the uniform 384 x 256 x 8 case with the
+characteristic farfield (the reference's CPU-runnable configuration).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -33,7 +38,9 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "D3Q27 MLUPS & %HBM peak"
 CELLS_PER_CHORD = 32
-WORKLOAD = "uniform NACA0012 384x256x8, chord 32, AoA 4, Re 3e4, Ma 0.1, characteristic farfield"
+WORKLOAD = ("two-level NACA0012, coarse 512x384x8 (chord 32) + fine 160x76x16 (chord 64) over "
+            "x in [-0.5c, 2c], y in [-0.6c, 0.6c], AoA 8, Re 3e4, Ma 0.1, legacy farfield")
+UNIFORM = "uniform NACA0012 384x256x8, chord 32, AoA 4, Re 3e4, Ma 0.1, characteristic farfield"
 BYTES_PER_CELL = {"f64": 27 * 2 * 8, "f32": 27 * 2 * 4, "f16": 27 * 2 * 2}
 
 
@@ -45,6 +52,22 @@ def case_parts():
                 transverse_chords=3.9266, span_chords=0.125, farfield="characteristic_transport_v1",
                 memory_limit_gib=64)
     return section, flow, grid
+
+
+def refined_parts():
+    from aerokinetic_gb300 import Flow, Grid, Project, Section, naca0012
+    from aerokinetic_gb300.refined_plan import RefinementSettings
+    section = Section((naca0012(),))
+    flow = Flow(reynolds=30000, alpha_deg=8, lattice_speed=0.1 / math.sqrt(3))
+    grid = Grid(cells_per_chord=CELLS_PER_CHORD, upstream_chords=5.0, downstream_chords=9.9938,
+                transverse_chords=5.9056, span_chords=0.25, memory_limit_gib=64)
+    refinement = RefinementSettings(upstream_chords=0.5, downstream_chords=1.0, transverse_chords=0.5)
+    return Project(section, flow, grid), refinement
+
+
+def refined_cells(plan):
+    fine = math.prod(2 * n for n in plan.box.shape)
+    return math.prod(plan.shape) + 2 * fine
 
 
 def peaks():
@@ -118,7 +141,7 @@ def cpu_cores():
         return os.cpu_count() or 1
 
 
-def oracle_case(threads):
+def oracle_uniform(threads):
     from aerokinetic_gb300 import Plan
     from oracle import oracle as O
     section, flow, grid = case_parts()
@@ -128,54 +151,69 @@ def oracle_case(threads):
     case = O.AirfoilCase([c.xy for c in section.normalized(flow.alpha_deg)], plan.shape, plan.origin, plan.dx,
                          plan.span, plan.relaxation_rate, flow.lattice_speed, grid.cells_per_chord, grid.farfield,
                          flow.perturbation, flow.seed, lead, threads)
-    return plan, case
+    return math.prod(plan.shape), case
+
+
+def oracle_refined(threads):
+    from aerokinetic_gb300.refined_plan import RefinedPlan
+    from oracle import oracle as O
+    from oracle.refined import RefinedCase
+    project, refinement = refined_parts()
+    plan = RefinedPlan.create(project, refinement)
+    sec, flow = project.section, project.flow
+    lead = O.leading_edge([e.xy for e in sec.elements], sec.moment_reference, sec.chord, flow.alpha_deg)
+    case = RefinedCase([c.xy for c in sec.normalized(flow.alpha_deg)], plan.shape, plan.origin,
+                       plan.coarse_level.dx, plan.coarse_level.dt, plan.coarse_level.tau_shear,
+                       plan.coarse_level.tau_bulk, plan.box.lower, plan.box.upper, flow.lattice_speed,
+                       flow.perturbation, flow.seed, lead, plan.span, threads)
+    return refined_cells(plan), case
 
 
 def oracle_run(case, steps, budget_s):
-    """Up to `steps` oracle steps (loads every 8), stopping after budget_s."""
+    """Up to `steps` oracle steps, stopping after budget_s."""
     done, start = 0, time.perf_counter()
     while done < steps:
         done += 1
-        case.step(sample=done % 8 == 0)
+        case.step()
         if time.perf_counter() - start >= budget_s:
             break
     return done, time.perf_counter() - start
 
 
-def oracle_sample(budget_s=15.0):
-    """The CPU oracle (C restatement, FP64, OpenMP on all host cores) on the
-    same case for a bounded sample of steps; returns MLUPS and the sample."""
+def oracle_sample(budget_s=15.0, refined=True):
+    """The CPU oracle (C restatement + numpy, FP64, OpenMP on all host cores)
+    on the same case for a bounded sample of steps; returns MLUPS and the sample."""
     cores = cpu_cores()
-    plan, case = oracle_case(cores)
-    case.step(sample=True)  # boundary set-up outside the timing
+    cells, case = (oracle_refined if refined else oracle_uniform)(cores)
+    case.step()  # first-step set-up outside the timing
     steps, elapsed = oracle_run(case, 10**9, budget_s)
-    cells = math.prod(plan.shape)
+    what = "two-level" if refined else "uniform"
     return {"value": cells * steps / elapsed / 1e6, "unit": "MLUPS", "cores": cores, "kind": "port",
-            "sample": f"{steps} steps of the same {plan.shape} case on {cores} host threads "
-                      f"(FP64 oracle, loads every 8 steps), {elapsed:.1f} s"}
+            "sample": f"{steps} steps of the same {what} case on {cores} host threads (FP64 oracle), "
+                      f"{elapsed:.1f} s"}
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
     cores = cpu_cores()
-    plan, case = oracle_case(cores)
-    oracle_run(case, args.warmup, 20.0)
+    cells, case = oracle_refined(cores)
+    oracle_run(case, args.warmup, 30.0)
     steps, elapsed = oracle_run(case, args.steps, 120.0)
-    cells = math.prod(plan.shape)
     value = cells * steps / elapsed / 1e6
-    sample = (f"{steps} of {args.steps} requested steps of the {plan.shape} case on {cores} host threads "
-              f"(FP64 oracle, loads every 8 steps), {elapsed:.1f} s, capped at 120 s")
+    sample = (f"{steps} of {args.steps} requested coarse steps of the two-level case on {cores} host threads "
+              f"(FP64 oracle), {elapsed:.1f} s, capped at 120 s")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "MLUPS", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "engine": "CPU oracle (C restatement of the reference step)",
+            "config": {"workload": WORKLOAD, "engine": "CPU oracle (restatement of the reference step)",
                        "l2": "host run"},
             "cpu_baseline": {"value": value, "unit": "MLUPS", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "reference_as_published": {"value": 20.0, "unit": "MLUPS",
-                                       "note": "lbmpy 1.4 CPU, 1 thread, 176x101x16 (profile_threads1.json)"}}
+            "reference_as_published": {"value": 0.53, "unit": "MLUPS",
+                                       "note": "lbmpy 1.4 CPU two-level step, 1 thread, coarse 128x69x16 + "
+                                               "fine 136x58x32 (BENCHMARK_CPU_CHECK.json)"}}
     print(json.dumps(line), flush=True)
 
 
@@ -186,7 +224,7 @@ def flush_l2(buf, stream):
 
 
 def measure_form(storage, steps, warmup, flush):
-    """Per-step timing of the stream-collide kernel of one storage form."""
+    """Per-step timing of the uniform case's stream-collide kernel in one storage form."""
     import torch
     from aerokinetic_gb300.solver import Solver
     section, flow, grid = case_parts()
@@ -215,102 +253,126 @@ def measure_form(storage, steps, warmup, flush):
 def run_engine(args, rank, world, local_rank):
     import torch
     from aerokinetic_gb300 import _native
+    from aerokinetic_gb300.refined import RefinedSolver
     from aerokinetic_gb300.solver import Solver
     torch.cuda.set_device(local_rank)
     dist = None
     if world > 1:
         import torch.distributed as dist
     lib = _native.load()
-    section, flow, grid = case_parts()
+    project, refinement = refined_parts()
 
-    # ---- headline: plain FP64 form, K steps in the timed region
-    solver = Solver(section, flow, grid, storage="f64")
-    case = solver._case
-    ms = np.zeros(4)
+    # ---- headline: the two-level case in FP64, K coarse steps in the timed region
+    solver = RefinedSolver(project, refinement, storage="f64")
+    plan = solver.plan
+    cells = refined_cells(plan)
+    ms = np.zeros(6)
     ptr = ms.ctypes.data_as(ctypes.c_void_p)
-    _native.check(lib.ak_step_timed(case, max(3, args.warmup), ptr))
+    _native.check(lib.ak_refined_step_timed(solver._handle, max(3, args.warmup), ptr))
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    launches0 = lib.ak_kernel_launches(case)
+    launches0 = lib.ak_kernel_launches(solver._coarse)
     with ClockSampler(local_rank) as clocks:
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
         ms[:] = 0
-        _native.check(lib.ak_step_timed(case, args.steps, ptr))
+        _native.check(lib.ak_refined_step_timed(solver._handle, args.steps, ptr))
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
-    launches = lib.ak_kernel_launches(case) - launches0
+    launches = lib.ak_kernel_launches(solver._coarse) - launches0
     elapsed_ms = float(ms[0])
-    bulk_ms = float(ms[1]) / args.steps
+    groups = {"coarse_collide_ms": ms[1] / args.steps, "coarse_stream_ms": ms[2] / args.steps,
+              "fine_collide_ms": ms[3] / args.steps, "fine_stream_ms": ms[4] / args.steps,
+              "interface_and_boundaries_ms": ms[5] / args.steps}
     if dist:
         t = torch.tensor([elapsed_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed_ms = float(t.item())
-    info = solver.info
-    cells = info["cells"]
     value = world * cells * args.steps / (elapsed_ms / 1e3) / 1e6
+    fine_padded = math.prod(n for n in (2 * plan.box.shape[0] + 4, 2 * plan.box.shape[1] + 4, 2 * plan.box.shape[2]))
+    coarse_cells = math.prod(plan.shape)
     solver.close()
     if rank != 0:
         return
+    hbm, peak_kind = peaks()
+    # the collision launches of one coarse step (one coarse, two fine), read and
+    # written once each
+    collide_bytes = (coarse_cells + 2 * fine_padded) * BYTES_PER_CELL["f64"]
+    collide_ms = groups["coarse_collide_ms"] + groups["fine_collide_ms"]
+    achieved = collide_bytes / (collide_ms / 1e3) / 1e9
 
     # ---- end to end through the public API: case set-up from the host
-    # description, the reference's compute loop (loads every 8 steps plus
-    # diagnostics), results back on the host
-    e2e_steps = max(64, min(args.steps, 2000))
+    # description, every coarse step returning its loads to the host
+    e2e_steps = max(32, min(args.steps, 500))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    s = Solver(section, flow, grid, storage="f64")
-    samples = 0
-    for i in range(e2e_steps // 8):
-        s.advance(8, sample_last=True)
-        s.diagnostics()
-        samples += 1
+    s = RefinedSolver(project, refinement, storage="f64")
+    for _ in range(e2e_steps):
+        s.step()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     s.close()
-    h2d = 8 * sum(len(c.xy) * 2 for c in section.normalized(flow.alpha_deg)) + 128
-    d2h = samples * (5 * 8 + 5 * 8)
+    h2d = 8 * sum(len(c.xy) * 2 for c in project.section.normalized(project.flow.alpha_deg)) + 256
 
-    # ---- the reduced-storage forms, step by step with an L2 flush
+    # ---- reduced-precision forms of the two-level case
     forms = {}
-    hbm, peak_kind = peaks()
+    for storage in ("f32", "f16"):
+        r = RefinedSolver(project, refinement, storage=storage)
+        m = np.zeros(6)
+        _native.check(lib.ak_refined_step_timed(r._handle, max(3, args.warmup), m.ctypes.data_as(ctypes.c_void_p)))
+        m[:] = 0
+        k = min(args.steps, 400)
+        _native.check(lib.ak_refined_step_timed(r._handle, k, m.ctypes.data_as(ctypes.c_void_p)))
+        r.close()
+        cb = (coarse_cells + 2 * fine_padded) * BYTES_PER_CELL[storage]
+        cms = (m[1] + m[3]) / k
+        forms[storage] = {"mlups": cells * k / (m[0] / 1e3) / 1e6, "ms_per_step": m[0] / k,
+                          "collide_achieved_gbs": cb / (cms / 1e3) / 1e9,
+                          "collide_frac_of_" + peak_kind: cb / (cms / 1e3) / 1e9 / hbm,
+                          "groups_ms": {"coarse_collide": m[1] / k, "coarse_stream": m[2] / k,
+                                        "fine_collide": m[3] / k, "fine_stream": m[4] / k,
+                                        "interface_and_boundaries": m[5] / k}}
+
+    # ---- the uniform case (the reference's CPU-runnable configuration)
+    uniform = {}
     for storage in ("f64", "f32", "f16"):
         m = measure_form(storage, steps=min(args.steps, 100), warmup=args.warmup, flush=True)
         bytes_launch = m["fluid_cells"] * BYTES_PER_CELL[storage]
-        achieved = bytes_launch / (m["bulk_ms"] / 1e3) / 1e9
-        forms[storage] = {"mlups": m["cells"] / (m["step_ms"] / 1e3) / 1e6,
-                          "kernel_mlups": m["cells"] / (m["bulk_ms"] / 1e3) / 1e6,
-                          "bulk_kernel_ms": m["bulk_ms"], "achieved_gbs": achieved,
-                          "frac_of_" + peak_kind: achieved / hbm, "bytes_per_cell": BYTES_PER_CELL[storage]}
+        a = bytes_launch / (m["bulk_ms"] / 1e3) / 1e9
+        uniform[storage] = {"mlups": m["cells"] / (m["step_ms"] / 1e3) / 1e6,
+                            "kernel_mlups": m["cells"] / (m["bulk_ms"] / 1e3) / 1e6,
+                            "stream_collide_ms": m["bulk_ms"], "achieved_gbs": a, "frac_of_" + peak_kind: a / hbm}
 
-    bytes_launch = info["fluid_cells"] * BYTES_PER_CELL["f64"]
-    achieved = bytes_launch / (bulk_ms / 1e3) / 1e9
     traffic = None
-    summary = ROOT / "profiles" / "stream_collide_f64_uniform_384x256x8.txt"
+    summary = ROOT / "profiles" / "collide_f64_refined_512x384x8.txt"
     if summary.exists():
         for line in summary.read_text().splitlines():
             if line.startswith("dram_bytes_per_launch:"):
                 traffic = float(line.split(":", 1)[1].split()[0])
-    cpu = oracle_sample(budget_s=15.0)
+    cpu = oracle_sample(budget_s=15.0, refined=True)
     line = {"metric": METRIC, "value": value, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "cells": cells, "fluid_cells": info["fluid_cells"],
-                       "storage": "f64 populations, two copies (pull A->B)",
-                       "l2": "inputs larger than L2 (2 x 185 MB); reduced forms flushed between steps",
+            "config": {"workload": WORKLOAD, "coarse_cells": coarse_cells,
+                       "fine_cells": math.prod(2 * n for n in plan.box.shape),
+                       "cell_updates_per_step": cells, "storage": "f64 populations, two copies per level",
+                       "l2": "inputs larger than L2 (coarse 2 x 686 MB); uniform forms flushed between steps",
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": "k_stream_collide<double>", "bytes_per_launch": bytes_launch,
-                         "kernel_ms": bulk_ms},
+                         "kernel": "k_collide<double> (one coarse + two fine launches per coarse step)",
+                         "bytes_per_launch": collide_bytes / 3, "kernel_ms": collide_ms / 3,
+                         "limit": "FP64 pipe (GB300 issues 2 FP64 instructions per clock per SM)"},
+            "groups_ms": groups,
             "forms": forms,
+            "uniform": {"workload": UNIFORM, **uniform},
             "cpu_baseline": cpu,
             "e2e": {"value": cells * e2e_steps / e2e_s / 1e6, "unit": "MLUPS", "steps": e2e_steps,
-                    "h2d_bytes_per_step": h2d / e2e_steps, "d2h_bytes_per_step": d2h / e2e_steps,
-                    "includes": "case set-up from host description, loads + diagnostics every 8 steps"},
+                    "h2d_bytes_per_step": h2d / e2e_steps, "d2h_bytes_per_step": 5 * 8 + 4,
+                    "includes": "case set-up from the host description, loads to the host every coarse step"},
             "gpu_launches": int(launches),
             "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)

@@ -174,6 +174,12 @@ int ak_refined_init_perturbed(ak_refined *r, double amp, double phase_y, double 
  * normalised frame's origin in fine lattice units. */
 int ak_refined_step(ak_refined *r, int32_t nsteps, double *loads);
 int64_t ak_refined_steps_done(const ak_refined *r);
+/* ak_refined_step without loads, timed with CUDA events on the case's stream:
+ * ms[0] whole interval, ms[1] coarse collide, ms[2] coarse stream, ms[3] fine
+ * collides, ms[4] fine streams, ms[5] the rest (interface transfers, face
+ * fluxes, boundaries, walls), milliseconds summed over the steps.  No
+ * counterpart in the reference; it exists for measurement. */
+int ak_refined_step_timed(ak_refined *r, int32_t nsteps, double *ms);
 /* The level's lattice (0 coarse, 1 fine block) for ak_get_pdf / ak_macros /
  * ak_get_wall_links; owned by the refined case. */
 ak_case *ak_refined_level(ak_refined *r, int32_t level);
