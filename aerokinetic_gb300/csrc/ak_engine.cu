@@ -71,6 +71,8 @@ struct ak_case {
     long long nouter = 0;
     int *sel_ubb = nullptr, *sel_out = nullptr;
     long long n_ubb = 0, n_out = 0;
+    int *ubb_cells = nullptr;  // (padded x, padded y, direction mask) per UBB cell
+    long long n_ubb_cells = 0;
     double *out_state = nullptr;
     double *ff_in = nullptr, *ff_der = nullptr;
     long long *ff_clock = nullptr;
@@ -129,8 +131,8 @@ int upload(ak_case *c, T **p, const std::vector<T> &v) {
 void release(ak_case *c) {
     void *ptrs[] = {c->pdf[0], c->pdf[1], c->flags, c->d_poly, c->d_start, c->d_count, c->keys, c->wall_q,
                     c->ox_, c->oy_, c->oz_, c->od, c->oobj, c->oedge, c->sel_ubb, c->sel_out, c->out_state,
-                    c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, c->partials, c->reduced, c->staging,
-                    c->d_ff, c->d_shift, c->ring_ru, c->ring_lr};
+                    c->ubb_cells, c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, c->partials, c->reduced,
+                    c->staging, c->d_ff, c->d_shift, c->ring_ru, c->ring_lr};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -273,6 +275,29 @@ int build_outer(ak_case *c, const std::vector<uint8_t> &hflags) {
     if (c->farfield == AK_FARFIELD_LEGACY) {
         c->n_ubb = (long long)sel_ubb.size();
         c->n_out = (long long)sel_out.size();
+        // the UBB links grouped by cell, face by face (coalesced along a face)
+        std::vector<int> cells;
+        auto ubb_cell = [&](int x, int y) {
+            if (hflags[(size_t)(y + 1) * nxp + (x + 1)] != FLAG_FLUID) return;
+            int mask = 0;
+            for (int d = 1; d < Q; ++d) {
+                const int gx = x + cx(d), gy = y + cy(d);
+                if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) continue;
+                if (gx < nx) mask |= 1 << d;
+            }
+            if (!mask) return;
+            cells.push_back(x + 1);
+            cells.push_back(y + 1);
+            cells.push_back(mask);
+        };
+        for (int x = 0; x < nx; ++x) ubb_cell(x, 0);
+        if (ny > 1)
+            for (int x = 0; x < nx; ++x) ubb_cell(x, ny - 1);
+        for (int y = 1; y < ny - 1; ++y) ubb_cell(0, y);
+        if (nx > 1)
+            for (int y = 1; y < ny - 1; ++y) ubb_cell(nx - 1, y);
+        c->n_ubb_cells = (long long)cells.size() / 3;
+        AK_TRY(upload(c, &c->ubb_cells, cells));
         AK_TRY(upload(c, &c->sel_ubb, sel_ubb));
         AK_TRY(upload(c, &c->sel_out, sel_out));
         AK_TRY(dalloc(c, &c->out_state, (size_t)(2 * c->n_out)));
@@ -422,8 +447,8 @@ int one_step(ak_case *c, bool sample, double *fixed_partials = nullptr, long lon
     // installation order; the outflow reads ghost values the UBB just wrote
     if (c->farfield == AK_FARFIELD_LEGACY) {
         if (c->n_ubb) {
-            k_ubb<S><<<(unsigned)blocks_for(c->n_ubb, TB), TB, 0, c->stream>>>(src, c->G, c->outer(), c->sel_ubb,
-                                                                               c->n_ubb, c->speed, 0.0, 0.0);
+            k_ubb<S><<<(unsigned)blocks_for(c->n_ubb_cells * c->nz, TB), TB, 0, c->stream>>>(
+                src, c->G, c->ubb_cells, c->n_ubb_cells, c->speed, 0.0, 0.0);
             AK_CUDA(cudaGetLastError());
             ++c->launches;
         }
@@ -472,7 +497,7 @@ int one_step(ak_case *c, bool sample, double *fixed_partials = nullptr, long lon
         AK_CUDA(cudaGetLastError());
         ++c->launches;
         if (sample) {
-            k_sum_partials<<<1, 64, 0, c->stream>>>(partials, (int)nb, 5 * c->n_elements, c->reduced);
+            k_sum_partials<<<5 * c->n_elements, 32, 0, c->stream>>>(partials, (int)nb, 5 * c->n_elements, c->reduced);
             AK_CUDA(cudaGetLastError());
             ++c->launches;
         }
@@ -939,7 +964,8 @@ struct ak_refined {
     double tau_s_c = 0, tau_b_c = 0, tau_s_f = 0, tau_b_f = 0;
     double free_g[Q];
     double *d_free = nullptr;
-    double *mom_old = nullptr, *mom_new = nullptr;
+    double *mom_old = nullptr, *mom_new = nullptr, *mom_half = nullptr;
+    double *pro_x = nullptr, *pro_xy = nullptr;  // donor moments after the x and the y prolongation pass
     Face faces[4];
     int nfaces = 0;
     long long offs[4] = {0, 0, 0, 0};
@@ -1023,6 +1049,20 @@ std::vector<FluxTerm> flux_terms(int axis) {
 }
 
 long long blocks3(long long n) { return (n + 255) / 256; }
+// direction-split kernels: 32 cells per 256-thread block
+long long split_blocks(long long cells) { return (cells + SPLIT_CELLS - 1) / SPLIT_CELLS; }
+
+// restriction of the fine block onto the covered coarse cells
+template <typename S>
+void launch_restrict(ak_refined *R, const Rescale &f2c, cudaStream_t st) {
+    const BoxSpec &B = R->B;
+    const long long ring = ring_count(B.bx, B.by, 3, 3) * B.bz;
+    const long long core = (long long)std::max(B.bx - 6, 0) * std::max(B.by - 6, 0) * B.bz;
+    const long long nb = std::max(split_blocks(ring), blocks3(core));
+    k_restrict<S, S><<<dim3((unsigned)nb, 2), SPLIT_THREADS, 0, st>>>(src_of<S>(R->coarse), R->coarse->G,
+                                                                       src_of<S>(R->fine), R->fine->G, B, R->pad,
+                                                                       R->d_free, f2c, R->d_flag);
+}
 
 template <typename S>
 int refined_init(ak_refined *R, double amp, double phase_y, double phase_z, double lead_x, double lead_y) {
@@ -1043,8 +1083,7 @@ int refined_init(ak_refined *R, double amp, double phase_y, double phase_z, doub
     }
     const Rescale f2c{R->tau_s_c * R->dt_c / (R->tau_s_f * R->dt_f), R->tau_b_c * R->dt_c / (R->tau_b_f * R->dt_f)};
     AK_CUDA(cudaMemsetAsync(R->d_flag, 0, sizeof(int), st));
-    k_restrict<S, S><<<(unsigned)blocks3((long long)R->B.bx * R->B.by * R->B.bz), 256, 0, st>>>(
-        src_of<S>(C), C->G, src_of<S>(F), F->G, R->B, R->pad, R->d_free, f2c, R->d_flag);
+    launch_restrict<S>(R, f2c, st);
     AK_CUDA(cudaGetLastError());
     // boundary data from the initial state, ghosts still holding the free
     // stream (refined_solver.py:224-262)
@@ -1068,24 +1107,24 @@ int refined_step(ak_refined *R) {
     ak_case *C = R->coarse, *F = R->fine;
     cudaStream_t st = C->stream;
     const BoxSpec &B = R->B;
-    const long long nblock = (long long)B.dnx * B.dny * C->nz;
+    const long long nring_block = ring_count(B.dnx, B.dny, DONOR_RING, DONOR_RING) * C->nz;
     dim3 gc((unsigned)blocks_for(C->nx, 128), (unsigned)C->ny, (unsigned)C->nz);
     dim3 gf((unsigned)blocks_for(F->nx, 128), (unsigned)F->ny, (unsigned)F->nz);
     const Rescale c2f{R->tau_s_f * R->dt_f / (R->tau_s_c * R->dt_c), R->tau_b_f * R->dt_f / (R->tau_b_c * R->dt_c)};
     const Rescale f2c{R->tau_s_c * R->dt_c / (R->tau_s_f * R->dt_f), R->tau_b_c * R->dt_c / (R->tau_b_f * R->dt_f)};
     mark(C);  // step start
     // donors before the coarse step
-    k_block_moments<S><<<(unsigned)blocks3(nblock), 256, 0, st>>>(src_of<S>(C), C->G, B, R->d_free, R->mom_old,
-                                                                   R->d_flag);
+    k_block_moments<S><<<(unsigned)split_blocks(nring_block), SPLIT_THREADS, 0, st>>>(
+        src_of<S>(C), C->G, B, R->d_free, R->mom_old, nullptr, nullptr, R->d_flag);
     mark(C);
     k_collide<S><<<gc, 128, 0, st>>>(src_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s, (T)C->omega_b);
     mark(C);
-    k_face_flux_coarse<S><<<dim3((unsigned)blocks3(R->max_face), R->nfaces), 256, 0, st>>>(
+    k_face_flux_coarse<S><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, st>>>(
         src_of<S>(C), C->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs,
         R->dx_c * R->dx_c * R->dx_c, R->reg_c);
     if (C->n_ubb)
-        k_ubb<S><<<(unsigned)blocks3(C->n_ubb), 256, 0, st>>>(src_of<S>(C), C->G, C->outer(), C->sel_ubb, C->n_ubb,
-                                                              C->speed, 0.0, 0.0);
+        k_ubb<S><<<(unsigned)blocks3(C->n_ubb_cells * C->nz), 256, 0, st>>>(src_of<S>(C), C->G, C->ubb_cells,
+                                                                            C->n_ubb_cells, C->speed, 0.0, 0.0);
     if (C->n_out)
         k_outflow<S><<<(unsigned)blocks3(C->n_out), 256, 0, st>>>(src_of<S>(C), C->G, C->outer(), C->sel_out,
                                                                   C->n_out, C->out_state, 1, 0, 0);
@@ -1095,25 +1134,33 @@ int refined_step(ak_refined *R) {
     AK_CUDA(cudaGetLastError());
     C->cur = 1 - C->cur;
     // donors after the coarse step
-    k_block_moments<S><<<(unsigned)blocks3(nblock), 256, 0, st>>>(src_of<S>(C), C->G, B, R->d_free, R->mom_new,
-                                                                   R->d_flag);
+    k_block_moments<S><<<(unsigned)split_blocks(nring_block), SPLIT_THREADS, 0, st>>>(
+        src_of<S>(C), C->G, B, R->d_free, R->mom_new, R->mom_old, R->mom_half, R->d_flag);
     AK_CUDA(cudaMemsetAsync(R->reg_f, 0, sizeof(double) * R->reg_doubles, st));
-    const long long nfine = (long long)F->nx * F->ny * F->nz;
+    const long long nband = ring_count(F->nx, F->ny, R->pad, R->pad) * F->nz;
+    const long long nprox = ring_count(F->nx, B.dny, R->pad, DONOR_RING) * C->nz;
+    const long long nproxy = ring_count(F->nx, F->ny, R->pad, R->pad) * C->nz;
     const long long nlinks = F->nkeys * F->nz * 3;
     const long long nb = blocks_for(nlinks, 256);
     for (int sub = 0; sub < 2; ++sub) {
-        k_donors<S><<<(unsigned)blocks3(nfine), 256, 0, st>>>(src_of<S>(F), F->G, B, C->nz, R->mom_old, R->mom_new,
-                                                              sub / 2.0, c2f, R->pad, R->d_flag);
+        // donor moments at the fine step's start: the old coarse state, then
+        // half-way (1 - 1/2) old + 1/2 new (refined_solver.py:311-318)
+        k_prolong_x<<<(unsigned)blocks3(nprox), 256, 0, st>>>(B, C->nz, R->pad, sub ? R->mom_half : R->mom_old,
+                                                               R->pro_x);
+        k_prolong_y<<<(unsigned)blocks3(nproxy), 256, 0, st>>>(B, C->nz, R->pad, R->pro_x, R->pro_xy);
+        k_donors<S><<<(unsigned)split_blocks(nband), SPLIT_THREADS, 0, st>>>(src_of<S>(F), F->G, C->nz, R->pro_xy,
+                                                                             c2f, R->pad, R->d_flag);
         mark(C);
         k_collide<S><<<gf, 128, 0, st>>>(src_of<S>(F), F->flags, F->G, F->shift_host, (T)F->omega_s, (T)F->omega_b);
         mark(C);
-        k_face_flux_fine<S><<<dim3((unsigned)blocks3(R->max_face), R->nfaces), 256, 0, st>>>(
+        k_face_flux_fine<S><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, st>>>(
             src_of<S>(F), F->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs, R->pad,
             R->dx_f * R->dx_f * R->dx_f, R->reg_f);
         if (nlinks) {
             k_walls<S><<<(unsigned)nb, 256, 0, st>>>(src_of<S>(F), F->G, F->keys, F->wall_q, F->nkeys, 1,
                                                      F->n_elements, F->ox, F->oy, F->partials);
-            k_sum_partials<<<1, 64, 0, st>>>(F->partials, (int)nb, 5 * F->n_elements, R->d_loads + sub * 5 * F->n_elements);
+            k_sum_partials<<<5 * F->n_elements, 32, 0, st>>>(F->partials, (int)nb, 5 * F->n_elements,
+                                                              R->d_loads + sub * 5 * F->n_elements);
         }
         mark(C);
         k_stream<S><<<gf, 128, 0, st>>>(src_of<S>(F), dst_of<S>(F), F->flags, F->G, 1);
@@ -1121,14 +1168,13 @@ int refined_step(ak_refined *R) {
         AK_CUDA(cudaGetLastError());
         F->cur = 1 - F->cur;
     }
-    k_reflux<S><<<dim3((unsigned)blocks3(R->max_face), R->nfaces), 256, 0, st>>>(
+    k_reflux<S><<<dim3((unsigned)split_blocks(R->max_face), R->nfaces), SPLIT_THREADS, 0, st>>>(
         src_of<S>(C), C->G, R->d_faces, R->nfaces, R->d_offs, R->reg_c, R->reg_f,
         1.0 / (R->dx_c * R->dx_c * R->dx_c), R->d_flag);
-    k_restrict<S, S><<<(unsigned)blocks3((long long)B.bx * B.by * B.bz), 256, 0, st>>>(
-        src_of<S>(C), C->G, src_of<S>(F), F->G, B, R->pad, R->d_free, f2c, R->d_flag);
+    launch_restrict<S>(R, f2c, st);
     AK_CUDA(cudaGetLastError());
     mark(C);  // step end
-    C->launches += 6 + 6 * 2 + (C->n_ubb ? 1 : 0) + (C->n_out ? 1 : 0) + (nlinks ? 0 : -4) + 1;
+    C->launches += 6 + 8 * 2 + (C->n_ubb ? 1 : 0) + (C->n_out ? 1 : 0) + (nlinks ? 0 : -4) + 1;
     C->steps += 1;
     F->steps += 2;
     R->steps += 1;
@@ -1217,6 +1263,9 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
     const long long nblock = (long long)B.dnx * B.dny * cd.nz;
     if (r == AK_OK) r = ralloc(R, &R->mom_old, (size_t)nblock * 10);
     if (r == AK_OK) r = ralloc(R, &R->mom_new, (size_t)nblock * 10);
+    if (r == AK_OK) r = ralloc(R, &R->mom_half, (size_t)nblock * 10);
+    if (r == AK_OK) r = ralloc(R, &R->pro_x, (size_t)(2 * B.bx + 2 * R->pad) * B.dny * cd.nz * 10);
+    if (r == AK_OK) r = ralloc(R, &R->pro_xy, (size_t)(2 * B.bx + 2 * R->pad) * (2 * B.by + 2 * R->pad) * cd.nz * 10);
     if (r == AK_OK) {
         R->nfaces = 0;
         long long off = 0;

@@ -185,15 +185,18 @@ __global__ void __launch_bounds__(256) k_walls(S *__restrict__ pdf, Grid G, cons
     }
 }
 
-// partials laid out [element][block][5]; one thread per (element, component)
+// partials laid out [element][block][5]; one warp per (element, component):
+// lane-strided sums combined by a fixed butterfly, so the result does not
+// depend on scheduling
 __global__ void k_sum_partials(const double *__restrict__ partials, int nblocks, int nvalues,
                                double *__restrict__ out) {
-    const int t = threadIdx.x;
+    const int t = blockIdx.x, lane = threadIdx.x;
     if (t >= nvalues) return;
     const int e = t / 5, k = t - 5 * (t / 5);
     double s = 0.0;
-    for (int b = 0; b < nblocks; ++b) s += partials[((long long)e * nblocks + b) * 5 + k];
-    out[t] = s;
+    for (int b = lane; b < nblocks; b += 32) s += partials[((long long)e * nblocks + b) * 5 + k];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) out[t] = s;
 }
 
 // ------------------------------------------------------------ outer ring
@@ -205,21 +208,31 @@ struct OuterLinks {
     long long n;
 };
 
-// compressible UBB (solver.py:131): g_inv(x+c) = g_d(x) - 6 (c.U) w_d rho(x)
+// compressible UBB (solver.py:131): g_inv(x+c) = g_d(x) - 6 (c.U) w_d rho(x).
+// One thread per boundary cell and z: cells[3 i] = padded x, cells[3 i + 1] =
+// padded y, cells[3 i + 2] = bit mask of the cell's UBB directions; the
+// density is summed once per cell, in direction order.
 template <typename S>
-__global__ void k_ubb(S *__restrict__ pdf, Grid G, OuterLinks L, const int *__restrict__ selected, long long n,
-                      double ux, double uy, double uz) {
+__global__ void k_ubb(S *__restrict__ pdf, Grid G, const int *__restrict__ cells, long long ncells, double ux,
+                      double uy, double uz) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int li = selected[i];
-    const int x = L.x[li], y = L.y[li], z = L.z[li], d = L.d[li];
-    double drho = 0.0;
+    if (i >= ncells * G.nz) return;
+    const int z = (int)(i / ncells);
+    const long long c = i - (long long)z * ncells;
+    const int x = cells[3 * c], y = cells[3 * c + 1], mask = cells[3 * c + 2];
+    double g[Q], drho = 0.0;
 #pragma unroll
-    for (int q = 0; q < Q; ++q) drho += load_g(pdf, G, q, x, y, z);
+    for (int q = 0; q < Q; ++q) {
+        g[q] = load_g(pdf, G, q, x, y, z);
+        drho += g[q];
+    }
     const double rho = drho + 1.0;
-    const double term = 6.0 * (cx(d) * ux + cy(d) * uy + cz(d) * uz) * weight(d);
-    const double gd = load_g(pdf, G, d, x, y, z);
-    store_g(pdf, G, inv(d), x + cx(d), y + cy(d), G.wrapz(z + cz(d)), gd - term * rho);
+#pragma unroll
+    for (int d = 1; d < Q; ++d) {
+        if (!((mask >> d) & 1)) continue;
+        const double term = 6.0 * (cx(d) * ux + cy(d) * uy + cz(d) * uz) * weight(d);
+        store_g(pdf, G, inv(d), x + cx(d), y + cy(d), G.wrapz(z + cz(d)), g[d] - term * rho);
+    }
 }
 
 // ExtrapolationOutflow (Geier et al. 2015 eq. F.1, normal +x): first-order

@@ -18,6 +18,8 @@
 //                diagonal links split over axis orderings
 // All interface arithmetic is FP64 whatever the population storage.
 #pragma once
+#include <type_traits>
+
 #include "ak_kernels.cuh"
 
 namespace ak {
@@ -30,64 +32,219 @@ __host__ __device__ constexpr int sb(int k) { return k < 3 ? k : (k == 3 ? 1 : 2
 // error flags of the transfer checks
 constexpr int XF_DENSITY = 1, XF_NEGATIVE = 2, XF_MACH = 4, XF_NONFINITE = 8;
 
-__device__ __forceinline__ void transfer_moments(const double g[Q], double m[10], int *flag) {
-    double drho = 0.0, j[3] = {0, 0, 0}, pi[6] = {0, 0, 0, 0, 0, 0};
-    bool negative = false;
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-        const double v = g[q];
-        const int c[3] = {cx(q), cy(q), cz(q)};
-        drho += v;
-        j[0] += c[0] * v;
-        j[1] += c[1] * v;
-        j[2] += c[2] * v;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) pi[k] += (double)(c[sa(k)] * c[sb(k)]) * v;
-        negative |= v + weight(q) < 0.0;
-    }
-    const double rho = drho + 1.0;
-    if (!(rho > 0.0)) atomicOr(flag, XF_DENSITY);
-    if (negative) atomicOr(flag, XF_NEGATIVE);
-    if (sqrt(j[0] * j[0] + j[1] * j[1] + j[2] * j[2]) / rho / sqrt(TCS2) > 0.3) atomicOr(flag, XF_MACH);
-    m[0] = rho;
-    m[1] = j[0];
-    m[2] = j[1];
-    m[3] = j[2];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        double p = pi[k];
-        if (k < 3) p -= drho * TCS2;
-        m[4 + k] = p - j[sa(k)] * j[sb(k)] / rho;
+// compile-time loop: f(std::integral_constant<int, i>) for i in [B, E)
+template <int B, int E, typename F>
+__device__ __forceinline__ void static_for(F &&f) {
+    if constexpr (B < E) {
+        f(std::integral_constant<int, B>{});
+        static_for<B + 1, E>(f);
     }
 }
 
-// zero-centred populations from (rho, j, Pi_neq), refinement.py:177-203
-__device__ __forceinline__ void transfer_populations(const double m[10], double g[Q], int *flag) {
+// running sums of one cell: drho, j (3), second moments (xx, yy, zz, xy, xz, yz);
+// the zero products of the lattice velocities are skipped
+template <int q>
+__device__ __forceinline__ void add_moments(double s[10], double v) {
+    constexpr int c[3] = {cx(q), cy(q), cz(q)};
+    s[0] += v;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        if (c[a] != 0) s[1 + a] += c[a] > 0 ? v : -v;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const int p = c[sa(k)] * c[sb(k)];
+        if (p != 0) s[4 + k] += p > 0 ? v : -v;
+    }
+}
+
+// (rho, j, Pi_neq) from the running sums, with the reference's density and
+// Mach <= 0.3 checks (refinement.py:140-173); report = 0 skips the checks.
+// The Mach test compares |j|^2 with (0.3 c_s rho)^2 (same decision up to the
+// rounding of the threshold) and the stress divides by rho through one
+// reciprocal: the FP64 pipe is the limit of these kernels.
+__device__ __forceinline__ void finish_moments(const double s[10], double m[10], int *flag, bool report) {
+    const double drho = s[0], rho = drho + 1.0, inv = 1.0 / rho;
+    if (report) {
+        if (!(rho > 0.0)) atomicOr(flag, XF_DENSITY);
+        if (s[1] * s[1] + s[2] * s[2] + s[3] * s[3] > 0.09 * TCS2 * rho * rho) atomicOr(flag, XF_MACH);
+    }
+    m[0] = rho;
+    m[1] = s[1];
+    m[2] = s[2];
+    m[3] = s[3];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        double p = s[4 + k];
+        if (k < 3) p -= drho * TCS2;
+        m[4 + k] = p - s[1 + sa(k)] * s[1 + sb(k)] * inv;
+    }
+}
+
+__device__ __forceinline__ void transfer_moments(const double g[Q], double m[10], int *flag) {
+    double s[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    bool negative = false;
+    static_for<0, Q>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        add_moments<q>(s, g[q]);
+        negative |= g[q] < -weight(q);
+    });
+    if (negative) atomicOr(flag, XF_NEGATIVE);
+    finish_moments(s, m, flag, true);
+}
+
+// checks of a moment set before populations are built from it
+__device__ __forceinline__ void check_fields(const double m[10], int *flag) {
     const double rho = m[0];
     if (!(rho > 0.0)) atomicOr(flag, XF_DENSITY);
-    if (sqrt(m[1] * m[1] + m[2] * m[2] + m[3] * m[3]) / rho / sqrt(TCS2) > 0.3) atomicOr(flag, XF_MACH);
-    const double u[3] = {m[1] / rho, m[2] / rho, m[3] / rho};
-    bool bad = false;
+    if (m[1] * m[1] + m[2] * m[2] + m[3] * m[3] > 0.09 * TCS2 * rho * rho) atomicOr(flag, XF_MACH);
+}
+
+// per-axis factors of the tensor-product equilibrium, fac[a][c + 1]:
+// 2/3 - u^2 for c = 0, (1/3 + u^2 + c u) / 2 otherwise
+__device__ __forceinline__ void axis_factors(const double m[10], double fac[9]) {
+    const double inv = 1.0 / m[0];
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-        const int c[3] = {cx(q), cy(q), cz(q)};
-        double eq = 1.0;
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-            eq *= c[a] == 0 ? 2.0 / 3.0 - u[a] * u[a] : (TCS2 + u[a] * u[a] + c[a] * u[a]) / 2.0;
-        eq *= rho;
-        double neq = 0.0;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            double h = (double)(c[sa(k)] * c[sb(k)]) - (k < 3 ? TCS2 : 0.0);
-            if (k >= 3) h *= 2.0;
-            neq += weight(q) * h / (2.0 * TCS2 * TCS2) * m[4 + k];
-        }
-        const double f = eq + neq;
-        bad |= !isfinite(f) || f < 0.0;
-        g[q] = f - weight(q);
+    for (int a = 0; a < 3; ++a) {
+        const double u = m[1 + a] * inv, uu = u * u;
+        fac[3 * a + 0] = (TCS2 + uu - u) / 2.0;
+        fac[3 * a + 1] = 2.0 / 3.0 - uu;
+        fac[3 * a + 2] = (TCS2 + uu + u) / 2.0;
     }
+}
+
+// zero-centred population q of (rho, j, Pi_neq) (refinement.py:177-203):
+// tensor-product equilibrium + second-order Hermite stress term
+template <int q>
+__device__ __forceinline__ double population(const double m[10], const double fac[9], bool &bad) {
+    constexpr int c[3] = {cx(q), cy(q), cz(q)};
+    double eq = fac[c[0] + 1] * fac[3 + c[1] + 1];
+    eq *= fac[6 + c[2] + 1];
+    eq *= m[0];
+    double neq = 0.0;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        double h = (double)(c[sa(k)] * c[sb(k)]) - (k < 3 ? TCS2 : 0.0);
+        if (k >= 3) h *= 2.0;
+        if (h != 0.0) neq += weight(q) * h / (2.0 * TCS2 * TCS2) * m[4 + k];
+    }
+    const double f = eq + neq;
+    bad |= !isfinite(f) || f < 0.0;
+    return f - weight(q);
+}
+
+__device__ __forceinline__ void transfer_populations(const double m[10], double g[Q], int *flag) {
+    check_fields(m, flag);
+    double fac[9];
+    axis_factors(m, fac);
+    bool bad = false;
+    static_for<0, Q>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        g[q] = population<q>(m, fac, bad);
+    });
     if (bad) atomicOr(flag, XF_NEGATIVE);
+}
+
+// ------------------------------------------------------------ direction-split blocks
+// The interface kernels run 256-thread blocks over 32 cells: the lane is the
+// cell slot (consecutive x, so every direction plane is read coalesced) and
+// warp w owns the directions w, w + 8, w + 16 (and w + 24 < 27) with
+// compile-time indices.  Per-cell sums cross the warps through shared memory
+// in a fixed order, so results do not depend on scheduling.
+constexpr int SPLIT_THREADS = 256, SPLIT_CELLS = 32, SPLIT_WARPS = 8;
+
+template <typename F>
+__device__ __forceinline__ void by_warp(F &&f) {
+    switch (threadIdx.x >> 5) {
+    case 0: f(std::integral_constant<int, 0>{}); break;
+    case 1: f(std::integral_constant<int, 1>{}); break;
+    case 2: f(std::integral_constant<int, 2>{}); break;
+    case 3: f(std::integral_constant<int, 3>{}); break;
+    case 4: f(std::integral_constant<int, 4>{}); break;
+    case 5: f(std::integral_constant<int, 5>{}); break;
+    case 6: f(std::integral_constant<int, 6>{}); break;
+    default: f(std::integral_constant<int, 7>{}); break;
+    }
+}
+
+// f(integral_constant<q>, slot) over the directions owned by warp W
+template <int W, typename F>
+__device__ __forceinline__ void owned(F &&f) {
+    f(std::integral_constant<int, W>{}, 0);
+    f(std::integral_constant<int, W + 8>{}, 1);
+    f(std::integral_constant<int, W + 16>{}, 2);
+    if constexpr (W + 24 < Q) f(std::integral_constant<int, W + 24>{}, 3);
+}
+
+// shared state of a direction-split block: per-warp partial sums and the
+// per-cell fields (moments + equilibrium factors) that warp 0 prepares
+constexpr int NFIELD = 19;  // m[10], fac[9]
+struct SplitShared {
+    double part[SPLIT_WARPS][10][SPLIT_CELLS];
+    int neg[SPLIT_WARPS][SPLIT_CELLS];
+    double field[2][NFIELD][SPLIT_CELLS];
+};
+
+__device__ __forceinline__ void put_partial(SplitShared &sh, const double s[10], bool neg) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 10; ++k) sh.part[w][k][lane] = s[k];
+    sh.neg[w][lane] = neg;
+}
+// block-wide sums of the cell slot, warps 0..7 in order (after a barrier)
+__device__ __forceinline__ void sum_partials(const SplitShared &sh, double t[10], bool &any_neg) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < 10; ++k) {
+        double v = sh.part[0][k][lane];
+#pragma unroll
+        for (int j = 1; j < SPLIT_WARPS; ++j) v += sh.part[j][k][lane];
+        t[k] = v;
+    }
+    any_neg = false;
+#pragma unroll
+    for (int j = 0; j < SPLIT_WARPS; ++j) any_neg |= sh.neg[j][lane] != 0;
+}
+__device__ __forceinline__ void put_fields(SplitShared &sh, int set, const double m[10]) {
+    const int lane = threadIdx.x & 31;
+    double fac[9];
+    axis_factors(m, fac);
+#pragma unroll
+    for (int k = 0; k < 10; ++k) sh.field[set][k][lane] = m[k];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) sh.field[set][10 + k][lane] = fac[k];
+}
+__device__ __forceinline__ void get_fields(const SplitShared &sh, int set, double m[10], double fac[9]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < 10; ++k) m[k] = sh.field[set][k][lane];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) fac[k] = sh.field[set][10 + k][lane];
+}
+
+// cells of an nx x ny rectangle outside its interior [wx, nx - wx) x
+// [wy, ny - wy) (the whole rectangle when no interior is left): the count,
+// and the b-th cell, rows first
+__host__ __device__ __forceinline__ long long ring_count(int nx, int ny, int wx, int wy) {
+    if (nx <= 2 * wx || ny <= 2 * wy) return (long long)nx * ny;
+    return 2LL * wy * nx + 2LL * wx * (ny - 2 * wy);
+}
+__device__ __forceinline__ void ring_cell(long long b, int nx, int ny, int wx, int wy, int &x, int &y) {
+    if (nx <= 2 * wx || ny <= 2 * wy) {
+        y = (int)(b / nx);
+        x = (int)(b - (long long)y * nx);
+        return;
+    }
+    const long long rows = (long long)wy * nx;
+    if (b < 2 * rows) {
+        const int r = (int)(b / nx);
+        x = (int)(b - (long long)r * nx);
+        y = r < wy ? r : ny - 2 * wy + r;
+        return;
+    }
+    b -= 2 * rows;
+    const int r = (int)(b / (2 * wx)), k = (int)(b - (long long)r * 2 * wx);
+    y = wy + r;
+    x = k < wx ? k : nx - 2 * wx + k;
 }
 
 struct Rescale {
@@ -171,31 +328,32 @@ struct Face {
     int fine_index;       // face index on the fine lattice (interior coordinates of the padded block)
 };
 
-// flux of one face patch entry (t1, t2) at lattice coordinates; periodic wraps
-// every axis (interior coordinates)
+// one term of a face patch entry at lattice coordinates p1, p2 (interior)
 template <typename S>
-__device__ void face_flux_entry(const S *pdf, const Grid &G, const FluxTerm *terms, int nterms, int axis, int index,
-                                int p1, int p2, bool periodic, double out[4]) {
+__device__ __forceinline__ void face_term_add(const S *pdf, const Grid &G, const FluxTerm &T, int axis, int index,
+                                              int p1, int p2, bool periodic, double acc[4]) {
     const int a1 = axis == 0 ? 1 : 0, a2 = axis == 2 ? 1 : 2;
     const int dims[3] = {G.nx, G.ny, G.nz};
-    for (int k = 0; k < 4; ++k) out[k] = 0.0;
-    for (int t = 0; t < nterms; ++t) {
-        const FluxTerm T = terms[t];
-        const int normal = axis == 0 ? cx(T.d) : (axis == 1 ? cy(T.d) : cz(T.d));
-        int c3[3];
-        c3[axis] = index + (normal < 0 ? 1 : 0);
-        c3[a1] = p1 + T.shift[a1];
-        c3[a2] = p2 + T.shift[a2];
-        if (periodic)
-            for (int a = 0; a < 3; ++a) c3[a] = (c3[a] % dims[a] + dims[a]) % dims[a];
-        else
-            c3[2] = (c3[2] % dims[2] + dims[2]) % dims[2];
-        const double v = load_g(pdf, G, T.d, c3[0] + 1, c3[1] + 1, c3[2]);
-        for (int k = 0; k < 4; ++k) out[k] += v * T.coef[k];
+    const int normal = axis == 0 ? cx(T.d) : (axis == 1 ? cy(T.d) : cz(T.d));
+    int c3[3];
+    c3[axis] = index + (normal < 0 ? 1 : 0);
+    c3[a1] = p1 + T.shift[a1];
+    c3[a2] = p2 + T.shift[a2];
+    if (periodic) {
+        for (int a = 0; a < 3; ++a) c3[a] = (c3[a] % dims[a] + dims[a]) % dims[a];
+    } else {
+        c3[2] = (c3[2] % dims[2] + dims[2]) % dims[2];
     }
+    const double v = load_g(pdf, G, T.d, c3[0] + 1, c3[1] + 1, c3[2]);
+    for (int k = 0; k < 4; ++k) acc[k] += v * T.coef[k];
 }
 
-// coarse faces: reg[face][t1][t2][4] = flux * dx^3
+__device__ __forceinline__ void warp_sum4(double acc[4]) {
+    for (int o = 16; o > 0; o >>= 1)
+        for (int k = 0; k < 4; ++k) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], o);
+}
+
+// coarse faces: reg[face][t1][t2][4] = flux * dx^3; one warp per entry
 template <typename S>
 __global__ void k_face_flux_coarse(const S *__restrict__ pdf, Grid G, const FluxTerm *__restrict__ terms0,
                                    const FluxTerm *__restrict__ terms1, int nterms, const Face *__restrict__ faces,
@@ -204,17 +362,23 @@ __global__ void k_face_flux_coarse(const S *__restrict__ pdf, Grid G, const Flux
     const int f = blockIdx.y;
     if (f >= nfaces) return;
     const Face F = faces[f];
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (i >= (long long)F.n1 * F.n2) return;
     const int t1 = (int)(i / F.n2), t2 = (int)(i - (long long)t1 * F.n2);
-    double out[4];
-    face_flux_entry(pdf, G, F.axis == 0 ? terms0 : terms1, nterms, F.axis, F.coarse_index, F.lo1 + t1, F.lo2 + t2,
-                    true, out);
-    double *r = reg + offsets[f] + 4 * i;
-    for (int k = 0; k < 4; ++k) r[k] = out[k] * scale;
+    const FluxTerm *terms = F.axis == 0 ? terms0 : terms1;
+    double acc[4] = {0, 0, 0, 0};
+    for (int t = lane; t < nterms; t += 32)
+        face_term_add(pdf, G, terms[t], F.axis, F.coarse_index, F.lo1 + t1, F.lo2 + t2, true, acc);
+    warp_sum4(acc);
+    if (lane == 0) {
+        double *r = reg + offsets[f] + 4 * i;
+        for (int k = 0; k < 4; ++k) r[k] = acc[k] * scale;
+    }
 }
 
-// fine faces: each coarse entry accumulates the sum of its 2 x 2 fine entries
+// fine faces: each coarse entry accumulates the sum of its 2 x 2 fine
+// entries; one warp per coarse entry
 template <typename S>
 __global__ void k_face_flux_fine(const S *__restrict__ pdf, Grid G, const FluxTerm *__restrict__ terms0,
                                  const FluxTerm *__restrict__ terms1, int nterms, const Face *__restrict__ faces,
@@ -223,22 +387,25 @@ __global__ void k_face_flux_fine(const S *__restrict__ pdf, Grid G, const FluxTe
     const int f = blockIdx.y;
     if (f >= nfaces) return;
     const Face F = faces[f];
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (i >= (long long)F.n1 * F.n2) return;
     const int t1 = (int)(i / F.n2), t2 = (int)(i - (long long)t1 * F.n2);
     // fine tangential origin: x and y start after the donor padding, z at 0
     const int a1 = F.axis == 0 ? 1 : 0, a2 = F.axis == 2 ? 1 : 2;
     const int o1 = a1 < 2 ? pad : 0, o2 = a2 < 2 ? pad : 0;
-    double sum[4] = {0, 0, 0, 0};
-    for (int s1 = 0; s1 < 2; ++s1)
-        for (int s2 = 0; s2 < 2; ++s2) {
-            double out[4];
-            face_flux_entry(pdf, G, F.axis == 0 ? terms0 : terms1, nterms, F.axis, F.fine_index,
-                            o1 + 2 * t1 + s1, o2 + 2 * t2 + s2, false, out);
-            for (int k = 0; k < 4; ++k) sum[k] += out[k];
-        }
-    double *r = reg + offsets[f] + 4 * i;
-    for (int k = 0; k < 4; ++k) r[k] += sum[k] * scale;
+    const FluxTerm *terms = F.axis == 0 ? terms0 : terms1;
+    double acc[4] = {0, 0, 0, 0};
+    for (int item = lane; item < 4 * nterms; item += 32) {
+        const int sub = item / nterms, t = item - sub * nterms;
+        face_term_add(pdf, G, terms[t], F.axis, F.fine_index, o1 + 2 * t1 + (sub & 1), o2 + 2 * t2 + (sub >> 1),
+                      false, acc);
+    }
+    warp_sum4(acc);
+    if (lane == 0) {
+        double *r = reg + offsets[f] + 4 * i;
+        for (int k = 0; k < 4; ++k) r[k] += acc[k] * scale;
+    }
 }
 
 // ------------------------------------------------------------ donors
@@ -254,138 +421,315 @@ __device__ __forceinline__ bool in_core(const BoxSpec &B, int cxi, int cyi) {
     return cxi >= B.lo[0] + 3 && cxi < B.hi[0] - 3 && cyi >= B.lo[1] + 3 && cyi < B.hi[1] - 3;
 }
 
-// moments of the donor block: coarse cells [lo-3, hi+3) in x and y (periodic
+// Moments of the donor block: coarse cells [lo-3, hi+3) in x and y (periodic
 // wrap, as the reference indexes them), all z; covered core cells take the
-// free-stream populations
+// free-stream populations.  Output out[k][z][y][x] (x fastest, n cells),
+// written on the ring of the block the prolongation reads (five cells wide);
+// with mix_from set, half also receives 0.5 mix_from + 0.5 out, the donor
+// moments half-way through the coarse step.
+constexpr int DONOR_RING = 5;
 template <typename S>
-__global__ void k_block_moments(const S *__restrict__ pdf, Grid G, BoxSpec B, const double *__restrict__ free_g,
-                                double *__restrict__ out, int *__restrict__ flag) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long n = (long long)B.dnx * B.dny * G.nz;
-    if (i >= n) return;
-    const int z = (int)(i % G.nz);
-    const long long xy = i / G.nz;
-    const int by = (int)(xy % B.dny), bx = (int)(xy / B.dny);
-    int cxi = B.dx0 + bx, cyi = B.dy0 + by;
-    cxi = (cxi % G.nx + G.nx) % G.nx;
-    cyi = (cyi % G.ny + G.ny) % G.ny;
-    double g[Q];
-    if (in_core(B, cxi, cyi)) {
-        for (int q = 0; q < Q; ++q) g[q] = free_g[q];
-    } else {
-        for (int q = 0; q < Q; ++q) g[q] = load_g(pdf, G, q, cxi + 1, cyi + 1, z);
+__global__ void __launch_bounds__(SPLIT_THREADS)
+    k_block_moments(const S *__restrict__ pdf, Grid G, BoxSpec B, const double *__restrict__ free_g,
+                    double *__restrict__ out, const double *__restrict__ mix_from, double *__restrict__ half,
+                    int *__restrict__ flag) {
+    __shared__ SplitShared sh;
+    const long long nring = ring_count(B.dnx, B.dny, DONOR_RING, DONOR_RING), nr = nring * G.nz;
+    if ((long long)blockIdx.x * SPLIT_CELLS >= nr) return;
+    const int lane = threadIdx.x & 31;
+    const long long i = (long long)blockIdx.x * SPLIT_CELLS + lane;
+    const bool valid = i < nr;
+    int bx = 0, by = 0, z = 0, cxi = 0, cyi = 0;
+    bool core = false;
+    if (valid) {
+        z = (int)(i / nring);
+        ring_cell(i - z * nring, B.dnx, B.dny, DONOR_RING, DONOR_RING, bx, by);
+        cxi = ((B.dx0 + bx) % G.nx + G.nx) % G.nx;
+        cyi = ((B.dy0 + by) % G.ny + G.ny) % G.ny;
+        core = in_core(B, cxi, cyi);
     }
-    double m[10];
-    transfer_moments(g, m, flag);
-    for (int k = 0; k < 10; ++k) out[i * 10 + k] = m[k];
+    double s[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    bool neg = false;
+    by_warp([&](auto wc) {
+        owned<decltype(wc)::value>([&](auto qc, int) {
+            constexpr int q = decltype(qc)::value;
+            double v = 0.0;
+            if (valid) v = core ? free_g[q] : load_g(pdf, G, q, cxi + 1, cyi + 1, z);
+            add_moments<q>(s, v);
+            neg |= v < -weight(q);
+        });
+    });
+    put_partial(sh, s, neg);
+    __syncthreads();
+    if ((threadIdx.x >> 5) != 0 || !valid) return;
+    double t[10], m[10];
+    bool any_neg;
+    sum_partials(sh, t, any_neg);
+    if (any_neg) atomicOr(flag, XF_NEGATIVE);
+    finish_moments(t, m, flag, true);
+    const long long n = (long long)B.dnx * B.dny * G.nz, j = ((long long)z * B.dny + by) * B.dnx + bx;
+#pragma unroll
+    for (int k = 0; k < 10; ++k) {
+        out[k * n + j] = m[k];
+        if (mix_from) half[k * n + j] = 0.5 * mix_from[k * n + j] + 0.5 * m[k];
+    }
 }
 
-// donor populations for the padding band of the fine block: prolongation of
-// the time-interpolated donor moments, stress rescaled coarse -> fine
-template <typename S>
-__global__ void k_donors(S *__restrict__ fine, Grid F, BoxSpec B, int nzc, const double *__restrict__ mold,
-                         const double *__restrict__ mnew, double fraction, Rescale r, int pad, int *__restrict__ flag) {
+// Donors for the padding band of the fine block: the donor moments are
+// prolonged one axis at a time, as the reference does (refinement.py:78-105):
+// children = centre -+ [11/64 (a+1 - a-1) - 3/128 (a+2 - a-2)].
+__device__ __forceinline__ double prolong_child(double am2, double am1, double a0, double ap1, double ap2, int odd) {
+    const double offset = 11.0 / 64.0 * (ap1 - am1) - 3.0 / 128.0 * (ap2 - am2);
+    return odd ? a0 + offset : a0 - offset;
+}
+
+// x pass: out[k][z][by][fx] (fx fastest, fx in [0, nfx = 2 (bx + 2))), on the
+// cells the y pass reads for the band: every fx of the five outer block rows
+// on each side, the band columns elsewhere
+__global__ void k_prolong_x(BoxSpec B, int nz, int pad, const double *__restrict__ m, double *__restrict__ out) {
+    const int nfx = 2 * (B.bx + 2);
+    const long long nring = ring_count(nfx, B.dny, pad, DONOR_RING);
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long n = (long long)F.nx * F.ny * F.nz;
-    if (i >= n) return;
-    const int fz = (int)(i % F.nz);
-    const long long xy = i / F.nz;
-    const int fy = (int)(xy % F.ny), fx = (int)(xy / F.ny);  // 0-based padded coordinates
-    const bool band = fx < pad || fx >= F.nx - pad || fy < pad || fy >= F.ny - pad;
-    if (!band) return;
-    // parent coarse cell relative to the donor block, and child side
-    const int px = (fx >> 1) + 2, py = (fy >> 1) + 2, pz = fz >> 1;  // block x = lo-3 + px
-    const double sgn[3] = {(fx & 1) ? 1.0 : -1.0, (fy & 1) ? 1.0 : -1.0, (fz & 1) ? 1.0 : -1.0};
-    double wts[3][5];
-    for (int a = 0; a < 3; ++a) {
-        wts[a][0] = sgn[a] * (3.0 / 128.0);
-        wts[a][1] = -sgn[a] * (11.0 / 64.0);
-        wts[a][2] = 1.0;
-        wts[a][3] = sgn[a] * (11.0 / 64.0);
-        wts[a][4] = -sgn[a] * (3.0 / 128.0);
+    if (i >= nring * nz) return;
+    const int z = (int)(i / nring);
+    int fx, by;
+    ring_cell(i - z * nring, nfx, B.dny, pad, DONOR_RING, fx, by);
+    const long long n = (long long)nfx * B.dny * nz, nblock = (long long)B.dnx * B.dny * nz;
+    const long long row = (long long)z * B.dny + by, o = row * nfx + fx, base = row * B.dnx + (fx >> 1);
+#pragma unroll
+    for (int k = 0; k < 10; ++k) {
+        const double *a = m + k * nblock + base;
+        out[k * n + o] = prolong_child(a[0], a[1], a[2], a[3], a[4], fx & 1);
     }
-    double m[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int kz = 0; kz < 5; ++kz) {
-        const int zz = ((pz + kz - 2) % nzc + nzc) % nzc;
-        for (int ky = 0; ky < 5; ++ky) {
-            const int yy = py + ky - 2;
-            for (int kx = 0; kx < 5; ++kx) {
-                const int xx = px + kx - 2;
-                const double w = wts[0][kx] * wts[1][ky] * wts[2][kz];
-                const long long j = ((long long)xx * B.dny + yy) * nzc + zz;
-                for (int k = 0; k < 10; ++k)
-                    m[k] += w * ((1.0 - fraction) * mold[j * 10 + k] + fraction * mnew[j * 10 + k]);
-            }
+}
+
+// y pass on the band: out[k][z][fy][fx] (fy in [0, nfy = 2 (by + 2)))
+__global__ void k_prolong_y(BoxSpec B, int nz, int pad, const double *__restrict__ in, double *__restrict__ out) {
+    const int nfx = 2 * (B.bx + 2), nfy = 2 * (B.by + 2);
+    const long long nring = ring_count(nfx, nfy, pad, pad);
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nring * nz) return;
+    const int z = (int)(i / nring);
+    int fx, fy;
+    ring_cell(i - z * nring, nfx, nfy, pad, pad, fx, fy);
+    const long long n = (long long)nfx * nfy * nz, nin = (long long)nfx * B.dny * nz;
+    const long long o = ((long long)z * nfy + fy) * nfx + fx, base = ((long long)z * B.dny + (fy >> 1)) * nfx + fx;
+#pragma unroll
+    for (int k = 0; k < 10; ++k) {
+        const double *a = in + k * nin + base;
+        out[k * n + o] = prolong_child(a[0], a[nfx], a[2 * nfx], a[3 * nfx], a[4 * nfx], fy & 1);
+    }
+}
+
+// z pass on the padding band (pad fine cells around the physical block in x
+// and y, every z), stress rescaled coarse -> fine, populations.  Warp w
+// prolongs moments w and w + 8, warp 0 rescales and prepares the fields,
+// every warp writes its own directions.
+template <typename S>
+__global__ void __launch_bounds__(SPLIT_THREADS)
+    k_donors(S *__restrict__ fine, Grid F, int nzc, const double *__restrict__ pxy, Rescale r, int pad,
+             int *__restrict__ flag) {
+    __shared__ SplitShared sh;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const long long nring = ring_count(F.nx, F.ny, pad, pad), n = nring * F.nz;
+    if ((long long)blockIdx.x * SPLIT_CELLS >= n) return;
+    const long long i = (long long)blockIdx.x * SPLIT_CELLS + lane;
+    const bool valid = i < n;
+    int fx = 0, fy = 0, fz = 0;
+    if (valid) {
+        fz = (int)(i / nring);
+        ring_cell(i - fz * nring, F.nx, F.ny, pad, pad, fx, fy);
+    }
+    const long long plane = (long long)F.nx * F.ny, nxy = plane * nzc, cell = (long long)fy * F.nx + fx;
+    const int pz = fz >> 1;
+    for (int k = w; k < 10; k += SPLIT_WARPS) {
+        double a[5];
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+            const int zz = ((pz + j - 2) % nzc + nzc) % nzc;
+            a[j] = valid ? pxy[k * nxy + zz * plane + cell] : (k == 0 ? 1.0 : 0.0);
         }
+        sh.field[0][k][lane] = prolong_child(a[0], a[1], a[2], a[3], a[4], fz & 1);
     }
-    rescale_stress(m, r);
-    double g[Q];
-    transfer_populations(m, g, flag);
-    for (int q = 0; q < Q; ++q) store_g(fine, F, q, fx + 1, fy + 1, fz, g[q]);
+    __syncthreads();
+    if (w == 0) {
+        double m[10];
+#pragma unroll
+        for (int k = 0; k < 10; ++k) m[k] = sh.field[0][k][lane];
+        rescale_stress(m, r);
+        if (valid) check_fields(m, flag);
+        put_fields(sh, 1, m);
+    }
+    __syncthreads();
+    double m[10], fac[9];
+    get_fields(sh, 1, m, fac);
+    bool bad = false;
+    by_warp([&](auto wc) {
+        owned<decltype(wc)::value>([&](auto qc, int) {
+            constexpr int q = decltype(qc)::value;
+            const double g = population<q>(m, fac, bad);
+            if (valid) store_g(fine, F, q, fx + 1, fy + 1, fz, g);
+        });
+    });
+    if (bad && valid) atomicOr(flag, XF_NEGATIVE);
 }
 
 // ------------------------------------------------------------ reflux, restriction
 // coarse cells just outside each face: equilibrium part of the state shifted
 // by the flux mismatch (interface.py:285-295)
 template <typename S>
-__global__ void k_reflux(S *__restrict__ pdf, Grid G, const Face *__restrict__ faces, int nfaces,
-                         const long long *__restrict__ offsets, const double *__restrict__ reg_c,
-                         const double *__restrict__ reg_f, double inv_volume, int *__restrict__ flag) {
+__global__ void __launch_bounds__(SPLIT_THREADS)
+    k_reflux(S *__restrict__ pdf, Grid G, const Face *__restrict__ faces, int nfaces,
+             const long long *__restrict__ offsets, const double *__restrict__ reg_c,
+             const double *__restrict__ reg_f, double inv_volume, int *__restrict__ flag) {
+    __shared__ SplitShared sh;
     const int f = blockIdx.y;
     if (f >= nfaces) return;
     const Face F = faces[f];
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (long long)F.n1 * F.n2) return;
-    const int t1 = (int)(i / F.n2), t2 = (int)(i - (long long)t1 * F.n2);
+    const long long n = (long long)F.n1 * F.n2;
+    if ((long long)blockIdx.x * SPLIT_CELLS >= n) return;
+    const int lane = threadIdx.x & 31;
+    const bool lead = (threadIdx.x >> 5) == 0;
+    const long long i = (long long)blockIdx.x * SPLIT_CELLS + lane;
+    const bool valid = i < n;
+    const long long e = valid ? i : 0;
+    const int t1 = (int)(e / F.n2), t2 = (int)(e - (long long)t1 * F.n2);
     const int a1 = F.axis == 0 ? 1 : 0, a2 = F.axis == 2 ? 1 : 2;
     int c3[3];
     c3[F.axis] = F.side < 0 ? F.coarse_index : F.coarse_index + 1;  // the cell outside the box
     c3[a1] = F.lo1 + t1;
     c3[a2] = F.lo2 + t2;
-    const double *rc = reg_c + offsets[f] + 4 * i, *rf = reg_f + offsets[f] + 4 * i;
-    double g[Q], m_old[10], m_new[10], p_old[Q], p_new[Q];
-    for (int q = 0; q < Q; ++q) g[q] = load_g(pdf, G, q, c3[0] + 1, c3[1] + 1, c3[2]);
-    transfer_moments(g, m_old, flag);
-    for (int k = 4; k < 10; ++k) m_old[k] = 0.0;
-    for (int k = 0; k < 10; ++k) m_new[k] = m_old[k];
-    for (int k = 0; k < 4; ++k) m_new[k] += F.side * (rf[k] - rc[k]) * inv_volume;
-    transfer_populations(m_new, p_new, flag);
-    transfer_populations(m_old, p_old, flag);
-    for (int q = 0; q < Q; ++q) g[q] += p_new[q] - p_old[q];
-    double chk[10];
-    transfer_moments(g, chk, flag);
-    for (int q = 0; q < Q; ++q) store_g(pdf, G, q, c3[0] + 1, c3[1] + 1, c3[2], g[q]);
+    double g[4] = {0, 0, 0, 0}, s[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    bool neg = false;
+    by_warp([&](auto wc) {
+        owned<decltype(wc)::value>([&](auto qc, int slot) {
+            constexpr int q = decltype(qc)::value;
+            g[slot] = valid ? load_g(pdf, G, q, c3[0] + 1, c3[1] + 1, c3[2]) : 0.0;
+            add_moments<q>(s, g[slot]);
+            neg |= g[slot] < -weight(q);
+        });
+    });
+    put_partial(sh, s, neg);
+    __syncthreads();
+    if (lead) {
+        double t[10], m_old[10], m_new[10];
+        bool any_neg;
+        sum_partials(sh, t, any_neg);
+        if (valid && any_neg) atomicOr(flag, XF_NEGATIVE);
+        finish_moments(t, m_old, flag, valid);
+        const double *rc = reg_c + offsets[f] + 4 * e, *rf = reg_f + offsets[f] + 4 * e;
+#pragma unroll
+        for (int k = 4; k < 10; ++k) m_old[k] = 0.0;
+#pragma unroll
+        for (int k = 0; k < 10; ++k) m_new[k] = m_old[k];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) m_new[k] += F.side * (rf[k] - rc[k]) * inv_volume;
+        if (valid) {
+            check_fields(m_new, flag);
+            check_fields(m_old, flag);
+        }
+        put_fields(sh, 0, m_new);
+        put_fields(sh, 1, m_old);
+    }
+    __syncthreads();
+    double m_new[10], f_new[9], m_old[10], f_old[9];
+    get_fields(sh, 0, m_new, f_new);
+    get_fields(sh, 1, m_old, f_old);
+    bool bad = false, neg2 = false;
+    double s2[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    by_warp([&](auto wc) {
+        owned<decltype(wc)::value>([&](auto qc, int slot) {
+            constexpr int q = decltype(qc)::value;
+            g[slot] += population<q>(m_new, f_new, bad) - population<q>(m_old, f_old, bad);
+            add_moments<q>(s2, g[slot]);
+            neg2 |= g[slot] < -weight(q);
+            if (valid) store_g(pdf, G, q, c3[0] + 1, c3[1] + 1, c3[2], g[slot]);
+        });
+    });
+    if (bad && valid) atomicOr(flag, XF_NEGATIVE);
+    // the shifted state passes the same checks (interface.py:293)
+    __syncthreads();
+    put_partial(sh, s2, neg2);
+    __syncthreads();
+    if (lead && valid) {
+        double t[10], chk[10];
+        bool any_neg;
+        sum_partials(sh, t, any_neg);
+        if (any_neg) atomicOr(flag, XF_NEGATIVE);
+        finish_moments(t, chk, flag, true);
+    }
 }
 
-// covered coarse cells: restriction of the fine state (core cells take the
-// free stream), stress rescaled fine -> coarse
+// Covered coarse cells: restriction of the fine state, stress rescaled
+// fine -> coarse.  blockIdx.y == 0: the three-cell ring of the box outside
+// its core, 32 coarse cells per block; warp w reads child w (x, y, z bits of
+// w), warp 0 averages the eight children and prepares the fields, every warp
+// writes its own directions.  blockIdx.y == 1: core cells take the free stream.
 template <typename Sc, typename Sf>
-__global__ void k_restrict(Sc *__restrict__ coarse, Grid G, const Sf *__restrict__ fine, Grid F, BoxSpec B, int pad,
-                           const double *__restrict__ free_g, Rescale r, int *__restrict__ flag) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long n = (long long)B.bx * B.by * B.bz;
-    if (i >= n) return;
-    const int z = (int)(i % B.bz);
-    const long long xy = i / B.bz;
-    const int by = (int)(xy % B.by), bx = (int)(xy / B.by);
-    const int cxi = B.lo[0] + bx, cyi = B.lo[1] + by, czi = B.lo[2] + z;
-    double g[Q];
-    if (in_core(B, cxi, cyi)) {
-        for (int q = 0; q < Q; ++q) g[q] = free_g[q];
-    } else {
-        double m[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-        for (int s = 0; s < 8; ++s) {
-            const int fx = pad + 2 * bx + (s & 1), fy = pad + 2 * by + ((s >> 1) & 1), fz = 2 * z + (s >> 2);
-            double gc[Q], mc[10];
-            for (int q = 0; q < Q; ++q) gc[q] = load_g(fine, F, q, fx + 1, fy + 1, fz);
-            transfer_moments(gc, mc, flag);
-            for (int k = 0; k < 10; ++k) m[k] += mc[k];
-        }
+__global__ void __launch_bounds__(SPLIT_THREADS)
+    k_restrict(Sc *__restrict__ coarse, Grid G, const Sf *__restrict__ fine, Grid F, BoxSpec B, int pad,
+               const double *__restrict__ free_g, Rescale r, int *__restrict__ flag) {
+    __shared__ SplitShared sh;
+    if (blockIdx.y == 1) {
+        const int cx0 = B.bx - 6, cy0 = B.by - 6;
+        if (cx0 <= 0 || cy0 <= 0) return;
+        const long long ncore = (long long)cx0 * cy0 * B.bz;
+        const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= ncore) return;
+        const int x = (int)(i % cx0);
+        const long long rest = i / cx0;
+        const int y = (int)(rest % cy0), z = (int)(rest / cy0);
+        for (int q = 0; q < Q; ++q)
+            store_g(coarse, G, q, B.lo[0] + 3 + x + 1, B.lo[1] + 3 + y + 1, B.lo[2] + z, free_g[q]);
+        return;
+    }
+    const long long nring = ring_count(B.bx, B.by, 3, 3), n = nring * B.bz;
+    if ((long long)blockIdx.x * SPLIT_CELLS >= n) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const long long i = (long long)blockIdx.x * SPLIT_CELLS + lane;
+    const bool valid = i < n;
+    int bx = 0, by = 0, z = 0;
+    if (valid) {
+        z = (int)(i / nring);
+        ring_cell(i - z * nring, B.bx, B.by, 3, 3, bx, by);
+    }
+    const int fx = pad + 2 * bx + (w & 1), fy = pad + 2 * by + ((w >> 1) & 1), fz = 2 * z + (w >> 2);
+    double s[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    bool neg = false;
+    static_for<0, Q>([&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        const double v = valid ? load_g(fine, F, q, fx + 1, fy + 1, fz) : 0.0;
+        add_moments<q>(s, v);
+        neg |= v < -weight(q);
+    });
+    double mc[10];
+    finish_moments(s, mc, flag, valid);
+    put_partial(sh, mc, neg);
+    __syncthreads();
+    if (w == 0) {
+        double m[10];
+        bool any_neg;
+        sum_partials(sh, m, any_neg);
+        if (valid && any_neg) atomicOr(flag, XF_NEGATIVE);
+#pragma unroll
         for (int k = 0; k < 10; ++k) m[k] *= 0.125;
         rescale_stress(m, r);
-        transfer_populations(m, g, flag);
+        if (valid) check_fields(m, flag);
+        put_fields(sh, 0, m);
     }
-    for (int q = 0; q < Q; ++q) store_g(coarse, G, q, cxi + 1, cyi + 1, czi, g[q]);
+    __syncthreads();
+    double m[10], fac[9];
+    get_fields(sh, 0, m, fac);
+    const int cxi = B.lo[0] + bx, cyi = B.lo[1] + by, czi = B.lo[2] + z;
+    bool bad = false;
+    by_warp([&](auto wc) {
+        owned<decltype(wc)::value>([&](auto qc, int) {
+            constexpr int q = decltype(qc)::value;
+            const double g = population<q>(m, fac, bad);
+            if (valid) store_g(coarse, G, q, cxi + 1, cyi + 1, czi, g);
+        });
+    });
+    if (bad && valid) atomicOr(flag, XF_NEGATIVE);
 }
 
 }  // namespace ak
