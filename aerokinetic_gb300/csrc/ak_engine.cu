@@ -979,6 +979,10 @@ struct ak_refined {
     double *d_loads = nullptr;
     long long steps = 0;
     std::vector<void *> owned;  // device buffers of the driver
+    // one captured coarse step per (coarse, fine) buffer parity, replayed by
+    // ak_refined_step; launches_per_step counts the kernels of one replay
+    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
+    long long launches_per_step = 0;
 };
 
 namespace {
@@ -996,6 +1000,11 @@ int ralloc(ak_refined *R, T **p, size_t n) {
 
 void refined_release(ak_refined *R) {
     if (R->coarse) cudaStreamSynchronize(R->coarse->stream);
+    for (cudaGraphExec_t &g : R->graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
     for (void *p : R->owned) cudaFree(p);
     if (R->coarse) {
         release(R->coarse);
@@ -1181,6 +1190,52 @@ int refined_step(ak_refined *R) {
     return AK_OK;
 }
 
+// One coarse step replayed from a CUDA graph: the step's kernel sequence is
+// captured once per buffer parity (the coarse copies swap every step, the
+// fine copies twice) and the host-side counters are advanced as the eager
+// step advances them.
+template <typename S>
+int refined_step_graphed(ak_refined *R) {
+    ak_case *C = R->coarse, *F = R->fine;
+    const int slot = C->cur | (F->cur << 1);
+    if (!R->graph[slot]) {
+        const int ccur = C->cur, fcur = F->cur;
+        const long long cs = C->steps, fs = F->steps, rs = R->steps, cl = C->launches;
+        std::vector<cudaEvent_t> *timing = C->timing;
+        C->timing = nullptr;
+        AK_CUDA(cudaStreamBeginCapture(C->stream, cudaStreamCaptureModeThreadLocal));
+        const int r = refined_step<S>(R);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(C->stream, &g);
+        C->timing = timing;
+        R->launches_per_step = C->launches - cl;
+        C->cur = ccur;
+        F->cur = fcur;
+        C->steps = cs;
+        F->steps = fs;
+        R->steps = rs;
+        C->launches = cl;
+        if (r != AK_OK || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            return r != AK_OK ? r : fail(AK_ERR_CUDA, std::string("step capture failed: ") + cudaGetErrorString(e));
+        }
+        const cudaError_t ei = cudaGraphInstantiate(&R->graph[slot], g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) {
+            R->graph[slot] = nullptr;
+            return fail(AK_ERR_CUDA, std::string("step graph instantiation failed: ") + cudaGetErrorString(ei));
+        }
+    }
+    AK_CUDA(cudaGraphLaunch(R->graph[slot], C->stream));
+    C->cur = 1 - C->cur;
+    C->launches += R->launches_per_step;
+    C->steps += 1;
+    F->steps += 2;
+    R->steps += 1;
+    return AK_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1350,7 +1405,9 @@ int ak_refined_step(ak_refined *R, int32_t nsteps, double *loads) {
     cudaStream_t st = R->coarse->stream;
     AK_CUDA(cudaMemsetAsync(R->d_flag, 0, sizeof(int), st));
     for (int s = 0; s < nsteps; ++s)
-        AK_TRY(with_storage(R->coarse, [&](auto *tag) { return refined_step<std::remove_pointer_t<decltype(tag)>>(R); }));
+        AK_TRY(with_storage(R->coarse, [&](auto *tag) {
+            return refined_step_graphed<std::remove_pointer_t<decltype(tag)>>(R);
+        }));
     int flag = 0;
     AK_CUDA(cudaMemcpyAsync(&flag, R->d_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
     const int n = R->fine->n_elements;

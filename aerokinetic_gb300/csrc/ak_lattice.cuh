@@ -281,13 +281,16 @@ __host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b) 
             const T E = htx * Cp + ux * Cs + T(0.5) * Cc, D = hux * Cp + T(0.5) * Cs;
             C[2] = E + D; C[0] = E - D; C[1] = omtx * Cp + m2ux * Cs - Cc;
         }
+        // the rest weights (equal for c_z = -1 and +1) enter the fused
+        // multiply-add chains as their first addend
 #pragma unroll
         for (int ix = 0; ix < 3; ++ix) {
-            const T E = A[ix] * rhtz + B[ix] * ruz + C[ix] * rh;
+            const T w_pm = T(weight(qof(ix, iy, 2))), w_0 = T(weight(qof(ix, iy, 1)));
+            const T E = A[ix] * rhtz + (B[ix] * ruz + (C[ix] * rh - w_pm));
             const T D = A[ix] * rhuz + B[ix] * rh;
-            g[qof(ix, iy, 2)] = (E + D) - T(weight(qof(ix, iy, 2)));
-            g[qof(ix, iy, 0)] = (E - D) - T(weight(qof(ix, iy, 0)));
-            g[qof(ix, iy, 1)] = (A[ix] * r0z + B[ix] * rm2uz - C[ix] * rho) - T(weight(qof(ix, iy, 1)));
+            g[qof(ix, iy, 2)] = E + D;
+            g[qof(ix, iy, 0)] = E - D;
+            g[qof(ix, iy, 1)] = A[ix] * r0z + (B[ix] * rm2uz - (C[ix] * rho + w_0));
         }
     }
 }

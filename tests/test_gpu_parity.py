@@ -261,3 +261,25 @@ def test_refined_startup_history_on_gpu(golden):
                 assert loads[k] == pytest.approx(row[k], abs=1e-11), (row["step"], k)
     finally:
         solver.close()
+
+
+def test_refined_graph_replay_matches_eager_steps(golden):
+    """ak_refined_step replays a captured coarse step (one graph per buffer
+    parity); ak_refined_step_timed issues the same kernels one by one: the
+    states agree bit for bit over an odd number of steps."""
+    import ctypes
+    from aerokinetic_gb300 import _native
+    from aerokinetic_gb300.refined import RefinedSolver
+    from aerokinetic_gb300.refined_plan import load_refined_project
+    project, refinement = load_refined_project(golden["histories"]["refined_startup"]["project"])
+    replay, eager = RefinedSolver(project, refinement), RefinedSolver(project, refinement)
+    try:
+        replay.advance(5)
+        ms = np.zeros(6)
+        _native.check(eager._lib.ak_refined_step_timed(eager._handle, 5, ms.ctypes.data_as(ctypes.c_void_p)))
+        assert ms[0] > 0
+        for a, b in zip(replay.states(), eager.states()):
+            assert np.array_equal(a, b)
+    finally:
+        replay.close()
+        eager.close()
