@@ -102,6 +102,10 @@ SIGNATURES = {
     "ak_refined_init_perturbed": ([_P, _D, _D, _D, _D, _D], ctypes.c_int),
     "ak_refined_step": ([_P, ctypes.c_int32, _P], ctypes.c_int),
     "ak_refined_steps_done": ([_P], ctypes.c_int64),
+    "ak_refined_track_budget": ([_P, ctypes.c_int32], ctypes.c_int),
+    "ak_refined_outer_flux": ([_P, _P], ctypes.c_int),
+    "ak_refined_integrals": ([_P, _P], ctypes.c_int),
+    "ak_refined_cumulative_loads": ([_P, _P], ctypes.c_int),
     "ak_refined_step_timed": ([_P, ctypes.c_int32, _P], ctypes.c_int),
     "ak_refined_level": ([_P, ctypes.c_int32], _P),
     "ak_last_error": ([], ctypes.c_char_p),

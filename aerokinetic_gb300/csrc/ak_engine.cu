@@ -981,8 +981,17 @@ struct ak_refined {
     std::vector<void *> owned;  // device buffers of the driver
     // one captured coarse step per (coarse, fine) buffer parity, replayed by
     // ak_refined_step; launches_per_step counts the kernels of one replay
-    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaGraphExec_t graph[8] = {};
     long long launches_per_step = 0;
+    // budget support: inflow through the outer x/y faces of each tracked step,
+    // and the per-level statistics of the conserved integrals / validity check
+    bool track_budget = false;
+    Face outer[4];
+    Face *d_outer = nullptr;
+    int outer_blocks = 0;
+    double *outer_partials = nullptr, *outer_out = nullptr;  // outer_out: last step [4], running sum [4]
+    double *cum_loads = nullptr;                              // wall loads summed over all steps [n * 5]
+    double *stats_partials = nullptr, *stats_out = nullptr;
 };
 
 namespace {
@@ -1058,6 +1067,8 @@ std::vector<FluxTerm> flux_terms(int axis) {
 }
 
 long long blocks3(long long n) { return (n + 255) / 256; }
+// fixed grid of the region statistics (results do not depend on the device)
+constexpr int STATS_BLOCKS = 4 * 152;
 // direction-split kernels: 32 cells per 256-thread block
 long long split_blocks(long long cells) { return (cells + SPLIT_CELLS - 1) / SPLIT_CELLS; }
 
@@ -1103,6 +1114,8 @@ int refined_init(ak_refined *R, double amp, double phase_y, double phase_z, doub
     }
     C->prepared = F->prepared = true;
     R->steps = 0;
+    AK_CUDA(cudaMemsetAsync(R->outer_out, 0, 8 * sizeof(double), st));
+    AK_CUDA(cudaMemsetAsync(R->cum_loads, 0, 5 * std::max(1, F->n_elements) * sizeof(double), st));
     AK_CUDA(cudaStreamSynchronize(st));
     int flag = 0;
     AK_CUDA(cudaMemcpy(&flag, R->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
@@ -1137,6 +1150,13 @@ int refined_step(ak_refined *R) {
     if (C->n_out)
         k_outflow<S><<<(unsigned)blocks3(C->n_out), 256, 0, st>>>(src_of<S>(C), C->G, C->outer(), C->sel_out,
                                                                   C->n_out, C->out_state, 1, 0, 0);
+    if (R->track_budget) {
+        k_outer_flux<S><<<dim3((unsigned)R->outer_blocks, 4), 256, 0, st>>>(
+            src_of<S>(C), C->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_outer, 4, R->outer_partials);
+        k_outer_final<<<1, 1, 0, st>>>(R->outer_partials, R->d_outer, 4, R->outer_blocks,
+                                       R->dx_c * R->dx_c * R->dx_c, R->outer_out);
+        C->launches += 2;
+    }
     mark(C);
     k_stream<S><<<gc, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, 0);
     mark(C);
@@ -1177,6 +1197,10 @@ int refined_step(ak_refined *R) {
         AK_CUDA(cudaGetLastError());
         F->cur = 1 - F->cur;
     }
+    if (nlinks) {
+        k_accumulate_loads<<<1, 128, 0, st>>>(R->d_loads, 5 * F->n_elements, R->cum_loads);
+        C->launches += 1;
+    }
     k_reflux<S><<<dim3((unsigned)split_blocks(R->max_face), R->nfaces), SPLIT_THREADS, 0, st>>>(
         src_of<S>(C), C->G, R->d_faces, R->nfaces, R->d_offs, R->reg_c, R->reg_f,
         1.0 / (R->dx_c * R->dx_c * R->dx_c), R->d_flag);
@@ -1197,7 +1221,7 @@ int refined_step(ak_refined *R) {
 template <typename S>
 int refined_step_graphed(ak_refined *R) {
     ak_case *C = R->coarse, *F = R->fine;
-    const int slot = C->cur | (F->cur << 1);
+    const int slot = C->cur | (F->cur << 1) | (R->track_budget ? 4 : 0);
     if (!R->graph[slot]) {
         const int ccur = C->cur, fcur = F->cur;
         const long long cs = C->steps, fs = F->steps, rs = R->steps, cl = C->launches;
@@ -1358,6 +1382,35 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
             if (r == AK_OK) cudaMemcpy(R->d_terms[axis], t.data(), t.size() * sizeof(FluxTerm), cudaMemcpyHostToDevice);
         }
     }
+    if (r == AK_OK) {
+        // outer x and y faces of the coarse lattice, in the order x-, x+, y-, y+
+        long long most = 1;
+        for (int k = 0; k < 4; ++k) {
+            Face f{};
+            f.axis = k / 2;
+            f.side = (k & 1) ? 1 : -1;
+            const int n_axis = f.axis == 0 ? cd.nx : cd.ny;
+            f.coarse_index = f.side < 0 ? -1 : n_axis - 1;
+            f.lo1 = 0;
+            f.n1 = f.axis == 0 ? cd.ny : cd.nx;
+            f.lo2 = 0;
+            f.n2 = cd.nz;
+            R->outer[k] = f;
+            most = std::max<long long>(most, (long long)f.n1 * f.n2);
+        }
+        R->outer_blocks = (int)blocks3(most);
+        r = ralloc(R, &R->d_outer, 4);
+        if (r == AK_OK) r = cudaMemcpy(R->d_outer, R->outer, sizeof R->outer, cudaMemcpyHostToDevice) == cudaSuccess
+                                ? AK_OK : fail(AK_ERR_CUDA, "upload failed");
+        if (r == AK_OK) r = ralloc(R, &R->outer_partials, (size_t)4 * R->outer_blocks * 4);
+        if (r == AK_OK) r = ralloc(R, &R->outer_out, 8);
+        if (r == AK_OK) r = ralloc(R, &R->cum_loads, (size_t)5 * std::max(1, cd.n_elements));
+        if (r == AK_OK) r = ralloc(R, &R->stats_partials, (size_t)STATS_BLOCKS * NSTAT);
+        if (r == AK_OK) r = ralloc(R, &R->stats_out, (size_t)2 * NSTAT);
+        if (r == AK_OK && (cudaMemset(R->outer_out, 0, 8 * sizeof(double)) != cudaSuccess ||
+                           cudaMemset(R->cum_loads, 0, 5 * std::max(1, cd.n_elements) * sizeof(double)) != cudaSuccess))
+            r = fail(AK_ERR_CUDA, "memset failed");
+    }
     if (r == AK_OK) r = ralloc(R, &R->d_flag, 1);
     if (r == AK_OK) r = ralloc(R, &R->d_loads, (size_t)2 * 5 * std::max(1, cd.n_elements));
     if (r == AK_OK) {
@@ -1425,6 +1478,50 @@ int ak_refined_step(ak_refined *R, int32_t nsteps, double *loads) {
 }
 
 int64_t ak_refined_steps_done(const ak_refined *R) { return R ? R->steps : -1; }
+
+int ak_refined_track_budget(ak_refined *R, int32_t enable) {
+    if (!R) return fail(AK_ERR_INVALID, "null case");
+    R->track_budget = enable != 0;
+    return AK_OK;
+}
+
+int ak_refined_outer_flux(ak_refined *R, double *out) {
+    if (!R || !out) return fail(AK_ERR_INVALID, "a case and an output array are required");
+    AK_CUDA(cudaStreamSynchronize(R->coarse->stream));
+    AK_CUDA(cudaMemcpy(out, R->outer_out, 8 * sizeof(double), cudaMemcpyDeviceToHost));
+    return AK_OK;
+}
+
+int ak_refined_cumulative_loads(ak_refined *R, double *out) {
+    if (!R || !out) return fail(AK_ERR_INVALID, "a case and an output array are required");
+    AK_CUDA(cudaStreamSynchronize(R->coarse->stream));
+    AK_CUDA(cudaMemcpy(out, R->cum_loads, 5 * std::max(1, R->fine->n_elements) * sizeof(double),
+                       cudaMemcpyDeviceToHost));
+    return AK_OK;
+}
+
+int ak_refined_integrals(ak_refined *R, double *out) {
+    if (!R || !out) return fail(AK_ERR_INVALID, "a case and an output array are required");
+    ak_case *C = R->coarse, *F = R->fine;
+    cudaStream_t st = C->stream;
+    const BoxSpec &B = R->B;
+    const Region rc{0, C->nx, 0, C->ny, B.lo[0], B.hi[0], B.lo[1], B.hi[1]};
+    const Region rf{R->pad, F->nx - R->pad, R->pad, F->ny - R->pad, 0, 0, 0, 0};
+    int r = with_storage(C, [&](auto *tag) {
+        using S = std::remove_pointer_t<decltype(tag)>;
+        k_region_stats<S><<<STATS_BLOCKS, 256, 0, st>>>(src_of<S>(C), C->G, C->flags, rc, R->stats_partials);
+        k_region_final<<<1, 1, 0, st>>>(R->stats_partials, STATS_BLOCKS, R->stats_out);
+        k_region_stats<S><<<STATS_BLOCKS, 256, 0, st>>>(src_of<S>(F), F->G, F->flags, rf, R->stats_partials);
+        k_region_final<<<1, 1, 0, st>>>(R->stats_partials, STATS_BLOCKS, R->stats_out + NSTAT);
+        C->launches += 4;
+        AK_CUDA(cudaGetLastError());
+        return AK_OK;
+    });
+    if (r != AK_OK) return r;
+    AK_CUDA(cudaMemcpyAsync(out, R->stats_out, 2 * NSTAT * sizeof(double), cudaMemcpyDeviceToHost, st));
+    AK_CUDA(cudaStreamSynchronize(st));
+    return AK_OK;
+}
 
 int ak_refined_step_timed(ak_refined *R, int32_t nsteps, double *ms) {
     if (!R || nsteps < 1 || !ms) return fail(AK_ERR_INVALID, "a case, nsteps >= 1 and an output array are required");

@@ -732,4 +732,130 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
     if (bad && valid) atomicOr(flag, XF_NEGATIVE);
 }
 
+// ------------------------------------------------------------ budgets and validity
+// Inflow of mass and momentum through the outer x and y faces of the coarse
+// lattice, from the state the streaming reads (refined_solver.py:215-222,
+// 274-278): partials[face][block][4] hold the block sums of the face flux.
+// The z pair of faces is left out: with z periodic its two fluxes are equal.
+template <typename S>
+__global__ void __launch_bounds__(256)
+    k_outer_flux(const S *__restrict__ pdf, Grid G, const FluxTerm *__restrict__ terms0,
+                 const FluxTerm *__restrict__ terms1, int nterms, const Face *__restrict__ faces, int nfaces,
+                 double *__restrict__ partials) {
+    const int f = blockIdx.y;
+    if (f >= nfaces) return;
+    const Face F = faces[f];
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double acc[4] = {0, 0, 0, 0};
+    if (i < (long long)F.n1 * F.n2) {
+        const int t1 = (int)(i / F.n2), t2 = (int)(i - (long long)t1 * F.n2);
+        const FluxTerm *terms = F.axis == 0 ? terms0 : terms1;
+        for (int t = 0; t < nterms; ++t)
+            face_term_add(pdf, G, terms[t], F.axis, F.coarse_index, F.lo1 + t1, F.lo2 + t2, false, acc);
+    }
+    block_sum_store<4>(acc, partials + (long long)f * 4 * gridDim.x);
+}
+
+// out[k] = sum over faces (in order) of -side * dx^3 * sum over blocks, for
+// this step; out[4 + k] accumulates it over the tracked steps
+__global__ void k_outer_final(const double *__restrict__ partials, const Face *__restrict__ faces, int nfaces,
+                              int nblocks, double volume, double *__restrict__ out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double total[4] = {0, 0, 0, 0};
+    for (int f = 0; f < nfaces; ++f) {
+        double s[4] = {0, 0, 0, 0};
+        for (int b = 0; b < nblocks; ++b)
+            for (int k = 0; k < 4; ++k) s[k] += partials[((long long)f * nblocks + b) * 4 + k];
+        for (int k = 0; k < 4; ++k) total[k] -= faces[f].side * s[k] * volume;
+    }
+    for (int k = 0; k < 4; ++k) {
+        out[k] = total[k];
+        out[4 + k] += total[k];
+    }
+}
+
+// running sums of the wall loads over coarse steps: cum[k] += both fine steps
+__global__ void k_accumulate_loads(const double *__restrict__ loads, int n, double *__restrict__ cum) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) cum[t] += loads[t] + loads[n + t];
+}
+
+// Statistics of one level's region (refined_solver.py:291-299, 347-361):
+// fluid cells of [x0, x1) x [y0, y1) x all z (interior coordinates) outside
+// [ex0, ex1) x [ey0, ey1).  partials[block][NSTAT] = max |u|^2, max |rho - 1|,
+// sum drho, sum j (3), cells, non-finite cells.
+struct Region {
+    int x0, x1, y0, y1, ex0, ex1, ey0, ey1;
+};
+constexpr int NSTAT = 8;
+template <typename S>
+__global__ void __launch_bounds__(256)
+    k_region_stats(const S *__restrict__ pdf, Grid G, const uint8_t *__restrict__ flags, Region R,
+                   double *__restrict__ partials) {
+    const int w = R.x1 - R.x0, h = R.y1 - R.y0;
+    const long long n = (long long)w * h * G.nz;
+    double a[NSTAT] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = R.x0 + (int)(i % w);
+        const long long r = i / w;
+        const int y = R.y0 + (int)(r % h), z = (int)(r / h);
+        if (x >= R.ex0 && x < R.ex1 && y >= R.ey0 && y < R.ey1) continue;
+        if (flags[(y + 1) * G.nxp + (x + 1)] != FLAG_FLUID) continue;
+        double drho = 0.0, j[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const double v = load_g(pdf, G, q, x + 1, y + 1, z);
+            drho += v;
+            if (cx(q)) j[0] += cx(q) > 0 ? v : -v;
+            if (cy(q)) j[1] += cy(q) > 0 ? v : -v;
+            if (cz(q)) j[2] += cz(q) > 0 ? v : -v;
+        }
+        const double rho = drho + 1.0;
+        const double u[3] = {j[0] / rho, j[1] / rho, j[2] / rho};
+        const double u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+        if (!isfinite(rho) || !isfinite(u2)) {
+            a[7] += 1.0;
+            continue;
+        }
+        a[0] = fmax(a[0], u2);
+        a[1] = fmax(a[1], fabs(rho - 1.0));
+        a[2] += drho;
+        a[3] += j[0];
+        a[4] += j[1];
+        a[5] += j[2];
+        a[6] += 1.0;
+    }
+    __shared__ double red[8][NSTAT];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        a[0] = fmax(a[0], __shfl_down_sync(0xffffffffu, a[0], o));
+        a[1] = fmax(a[1], __shfl_down_sync(0xffffffffu, a[1], o));
+        for (int k = 2; k < NSTAT; ++k) a[k] += __shfl_down_sync(0xffffffffu, a[k], o);
+    }
+    if (lane == 0)
+        for (int k = 0; k < NSTAT; ++k) red[warp][k] = a[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int nw = blockDim.x >> 5;
+        for (int wv = 1; wv < nw; ++wv) {
+            red[0][0] = fmax(red[0][0], red[wv][0]);
+            red[0][1] = fmax(red[0][1], red[wv][1]);
+            for (int k = 2; k < NSTAT; ++k) red[0][k] += red[wv][k];
+        }
+        for (int k = 0; k < NSTAT; ++k) partials[(long long)blockIdx.x * NSTAT + k] = red[0][k];
+    }
+}
+
+__global__ void k_region_final(const double *__restrict__ partials, int nblocks, double *__restrict__ out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double a[NSTAT];
+    for (int k = 0; k < NSTAT; ++k) a[k] = partials[k];
+    for (int b = 1; b < nblocks; ++b) {
+        a[0] = fmax(a[0], partials[b * NSTAT]);
+        a[1] = fmax(a[1], partials[b * NSTAT + 1]);
+        for (int k = 2; k < NSTAT; ++k) a[k] += partials[b * NSTAT + k];
+    }
+    for (int k = 0; k < NSTAT; ++k) out[k] = a[k];
+}
+
 }  // namespace ak

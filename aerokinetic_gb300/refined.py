@@ -7,25 +7,47 @@ Same construction and step interface as src/aerokinetic/refined_solver.py:115-34
 restriction) in the engine's sm_103a kernels (include/aerokinetic_gb300.h,
 ak_refined_*).
 """
+import csv
 import ctypes
+from dataclasses import asdict
+import hashlib
+import json
+import math
+from pathlib import Path
 
 import numpy as np
 
 from . import _native
 from ._native import check
-from .refined_plan import RefinedPlan, RefinementSettings
-from .solver import _leading_edge, _ptr
+from .project import write_json
+from .refined_plan import RefinedPlan, RefinementSettings, refined_project_dict
+from .solver import _duration_steps, _leading_edge, _ptr
 
 __all__ = ["RefinedSolver", "RefinementSettings", "RefinedPlan"]
 
 
+def _jsonable(value):
+    """Plan dictionaries hold dataclasses and tuples: plain JSON values."""
+    if isinstance(value, dict):
+        return {k: _jsonable(v) for k, v in value.items()}
+    if isinstance(value, (list, tuple)):
+        return [_jsonable(v) for v in value]
+    if isinstance(value, np.generic):
+        return value.item()
+    return value
+
+
 class RefinedSolver:
+    """Two-level solver.  budget=True (the reference's behaviour) closes the
+    mass and momentum budget of every step() (refined_solver.py:311-343);
+    budget=False skips the per-step integrals and outer-face fluxes."""
     pad = 2
 
-    def __init__(self, project, refinement=RefinementSettings(), progress=None, storage="f64"):
+    def __init__(self, project, refinement=RefinementSettings(), progress=None, storage="f64", budget=True):
         if storage not in _native.STORAGE:
             raise ValueError(f"storage must be one of {sorted(_native.STORAGE)}")
         self.project, self.refinement, self.storage = project, refinement, storage
+        self.budget = bool(budget)
         self.section, self.flow, self.grid = project.section, project.flow, project.grid
         self.plan = RefinedPlan.create(project, refinement)
         if self.plan.estimated_memory_gib > self.grid.memory_limit_gib:
@@ -61,6 +83,16 @@ class RefinedSolver:
         self._coarse = ctypes.c_void_p(self._lib.ak_refined_level(handle, 0))
         self._fine = ctypes.c_void_p(self._lib.ak_refined_level(handle, 1))
         self.fine_shape = tuple(2 * n for n in box.shape)
+        check(self._lib.ak_refined_track_budget(handle, int(self.budget)))
+        info = _native.CaseInfo()
+        check(self._lib.ak_case_get_info(self._fine, ctypes.byref(info)))
+        self.wall_fallback_links = int(info.fallback_links)
+        self.fine_fluid_cells = int(info.fluid_cells) - self._band_cells()
+        self.coarse_owned_cells = (nx * ny - box.shape[0] * box.shape[1]) * nz
+
+    def _band_cells(self):
+        fx, fy, fz = self.fine_shape
+        return ((fx + 2 * self.pad) * (fy + 2 * self.pad) - fx * fy) * fz
 
     def initialize_flow(self):
         """Free stream plus the seeded perturbation on both levels (refined_solver.py:224-269)."""
@@ -71,6 +103,9 @@ class RefinedSolver:
         check(self._lib.ak_refined_init_perturbed(self._handle, amp, phase_y, phase_z, float(leading[0]),
                                                   float(leading[1])))
         self.steps = 0
+        self.initialized = True
+        self.last_loads, self.last_budget = None, {}
+        self._integrals = self._initial_integrals = self.conserved_integrals()
 
     def _record(self, raw):
         f = self.fine_level
@@ -87,16 +122,135 @@ class RefinedSolver:
             record["time_s"] = (self.steps - 0.5) * self.plan.dt_seconds
         return record
 
+    # ------------------------------------------------------------ stepping
     def advance(self, nsteps):
-        """nsteps coarse steps in one engine call; loads of the last one."""
-        raw = np.zeros((len(self.contours), 5))
-        check(self._lib.ak_refined_step(self._handle, int(nsteps), _ptr(raw)))
-        self.steps += int(nsteps)
-        self.last_loads = self._record(raw)
-        return self.last_loads
+        """nsteps coarse steps; loads (and, with budget, the budget) of the last one."""
+        nsteps = int(nsteps)
+        if nsteps < 1:
+            raise ValueError("nsteps must be >= 1")
+        if not self.initialized:
+            raise RuntimeError("The refined state is invalid; initialize_flow() first")
+        try:
+            if nsteps > 1:
+                check(self._lib.ak_refined_step(self._handle, nsteps - 1, None))
+                self.steps += nsteps - 1
+                self._integrals = None
+            before = self._integrals if self._integrals is not None else (
+                self.conserved_integrals() if self.budget else None)
+            raw = np.zeros((len(self.contours), 5))
+            check(self._lib.ak_refined_step(self._handle, 1, _ptr(raw)))
+            self.steps += 1
+        except Exception:
+            self.initialized = False
+            raise
+        record = self._record(raw)
+        if self.budget:
+            self._close_budget(before, raw)
+        self.last_loads = record
+        return record
 
     def step(self):
         return self.advance(1)
+
+    def _close_budget(self, before, raw):
+        """refined_solver.py:329-339 from the engine's integrals and outer-face flux."""
+        f = self.fine_level
+        flux = np.zeros(8)
+        check(self._lib.ak_refined_outer_flux(self._handle, _ptr(flux)))
+        after = self.conserved_integrals()
+        self._integrals = after
+        unit = f.lattice_velocity_unit
+        external = flux[:4].copy()
+        external[1:] *= unit
+        impulse = raw[:, :3].sum(axis=0) * f.dx ** 3 * unit
+        wall_mass = float(raw[:, 4].sum() * f.dx ** 3)
+        mass_residual = after["mass"] - before["mass"] - external[0] - wall_mass
+        momentum_residual = np.array(after["momentum"]) - before["momentum"] - external[1:] + impulse
+        volume = self.coarse_owned_cells * self.coarse_level.dx ** 3 + self.fine_fluid_cells * f.dx ** 3
+        self.last_budget = {"mass_residual_per_volume": float(mass_residual / volume),
+                            "momentum_residual_per_volume": (momentum_residual / volume).tolist(),
+                            "wall_mass_exchange": wall_mass, "external_mass_in": float(external[0]),
+                            "wall_impulse": impulse.tolist(), "external_impulse_in": external[1:].tolist()}
+
+    # ------------------------------------------------------------ integrals, validity
+    def _stats(self):
+        out = np.zeros(16)
+        check(self._lib.ak_refined_integrals(self._handle, _ptr(out)))
+        return out[:8], out[8:]
+
+    def conserved_integrals(self):
+        """Mass and momentum of the coarse cells outside the fine box and the
+        fine fluid cells (refined_solver.py:291-299), common units."""
+        mass, impulse = 0.0, np.zeros(3)
+        for st, level in zip(self._stats(), (self.coarse_level, self.fine_level)):
+            if st[7]:
+                return {"mass": float("nan"), "momentum": [float("nan")] * 3}
+            volume = level.dx ** 3
+            mass += (st[6] + st[2]) * volume
+            impulse += st[3:6] * volume * level.lattice_velocity_unit
+        return {"mass": float(mass), "momentum": impulse.tolist()}
+
+    @property
+    def cumulative_wall_impulse(self):
+        cum = self._cumulative_loads()
+        return cum[:, :3].sum(axis=0) * self.fine_level.dx ** 3 * self.fine_level.lattice_velocity_unit
+
+    @property
+    def cumulative_wall_mass_exchange(self):
+        return float(self._cumulative_loads()[:, 4].sum() * self.fine_level.dx ** 3)
+
+    @property
+    def cumulative_external_in(self):
+        flux = np.zeros(8)
+        check(self._lib.ak_refined_outer_flux(self._handle, _ptr(flux)))
+        out = flux[4:].copy()
+        out[1:] *= self.fine_level.lattice_velocity_unit
+        return out
+
+    def _cumulative_loads(self):
+        cum = np.zeros((len(self.contours), 5))
+        check(self._lib.ak_refined_cumulative_loads(self._handle, _ptr(cum)))
+        return cum
+
+    def diagnostics(self):
+        """Local Mach and density guards over both leaves (refined_solver.py:347-361)."""
+        mach = density_error = 0.0
+        for st in self._stats():
+            if st[7]:
+                mach = density_error = float("nan")
+                break
+            mach = max(mach, math.sqrt(st[0]) * math.sqrt(3))
+            density_error = max(density_error, float(st[1]))
+        if not (mach <= 0.3 and density_error <= 0.1):
+            raise RuntimeError(f"Refined low-Mach state invalid: max Ma={mach:.5g}, density deviation={density_error:.5g}")
+        wall_mass = self.cumulative_wall_mass_exchange
+        return {"local_mach_max": mach, "density_error_max": density_error,
+                "wall_fallback_links_including_donors": self.wall_fallback_links,
+                "coarse_boundary_calls": self.coarse_boundary_calls, "fine_boundary_calls": self.fine_boundary_calls,
+                "cumulative_wall_mass_exchange": wall_mass,
+                "cumulative_wall_mass_exchange_over_initial_mass": wall_mass / self._initial_integrals["mass"],
+                "last_budget": self.last_budget}
+
+    @property
+    def fine_steps(self):
+        return 2 * self.steps
+
+    @property
+    def coarse_boundary_calls(self):
+        return self.steps
+
+    @property
+    def fine_boundary_calls(self):
+        return 2 * self.steps
+
+    @property
+    def time(self):
+        return self.steps * self.coarse_level.dt
+
+    @property
+    def case_fingerprint(self):
+        data = {"project_case": self.project.case_fingerprint, "refinement": asdict(self.refinement)}
+        return hashlib.sha256(json.dumps(data, sort_keys=True, separators=(",", ":")).encode()).hexdigest()
 
     def states(self):
         """Coarse populations (covered cells virtual) and the physical fine block, (x, y, z, 27)."""
@@ -107,6 +261,185 @@ class RefinedSolver:
         padded = np.empty((fx + 2 * self.pad, fy + 2 * self.pad, fz, 27))
         check(self._lib.ak_get_pdf(self._fine, _ptr(padded)))
         return coarse, padded[self.pad:-self.pad, self.pad:-self.pad]
+
+    # ------------------------------------------------------------ frames and runs
+    def level_macros(self):
+        """(rho, u) of both levels in lattice units: the coarse lattice and the
+        physical fine block, each (nx, ny, nz) and (nx, ny, nz, 3)."""
+        out = []
+        for handle, shape, crop in ((self._coarse, tuple(self.plan.shape), 0),
+                                    (self._fine, tuple(self.fine_shape), self.pad)):
+            full = (shape[0] + 2 * crop, shape[1] + 2 * crop, shape[2])
+            rho, u = np.empty(full), np.empty(full + (3,))
+            check(self._lib.ak_macros(handle, _ptr(rho), _ptr(u)))
+            if crop:
+                rho, u = rho[crop:-crop, crop:-crop], u[crop:-crop, crop:-crop]
+            out.append((rho, u))
+        return out
+
+    def slice_data(self, z_plane=None):
+        """Mid-span (or z_plane) section of both levels, the keys of
+        interface_visualization.py:16-42 with zero background velocity."""
+        z_plane = self.plan.span / 2 if z_plane is None else float(z_plane)
+        unit = self.coarse_level.lattice_velocity_unit
+        saved = {"time": self.time, "z_plane": z_plane, "background_velocity_lattice": np.zeros(3),
+                 "velocity_unit": unit}
+        box = self.plan.box
+        origins = ((self.plan.origin[0], self.plan.origin[1]),
+                   (self.plan.origin[0] + box.lower[0] * self.coarse_level.dx,
+                    self.plan.origin[1] + box.lower[1] * self.coarse_level.dx))
+        solid = self._fine_solid_xy()
+        for label, (rho, u), (ox, oy), dx in zip(("coarse", "fine"), self.level_macros(), origins,
+                                                  (self.coarse_level.dx, self.fine_level.dx)):
+            nx, ny, nz = rho.shape
+            zz = (np.arange(nz) + 0.5) * dx
+            if not zz[0] <= z_plane <= zz[-1]:
+                raise ValueError("Slice plane needs bracketing cell centres on both levels; extrapolation is unsupported")
+            upper = min(nz - 1, max(1, int(np.searchsorted(zz, z_plane))))
+            lower = upper - 1
+            fraction = (z_plane - zz[lower]) / (zz[upper] - zz[lower])
+            r = (1 - fraction) * rho[:, :, lower] + fraction * rho[:, :, upper]
+            j = (1 - fraction) * (rho * u.transpose(3, 0, 1, 2))[..., lower] + fraction * (
+                rho * u.transpose(3, 0, 1, 2))[..., upper]
+            velocity = np.moveaxis(j / r, 0, -1) * unit
+            if label == "coarse":
+                mask = np.zeros((nx, ny), bool)
+                mask[box.lower[0]:box.upper[0], box.lower[1]:box.upper[1]] = True
+            else:
+                mask = solid
+            saved[f"{label}_speed"] = np.linalg.norm(velocity, axis=-1)
+            saved[f"{label}_velocity_perturbation"] = velocity
+            saved[f"{label}_rho"] = r
+            saved[f"{label}_mask"] = mask
+            saved[f"{label}_dx"] = dx
+            saved[f"{label}_x_edges"] = ox + np.arange(nx + 1) * dx
+            saved[f"{label}_y_edges"] = oy + np.arange(ny + 1) * dx
+        return saved
+
+    def _fine_solid_xy(self):
+        if getattr(self, "_solid_cache", None) is None:
+            flags = np.zeros((self.fine_shape[0] + 2 * self.pad, self.fine_shape[1] + 2 * self.pad), dtype=np.uint8)
+            check(self._lib.ak_get_flags(self._fine, _ptr(flags)))
+            self._solid_cache = flags[self.pad:-self.pad, self.pad:-self.pad] != 0
+        return self._solid_cache
+
+    def save_frame(self, path):
+        """Mid-span section of both levels as .npz (refined_visualization.py:13-38)."""
+        data = self.slice_data()
+        data.update(format="aerokinetic_refined_slice", t_star=self.time,
+                    contours_json=json.dumps([c.xy.tolist() for c in self.contours]),
+                    fine_cells_per_chord=2 * self.grid.cells_per_chord)
+        if self.flow.physical_speed is not None:
+            data["physical_speed"] = self.flow.physical_speed
+            data["physical_dynamic_pressure"] = 0.5 * self.flow.atmosphere.rho * self.flow.physical_speed ** 2
+        for level in ("coarse", "fine"):
+            mask = data[f"{level}_mask"]
+            velocity = data[f"{level}_velocity_perturbation"].copy()
+            if level == "fine":
+                velocity[mask] = np.nan
+            cp = (data[f"{level}_rho"] - 1) / (1.5 * self.flow.lattice_speed ** 2)
+            cp[mask] = np.nan
+            dx = float(data[f"{level}_dx"])
+            omega = np.gradient(velocity[..., 1], dx, axis=0) - np.gradient(velocity[..., 0], dx, axis=1)
+            omega[mask] = np.nan
+            data[f"{level}_cp"] = cp
+            data[f"{level}_omega_z"] = omega
+            data[f"{level}_speed"][mask] = np.nan
+        path = Path(path)
+        tmp = path.with_name(path.name + ".tmp")
+        with open(tmp, "wb") as handle:
+            np.savez_compressed(handle, **data)
+        tmp.replace(path)
+        return path
+
+    def run(self, output, *, callback=None, stop_event=None, resume=False, residual_callback=None):
+        """Run the project's RunSettings and write project.json, history.csv,
+        metadata.json, summary.json and frames (refined_run.py:19-156) for new
+        runs; checks, samples, frames, the callback/stop_event contract and the
+        failed-run report follow the reference."""
+        if resume:
+            raise NotImplementedError("resume needs the GPU checkpoint format, which this engine does not write yet")
+        settings = self.project.run
+        requested = _duration_steps(settings.duration_convective, self.coarse_level.dt)
+        output = Path(output)
+        if output.exists() and any(output.iterdir()):
+            raise FileExistsError("Use a new/empty refined result directory")
+        output.mkdir(parents=True, exist_ok=True)
+        (output / "frames").mkdir()
+        history = output / "history.csv"
+        columns = ["step", "t_star", "cl", "cd", "cm"]
+        if self.plan.dt_seconds is not None:
+            columns.append("time_s")
+        end_step = self.steps + requested
+        metadata = {"format": "aerokinetic_refined_run", "version": "aerokinetic_gb300",
+                    "case_fingerprint": self.case_fingerprint, "flow": asdict(self.flow),
+                    "grid": asdict(self.grid), "refinement": asdict(self.refinement),
+                    "plan": _jsonable(self.plan.as_dict()), "run": asdict(settings), "start_step": self.steps,
+                    "contours": [{"name": e.name, "xy": e.xy.tolist()} for e in self.section.elements],
+                    "coefficient_convention": "Cl up; Cd downstream; Cm nose-up about the chosen reference; area=c*periodic_span",
+                    "force_time": "average of both fine momentum-transfer intervals; timestamp at coarse interval midpoint",
+                    "experimental_validation": "not_performed", "resume_supported": False,
+                    "storage": self.storage, "reference_chord_input_units": self.section.chord,
+                    "moment_reference_input_units": self.section.moment_reference}
+        write_json(output / "project.json", refined_project_dict(self.project, self.refinement))
+        with history.open("w", newline="", encoding="utf-8") as handle:
+            csv.DictWriter(handle, fieldnames=columns).writeheader()
+        self.save_frame(output / "frames" / f"frame_{self.steps:09d}.npz")
+        metadata.update(status="running", target_steps=end_step)
+        write_json(output / "metadata.json", metadata)
+        status, error, reason = "completed", None, "duration_reached"
+        try:
+            with history.open("a", newline="", encoding="utf-8") as handle:
+                writer = csv.DictWriter(handle, fieldnames=columns)
+                while self.steps < end_step:
+                    if stop_event is not None and stop_event.is_set():
+                        status, reason = "stopped", "user_stopped"
+                        break
+                    # steps up to the next one that checks, samples or writes a frame
+                    nxt = end_step
+                    for every in (settings.check_every, settings.sample_every, settings.frame_every):
+                        nxt = min(nxt, (self.steps // every + 1) * every)
+                    record = self.advance(nxt - self.steps)
+                    if self.steps % settings.check_every == 0:
+                        self.diagnostics()
+                    if self.steps % settings.sample_every == 0:
+                        writer.writerow({k: record[k] for k in columns})
+                        handle.flush()
+                        if callback is not None and callback(self, record) is False:
+                            status, reason = "stopped", "user_stopped"
+                    if self.steps % settings.frame_every == 0:
+                        self.save_frame(output / "frames" / f"frame_{self.steps:09d}.npz")
+                    if status == "stopped":
+                        break
+            self.diagnostics()
+            self.save_frame(output / "frames" / f"frame_{self.steps:09d}.npz")
+        except Exception as failure:
+            status, error, reason = "failed", f"{type(failure).__name__}: {failure}", "failed"
+        with history.open(newline="", encoding="utf-8") as handle:
+            rows = list(csv.DictReader(handle))
+        selected = [r for r in rows if float(r["t_star"]) >= settings.average_after]
+        mean = {n: float(np.mean([float(r[n]) for r in selected])) for n in ("cl", "cd", "cm")} if selected else None
+        rms = {n: float(np.std([float(r[n]) for r in selected])) for n in ("cl", "cd", "cm")} if selected else None
+        final = {"state": "invalid"}
+        if self.initialized:
+            try:
+                final = self.diagnostics()
+            except Exception as failure:
+                status, error, reason = "failed", f"{type(failure).__name__}: {failure}", "failed"
+                self.initialized = False
+        summary = {"status": status, "steps": self.steps, "fine_steps": self.fine_steps, "t_star": self.time,
+                   "average_after_t_star": settings.average_after, "samples": len(rows),
+                   "averaging_samples": len(selected), "mean": mean, "rms": rms,
+                   "experimental_validation": "not_performed", "statistical_convergence": "not_established",
+                   "diagnostics": final, "termination_reason": reason}
+        if error:
+            summary["error"] = error
+        metadata.update(status=status, completed_steps=self.steps, termination_reason=reason)
+        write_json(output / "metadata.json", metadata)
+        write_json(output / "summary.json", summary)
+        if error:
+            raise RuntimeError(error)
+        return summary
 
     def close(self):
         if getattr(self, "_handle", None):

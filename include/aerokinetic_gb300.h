@@ -171,9 +171,30 @@ int ak_refined_init_perturbed(ak_refined *r, double amp, double phase_y, double 
 /* nsteps coarse steps (PeriodicRefinedBox._step_once, interface.py:311-352);
  * loads[n_elements * 5] = fine-lattice (Fx, Fy, Fz, Mz, mass) of the last
  * coarse step summed over its two fine steps (walls.py:68-95), Mz about the
- * normalised frame's origin in fine lattice units. */
+ * normalised frame's origin in fine lattice units.  The step's kernels are
+ * captured once per buffer parity into CUDA graphs and replayed. */
 int ak_refined_step(ak_refined *r, int32_t nsteps, double *loads);
 int64_t ak_refined_steps_done(const ak_refined *r);
+/* With enable != 0, every following step also measures the inflow through
+ * the outer x and y faces of the coarse lattice after its boundaries
+ * (refined_solver.py:274-278, the samplers of refined_solver.py:215-222). */
+int ak_refined_track_budget(ak_refined *r, int32_t enable);
+/* out[0..3] = inflow (mass, jx, jy, jz) of the last tracked step, coarse
+ * lattice units times dx^3: the reference's _interval_external_in before its
+ * momentum is scaled to common velocity units; out[4..7] = its sum over the
+ * tracked steps since initialisation (cumulative_external_in,
+ * refined_solver.py:342). */
+int ak_refined_outer_flux(ak_refined *r, double *out);
+/* out[n_elements * 5] = fine-lattice (Fx, Fy, Fz, Mz, mass) summed over every
+ * step since initialisation (cumulative_wall_impulse and
+ * cumulative_wall_mass_exchange, refined_solver.py:340-341). */
+int ak_refined_cumulative_loads(ak_refined *r, double *out);
+/* Per-level statistics for conserved_integrals and diagnostics
+ * (refined_solver.py:291-299, 347-361): out[0..7] coarse cells outside the
+ * fine box, out[8..15] fluid cells of the physical fine block, each
+ * (max |u|^2, max |rho - 1|, sum (rho - 1), sum jx, sum jy, sum jz, cells,
+ * non-finite cells) in the level's lattice units. */
+int ak_refined_integrals(ak_refined *r, double *out);
 /* ak_refined_step without loads, timed with CUDA events on the case's stream:
  * ms[0] whole interval, ms[1] coarse collide, ms[2] coarse stream, ms[3] fine
  * collides, ms[4] fine streams, ms[5] the rest (interface transfers, face

@@ -200,6 +200,9 @@ class RefinedCase:
         self.coarse_owned = np.ones(self.shape, bool)
         self.coarse_owned[self.box] = False
         self._faces()
+        self._outer_samplers()
+        self.external_in = None
+        self.outer_convention = "padded"
         self._lattices(threads)
         self._initialise(perturbation, seed, leading)
         self.steps = 0
@@ -224,6 +227,40 @@ class RefinedCase:
                 self.reflux_support[outside] = True
                 self.faces.append((axis, side, outside, FaceFlux(self.shape, axis, cidx, cranges, True),
                                    FaceFlux(self.padded, axis, fidx, franges, False)))
+
+    # refined_solver.py:215-222: flux samplers on the six outer faces of the
+    # padded coarse lattice (the z pair cancels: its ghosts are periodic copies)
+    def _outer_samplers(self):
+        padded = tuple(n + 2 for n in self.shape)
+        self.outer = []
+        for axis in range(3):
+            ranges = [(1, self.shape[a] + 1) for a in range(3) if a != axis]
+            for side, index in ((-1, 0), (1, self.shape[axis])):
+                self.outer.append((axis, side, FaceFlux(padded, axis, index, ranges, False)))
+
+    def _wrapped_view(self, pdf):
+        """The padded coarse state as a lattice that wraps z by index holds it.
+
+        With z ghost layers (the reference's layout) a ghost-column population
+        that streaming pulls across the periodic z seam is written into a z
+        ghost layer, while its slot in the interior layer keeps an older value;
+        with z wrapped by index it lives in the interior layer.  The outer-face
+        samplers read such slots, so the two layouts can give slightly
+        different outer fluxes (on the refined start-up case the budgets agree
+        to 1e-17 per volume); with outer_convention "wrapped" the samplers read
+        this view, the engine's layout."""
+        nz = self.shape[2]
+        c, _, _ = O.stencil()
+        view = pdf.copy()
+        ring = np.ones(view.shape[:2], bool)
+        ring[1:-1, 1:-1] = False
+        for q in np.where(c[:, 2] == 1)[0]:
+            view[ring, nz, q] = pdf[ring, 0, q]
+        for q in np.where(c[:, 2] == -1)[0]:
+            view[ring, 1, q] = pdf[ring, nz + 1, q]
+        view[:, :, 0] = view[:, :, nz]
+        view[:, :, nz + 1] = view[:, :, 1]
+        return view
 
     def _lattices(self, threads):
         c = self.coarse_level
@@ -377,6 +414,11 @@ class RefinedCase:
         lat.sync()
         lat.apply_boundaries()
         measured = self._measure() if lat is self.fine else None
+        if lat is self.coarse and self.external_in is not None:
+            # refined_solver.py:274-278: inflow through the outer faces
+            pdf = lat.pdf if self.outer_convention == "padded" else self._wrapped_view(lat.pdf)
+            for _, side, sampler in self.outer:
+                self.external_in -= side * sampler(pdf).sum(axis=(0, 1)) * self.coarse_level.dx ** 3
         nx, ny, nz = lat.shape
         O.lib().ako_stream(O._p(lat.pdf), O._p(lat.tmp), nx, ny, nz)
         lat.pdf, lat.tmp = lat.tmp, lat.pdf
@@ -433,4 +475,57 @@ class RefinedCase:
         q_area = 0.5 * self.span
         force = impulse / c.dt
         return {"step": self.steps, "cl": float(force[1] / q_area), "cd": float(force[0] / q_area),
-                "cm": float(-(moment / c.dt) / q_area), "wall_mass": float(sum(w[2] for w in walls) * volume)}
+                "cm": float(-(moment / c.dt) / q_area), "wall_mass": float(sum(w[2] for w in walls) * volume),
+                "wall_impulse": impulse}
+
+    def fine_fluid(self):
+        return np.broadcast_to((self.fine.flags[1:-1, 1:-1, 1:-1] == 0)[self.fine_slices], self.fine_shape)
+
+    # refined_solver.py:291-299
+    def conserved_integrals(self):
+        mass, impulse = 0.0, np.zeros(3)
+        c, _, _ = O.stencil()
+        views = (self.coarse.interior(), self.fine.interior()[self.fine_slices])
+        for pdf, owned, level in zip(views, (self.coarse_owned, self.fine_fluid()),
+                                      (self.coarse_level, self.fine_level)):
+            rho = pdf.sum(axis=-1) + 1
+            j = pdf @ c.astype(np.float64)
+            mass += rho[owned].sum() * level.dx ** 3
+            impulse += j[owned].sum(axis=0) * level.dx ** 3 * level.velocity_unit
+        return {"mass": float(mass), "momentum": impulse.tolist()}
+
+    # refined_solver.py:311-343: the step plus its mass and momentum budget
+    def step_with_budget(self):
+        before = self.conserved_integrals()
+        self.external_in = np.zeros(4)
+        try:
+            record = self.step()
+        finally:
+            external, self.external_in = self.external_in, None
+        after = self.conserved_integrals()
+        unit = self.fine_level.velocity_unit
+        external[1:] *= unit
+        impulse = record["wall_impulse"]
+        mass_residual = after["mass"] - before["mass"] - external[0] - record["wall_mass"]
+        momentum_residual = np.array(after["momentum"]) - before["momentum"] - external[1:] + impulse
+        volume = (np.count_nonzero(self.coarse_owned) * self.coarse_level.dx ** 3
+                  + np.count_nonzero(self.fine_fluid()) * self.fine_level.dx ** 3)
+        record["budget"] = {"mass_residual_per_volume": float(mass_residual / volume),
+                            "momentum_residual_per_volume": (momentum_residual / volume).tolist(),
+                            "wall_mass_exchange": record["wall_mass"], "external_mass_in": float(external[0]),
+                            "wall_impulse": impulse.tolist(), "external_impulse_in": external[1:].tolist()}
+        return record
+
+    # refined_solver.py:347-361 (the numeric part): leaf moments over owned
+    # coarse cells and fine fluid cells
+    def diagnostics(self):
+        mach, density_error = 0.0, 0.0
+        fine = self.fine.interior()[self.fine_slices].copy()
+        fine[~self.fine_fluid()] = self.free_pdf
+        for pdf, owned in ((self.coarse.interior(), self.coarse_owned), (fine, self.fine_fluid())):
+            m = self.T.moments(pdf)
+            rho = m[..., 0][owned]
+            u = m[..., 1:4][owned] / rho[:, None]
+            mach = max(mach, float(np.linalg.norm(u, axis=-1).max() * math.sqrt(3)))
+            density_error = max(density_error, float(np.max(abs(rho - 1))))
+        return {"local_mach_max": mach, "density_error_max": density_error}

@@ -283,3 +283,74 @@ def test_refined_graph_replay_matches_eager_steps(golden):
     finally:
         replay.close()
         eager.close()
+
+
+def test_refined_budget_integrals_and_diagnostics_match_oracle(golden):
+    """conserved_integrals, the per-step budget (last_budget) and diagnostics
+    (refined_solver.py:291-361) against the oracle sampling the outer faces in
+    the engine's z-wrapped layout; residuals within the reference's gates."""
+    solver, oracle = refined_pair(golden["histories"]["refined_startup"])
+    oracle.outer_convention = "wrapped"
+    try:
+        mine, theirs = solver.conserved_integrals(), oracle.conserved_integrals()
+        assert mine["mass"] == pytest.approx(theirs["mass"], rel=1e-14)
+        # the reference's momentum integral (pdf @ stencil, then a sum over
+        # axis 0) carries ~3.5e-12 relative rounding on this case against an
+        # exactly rounded sum (math.fsum); the engine's tree sum is closer to it
+        np.testing.assert_allclose(mine["momentum"], theirs["momentum"], rtol=1e-10, atol=1e-16)
+        wall_mass = 0.0
+        for s in range(1, 4):
+            solver.step()
+            ref = oracle.step_with_budget()["budget"]
+            got = solver.last_budget
+            assert abs(got["mass_residual_per_volume"]) <= 5e-11
+            assert max(map(abs, got["momentum_residual_per_volume"])) <= 2e-12
+            for key in ("wall_mass_exchange", "external_mass_in"):
+                assert got[key] == pytest.approx(ref[key], rel=1e-9, abs=1e-14), (s, key)
+            for key in ("wall_impulse", "external_impulse_in"):
+                np.testing.assert_allclose(got[key], ref[key], rtol=1e-9, atol=1e-14)
+            np.testing.assert_allclose(got["momentum_residual_per_volume"], ref["momentum_residual_per_volume"],
+                                       rtol=0, atol=1e-12)
+            wall_mass += ref["wall_mass_exchange"]
+        assert solver.cumulative_wall_mass_exchange == pytest.approx(wall_mass, rel=1e-9, abs=1e-14)
+        ours, ref = solver.diagnostics(), oracle.diagnostics()
+        assert ours["local_mach_max"] == pytest.approx(ref["local_mach_max"], rel=1e-12)
+        assert ours["density_error_max"] == pytest.approx(ref["density_error_max"], rel=1e-10)
+        assert ours["fine_boundary_calls"] == 6 and ours["last_budget"] is solver.last_budget
+    finally:
+        solver.close()
+
+
+def test_refined_run_writes_history_frames_and_summary(golden, tmp_path):
+    """RefinedSolver.run (refined_run.py:19-156) for a new run: history rows at
+    sample_every, frames, metadata and summary with the guards' diagnostics."""
+    import csv
+    import dataclasses
+    import json
+    from aerokinetic_gb300.project import RunSettings
+    from aerokinetic_gb300.refined import RefinedSolver
+    from aerokinetic_gb300.refined_plan import load_refined_project
+    project, refinement = load_refined_project(golden["histories"]["refined_startup"]["project"])
+    settings = RunSettings(duration_convective=0.1, sample_every=4, frame_every=16, check_every=4, average_after=0.0)
+    project = dataclasses.replace(project, run=settings)
+    solver = RefinedSolver(project, refinement)
+    try:
+        steps = int(np.ceil(0.1 / solver.coarse_level.dt - 1e-9))
+        summary = solver.run(tmp_path / "out")
+        assert summary["status"] == "completed" and summary["steps"] == steps
+        rows = list(csv.DictReader((tmp_path / "out" / "history.csv").open()))
+        assert [int(r["step"]) for r in rows] == list(range(4, steps + 1, 4))
+        assert summary["samples"] == len(rows) and summary["mean"] is not None
+        assert summary["diagnostics"]["local_mach_max"] < 0.3
+        meta = json.loads((tmp_path / "out" / "metadata.json").read_text())
+        assert meta["status"] == "completed" and meta["case_fingerprint"] == solver.case_fingerprint
+        frames = sorted((tmp_path / "out" / "frames").glob("frame_*.npz"))
+        assert len(frames) >= 2
+        with np.load(frames[-1]) as frame:
+            assert frame["coarse_speed"].shape == tuple(solver.plan.shape[:2])
+            assert frame["fine_speed"].shape == tuple(solver.fine_shape[:2])
+            assert np.isnan(frame["fine_cp"][frame["fine_mask"]]).all()
+        with pytest.raises(FileExistsError):
+            solver.run(tmp_path / "out")
+    finally:
+        solver.close()

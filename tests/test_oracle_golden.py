@@ -244,3 +244,36 @@ def test_refined_startup_history(golden):
             loads = case.step()
         for k in ("cl", "cd", "cm"):
             assert loads[k] == pytest.approx(row[k], abs=1e-12)
+
+
+def _refined_startup_case(golden):
+    from aerokinetic_gb300.refined_plan import RefinedPlan, load_refined_project
+    from oracle.refined import RefinedCase
+    project, refinement = load_refined_project(golden["histories"]["refined_startup"]["project"])
+    plan = RefinedPlan.create(project, refinement)
+    sec, flow = project.section, project.flow
+    lead = O.leading_edge([e.xy for e in sec.elements], sec.moment_reference, sec.chord, flow.alpha_deg)
+    return RefinedCase([c.xy for c in sec.normalized(flow.alpha_deg)], plan.shape, plan.origin, plan.coarse_level.dx,
+                       plan.coarse_level.dt, plan.coarse_level.tau_shear, plan.coarse_level.tau_bulk,
+                       plan.box.lower, plan.box.upper, flow.lattice_speed, flow.perturbation, flow.seed, lead,
+                       plan.span, oracle_threads())
+
+
+def test_refined_budget_closes_within_reference_gates(golden):
+    """The per-step mass and momentum budget (refined_solver.py:311-343) closes
+    within the reference's own gates (tests/test_run_controls.py:82-83: mass
+    5e-11, momentum 2e-12 per volume) with the outer faces sampled from the
+    reference's padded layout and from the z-wrapped layout the engine uses;
+    the two layouts give the same budget to 1e-15 per volume."""
+    padded, wrapped = _refined_startup_case(golden), _refined_startup_case(golden)
+    wrapped.outer_convention = "wrapped"
+    for _ in range(2):
+        a, b = padded.step_with_budget()["budget"], wrapped.step_with_budget()["budget"]
+        for budget in (a, b):
+            assert abs(budget["mass_residual_per_volume"]) <= 5e-11
+            assert max(map(abs, budget["momentum_residual_per_volume"])) <= 2e-12
+        assert abs(a["mass_residual_per_volume"] - b["mass_residual_per_volume"]) <= 1e-15
+        assert np.allclose(a["external_impulse_in"], b["external_impulse_in"], rtol=0, atol=1e-15)
+        assert a["wall_mass_exchange"] == b["wall_mass_exchange"]
+    diag = padded.diagnostics()
+    assert 0 < diag["local_mach_max"] < 0.3 and 0 < diag["density_error_max"] < 0.1
