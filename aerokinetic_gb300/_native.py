@@ -106,6 +106,13 @@ SIGNATURES = {
     "ak_refined_outer_flux": ([_P, _P], ctypes.c_int),
     "ak_refined_integrals": ([_P, _P], ctypes.c_int),
     "ak_refined_cumulative_loads": ([_P, _P], ctypes.c_int),
+    "ak_batch_create": ([_P, ctypes.c_int32, _P], ctypes.c_int),
+    "ak_batch_destroy": ([_P], ctypes.c_int),
+    "ak_batch_step": ([_P, ctypes.c_int32, _P], ctypes.c_int),
+    "ak_batch_tune": ([_P, ctypes.c_int32, _P], ctypes.c_int),
+    "ak_batch_launches": ([_P], ctypes.c_int64),
+    "ak_batch_steps_done": ([_P], ctypes.c_int64),
+    "ak_batch_stream": ([_P], _P),
     "ak_refined_step_timed": ([_P, ctypes.c_int32, _P], ctypes.c_int),
     "ak_refined_level": ([_P, ctypes.c_int32], _P),
     "ak_last_error": ([], ctypes.c_char_p),

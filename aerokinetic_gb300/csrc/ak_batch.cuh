@@ -1,0 +1,120 @@
+// ak_batch.cuh -- many independent uniform cases advanced by one set of
+// launches per step.
+//
+// A batch holds a device array of per-case descriptors (BatchCase) and, for
+// every kernel of the uniform step, a packed work table of (case, chunk)
+// items: the characteristic farfield's ring macros and links, the Bouzidi
+// wall links and the fused stream-collide blocks.  A step is therefore four
+// launches (five when loads are sampled) whatever the number of cases, each
+// kernel running the same per-item body as the single-case kernel
+// (ak_kernels.cuh) on the item's case, so a case computes the same bits alone
+// and in any mix.  The stream-collide launch is persistent: a fixed grid of
+// CTAs strides over the packed block table, whose block width, grid size and
+// ordering (case-major or interleaved) the host tunes per batch.
+#pragma once
+#include "ak_kernels.cuh"
+
+namespace ak {
+
+template <typename S>
+struct BatchCase {
+    S *pdf[2];
+    const uint8_t *flags;
+    Grid G;
+    typename Store<S>::T omega_s, omega_b;
+    int cur0;  // copy holding the case's state at batch parity 0
+    int n_elements;
+    double ox, oy;
+    // characteristic farfield
+    OuterLinks L;
+    FarfieldParams P;
+    Ring R;
+    double *ff_in, *ff_der;
+    long long *ff_clock;
+    const double *ff_lo, *ff_hi;
+    // Bouzidi walls and their load partials [element][block][5]
+    const WallKey *keys;
+    const double *wall_q;
+    long long nkeys;
+    double *partials;
+    long long wall_blocks;
+};
+
+struct WorkItem {
+    int c;      // case
+    int chunk;  // block of that case's items
+};
+
+template <typename S>
+__device__ __forceinline__ S *batch_src(const BatchCase<S> &c, int parity) {
+    return c.pdf[c.cur0 ^ parity];
+}
+
+template <typename S>
+__global__ void __launch_bounds__(256)
+    k_batch_ring_macros(const BatchCase<S> *__restrict__ cases, const WorkItem *__restrict__ work, int parity) {
+    const WorkItem w = work[blockIdx.x];
+    const BatchCase<S> &c = cases[w.c];
+    const long long i = (long long)w.chunk * blockDim.x + threadIdx.x;
+    if (i >= c.R.n * c.G.nz) return;
+    ring_macro_item(batch_src(c, parity), c.G, c.R, i);
+}
+
+template <typename S>
+__global__ void __launch_bounds__(256)
+    k_batch_farfield(const BatchCase<S> *__restrict__ cases, const WorkItem *__restrict__ work, int parity) {
+    const WorkItem w = work[blockIdx.x];
+    const BatchCase<S> &c = cases[w.c];
+    const long long i = (long long)w.chunk * blockDim.x + threadIdx.x;
+    if (i >= c.L.n) return;
+    farfield_link(batch_src(c, parity), c.G, c.L, c.P, c.R, c.ff_in, c.ff_der, c.ff_clock, c.ff_lo, c.ff_hi, 0, i);
+}
+
+template <typename S>
+__global__ void __launch_bounds__(256) k_batch_walls(const BatchCase<S> *__restrict__ cases,
+                                                     const WorkItem *__restrict__ work, int parity, int sample) {
+    const WorkItem w = work[blockIdx.x];
+    const BatchCase<S> &c = cases[w.c];
+    const long long tid = (long long)w.chunk * blockDim.x + threadIdx.x;
+    double acc[5] = {0, 0, 0, 0, 0};
+    int element = -1;
+    if (tid < c.nkeys * c.G.nz * 3) wall_link(batch_src(c, parity), c.G, c.keys, c.wall_q, tid, sample, c.ox, c.oy, acc, element);
+    if (!sample) return;
+    wall_block_sums(acc, element, c.n_elements, c.partials, w.chunk, c.wall_blocks);
+}
+
+// loads[case][MAX_ELEMENTS * 5]: the per-element sums of k_sum_partials, in
+// the same lane-strided order
+template <typename S>
+__global__ void k_batch_sum_partials(const BatchCase<S> *__restrict__ cases, double *__restrict__ loads) {
+    const BatchCase<S> &c = cases[blockIdx.y];
+    const int t = blockIdx.x, lane = threadIdx.x;
+    if (t >= 5 * c.n_elements) return;
+    const int e = t / 5, k = t - 5 * (t / 5);
+    double s = 0.0;
+    for (long long b = lane; b < c.wall_blocks; b += 32) s += c.partials[((long long)e * c.wall_blocks + b) * 5 + k];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) loads[(long long)blockIdx.y * 5 * MAX_ELEMENTS + t] = s;
+}
+
+// fused pull-stream + collision over the packed block table; block chunk of
+// a case covers x in [bx * TB, bx * TB + TB) of row (y, z)
+template <typename S, int TB>
+__global__ void __launch_bounds__(TB, Store<S>::MIN_BLOCKS * 128 / TB)
+    k_batch_bulk(const BatchCase<S> *__restrict__ cases, const WorkItem *__restrict__ work, long long n_work,
+                 int parity) {
+    for (long long e = blockIdx.x; e < n_work; e += gridDim.x) {
+        const WorkItem w = work[e];
+        const BatchCase<S> &c = cases[w.c];
+        const Grid G = c.G;
+        const int nbx = (G.nx + TB - 1) / TB;
+        const int bx = w.chunk % nbx, r = w.chunk / nbx;
+        const int y = r % G.ny + 1, z = r / G.ny;
+        const int x = bx * TB + threadIdx.x + 1;
+        if (x <= G.nx)
+            stream_collide_cell(c.pdf[c.cur0 ^ parity], c.pdf[c.cur0 ^ parity ^ 1], c.flags, G, G.shift, c.omega_s,
+                                c.omega_b, x, y, z);
+    }
+}
+
+}  // namespace ak

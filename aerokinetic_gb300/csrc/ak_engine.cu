@@ -16,6 +16,7 @@
 #include "../../include/aerokinetic_gb300.h"
 #include "ak_geometry.cuh"
 #include "ak_transfer.cuh"
+#include "ak_batch.cuh"
 
 using namespace ak;
 
@@ -1559,5 +1560,392 @@ int ak_refined_step_timed(ak_refined *R, int32_t nsteps, double *ms) {
     AK_CUDA(e);
     return AK_OK;
 }
+
+}  // extern "C"
+
+// ==================================================================== batch
+// Independent uniform cases with the characteristic farfield, stepped by one
+// set of launches per step (ak_batch.cuh).  The batch borrows the cases: it
+// owns only its descriptors, work tables, stream and graphs.
+struct ak_batch {
+    std::vector<ak_case *> cases;
+    std::vector<int> cur0;
+    int storage = 0, device = 0, sms = 0;
+    cudaStream_t stream = nullptr;
+    void *d_cases = nullptr;
+    WorkItem *w_ring = nullptr, *w_ff = nullptr, *w_walls = nullptr, *w_bulk = nullptr;
+    long long n_ring = 0, n_ff = 0, n_walls = 0, n_bulk = 0;
+    double *loads = nullptr;  // [case][MAX_ELEMENTS * 5]
+    int parity = 0;
+    long long steps = 0, launches = 0;
+    // stream-collide schedule: block width, CTAs per SM of the persistent
+    // grid, table order (0 case-major, 1 interleaved)
+    int tb = 128, per_sm = 4, order = 0;
+    cudaGraphExec_t graph[4] = {};  // (parity, sample)
+};
+
+namespace {
+
+void batch_drop_graphs(ak_batch *B) {
+    for (cudaGraphExec_t &g : B->graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+}
+
+void batch_release(ak_batch *B) {
+    if (B->stream) cudaStreamSynchronize(B->stream);
+    batch_drop_graphs(B);
+    for (void *p : {(void *)B->d_cases, (void *)B->w_ring, (void *)B->w_ff, (void *)B->w_walls, (void *)B->w_bulk,
+                    (void *)B->loads})
+        if (p) cudaFree(p);
+    if (B->stream) cudaStreamDestroy(B->stream);
+}
+
+int upload_work(WorkItem **dst, const std::vector<WorkItem> &v) {
+    if (*dst) cudaFree(*dst);
+    *dst = nullptr;
+    const size_t n = std::max<size_t>(1, v.size());
+    cudaError_t e = cudaMalloc((void **)dst, n * sizeof(WorkItem));
+    if (e != cudaSuccess)
+        return fail(e == cudaErrorMemoryAllocation ? AK_ERR_NOMEM : AK_ERR_CUDA,
+                    std::string("batch table allocation failed: ") + cudaGetErrorString(e));
+    if (!v.empty()) AK_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(WorkItem), cudaMemcpyHostToDevice));
+    return AK_OK;
+}
+
+// chunks of 256 items per case, case after case
+std::vector<WorkItem> chunk_table(const std::vector<long long> &items) {
+    std::vector<WorkItem> out;
+    for (size_t c = 0; c < items.size(); ++c)
+        for (long long k = 0; k < blocks_for(items[c], 256); ++k) out.push_back(WorkItem{(int)c, (int)k});
+    return out;
+}
+
+// the stream-collide blocks of every case for block width tb
+std::vector<WorkItem> bulk_table(const ak_batch *B, int tb, int order) {
+    std::vector<long long> count;
+    for (const ak_case *c : B->cases) count.push_back(blocks_for(c->nx, tb) * c->ny * c->nz);
+    std::vector<WorkItem> out;
+    if (order == 0) {
+        for (size_t c = 0; c < count.size(); ++c)
+            for (long long k = 0; k < count[c]; ++k) out.push_back(WorkItem{(int)c, (int)k});
+    } else {
+        // round robin over the cases, so every stretch of the table mixes cases
+        const long long most = *std::max_element(count.begin(), count.end());
+        for (long long k = 0; k < most; ++k)
+            for (size_t c = 0; c < count.size(); ++c)
+                if (k < count[c]) out.push_back(WorkItem{(int)c, (int)k});
+    }
+    return out;
+}
+
+template <typename S>
+int bulk_launch(ak_batch *B, int tb, int grid, int parity) {
+    const BatchCase<S> *cases = (const BatchCase<S> *)B->d_cases;
+    switch (tb) {
+    case 64: k_batch_bulk<S, 64><<<grid, 64, 0, B->stream>>>(cases, B->w_bulk, B->n_bulk, parity); break;
+    case 128: k_batch_bulk<S, 128><<<grid, 128, 0, B->stream>>>(cases, B->w_bulk, B->n_bulk, parity); break;
+    case 256: k_batch_bulk<S, 256><<<grid, 256, 0, B->stream>>>(cases, B->w_bulk, B->n_bulk, parity); break;
+    default: return fail(AK_ERR_INVALID, "unsupported block width");
+    }
+    AK_CUDA(cudaGetLastError());
+    return AK_OK;
+}
+
+template <typename S>
+int bulk_occupancy(int tb, int *blocks) {
+    cudaError_t e = cudaErrorInvalidValue;
+    if (tb == 64) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_batch_bulk<S, 64>, 64, 0);
+    if (tb == 128) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_batch_bulk<S, 128>, 128, 0);
+    if (tb == 256) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, k_batch_bulk<S, 256>, 256, 0);
+    if (e != cudaSuccess) return fail(AK_ERR_CUDA, std::string("occupancy query failed: ") + cudaGetErrorString(e));
+    return AK_OK;
+}
+
+template <typename S>
+int batch_enqueue(ak_batch *B, int parity, bool sample) {
+    const BatchCase<S> *cases = (const BatchCase<S> *)B->d_cases;
+    if (B->n_ring) {
+        k_batch_ring_macros<S><<<(unsigned)B->n_ring, 256, 0, B->stream>>>(cases, B->w_ring, parity);
+        AK_CUDA(cudaGetLastError());
+    }
+    if (B->n_ff) {
+        k_batch_farfield<S><<<(unsigned)B->n_ff, 256, 0, B->stream>>>(cases, B->w_ff, parity);
+        AK_CUDA(cudaGetLastError());
+    }
+    if (B->n_walls) {
+        k_batch_walls<S><<<(unsigned)B->n_walls, 256, 0, B->stream>>>(cases, B->w_walls, parity, sample ? 1 : 0);
+        AK_CUDA(cudaGetLastError());
+    }
+    if (sample) {
+        k_batch_sum_partials<S><<<dim3(5 * MAX_ELEMENTS, (unsigned)B->cases.size()), 32, 0, B->stream>>>(cases,
+                                                                                                      B->loads);
+        AK_CUDA(cudaGetLastError());
+    }
+    AK_TRY(bulk_launch<S>(B, B->tb, B->per_sm * B->sms, parity));
+    return AK_OK;
+}
+
+long long batch_step_launches(const ak_batch *B, bool sample) {
+    return (B->n_ring ? 1 : 0) + (B->n_ff ? 1 : 0) + (B->n_walls ? 1 : 0) + (sample ? 1 : 0) + 1;
+}
+
+template <typename S>
+int batch_build(ak_batch *B) {
+    std::vector<BatchCase<S>> host;
+    std::vector<long long> ring, ff, walls;
+    for (size_t i = 0; i < B->cases.size(); ++i) {
+        ak_case *c = B->cases[i];
+        BatchCase<S> d{};
+        d.pdf[0] = (S *)c->pdf[0];
+        d.pdf[1] = (S *)c->pdf[1];
+        d.flags = c->flags;
+        d.G = c->G;
+        d.omega_s = (typename Store<S>::T)c->omega_s;
+        d.omega_b = (typename Store<S>::T)c->omega_b;
+        d.cur0 = B->cur0[i];
+        d.n_elements = c->n_elements;
+        d.ox = c->ox;
+        d.oy = c->oy;
+        d.L = c->outer();
+        d.P = c->ff();
+        d.R = c->ring();
+        d.ff_in = c->ff_in;
+        d.ff_der = c->ff_der;
+        d.ff_clock = c->ff_clock;
+        d.ff_lo = c->ff_lo;
+        d.ff_hi = c->ff_hi;
+        d.keys = c->keys;
+        d.wall_q = c->wall_q;
+        d.nkeys = c->nkeys;
+        const long long nlinks = c->nkeys * c->nz * 3;
+        d.wall_blocks = blocks_for(nlinks, 256);
+        if (nlinks) AK_TRY(ensure_partials(c, d.wall_blocks * 5 * c->n_elements));
+        d.partials = c->partials;
+        host.push_back(d);
+        ring.push_back(c->ring_n * c->nz);
+        ff.push_back(c->nouter);
+        walls.push_back(nlinks);
+    }
+    AK_CUDA(cudaMalloc(&B->d_cases, host.size() * sizeof(BatchCase<S>)));
+    AK_CUDA(cudaMemcpy(B->d_cases, host.data(), host.size() * sizeof(BatchCase<S>), cudaMemcpyHostToDevice));
+    const std::vector<WorkItem> tr = chunk_table(ring), tf = chunk_table(ff), tw = chunk_table(walls);
+    B->n_ring = (long long)tr.size();
+    B->n_ff = (long long)tf.size();
+    B->n_walls = (long long)tw.size();
+    AK_TRY(upload_work(&B->w_ring, tr));
+    AK_TRY(upload_work(&B->w_ff, tf));
+    AK_TRY(upload_work(&B->w_walls, tw));
+    const std::vector<WorkItem> tb = bulk_table(B, B->tb, B->order);
+    B->n_bulk = (long long)tb.size();
+    AK_TRY(upload_work(&B->w_bulk, tb));
+    int occ = 0;
+    AK_TRY(bulk_occupancy<S>(B->tb, &occ));
+    B->per_sm = std::max(1, occ);
+    AK_CUDA(cudaMalloc(&B->loads, B->cases.size() * 5 * MAX_ELEMENTS * sizeof(double)));
+    AK_CUDA(cudaMemset(B->loads, 0, B->cases.size() * 5 * MAX_ELEMENTS * sizeof(double)));
+    return AK_OK;
+}
+
+// one batch step from a CUDA graph captured per (parity, sample)
+template <typename S>
+int batch_step_graphed(ak_batch *B, bool sample) {
+    const int slot = B->parity | (sample ? 2 : 0);
+    if (!B->graph[slot]) {
+        AK_CUDA(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
+        const int r = batch_enqueue<S>(B, B->parity, sample);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(B->stream, &g);
+        if (r != AK_OK || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            return r != AK_OK ? r : fail(AK_ERR_CUDA, std::string("batch capture failed: ") + cudaGetErrorString(e));
+        }
+        const cudaError_t ei = cudaGraphInstantiate(&B->graph[slot], g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) {
+            B->graph[slot] = nullptr;
+            return fail(AK_ERR_CUDA, std::string("batch graph instantiation failed: ") + cudaGetErrorString(ei));
+        }
+    }
+    AK_CUDA(cudaGraphLaunch(B->graph[slot], B->stream));
+    B->launches += batch_step_launches(B, sample);
+    B->parity ^= 1;
+    B->steps += 1;
+    return AK_OK;
+}
+
+template <typename F>
+int batch_dispatch(ak_batch *B, F &&f) {
+    switch (B->storage) {
+    case AK_STORAGE_F64: return f((double *)nullptr);
+    case AK_STORAGE_F32: return f((float *)nullptr);
+    case AK_STORAGE_F16: return f((__half *)nullptr);
+    }
+    return fail(AK_ERR_INVALID, "unknown storage");
+}
+
+// the cases' host-side state after the batch's steps
+void batch_sync_cases(ak_batch *B, long long nsteps) {
+    for (size_t i = 0; i < B->cases.size(); ++i) {
+        ak_case *c = B->cases[i];
+        c->cur = B->cur0[i] ^ B->parity;
+        c->steps += nsteps;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int ak_batch_create(ak_case *const *cases, int32_t n, ak_batch **out) {
+    if (!out) return fail(AK_ERR_INVALID, "an output handle is required");
+    *out = nullptr;
+    if (!cases || n < 1) return fail(AK_ERR_INVALID, "a batch needs at least one case");
+    ak_batch *B = new ak_batch();
+    int r = AK_OK;
+    for (int i = 0; i < n && r == AK_OK; ++i) {
+        ak_case *c = cases[i];
+        if (!c)
+            r = fail(AK_ERR_INVALID, "null case in the batch");
+        else if (i && (c->storage != cases[0]->storage || c->device != cases[0]->device))
+            r = fail(AK_ERR_INVALID, "the cases of a batch share one storage form and one device");
+        else if (c->farfield != AK_FARFIELD_CHARACTERISTIC || c->periodic_xy)
+            r = fail(AK_ERR_INVALID, "batches hold uniform cases with the characteristic farfield");
+        else if (std::find(B->cases.begin(), B->cases.end(), c) != B->cases.end())
+            r = fail(AK_ERR_INVALID, "a case appears twice in the batch");
+        else
+            B->cases.push_back(c);
+    }
+    if (r == AK_OK) {
+        ak_case *c0 = B->cases[0];
+        B->storage = c0->storage;
+        B->device = c0->device;
+        if (cudaSetDevice(B->device) != cudaSuccess ||
+            cudaDeviceGetAttribute(&B->sms, cudaDevAttrMultiProcessorCount, B->device) != cudaSuccess)
+            r = fail(AK_ERR_CUDA, "device query failed");
+    }
+    if (r == AK_OK && cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess)
+        r = fail(AK_ERR_CUDA, "stream creation failed");
+    // boundary data of cases that have not stepped yet, then hand-over
+    for (size_t i = 0; r == AK_OK && i < B->cases.size(); ++i) {
+        ak_case *c = B->cases[i];
+        if (!c->prepared)
+            r = with_storage(c, [&](auto *tag) { return prepare_boundaries<std::remove_pointer_t<decltype(tag)>>(c); });
+        if (r == AK_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) r = fail(AK_ERR_CUDA, "case sync failed");
+        B->cur0.push_back(c->cur);
+    }
+    if (r == AK_OK) r = batch_dispatch(B, [&](auto *tag) { return batch_build<std::remove_pointer_t<decltype(tag)>>(B); });
+    if (r != AK_OK) {
+        std::string keep = g_error;
+        batch_release(B);
+        delete B;
+        g_error = keep;
+        return r;
+    }
+    *out = B;
+    return AK_OK;
+}
+
+int ak_batch_destroy(ak_batch *B) {
+    if (!B) return AK_OK;
+    batch_release(B);
+    delete B;
+    return AK_OK;
+}
+
+int ak_batch_step(ak_batch *B, int32_t nsteps, double *loads) {
+    if (!B) return fail(AK_ERR_INVALID, "null batch");
+    if (nsteps < 1) return fail(AK_ERR_INVALID, "nsteps must be >= 1");
+    for (size_t i = 0; i < B->cases.size(); ++i)
+        if (B->cases[i]->cur != (B->cur0[i] ^ B->parity))
+            return fail(AK_ERR_INVALID, "a case of the batch was stepped outside it; rebuild the batch");
+    AK_CUDA(cudaSetDevice(B->device));
+    int r = AK_OK;
+    long long done = 0;
+    for (int s = 0; s < nsteps && r == AK_OK; ++s) {
+        const bool sample = loads && s == nsteps - 1;
+        r = batch_dispatch(B, [&](auto *tag) {
+            return batch_step_graphed<std::remove_pointer_t<decltype(tag)>>(B, sample);
+        });
+        if (r == AK_OK) ++done;
+    }
+    batch_sync_cases(B, done);
+    if (r != AK_OK) return r;
+    if (loads)
+        AK_CUDA(cudaMemcpyAsync(loads, B->loads, B->cases.size() * 5 * MAX_ELEMENTS * sizeof(double),
+                                cudaMemcpyDeviceToHost, B->stream));
+    AK_CUDA(cudaStreamSynchronize(B->stream));
+    return AK_OK;
+}
+
+int ak_batch_tune(ak_batch *B, int32_t trials, double *report) {
+    if (!B || trials < 1) return fail(AK_ERR_INVALID, "a batch and trials >= 1 are required");
+    AK_CUDA(cudaSetDevice(B->device));
+    // the stream-collide launch reads one copy and writes the other's fluid
+    // cells, which the next step rewrites whole: timing it leaves no trace
+    return batch_dispatch(B, [&](auto *tag) -> int {
+        using S = std::remove_pointer_t<decltype(tag)>;
+        cudaEvent_t a, b;
+        AK_CUDA(cudaEventCreate(&a));
+        AK_CUDA(cudaEventCreate(&b));
+        const int tb0 = B->tb, per0 = B->per_sm, order0 = B->order;
+        double best = 1e30, first = 0.0;
+        int best_tb = tb0, best_per = per0, best_order = order0;
+        int r = AK_OK;
+        for (int order = 0; order < 2 && r == AK_OK; ++order)
+            for (int tb : {64, 128, 256}) {
+                if (r != AK_OK) break;
+                int occ = 0;
+                r = bulk_occupancy<S>(tb, &occ);
+                if (r != AK_OK || occ < 1) break;
+                const std::vector<WorkItem> t = bulk_table(B, tb, order);
+                B->n_bulk = (long long)t.size();
+                r = upload_work(&B->w_bulk, t);
+                for (int per = 1; per <= occ && r == AK_OK; per *= 2) {
+                    r = bulk_launch<S>(B, tb, per * B->sms, B->parity);  // warm
+                    cudaEventRecord(a, B->stream);
+                    for (int k = 0; k < trials && r == AK_OK; ++k) r = bulk_launch<S>(B, tb, per * B->sms, B->parity);
+                    cudaEventRecord(b, B->stream);
+                    if (cudaEventSynchronize(b) != cudaSuccess) r = fail(AK_ERR_CUDA, "tuning launch failed");
+                    float ms = 0.0f;
+                    cudaEventElapsedTime(&ms, a, b);
+                    const double per_launch = ms / trials;
+                    if (tb == tb0 && order == order0 && per == per0) first = per_launch;
+                    if (r == AK_OK && per_launch < best) {
+                        best = per_launch;
+                        best_tb = tb;
+                        best_per = per;
+                        best_order = order;
+                    }
+                    B->launches += trials + 1;
+                }
+            }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        if (r != AK_OK) return r;
+        B->tb = best_tb;
+        B->per_sm = best_per;
+        B->order = best_order;
+        const std::vector<WorkItem> t = bulk_table(B, B->tb, B->order);
+        B->n_bulk = (long long)t.size();
+        AK_TRY(upload_work(&B->w_bulk, t));
+        batch_drop_graphs(B);
+        if (report) {
+            report[0] = B->tb;
+            report[1] = B->per_sm;
+            report[2] = B->order;
+            report[3] = best;
+            report[4] = first;
+        }
+        return AK_OK;
+    });
+}
+
+int64_t ak_batch_launches(const ak_batch *B) { return B ? B->launches : -1; }
+int64_t ak_batch_steps_done(const ak_batch *B) { return B ? B->steps : -1; }
+void *ak_batch_stream(const ak_batch *B) { return B ? (void *)B->stream : nullptr; }
 
 }  // extern "C"

@@ -68,15 +68,19 @@ __device__ __forceinline__ void store_g(S *pdf, const Grid &G, int q, int x, int
 }
 
 // ------------------------------------------------------------ bulk step
-template <typename S>
-__global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
-    k_stream_collide(const S *__restrict__ src, S *__restrict__ dst, const uint8_t *__restrict__ flags, Grid G,
-                     Shift27 shift, typename Store<S>::T omega_s, typename Store<S>::T omega_b) {
+// shift of direction q: by value in the single-case kernel (constant bank),
+// from the case's device table in the batched one
+__device__ __forceinline__ float shift_at(const Shift27 &s, int q) { return s.v[q]; }
+__device__ __forceinline__ float shift_at(const float *s, int q) { return __ldg(s + q); }
+
+// pull the 27 populations of interior cell (x, y, z) (padded x, y), collide,
+// store into dst if the column is fluid
+template <typename S, typename Shift>
+__device__ __forceinline__ void stream_collide_cell(const S *__restrict__ src, S *__restrict__ dst,
+                                                    const uint8_t *__restrict__ flags, const Grid &G,
+                                                    const Shift &shift, typename Store<S>::T omega_s,
+                                                    typename Store<S>::T omega_b, int x, int y, int z) {
     using T = typename Store<S>::T;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int y = blockIdx.y + 1;
-    const int z = blockIdx.z;
-    if (x > G.nx) return;
     // the column flag only gates the stores, so the 27 loads issue at once
     const bool fluid = __ldg(flags + y * G.nxp + x) == FLAG_FLUID;
     T g[Q];
@@ -84,7 +88,7 @@ __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
     for (int q = 0; q < Q; ++q) {
         const int zs = G.wrapz(z - cz(q));
         g[q] = AK_CHECK(G, q, x - cx(q), y - cy(q), zs, 3)
-                   ? Store<S>::load(src + q * G.qs + G.cell(x - cx(q), y - cy(q), zs), q, shift.v[q])
+                   ? Store<S>::load(src + q * G.qs + G.cell(x - cx(q), y - cy(q), zs), q, shift_at(shift, q))
                    : T(0);
     }
     if constexpr (sizeof(T) == 8)
@@ -94,7 +98,18 @@ __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
     if (!fluid) return;
     const long long c = G.cell(x, y, z);
 #pragma unroll
-    for (int q = 0; q < Q; ++q) Store<S>::store(dst + q * G.qs + c, q, g[q], shift.v[q]);
+    for (int q = 0; q < Q; ++q) Store<S>::store(dst + q * G.qs + c, q, g[q], shift_at(shift, q));
+}
+
+template <typename S>
+__global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
+    k_stream_collide(const S *__restrict__ src, S *__restrict__ dst, const uint8_t *__restrict__ flags, Grid G,
+                     Shift27 shift, typename Store<S>::T omega_s, typename Store<S>::T omega_b) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int y = blockIdx.y + 1;
+    const int z = blockIdx.z;
+    if (x > G.nx) return;
+    stream_collide_cell(src, dst, flags, G, shift, omega_s, omega_b, x, y, z);
 }
 
 // ------------------------------------------------------------ walls
@@ -107,7 +122,13 @@ struct WallKey {
 // Block reduction of nv doubles per thread into shared partials; thread 0 of
 // the block writes them to out[blockIdx.x * nv ...] in a fixed order.
 template <int NV>
+__device__ void block_sum_store_at(double (&v)[NV], double *out, long long block);
+template <int NV>
 __device__ void block_sum_store(double (&v)[NV], double *out) {
+    block_sum_store_at<NV>(v, out, blockIdx.x);
+}
+template <int NV>
+__device__ void block_sum_store_at(double (&v)[NV], double *out, long long block) {
     __shared__ double red[32][NV];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -122,15 +143,68 @@ __device__ void block_sum_store(double (&v)[NV], double *out) {
         for (int k = 0; k < NV; ++k) {
             double s = 0.0;
             for (int w = 0; w < nw; ++w) s += red[w][k];
-            out[(long long)blockIdx.x * NV + k] = s;
+            out[block * NV + k] = s;
         }
+    }
+}
+
+// link tid of the compacted keys (nz * 3 links per key): the Bouzidi value
+// stored into the solid cell, and with sample the link's load contribution
+template <typename S>
+__device__ __forceinline__ void wall_link(S *__restrict__ pdf, const Grid &G, const WallKey *__restrict__ keys,
+                                          const double *__restrict__ qs, long long tid, int sample, double ox,
+                                          double oy, double acc[5], int &element) {
+    const long long k = tid / (3LL * G.nz);
+    const int rem = (int)(tid - k * 3LL * G.nz);
+    const int z = rem / 3, icz = rem - 3 * (rem / 3);
+    const WallKey key = keys[k];
+    const int ex = cx(key.d2), ey = cy(key.d2), ez = icz - 1;
+    const int d = qof(ex + 1, ey + 1, icz), di = inv(d);
+    const double q = qs[k];
+    const double f_xf = load_g(pdf, G, d, key.x, key.y, z);
+    const double f_xf_inv = load_g(pdf, G, di, key.x, key.y, z);
+    double v;
+    if (q >= 0.5) {
+        v = (0.5 * (f_xf + f_xf_inv * (2.0 * q - 1.0))) / q;
+    } else if (q > 0.0) {
+        const double d_x2f = load_g(pdf, G, d, key.x - ex, key.y - ey, G.wrapz(z - ez));
+        v = 2.0 * q * f_xf + (1.0 - 2.0 * q) * d_x2f;
+    } else {
+        v = f_xf;
+    }
+    store_g(pdf, G, di, key.x + ex, key.y + ey, G.wrapz(z + ez), v);
+    if (sample) {
+        // the stored value is what the fluid will pull; use it as g_in
+        const double gin = load_g(pdf, G, di, key.x + ex, key.y + ey, G.wrapz(z + ez));
+        const double s = f_xf + gin;
+        const double fx = ex * s, fy = ey * s, fz = ez * s;
+        const double rx = (double)(key.x - 1) + 0.5 + ox, ry = (double)(key.y - 1) + 0.5 + oy;
+        acc[0] = fx;
+        acc[1] = fy;
+        acc[2] = fz;
+        acc[3] = rx * fy - ry * fx;
+        acc[4] = gin - f_xf;
+        element = key.element;
+    }
+}
+
+// per-element block sums of the links' load contributions:
+// partials[element][block][5], nblocks blocks per element
+__device__ __forceinline__ void wall_block_sums(const double acc[5], int element, int n_elements, double *partials,
+                                                long long block, long long nblocks) {
+    for (int e = 0; e < n_elements; ++e) {
+        double v[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) v[k] = element == e ? acc[k] : 0.0;
+        block_sum_store_at<5>(v, partials + (long long)e * 5 * nblocks, block);
+        __syncthreads();
     }
 }
 
 // NoSlipLinearBouzidi (solver.py:139-143) over all links of the compacted keys,
 // written into the solid cells of pdf; optionally the per-element loads of
 // solver.py:217-243: F = sum c_d (g_out + g_in), Mz = sum rx Fy - ry Fx,
-// mass = sum g_in - g_out.  Partials: [block][element][5].
+// mass = sum g_in - g_out.  Partials: [element][block][5].
 constexpr int MAX_ELEMENTS = 8;
 template <typename S>
 __global__ void __launch_bounds__(256) k_walls(S *__restrict__ pdf, Grid G, const WallKey *__restrict__ keys,
@@ -138,51 +212,11 @@ __global__ void __launch_bounds__(256) k_walls(S *__restrict__ pdf, Grid G, cons
                                                int n_elements, double ox, double oy,
                                                double *__restrict__ partials) {
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long nlinks = nkeys * G.nz * 3;
     double acc[5] = {0, 0, 0, 0, 0};
     int element = -1;
-    if (tid < nlinks) {
-        const long long k = tid / (3LL * G.nz);
-        const int rem = (int)(tid - k * 3LL * G.nz);
-        const int z = rem / 3, icz = rem - 3 * (rem / 3);
-        const WallKey key = keys[k];
-        const int ex = cx(key.d2), ey = cy(key.d2), ez = icz - 1;
-        const int d = qof(ex + 1, ey + 1, icz), di = inv(d);
-        const double q = qs[k];
-        const double f_xf = load_g(pdf, G, d, key.x, key.y, z);
-        const double f_xf_inv = load_g(pdf, G, di, key.x, key.y, z);
-        double v;
-        if (q >= 0.5) {
-            v = (0.5 * (f_xf + f_xf_inv * (2.0 * q - 1.0))) / q;
-        } else if (q > 0.0) {
-            const double d_x2f = load_g(pdf, G, d, key.x - ex, key.y - ey, G.wrapz(z - ez));
-            v = 2.0 * q * f_xf + (1.0 - 2.0 * q) * d_x2f;
-        } else {
-            v = f_xf;
-        }
-        store_g(pdf, G, di, key.x + ex, key.y + ey, G.wrapz(z + ez), v);
-        if (sample) {
-            // the stored value is what the fluid will pull; use it as g_in
-            const double gin = load_g(pdf, G, di, key.x + ex, key.y + ey, G.wrapz(z + ez));
-            const double s = f_xf + gin;
-            const double fx = ex * s, fy = ey * s, fz = ez * s;
-            const double rx = (double)(key.x - 1) + 0.5 + ox, ry = (double)(key.y - 1) + 0.5 + oy;
-            acc[0] = fx;
-            acc[1] = fy;
-            acc[2] = fz;
-            acc[3] = rx * fy - ry * fx;
-            acc[4] = gin - f_xf;
-            element = key.element;
-        }
-    }
+    if (tid < nkeys * G.nz * 3) wall_link(pdf, G, keys, qs, tid, sample, ox, oy, acc, element);
     if (!sample) return;
-    for (int e = 0; e < n_elements; ++e) {
-        double v[5];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) v[k] = element == e ? acc[k] : 0.0;
-        block_sum_store<5>(v, partials + (long long)e * 5 * gridDim.x);
-        __syncthreads();
-    }
+    wall_block_sums(acc, element, n_elements, partials, blockIdx.x, gridDim.x);
 }
 
 // partials laid out [element][block][5]; one warp per (element, component):
@@ -333,9 +367,7 @@ __device__ __forceinline__ void ring_cell(const Grid &G, long long r, int &x, in
 }
 
 template <typename S>
-__global__ void k_ring_macros(const S *__restrict__ pdf, Grid G, Ring R) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= R.n * G.nz) return;
+__device__ __forceinline__ void ring_macro_item(const S *__restrict__ pdf, const Grid &G, const Ring &R, long long i) {
     const long long r = i / G.nz;
     const int z = (int)(i - r * G.nz);
     int x, y;
@@ -344,6 +376,13 @@ __global__ void k_ring_macros(const S *__restrict__ pdf, Grid G, Ring R) {
     macro_at(pdf, G, x + 1, y + 1, z, rho, u);
     R.ru[i] = Macro4{rho, u[0], u[1], u[2]};
     R.lr[i] = log(rho);
+}
+
+template <typename S>
+__global__ void k_ring_macros(const S *__restrict__ pdf, Grid G, Ring R) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= R.n * G.nz) return;
+    ring_macro_item(pdf, G, R, i);
 }
 
 __device__ __forceinline__ void ring_get(const Grid &G, const Ring &R, int px, int py, int z, double &rho,
@@ -400,12 +439,11 @@ __device__ __forceinline__ double feq_dir(double r, const double v[3], int q) {
 }
 
 template <typename S>
-__global__ void __launch_bounds__(256) k_farfield(S *__restrict__ pdf, Grid G, OuterLinks L, FarfieldParams P, Ring R,
-                                                  double *__restrict__ incoming, double *__restrict__ derivative,
-                                                  long long *__restrict__ clock, const double *__restrict__ init_lo,
-                                                  const double *__restrict__ init_hi, int prepare) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= L.n) return;
+__device__ __forceinline__ void farfield_link(S *__restrict__ pdf, const Grid &G, const OuterLinks &L,
+                                              const FarfieldParams &P, const Ring &R, double *__restrict__ incoming,
+                                              double *__restrict__ derivative, long long *__restrict__ clock,
+                                              const double *__restrict__ init_lo, const double *__restrict__ init_hi,
+                                              int prepare, long long i) {
     const int x = L.x[i], y = L.y[i], z = L.z[i], d = L.d[i], di = inv(d);
 #ifdef AK_CHECKED
     if (L.obj[i] < 0 || L.obj[i] >= P.nobj) {
@@ -475,6 +513,16 @@ __global__ void __launch_bounds__(256) k_farfield(S *__restrict__ pdf, Grid G, O
     } else if (o.mode == 2) {
         clock[i] += 1;
     }
+}
+
+template <typename S>
+__global__ void __launch_bounds__(256) k_farfield(S *__restrict__ pdf, Grid G, OuterLinks L, FarfieldParams P, Ring R,
+                                                  double *__restrict__ incoming, double *__restrict__ derivative,
+                                                  long long *__restrict__ clock, const double *__restrict__ init_lo,
+                                                  const double *__restrict__ init_hi, int prepare) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= L.n) return;
+    farfield_link(pdf, G, L, P, R, incoming, derivative, clock, init_lo, init_hi, prepare, i);
 }
 
 // glancing faces: initial invariant u.n - cs ln(rho/rho_inf) - un_inf on the

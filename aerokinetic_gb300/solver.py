@@ -124,11 +124,15 @@ class Solver:
         self.steps += int(nsteps)
         if out is None:
             return None
-        loads = self._coefficients(out)
+        self.last_loads = self._record(out)
+        return self.last_loads
+
+    def _record(self, per_element):
+        """The sample-step record of solver.py:262-279 from per-element lattice loads."""
+        loads = self._coefficients(per_element)
         loads.update(step=self.steps, t_star=(self.steps - 0.5) * self.plan.dt_convective)
         if self.plan.dt_seconds is not None:
             loads["time_s"] = (self.steps - 0.5) * self.plan.dt_seconds
-        self.last_loads = loads
         return loads
 
     def step(self, sample=False):

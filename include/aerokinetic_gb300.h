@@ -205,6 +205,33 @@ int ak_refined_step_timed(ak_refined *r, int32_t nsteps, double *ms);
  * ak_get_wall_links; owned by the refined case. */
 ak_case *ak_refined_level(ak_refined *r, int32_t level);
 
+/* ---- batches of independent uniform cases --------------------------------
+ * No reference counterpart: the reference runs one case per process.  A batch
+ * borrows n uniform cases with the characteristic farfield (one storage form,
+ * one device) and advances them together: per step one launch each for the
+ * farfield ring macros, the farfield links and the Bouzidi walls of every
+ * case, and one persistent stream-collide launch over a packed table of all
+ * cases' blocks, replayed from CUDA graphs.  A case computes the same bits
+ * alone (ak_step) and in a batch.  While a case belongs to a batch, step it
+ * only through the batch; its state can be read with the per-case calls. */
+typedef struct ak_batch ak_batch;
+int ak_batch_create(ak_case *const *cases, int32_t n, ak_batch **out);
+int ak_batch_destroy(ak_batch *b);
+/* nsteps steps of every case; with loads non-null, loads[case * 40 + element
+ * * 5 + k] = that case's per-element (Fx, Fy, Fz, Mz, mass) of the last step,
+ * as ak_step returns them. */
+int ak_batch_step(ak_batch *b, int32_t nsteps, double *loads);
+/* Times the stream-collide launch for every block width (64, 128, 256),
+ * persistent grid size (1, 2, 4, ... CTAs per SM up to the occupancy limit)
+ * and table order (case-major, interleaved), trials launches each, and keeps
+ * the fastest.  The cases' state is unchanged.  report[5] = chosen width,
+ * CTAs per SM, order, its ms per launch, the previous schedule's ms. */
+int ak_batch_tune(ak_batch *b, int32_t trials, double *report);
+int64_t ak_batch_launches(const ak_batch *b);
+int64_t ak_batch_steps_done(const ak_batch *b);
+/* The batch's CUDA stream (cudaStream_t), for callers that time it. */
+void *ak_batch_stream(const ak_batch *b);
+
 /* Message of the last failure on this thread ("" if none). */
 const char *ak_last_error(void);
 /* Library build identification, e.g. "aerokinetic_gb300 sm_103a". */

@@ -1,0 +1,93 @@
+"""Batches of independent uniform cases (ak_batch_*): same bits alone and in a mix."""
+import numpy as np
+import pytest
+
+from aerokinetic_gb300 import Flow, Grid, Section, naca4
+
+
+def _parts(chord, alpha, reynolds, seed, farfield="characteristic_transport_v1"):
+    section = Section((naca4("0012", 41),))
+    flow = Flow(reynolds=reynolds, alpha_deg=alpha, lattice_speed=0.05, seed=seed)
+    grid = Grid(cells_per_chord=chord, upstream_chords=2.0, downstream_chords=3.0, transverse_chords=1.5,
+                span_chords=0.25, farfield=farfield, memory_limit_gib=8)
+    return section, flow, grid
+
+
+CASES = [(16, 4.0, 2e4, 1), (24, -2.0, 5e4, 2), (16, 10.0, 1e4, 3), (20, 6.0, 3e4, 4)]
+
+
+def _solvers(storage, cases=CASES):
+    from aerokinetic_gb300.solver import Solver
+    return [Solver(*_parts(*c), storage=storage) for c in cases]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage", ["f64", "f16"])
+def test_batch_matches_cases_stepped_alone(storage):
+    """Every case of a mixed-size batch ends bit-identical to the same case
+    stepped alone, and its sampled loads are the same numbers."""
+    from aerokinetic_gb300.batch import Batch
+    alone, mixed = _solvers(storage), _solvers(storage)
+    try:
+        with Batch(mixed) as batch:
+            for chunk in (7, 1, 12):
+                records = batch.advance(chunk)
+                for solver, record in zip(alone, records):
+                    ref = solver.advance(chunk, sample_last=True)
+                    for key in ("cl", "cd", "cm", "step"):
+                        assert record[key] == ref[key], key
+            batch.advance(5, sample_last=False)
+            for solver in alone:
+                solver.advance(5)
+            assert batch.launches >= 4 * 25
+        for a, b in zip(alone, mixed):
+            assert a.steps == b.steps == 25
+            assert np.array_equal(a.pdf(), b.pdf())
+            assert a.diagnostics() == b.diagnostics()
+    finally:
+        for s in alone + mixed:
+            s.close()
+
+
+@pytest.mark.gpu
+def test_batch_tuning_leaves_the_state_unchanged():
+    from aerokinetic_gb300.batch import Batch
+    alone, mixed = _solvers("f32"), _solvers("f32")
+    try:
+        with Batch(mixed) as batch:
+            batch.advance(3, sample_last=False)
+            schedule = batch.tune(trials=2)
+            assert schedule["block_width"] in (64, 128, 256) and schedule["ctas_per_sm"] >= 1
+            batch.advance(4, sample_last=False)
+        for solver in alone:
+            solver.advance(7)
+        for a, b in zip(alone, mixed):
+            assert np.array_equal(a.pdf(), b.pdf())
+    finally:
+        for s in alone + mixed:
+            s.close()
+
+
+@pytest.mark.gpu
+def test_batch_rejects_what_it_cannot_run():
+    from aerokinetic_gb300 import _native
+    from aerokinetic_gb300.batch import Batch
+    from aerokinetic_gb300.solver import Solver
+    legacy = Solver(*_parts(16, 4.0, 2e4, 1, farfield="legacy"))
+    a, b = _solvers("f64", CASES[:1])[0], _solvers("f32", CASES[1:2])[0]
+    try:
+        with pytest.raises(ValueError, match="characteristic"):
+            Batch([legacy])
+        with pytest.raises(ValueError, match="storage"):
+            Batch([a, b])
+        with pytest.raises(ValueError, match="twice"):
+            Batch([a, a])
+        with Batch([a]) as batch:
+            batch.advance(2, sample_last=False)
+            a.advance(1)  # stepped outside the batch
+            with pytest.raises(ValueError, match="outside"):
+                batch.advance(1)
+        assert isinstance(_native.load().ak_batch_launches(None), int)
+    finally:
+        for s in (legacy, a, b):
+            s.close()
