@@ -250,6 +250,124 @@ def measure_form(storage, steps, warmup, flush):
             "step_ms": total / steps}
 
 
+def batch_case_parts(i, base_seed=2026):
+    """Case i of the polar-sweep batch: chord cells from {24, 32, 48, 64}, a
+    12c x 8c domain with a periodic span of 4 cells (the plan's minimum of 8),
+    AoA U[-4, 16] deg, Re log-uniform on [1e4, 1e5], drawn from
+    default_rng(base_seed + i); the perturbation phase from the case's seed."""
+    from aerokinetic_gb300 import Flow, Grid, Section, naca0012
+    rng = np.random.default_rng(base_seed + i)
+    chord = int(rng.choice([24, 32, 48, 64]))
+    flow = Flow(reynolds=float(10 ** rng.uniform(4, 5)), alpha_deg=float(rng.uniform(-4, 16)),
+                lattice_speed=0.1 / math.sqrt(3), seed=base_seed + i)
+    grid = Grid(cells_per_chord=chord, upstream_chords=4.0, downstream_chords=7.0, transverse_chords=3.9,
+                span_chords=4 / chord, farfield="characteristic_transport_v1", memory_limit_gib=64)
+    return Section((naca0012(81),)), flow, grid
+
+
+def stream_ms(lib, stream_handle, fn):
+    """Milliseconds of fn() measured by CUDA events on the given stream."""
+    import torch
+    stream = torch.cuda.ExternalStream(stream_handle)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return float(a.elapsed_time(b))
+
+
+def run_batch(steps, n_cases=64, solve_steps=5000):
+    """Batched polar sweep (64 uneven cases) against the same cases solved one
+    after another in the plain FP64 form.  Throughputs are measured over
+    `steps` batch steps and scaled to solve_steps per case."""
+    from aerokinetic_gb300 import Plan
+    from aerokinetic_gb300.batch import Batch
+    from aerokinetic_gb300.solver import Solver
+    lib = None
+    parts = [batch_case_parts(i) for i in range(n_cases)]
+    cells = [math.prod(Plan.create(*p).shape) for p in parts]
+    out = {"workload": f"{n_cases} NACA0012 cases, chord cells in {{24, 32, 48, 64}}, 12c x 8c x 8 (span 4 "
+                       "requested, plan minimum 8), AoA U[-4, 16], Re log-U[1e4, 1e5], characteristic farfield",
+           "cases": n_cases, "cells": int(sum(cells)), "solve_steps": solve_steps, "measured_steps": steps}
+    for storage in ("f16", "f32"):
+        solvers = [Solver(*p, storage=storage) for p in parts]
+        with Batch(solvers) as batch:
+            lib = batch._lib
+            batch.advance(3, sample_last=False)
+            schedule = batch.tune(trials=3)
+            batch.advance(3, sample_last=False)
+            launches0 = batch.launches
+            ms = stream_ms(lib, batch.stream, lambda: batch.advance(steps, sample_last=False))
+            launches = batch.launches - launches0
+        for solver in solvers:
+            solver.close()
+        step_ms = ms / steps
+        out[storage] = {"ms_per_step": step_ms, "mlups": sum(cells) / (step_ms / 1e3) / 1e6,
+                        "solves_per_hour": n_cases / (solve_steps * step_ms / 1e3) * 3600,
+                        "launches_per_step": launches / steps, "schedule": schedule,
+                        "achieved_gbs": sum(cells) * BYTES_PER_CELL[storage] / (step_ms / 1e3) / 1e9}
+    # plain form, one case at a time: per-step time of one case of each chord,
+    # set-up time included once per case
+    per_chord = {}
+    for i, p in enumerate(parts):
+        chord = p[2].cells_per_chord
+        if chord in per_chord:
+            continue
+        t0 = time.perf_counter()
+        solver = Solver(*p, storage="f64")
+        solver.advance(3)
+        setup_s = time.perf_counter() - t0
+        k = max(10, min(steps, 40))
+        ms = stream_ms(solver._lib, solver._lib.ak_case_stream(solver._case), lambda: solver.advance(k))
+        per_chord[chord] = (ms / k, setup_s)
+        solver.close()
+    total_s = sum(per_chord[p[2].cells_per_chord][0] * solve_steps / 1e3 + per_chord[p[2].cells_per_chord][1]
+                  for p in parts)
+    out["plain_sequential"] = {"solves_per_hour": n_cases / total_s * 3600, "form": "f64, one case at a time",
+                               "ms_per_step_by_chord": {str(c): v[0] for c, v in sorted(per_chord.items())}}
+    out["speedup_f16_vs_plain"] = out["f16"]["solves_per_hour"] / out["plain_sequential"]["solves_per_hour"]
+    return out
+
+
+def run_serving(n_requests=16, rate_per_s=20.0, seed=7):
+    """Continuous batching of NACA 4-digit solves (optionally flapped) with
+    Poisson arrivals; latencies and solves per hour against the same requests
+    solved one after another in the plain FP64 form, and the served
+    coefficients' error against those plain results."""
+    from aerokinetic_gb300.serve import Server, poisson_arrivals, random_requests
+    from aerokinetic_gb300.solver import Solver
+    requests = random_requests(n_requests, seed=seed, chord=(24, 48), span=(4, 8), steps=(1000, 3000), window=500)
+    arrivals = poisson_arrivals(rate_per_s, n_requests, seed=seed)
+    server = Server(memory_budget_gib=64.0, storage="f32", chunk=250)
+    results = server.run(requests, arrivals)
+    by_name = {r.name: r for r in requests}
+    plain_s, worst = 0.0, {"cl": 0.0, "cd": 0.0, "cm": 0.0}
+    for res in results:
+        req = by_name[res.name]
+        t0 = time.perf_counter()
+        solver = Solver(req.section, req.flow, req.grid, storage="f64")
+        solver.advance(res.steps - 1)
+        ref = solver.advance(1, sample_last=True)
+        plain_s += time.perf_counter() - t0
+        solver.close()
+        for k in worst:
+            # relative to the plain value, with a floor of 0.05 so that a
+            # coefficient crossing zero does not divide by ~0
+            worst[k] = max(worst[k], abs(getattr(res, k) - ref[k]) / max(abs(ref[k]), 0.05))
+    stats = dict(server.stats)
+    stats.update({"workload": f"{n_requests} requests, Poisson arrivals at {rate_per_s}/s, NACA 4-digit m U[0, 0.04], "
+                              "p U[0.3, 0.5], t U[0.09, 0.15], half with a 0.3c flap at U[0, 25] deg, chord 24-48 "
+                              "cells, span 4-8, AoA U[-4, 14], Re log-U[1e4, 1e5], 1000-3000 steps or Cl settled "
+                              "to 1e-4 over 500 steps",
+                  "plain_sequential_solves_per_hour": len(results) / plain_s * 3600,
+                  "speedup_vs_plain": stats["solves_per_hour"] / (len(results) / plain_s * 3600),
+                  "max_relative_error_vs_f64": worst, "error_floor": 0.05,
+                  "converged": sum(r.converged for r in results)})
+    return stats
+
+
 def run_engine(args, rank, world, local_rank):
     import torch
     from aerokinetic_gb300 import _native
@@ -363,6 +481,9 @@ def run_engine(args, rank, world, local_rank):
                             "kernel_mlups": m["cells"] / (m["bulk_ms"] / 1e3) / 1e6,
                             "stream_collide_ms": m["bulk_ms"], "achieved_gbs": a, "frac_of_" + peak_kind: a / hbm}
 
+    batch = run_batch(steps=min(args.steps, 100))
+    serving = run_serving()
+
     traffic = None
     summary = ROOT / "profiles" / "collide_f64_refined_512x384x8.txt"
     if summary.exists():
@@ -391,6 +512,8 @@ def run_engine(args, rank, world, local_rank):
                     "h2d_bytes_per_step": h2d / e2e_steps, "d2h_bytes_per_step": 5 * 8 + 4,
                     "includes": "case set-up from the host description; every coarse step returns its loads and "
                                 "closes the mass/momentum budget (RefinedSolver.step)"},
+            "batch": batch,
+            "serving": serving,
             "gpu_launches": int(launches),
             "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)
