@@ -206,6 +206,14 @@ void build_farfield_objects(ak_case *c) {
                 }
                 o.active[a] = !(o.ut_inf[a] == 0.0 && !row);
             }
+            for (int a = 0; a < 3; ++a) {
+                o.nh_f[a] = (float)o.nh[a];
+                o.ut_inf_f[a] = (float)o.ut_inf[a];
+                o.vel_f[a] = (float)o.vel[a];
+                for (int b = 0; b < 3; ++b) o.P_f[a][b] = (float)o.P[a][b];
+            }
+            o.un_inf_f = (float)o.un_inf;
+            o.density_f = (float)o.density;
         }
 }
 
@@ -226,12 +234,25 @@ int build_outer(ak_case *c, const std::vector<uint8_t> &hflags) {
     std::vector<signed char> D, OBJ, EDGE;
     std::vector<int> sel_ubb, sel_out;
     const int nx = c->nx, ny = c->ny, nz = c->nz, nxp = nx + 2;
-    auto push = [&](int x, int y) {  // interior coordinates
-        if (hflags[(size_t)(y + 1) * nxp + (x + 1)] != FLAG_FLUID) return;
-        for (int d = 1; d < Q; ++d) {
-            const int gx = x + cx(d), gy = y + cy(d);
-            if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) continue;
-            for (int z = 0; z < nz; ++z) {
+    // boundary fluid cells face by face; links ordered (z, direction, cell) so
+    // that consecutive links touch consecutive cells of a face (coalesced)
+    std::vector<std::pair<int, int>> cells;  // interior coordinates
+    auto add = [&](int x, int y) {
+        if (hflags[(size_t)(y + 1) * nxp + (x + 1)] == FLAG_FLUID) cells.emplace_back(x, y);
+    };
+    for (int x = 0; x < nx; ++x) add(x, 0);
+    if (ny > 1)
+        for (int x = 0; x < nx; ++x) add(x, ny - 1);
+    for (int y = 1; y < ny - 1; ++y) add(0, y);
+    if (nx > 1)
+        for (int y = 1; y < ny - 1; ++y) add(nx - 1, y);
+    bool foot_outside = false;
+    for (int z = 0; z < nz; ++z)
+        for (int d = 1; d < Q; ++d)
+            for (const auto &cell : cells) {
+                const int x = cell.first, y = cell.second;
+                const int gx = x + cx(d), gy = y + cy(d);
+                if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) continue;
                 const long long idx = (long long)X.size();
                 X.push_back(x + 1);
                 Y.push_back(y + 1);
@@ -249,22 +270,12 @@ int build_outer(ak_case *c, const std::vector<uint8_t> &hflags) {
                     OBJ.push_back((signed char)k);
                     const FarfieldObject &o = c->ff_host[k];
                     const int fx = x + cx(d) - o.normal[0], fy = y + cy(d) - o.normal[1];
-                    if (fx < 0 || fx >= nx || fy < 0 || fy >= ny) return;  // checked below
+                    foot_outside |= fx < 0 || fx >= nx || fy < 0 || fy >= ny;
                     EDGE.push_back((signed char)(fx == 0 ? -1 : (fx == nx - 1 ? 1 : 0)));
                     EDGE.push_back((signed char)(fy == 0 ? -1 : (fy == ny - 1 ? 1 : 0)));
                 }
             }
-        }
-    };
-    for (int x = 0; x < nx; ++x) {
-        push(x, 0);
-        if (ny > 1) push(x, ny - 1);
-    }
-    for (int y = 1; y < ny - 1; ++y) {
-        push(0, y);
-        if (nx > 1) push(nx - 1, y);
-    }
-    if (c->farfield == AK_FARFIELD_CHARACTERISTIC && EDGE.size() != 2 * X.size())
+    if (c->farfield == AK_FARFIELD_CHARACTERISTIC && foot_outside)
         return fail(AK_ERR_INVALID, "farfield foot cell outside the domain; the lattice is too small");
     c->nouter = (long long)X.size();
     AK_TRY(upload(c, &c->ox_, X));
@@ -420,7 +431,7 @@ int prepare_boundaries(ak_case *c) {
                 src, c->G, c->outer(), c->ff(), c->ring(), c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, 1);
             AK_CUDA(cudaGetLastError());
         }
-        k_glancing_rows<<<(unsigned)blocks_for((long long)c->nx * c->nz, T), T, 0, c->stream>>>(c->G, c->ff(), c->ring(),
+        k_glancing_rows<typename Store<S>::T><<<(unsigned)blocks_for((long long)c->nx * c->nz, T), T, 0, c->stream>>>(c->G, c->ff(), c->ring(),
                                                                                                c->ff_lo, c->ff_hi);
         AK_CUDA(cudaGetLastError());
     }

@@ -316,7 +316,12 @@ struct FarfieldObject {
     int active[3];       // axes carrying a transverse term
     double density;
     double vel[3];
+    // the same constants rounded to FP32, read by the FP32-arithmetic forms
+    float nh_f[3], un_inf_f, ut_inf_f[3], P_f[3][3], density_f, vel_f[3];
 };
+// an object constant in the arithmetic type T
+__device__ __forceinline__ double ffv(double d, float, double) { return d; }
+__device__ __forceinline__ float ffv(double, float f, float) { return f; }
 // the eight objects live in device memory (indexed per link at run time)
 struct FarfieldParams {
     const FarfieldObject *obj;
@@ -338,6 +343,32 @@ __device__ __forceinline__ void macro_at(const S *pdf, const Grid &G, int x, int
     for (int a = 0; a < 3; ++a) u[a] = j[a] / rho;
 }
 
+// density, velocity and ln(density) of one cell in the storage form's
+// arithmetic type (FP64 for the plain form, FP32 for the others)
+template <typename S>
+__device__ __forceinline__ void macro_lr(const S *pdf, const Grid &G, int x, int y, int z,
+                                         typename Store<S>::T &rho, typename Store<S>::T u[3],
+                                         typename Store<S>::T &lr) {
+    using T = typename Store<S>::T;
+    if constexpr (sizeof(T) == 8) {
+        macro_at(pdf, G, x, y, z, rho, u);
+        lr = log(rho);
+    } else {
+        T d = 0, j[3] = {0, 0, 0};
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const T g = Store<S>::load(pdf + q * G.qs + G.cell(x, y, z), q, G.shift[q]);
+            d += g;
+            if (cx(q)) j[0] += cx(q) > 0 ? g : -g;
+            if (cy(q)) j[1] += cy(q) > 0 ? g : -g;
+            if (cz(q)) j[2] += cz(q) > 0 ? g : -g;
+        }
+        rho = T(1) + d;
+        for (int a = 0; a < 3; ++a) u[a] = j[a] / rho;
+        lr = log1pf(d);
+    }
+}
+
 // The farfield reads density, velocity and ln(rho) of the fluid cells next to
 // the ghost ring only (the feet of its links and their neighbours along the
 // boundary).  They are computed once per step for that one-cell-wide band
@@ -347,10 +378,20 @@ struct alignas(32) Macro4 {
     double rho, ux, uy, uz;
 };
 struct Ring {
-    Macro4 *ru;   // (rho, ux, uy, uz) per ring cell and z
-    double *lr;   // ln(rho)
+    Macro4 *ru;   // (rho, ux, uy, uz) per z and ring cell (float4 in the FP32 forms)
+    double *lr;   // ln(rho) (float in the FP32 forms)
     long long n;  // ring cells per z-plane: 2 nx + 2 (ny - 2)
 };
+template <typename T>
+__device__ __forceinline__ void ring_put(const Ring &R, long long i, T rho, const T u[3], T lr) {
+    if constexpr (sizeof(T) == 8) {
+        R.ru[i] = Macro4{rho, u[0], u[1], u[2]};
+        R.lr[i] = lr;
+    } else {
+        reinterpret_cast<float4 *>(R.ru)[i] = make_float4(rho, u[0], u[1], u[2]);
+        reinterpret_cast<float *>(R.lr)[i] = lr;
+    }
+}
 __device__ __forceinline__ long long ring_index(const Grid &G, int x, int y) {  // interior coordinates
     if (y == 0) return x;
     if (y == G.ny - 1) return G.nx + x;
@@ -368,14 +409,14 @@ __device__ __forceinline__ void ring_cell(const Grid &G, long long r, int &x, in
 
 template <typename S>
 __device__ __forceinline__ void ring_macro_item(const S *__restrict__ pdf, const Grid &G, const Ring &R, long long i) {
-    const long long r = i / G.nz;
-    const int z = (int)(i - r * G.nz);
+    using T = typename Store<S>::T;
+    const int z = (int)(i / R.n);
+    const long long r = i - (long long)z * R.n;
     int x, y;
     ring_cell(G, r, x, y);
-    double rho, u[3];
-    macro_at(pdf, G, x + 1, y + 1, z, rho, u);
-    R.ru[i] = Macro4{rho, u[0], u[1], u[2]};
-    R.lr[i] = log(rho);
+    T rho, u[3], lr;
+    macro_lr(pdf, G, x + 1, y + 1, z, rho, u, lr);
+    ring_put(R, i, rho, u, lr);
 }
 
 template <typename S>
@@ -385,55 +426,68 @@ __global__ void k_ring_macros(const S *__restrict__ pdf, Grid G, Ring R) {
     ring_macro_item(pdf, G, R, i);
 }
 
-__device__ __forceinline__ void ring_get(const Grid &G, const Ring &R, int px, int py, int z, double &rho,
-                                         double u[3], double &lr) {  // padded x, y
-    const long long i = ring_index(G, px - 1, py - 1) * G.nz + z;
-    const Macro4 v = R.ru[i];
-    rho = v.rho;
-    u[0] = v.ux;
-    u[1] = v.uy;
-    u[2] = v.uz;
-    lr = R.lr[i];
+template <typename T>
+__device__ __forceinline__ void ring_get(const Grid &G, const Ring &R, int px, int py, int z, T &rho, T u[3],
+                                         T &lr) {  // padded x, y
+    const long long i = (long long)z * R.n + ring_index(G, px - 1, py - 1);
+    if constexpr (sizeof(T) == 8) {
+        const Macro4 v = R.ru[i];
+        rho = v.rho;
+        u[0] = v.ux;
+        u[1] = v.uy;
+        u[2] = v.uz;
+        lr = R.lr[i];
+    } else {
+        const float4 v = reinterpret_cast<const float4 *>(R.ru)[i];
+        rho = v.x;
+        u[0] = v.y;
+        u[1] = v.z;
+        u[2] = v.w;
+        lr = reinterpret_cast<const float *>(R.lr)[i];
+    }
 }
 
 // transverse term F of the evolving outflow invariant (farfield.py:162-180)
-__device__ double farfield_transverse(const Grid &G, const Ring &R, const FarfieldObject &o, const int foot[3],
-                                      const signed char edge[3], const double u[3], double rm) {
-    double F = 0.0;
+template <typename T>
+__device__ T farfield_transverse(const Grid &G, const Ring &R, const FarfieldObject &o, const int foot[3],
+                                 const signed char edge[3], const T u[3], T rm) {
+    T F = 0;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         if (!o.active[a]) continue;
         const int e = edge[a];
         const int off1 = e == -1 ? 1 : -1;
         const int off2 = e == 0 ? 1 : -2 * e;
-        const double c0 = 1.5 * e;
-        const double c1 = e == 0 ? -0.5 : -2.0 * e;
-        const double c2 = e == 0 ? 0.5 : 0.5 * e;
+        const T c0 = T(1.5) * e;
+        const T c1 = e == 0 ? T(-0.5) : T(-2.0) * e;
+        const T c2 = e == 0 ? T(0.5) : T(0.5) * e;
         int s1[3] = {foot[0], foot[1], foot[2]}, s2[3] = {foot[0], foot[1], foot[2]};
         s1[a] += off1;
         s2[a] += off2;
         s1[2] = G.wrapz(s1[2]);
         s2[2] = G.wrapz(s2[2]);
-        double r1, v1[3], l1, r2, v2[3], l2;
+        T r1, v1[3], l1, r2, v2[3], l2;
         ring_get(G, R, s1[0], s1[1], s1[2], r1, v1, l1);
         ring_get(G, R, s2[0], s2[1], s2[2], r2, v2, l2);
-        double du[3];
+        T du[3];
         for (int b = 0; b < 3; ++b) du[b] = c0 * u[b] + c1 * v1[b] + c2 * v2[b];
         // ln(rho / density) with density 1 for every object
-        const double rm1 = o.nh[0] * v1[0] + o.nh[1] * v1[1] + o.nh[2] * v1[2] - CS * l1;
-        const double rm2 = o.nh[0] * v2[0] + o.nh[1] * v2[1] + o.nh[2] * v2[2] - CS * l2;
-        F += o.un_inf * (o.P[a][0] * du[0] + o.P[a][1] * du[1] + o.P[a][2] * du[2]) -
-             o.ut_inf[a] * (c0 * rm + c1 * rm1 + c2 * rm2);
+        const T nh[3] = {ffv(o.nh[0], o.nh_f[0], T(0)), ffv(o.nh[1], o.nh_f[1], T(0)), ffv(o.nh[2], o.nh_f[2], T(0))};
+        const T rm1 = nh[0] * v1[0] + nh[1] * v1[1] + nh[2] * v1[2] - T(CS) * l1;
+        const T rm2 = nh[0] * v2[0] + nh[1] * v2[1] + nh[2] * v2[2] - T(CS) * l2;
+        F += ffv(o.un_inf, o.un_inf_f, T(0)) * (ffv(o.P[a][0], o.P_f[a][0], T(0)) * du[0] + ffv(o.P[a][1], o.P_f[a][1], T(0)) * du[1] + ffv(o.P[a][2], o.P_f[a][2], T(0)) * du[2]) -
+             ffv(o.ut_inf[a], o.ut_inf_f[a], T(0)) * (c0 * rm + c1 * rm1 + c2 * rm2);
     }
     return F;
 }
 
-__device__ __forceinline__ double feq_dir(double r, const double v[3], int q) {
+template <typename T>
+__device__ __forceinline__ T feq_dir(T r, const T v[3], int q) {
     const int c[3] = {cx(q), cy(q), cz(q)};
-    double p = r;
+    T p = r;
     for (int a = 0; a < 3; ++a) {
-        const double cc = (double)c[a], w = v[a];
-        p *= 2.0 / 3.0 - w * w + (1.5 * w * w - 0.5) * cc * cc + cc * w / 2.0;
+        const T cc = (T)c[a], w = v[a];
+        p *= T(2.0 / 3.0) - w * w + (T(1.5) * w * w - T(0.5)) * cc * cc + cc * w / T(2.0);
     }
     return p;
 }
@@ -444,6 +498,7 @@ __device__ __forceinline__ void farfield_link(S *__restrict__ pdf, const Grid &G
                                               double *__restrict__ derivative, long long *__restrict__ clock,
                                               const double *__restrict__ init_lo, const double *__restrict__ init_hi,
                                               int prepare, long long i) {
+    using T = typename Store<S>::T;
     const int x = L.x[i], y = L.y[i], z = L.z[i], d = L.d[i], di = inv(d);
 #ifdef AK_CHECKED
     if (L.obj[i] < 0 || L.obj[i] >= P.nobj) {
@@ -455,15 +510,17 @@ __device__ __forceinline__ void farfield_link(S *__restrict__ pdf, const Grid &G
     // foot = x + c_d - n: a fluid cell next to the ghost cell, wrapped in z
     const int foot[3] = {x + cx(d) - o.normal[0], y + cy(d) - o.normal[1], G.wrapz(z + cz(d) - o.normal[2])};
     const signed char edge[3] = {L.edge[2 * i], L.edge[2 * i + 1], 0};
-    double rho, u[3], lr;
+    T rho, u[3], lr;
     ring_get(G, R, foot[0], foot[1], foot[2], rho, u, lr);
-    const double un = o.nh[0] * u[0] + o.nh[1] * u[1] + o.nh[2] * u[2];
-    const double rm = un - CS * lr, rp = un + CS * lr;
+    const T nh[3] = {ffv(o.nh[0], o.nh_f[0], T(0)), ffv(o.nh[1], o.nh_f[1], T(0)), ffv(o.nh[2], o.nh_f[2], T(0))};
+    const T un_inf = ffv(o.un_inf, o.un_inf_f, T(0));
+    const T un = nh[0] * u[0] + nh[1] * u[1] + nh[2] * u[2];
+    const T rm = un - T(CS) * lr, rp = un + T(CS) * lr;
     if (prepare) {
         // farfield.py:84-113: seed the trapezoid so the first update returns
         // the actual initial invariant
         if (o.mode == 1) {
-            const double F = farfield_transverse(G, R, o, foot, edge, u, rm);
+            const T F = farfield_transverse(G, R, o, foot, edge, u, rm);
             incoming[i] = rm - F;
             derivative[i] = F;
         } else if (o.mode == 2) {
@@ -474,39 +531,40 @@ __device__ __forceinline__ void farfield_link(S *__restrict__ pdf, const Grid &G
         }
         return;
     }
-    double value, F = 0.0;
+    T value, F = 0;
     if (o.mode == 1) {
         F = farfield_transverse(G, R, o, foot, edge, u, rm);
-        value = incoming[i] + (F + derivative[i]) / 2.0;
+        value = T(incoming[i]) + (F + T(derivative[i])) / T(2.0);
     } else if (o.mode == 2) {
         // one linear interpolation of the saved initial invariant at the shift
         // U * clock along x (the only axis with U != 0), zero outside
         const double target = (double)(foot[0] - 1) - o.vel[0] * (double)clock[i];
         const int lower = (int)floor(target);
-        const double frac = target - lower;
+        const T frac = T(target - lower);
         const double *row = o.normal[1] < 0 ? init_lo : init_hi;
-        double sum = 0.0;
+        T sum = 0;
         for (int bit = 0; bit < 2; ++bit) {
             const int k = lower + bit;
-            const double w = bit ? frac : 1.0 - frac;
+            const T w = bit ? frac : T(1) - frac;
             const int kc = k < 0 ? 0 : (k > G.nx - 1 ? G.nx - 1 : k);
-            const double sample = row[(long long)kc * G.nz + foot[2]];
-            sum += w * ((k >= 0 && k < G.nx) ? sample : 0.0);
+            const T sample = T(row[(long long)kc * G.nz + foot[2]]);
+            sum += w * ((k >= 0 && k < G.nx) ? sample : T(0));
         }
-        value = o.un_inf + sum;
+        value = un_inf + sum;
     } else {
-        value = o.un_inf;
+        value = un_inf;
     }
-    const double unb = (rp + value) / 2.0;
-    const double rhob = o.density * exp((rp - value) / (2.0 * CS));
-    double ub[3];
+    const T unb = (rp + value) / T(2.0);
+    const T rhob = ffv(o.density, o.density_f, T(0)) * exp((rp - value) / (T(2.0) * T(CS)));
+    T ub[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        const double tangential = unb >= 0.0 ? u[a] - o.nh[a] * un : o.vel[a] - o.nh[a] * o.un_inf;
-        ub[a] = o.nh[a] * unb + tangential;
+        const T tangential = unb >= T(0) ? u[a] - nh[a] * un : ffv(o.vel[a], o.vel_f[a], T(0)) - nh[a] * un_inf;
+        ub[a] = nh[a] * unb + tangential;
     }
-    const double ghost = load_g(pdf, G, di, foot[0], foot[1], foot[2]) + feq_dir(rhob, ub, di) - feq_dir(rho, u, di);
-    store_g(pdf, G, di, x + cx(d), y + cy(d), G.wrapz(z + cz(d)), ghost);
+    const T foot_g = (T)Store<S>::load(pdf + di * G.qs + G.cell(foot[0], foot[1], foot[2]), di, G.shift[di]);
+    const T ghost = foot_g + feq_dir(rhob, ub, di) - feq_dir(rho, u, di);
+    store_g(pdf, G, di, x + cx(d), y + cy(d), G.wrapz(z + cz(d)), (double)ghost);
     if (o.mode == 1) {
         incoming[i] = value;
         derivative[i] = F;
@@ -527,6 +585,7 @@ __global__ void __launch_bounds__(256) k_farfield(S *__restrict__ pdf, Grid G, O
 
 // glancing faces: initial invariant u.n - cs ln(rho/rho_inf) - un_inf on the
 // fluid row next to the face (the only row the transport reads)
+template <typename T>
 __global__ void k_glancing_rows(Grid G, FarfieldParams P, Ring R, double *__restrict__ lo, double *__restrict__ hi) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (long long)G.nx * G.nz) return;
@@ -535,9 +594,9 @@ __global__ void k_glancing_rows(Grid G, FarfieldParams P, Ring R, double *__rest
         const FarfieldObject &o = P.obj[k];
         if (o.mode != 2) continue;
         const int y = o.normal[1] < 0 ? 1 : G.ny;
-        double rho, u[3], lr;
+        T rho, u[3], lr;
         ring_get(G, R, x, y, z, rho, u, lr);
-        const double v = o.nh[0] * u[0] + o.nh[1] * u[1] + o.nh[2] * u[2] - CS * lr - o.un_inf;
+        const T v = ffv(o.nh[0], o.nh_f[0], T(0)) * u[0] + ffv(o.nh[1], o.nh_f[1], T(0)) * u[1] + ffv(o.nh[2], o.nh_f[2], T(0)) * u[2] - T(CS) * lr - ffv(o.un_inf, o.un_inf_f, T(0));
         (o.normal[1] < 0 ? lo : hi)[i] = v;
     }
 }
