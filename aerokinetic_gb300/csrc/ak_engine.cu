@@ -995,6 +995,8 @@ struct ak_refined {
     // ak_refined_step; launches_per_step counts the kernels of one replay
     cudaGraphExec_t graph[8] = {};
     long long launches_per_step = 0;
+    cudaStream_t side = nullptr;  // the first fine step's stream inside the captured graphs
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // budget support: inflow through the outer x/y faces of each tracked step,
     // and the per-level statistics of the conserved integrals / validity check
     bool track_budget = false;
@@ -1027,6 +1029,9 @@ void refined_release(ak_refined *R) {
             g = nullptr;
         }
     for (void *p : R->owned) cudaFree(p);
+    if (R->ev_fork) cudaEventDestroy(R->ev_fork);
+    if (R->ev_join) cudaEventDestroy(R->ev_join);
+    if (R->side) cudaStreamDestroy(R->side);
     if (R->coarse) {
         release(R->coarse);
         delete R->coarse;
@@ -1136,7 +1141,7 @@ int refined_init(ak_refined *R, double amp, double phase_y, double phase_z, doub
 }
 
 template <typename S>
-int refined_step(ak_refined *R) {
+int refined_step(ak_refined *R, bool fork = false) {
     using T = typename Store<S>::T;
     ak_case *C = R->coarse, *F = R->fine;
     cudaStream_t st = C->stream;
@@ -1146,69 +1151,93 @@ int refined_step(ak_refined *R) {
     dim3 gf((unsigned)blocks_for(F->nx, 128), (unsigned)F->ny, (unsigned)F->nz);
     const Rescale c2f{R->tau_s_f * R->dt_f / (R->tau_s_c * R->dt_c), R->tau_b_f * R->dt_f / (R->tau_b_c * R->dt_c)};
     const Rescale f2c{R->tau_s_c * R->dt_c / (R->tau_s_f * R->dt_f), R->tau_b_c * R->dt_c / (R->tau_b_f * R->dt_f)};
-    mark(C);  // step start
-    // donors before the coarse step
-    k_block_moments<S><<<(unsigned)split_blocks(nring_block), SPLIT_THREADS, 0, st>>>(
-        src_of<S>(C), C->G, B, R->d_free, R->mom_old, nullptr, nullptr, R->d_flag);
-    mark(C);
-    k_collide<S><<<gc, 128, 0, st>>>(src_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s, (T)C->omega_b);
-    mark(C);
-    k_face_flux_coarse<S><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, st>>>(
-        src_of<S>(C), C->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs,
-        R->dx_c * R->dx_c * R->dx_c, R->reg_c);
-    if (C->n_ubb)
-        k_ubb<S><<<(unsigned)blocks3(C->n_ubb_cells * C->nz), 256, 0, st>>>(src_of<S>(C), C->G, C->ubb_cells,
-                                                                            C->n_ubb_cells, C->speed, 0.0, 0.0);
-    if (C->n_out)
-        k_outflow<S><<<(unsigned)blocks3(C->n_out), 256, 0, st>>>(src_of<S>(C), C->G, C->outer(), C->sel_out,
-                                                                  C->n_out, C->out_state, 1, 0, 0);
-    if (R->track_budget) {
-        k_outer_flux<S><<<dim3((unsigned)R->outer_blocks, 4), 256, 0, st>>>(
-            src_of<S>(C), C->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_outer, 4, R->outer_partials);
-        k_outer_final<<<1, 1, 0, st>>>(R->outer_partials, R->d_outer, 4, R->outer_blocks,
-                                       R->dx_c * R->dx_c * R->dx_c, R->outer_out);
-        C->launches += 2;
-    }
-    mark(C);
-    k_stream<S><<<gc, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, 0);
-    mark(C);
-    AK_CUDA(cudaGetLastError());
-    C->cur = 1 - C->cur;
-    // donors after the coarse step
-    k_block_moments<S><<<(unsigned)split_blocks(nring_block), SPLIT_THREADS, 0, st>>>(
-        src_of<S>(C), C->G, B, R->d_free, R->mom_new, R->mom_old, R->mom_half, R->d_flag);
-    AK_CUDA(cudaMemsetAsync(R->reg_f, 0, sizeof(double) * R->reg_doubles, st));
     const long long nband = ring_count(F->nx, F->ny, R->pad, R->pad) * F->nz;
     const long long nprox = ring_count(F->nx, B.dny, R->pad, DONOR_RING) * C->nz;
     const long long nproxy = ring_count(F->nx, F->ny, R->pad, R->pad) * C->nz;
     const long long nlinks = F->nkeys * F->nz * 3;
     const long long nb = blocks_for(nlinks, 256);
-    for (int sub = 0; sub < 2; ++sub) {
+
+    // coarse collide, face fluxes, outer boundary, stream, donors after the step
+    auto coarse_part = [&]() -> int {
+        mark(C);
+        k_collide<S><<<gc, 128, 0, st>>>(src_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s,
+                                         (T)C->omega_b);
+        mark(C);
+        k_face_flux_coarse<S><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, st>>>(
+            src_of<S>(C), C->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs,
+            R->dx_c * R->dx_c * R->dx_c, R->reg_c);
+        if (C->n_ubb)
+            k_ubb<S><<<(unsigned)blocks3(C->n_ubb_cells * C->nz), 256, 0, st>>>(src_of<S>(C), C->G, C->ubb_cells,
+                                                                                C->n_ubb_cells, C->speed, 0.0, 0.0);
+        if (C->n_out)
+            k_outflow<S><<<(unsigned)blocks3(C->n_out), 256, 0, st>>>(src_of<S>(C), C->G, C->outer(), C->sel_out,
+                                                                      C->n_out, C->out_state, 1, 0, 0);
+        if (R->track_budget) {
+            k_outer_flux<S><<<dim3((unsigned)R->outer_blocks, 4), 256, 0, st>>>(
+                src_of<S>(C), C->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_outer, 4, R->outer_partials);
+            k_outer_final<<<1, 1, 0, st>>>(R->outer_partials, R->d_outer, 4, R->outer_blocks,
+                                           R->dx_c * R->dx_c * R->dx_c, R->outer_out);
+            C->launches += 2;
+        }
+        mark(C);
+        k_stream<S><<<gc, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, 0);
+        mark(C);
+        AK_CUDA(cudaGetLastError());
+        C->cur = 1 - C->cur;
+        k_block_moments<S><<<(unsigned)split_blocks(nring_block), SPLIT_THREADS, 0, st>>>(
+            src_of<S>(C), C->G, B, R->d_free, R->mom_new, R->mom_old, R->mom_half, R->d_flag);
+        AK_CUDA(cudaGetLastError());
+        return AK_OK;
+    };
+    // one fine step on stream s: donors, collide, face fluxes, walls, stream
+    auto fine_part = [&](int sub, cudaStream_t s) -> int {
         // donor moments at the fine step's start: the old coarse state, then
         // half-way (1 - 1/2) old + 1/2 new (refined_solver.py:311-318)
-        k_prolong_x<<<(unsigned)blocks3(nprox), 256, 0, st>>>(B, C->nz, R->pad, sub ? R->mom_half : R->mom_old,
-                                                               R->pro_x);
-        k_prolong_y<<<(unsigned)blocks3(nproxy), 256, 0, st>>>(B, C->nz, R->pad, R->pro_x, R->pro_xy);
-        k_donors<S><<<(unsigned)split_blocks(nband), SPLIT_THREADS, 0, st>>>(src_of<S>(F), F->G, C->nz, R->pro_xy,
-                                                                             c2f, R->pad, R->d_flag);
+        k_prolong_x<<<(unsigned)blocks3(nprox), 256, 0, s>>>(B, C->nz, R->pad, sub ? R->mom_half : R->mom_old,
+                                                              R->pro_x);
+        k_prolong_y<<<(unsigned)blocks3(nproxy), 256, 0, s>>>(B, C->nz, R->pad, R->pro_x, R->pro_xy);
+        k_donors<S><<<(unsigned)split_blocks(nband), SPLIT_THREADS, 0, s>>>(src_of<S>(F), F->G, C->nz, R->pro_xy,
+                                                                            c2f, R->pad, R->d_flag);
         mark(C);
-        k_collide<S><<<gf, 128, 0, st>>>(src_of<S>(F), F->flags, F->G, F->shift_host, (T)F->omega_s, (T)F->omega_b);
+        k_collide<S><<<gf, 128, 0, s>>>(src_of<S>(F), F->flags, F->G, F->shift_host, (T)F->omega_s, (T)F->omega_b);
         mark(C);
-        k_face_flux_fine<S><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, st>>>(
+        k_face_flux_fine<S><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, s>>>(
             src_of<S>(F), F->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs, R->pad,
             R->dx_f * R->dx_f * R->dx_f, R->reg_f);
         if (nlinks) {
-            k_walls<S><<<(unsigned)nb, 256, 0, st>>>(src_of<S>(F), F->G, F->keys, F->wall_q, F->nkeys, 1,
-                                                     F->n_elements, F->ox, F->oy, F->partials);
-            k_sum_partials<<<5 * F->n_elements, 32, 0, st>>>(F->partials, (int)nb, 5 * F->n_elements,
-                                                              R->d_loads + sub * 5 * F->n_elements);
+            k_walls<S><<<(unsigned)nb, 256, 0, s>>>(src_of<S>(F), F->G, F->keys, F->wall_q, F->nkeys, 1,
+                                                    F->n_elements, F->ox, F->oy, F->partials);
+            k_sum_partials<<<5 * F->n_elements, 32, 0, s>>>(F->partials, (int)nb, 5 * F->n_elements,
+                                                             R->d_loads + sub * 5 * F->n_elements);
         }
         mark(C);
-        k_stream<S><<<gf, 128, 0, st>>>(src_of<S>(F), dst_of<S>(F), F->flags, F->G, 1);
+        k_stream<S><<<gf, 128, 0, s>>>(src_of<S>(F), dst_of<S>(F), F->flags, F->G, 1);
         mark(C);
         AK_CUDA(cudaGetLastError());
         F->cur = 1 - F->cur;
+        return AK_OK;
+    };
+
+    mark(C);  // step start
+    // donors before the coarse step
+    k_block_moments<S><<<(unsigned)split_blocks(nring_block), SPLIT_THREADS, 0, st>>>(
+        src_of<S>(C), C->G, B, R->d_free, R->mom_old, nullptr, nullptr, R->d_flag);
+    if (fork) {
+        // the first fine step needs only the donors before the coarse step:
+        // it runs on the side stream beside the coarse step (captured graphs)
+        AK_CUDA(cudaEventRecord(R->ev_fork, st));
+        AK_CUDA(cudaStreamWaitEvent(R->side, R->ev_fork, 0));
+        AK_CUDA(cudaMemsetAsync(R->reg_f, 0, sizeof(double) * R->reg_doubles, R->side));
+        AK_TRY(fine_part(0, R->side));
+        AK_CUDA(cudaEventRecord(R->ev_join, R->side));
+        AK_TRY(coarse_part());
+        AK_CUDA(cudaStreamWaitEvent(st, R->ev_join, 0));
+    } else {
+        AK_TRY(coarse_part());
+        AK_CUDA(cudaMemsetAsync(R->reg_f, 0, sizeof(double) * R->reg_doubles, st));
+        AK_TRY(fine_part(0, st));
     }
+    AK_TRY(fine_part(1, st));
     if (nlinks) {
         k_accumulate_loads<<<1, 128, 0, st>>>(R->d_loads, 5 * F->n_elements, R->cum_loads);
         C->launches += 1;
@@ -1240,7 +1269,7 @@ int refined_step_graphed(ak_refined *R) {
         std::vector<cudaEvent_t> *timing = C->timing;
         C->timing = nullptr;
         AK_CUDA(cudaStreamBeginCapture(C->stream, cudaStreamCaptureModeThreadLocal));
-        const int r = refined_step<S>(R);
+        const int r = refined_step<S>(R, true);
         cudaGraph_t g = nullptr;
         const cudaError_t e = cudaStreamEndCapture(C->stream, &g);
         C->timing = timing;
@@ -1423,6 +1452,10 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
                            cudaMemset(R->cum_loads, 0, 5 * std::max(1, cd.n_elements) * sizeof(double)) != cudaSuccess))
             r = fail(AK_ERR_CUDA, "memset failed");
     }
+    if (r == AK_OK && (cudaStreamCreateWithFlags(&R->side, cudaStreamNonBlocking) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&R->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&R->ev_join, cudaEventDisableTiming) != cudaSuccess))
+        r = fail(AK_ERR_CUDA, "stream or event creation failed");
     if (r == AK_OK) r = ralloc(R, &R->d_flag, 1);
     if (r == AK_OK) r = ralloc(R, &R->d_loads, (size_t)2 * 5 * std::max(1, cd.n_elements));
     if (r == AK_OK) {
