@@ -257,11 +257,13 @@ __host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b) 
     const T phy[3] = {T(0.5) * (ty - uy), T(1) - ty, T(0.5) * (ty + uy)};
     const T psy[3] = {uy - T(0.5), T(-2) * uy, uy + T(0.5)};
     const T chy[3] = {T(0.5), T(-1), T(0.5)};
-    // x-functions in the E/D split
+    // x-functions: phi_x(+-1) = (t_x +- u_x) / 2, psi_x(+-1) = u_x +- 1/2
     const T htx = T(0.5) * tx, hux = T(0.5) * ux, omtx = T(1) - tx, m2ux = T(-2) * ux;
-    // rho-scaled z-functions in the E/D split
+    const T px2 = htx + hux, px0 = htx - hux, sx2 = ux + T(0.5), sx0 = ux - T(0.5);
+    // rho-scaled z-functions, the c_z = +1 and -1 rows as sums and differences
     const T rhtz = T(0.5) * rho * tz, rhuz = T(0.5) * rho * uz, rh = T(0.5) * rho;
     const T r0z = rho * (T(1) - tz), rm2uz = T(-2) * rho * uz, ruz = rho * uz;
+    const T pz2 = rhtz + rhuz, pz0 = rhtz - rhuz, qz2 = ruz + rh, qz0 = ruz - rh;
 #pragma unroll
     for (int iy = 0; iy < 3; ++iy) {
         // coefficients of phi_x, psi_x, chi_x in A, B, C for this c_y
@@ -270,26 +272,25 @@ __host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b) 
         const T Cp = kCphi * chy[iy], Cs = kCpsi * psy[iy], Cc = kCchi * phy[iy] + k8 * chy[iy];
         T A[3], B[3], C[3];
         {
-            const T E = htx * Ap + ux * As + T(0.5) * Ac, D = hux * Ap + T(0.5) * As;
-            A[2] = E + D; A[0] = E - D; A[1] = omtx * Ap + m2ux * As - Ac;
+            const T hc = T(0.5) * Ac;
+            A[2] = px2 * Ap + (sx2 * As + hc); A[0] = px0 * Ap + (sx0 * As + hc); A[1] = omtx * Ap + (m2ux * As - Ac);
         }
         {
-            const T E = htx * Bp + ux * Bs + T(0.5) * Bc, D = hux * Bp + T(0.5) * Bs;
-            B[2] = E + D; B[0] = E - D; B[1] = omtx * Bp + m2ux * Bs - Bc;
+            const T hc = T(0.5) * Bc;
+            B[2] = px2 * Bp + (sx2 * Bs + hc); B[0] = px0 * Bp + (sx0 * Bs + hc); B[1] = omtx * Bp + (m2ux * Bs - Bc);
         }
         {
-            const T E = htx * Cp + ux * Cs + T(0.5) * Cc, D = hux * Cp + T(0.5) * Cs;
-            C[2] = E + D; C[0] = E - D; C[1] = omtx * Cp + m2ux * Cs - Cc;
+            const T hc = T(0.5) * Cc;
+            C[2] = px2 * Cp + (sx2 * Cs + hc); C[0] = px0 * Cp + (sx0 * Cs + hc); C[1] = omtx * Cp + (m2ux * Cs - Cc);
         }
         // the rest weights (equal for c_z = -1 and +1) enter the fused
         // multiply-add chains as their first addend
 #pragma unroll
         for (int ix = 0; ix < 3; ++ix) {
             const T w_pm = T(weight(qof(ix, iy, 2))), w_0 = T(weight(qof(ix, iy, 1)));
-            const T E = A[ix] * rhtz + (B[ix] * ruz + (C[ix] * rh - w_pm));
-            const T D = A[ix] * rhuz + B[ix] * rh;
-            g[qof(ix, iy, 2)] = E + D;
-            g[qof(ix, iy, 0)] = E - D;
+            const T cw = C[ix] * rh - w_pm;
+            g[qof(ix, iy, 2)] = A[ix] * pz2 + (B[ix] * qz2 + cw);
+            g[qof(ix, iy, 0)] = A[ix] * pz0 + (B[ix] * qz0 + cw);
             g[qof(ix, iy, 1)] = A[ix] * r0z + (B[ix] * rm2uz - (C[ix] * rho + w_0));
         }
     }
