@@ -106,6 +106,11 @@ SIGNATURES = {
     "ak_refined_outer_flux": ([_P, _P], ctypes.c_int),
     "ak_refined_integrals": ([_P, _P], ctypes.c_int),
     "ak_refined_cumulative_loads": ([_P, _P], ctypes.c_int),
+    "ak_boundary_state_size": ([_P, _P, _P], ctypes.c_int),
+    "ak_get_boundary_state": ([_P, _P, _P], ctypes.c_int),
+    "ak_set_boundary_state": ([_P, _P, _P], ctypes.c_int),
+    "ak_set_steps_done": ([_P, ctypes.c_int64], ctypes.c_int),
+    "ak_refined_restore_counters": ([_P, ctypes.c_int64, _P, _P], ctypes.c_int),
     "ak_batch_create": ([_P, ctypes.c_int32, _P], ctypes.c_int),
     "ak_batch_destroy": ([_P], ctypes.c_int),
     "ak_batch_step": ([_P, ctypes.c_int32, _P], ctypes.c_int),

@@ -930,6 +930,108 @@ int ak_set_pdf(ak_case *c, const double *pdf) {
     return AK_OK;
 }
 
+// ---- outer-boundary history for checkpoints
+namespace {
+long long boundary_values(const ak_case *c) {
+    if (c->farfield == AK_FARFIELD_CHARACTERISTIC) return 1 + 3 * c->nouter + 2LL * c->nx * c->nz;
+    if (c->farfield == AK_FARFIELD_LEGACY) return 1 + 2 * c->n_out;
+    return 1;
+}
+int boundary_rows(ak_case *c, std::vector<int32_t> &rows) {
+    const long long n = c->nouter;
+    std::vector<int> x(n), y(n), z(n);
+    std::vector<signed char> d(n);
+    if (n) {
+        AK_CUDA(cudaMemcpy(x.data(), c->ox_, n * sizeof(int), cudaMemcpyDeviceToHost));
+        AK_CUDA(cudaMemcpy(y.data(), c->oy_, n * sizeof(int), cudaMemcpyDeviceToHost));
+        AK_CUDA(cudaMemcpy(z.data(), c->oz_, n * sizeof(int), cudaMemcpyDeviceToHost));
+        AK_CUDA(cudaMemcpy(d.data(), c->od, n * sizeof(signed char), cudaMemcpyDeviceToHost));
+    }
+    rows.resize(4 * n);
+    for (long long k = 0; k < n; ++k) {
+        rows[4 * k] = x[k] - 1;
+        rows[4 * k + 1] = y[k] - 1;
+        rows[4 * k + 2] = z[k];
+        rows[4 * k + 3] = d[k];
+    }
+    return AK_OK;
+}
+}  // namespace
+
+int ak_boundary_state_size(ak_case *c, int64_t *n_links, int64_t *n_values) {
+    AK_TRY(check_case(c));
+    if (!n_links || !n_values) return fail(AK_ERR_INVALID, "null output");
+    *n_links = c->nouter;
+    *n_values = boundary_values(c);
+    return AK_OK;
+}
+
+int ak_get_boundary_state(ak_case *c, int32_t *rows, double *values) {
+    AK_TRY(check_case(c));
+    if ((!rows && c->nouter) || !values) return fail(AK_ERR_INVALID, "null output");
+    AK_CUDA(cudaStreamSynchronize(c->stream));
+    std::vector<int32_t> r;
+    AK_TRY(boundary_rows(c, r));
+    if (!r.empty()) std::memcpy(rows, r.data(), r.size() * sizeof(int32_t));
+    values[0] = c->prepared ? 1.0 : 0.0;
+    double *v = values + 1;
+    const long long n = c->nouter;
+    if (c->farfield == AK_FARFIELD_CHARACTERISTIC) {
+        std::vector<long long> clock(n);
+        if (n) {
+            AK_CUDA(cudaMemcpy(v, c->ff_in, n * sizeof(double), cudaMemcpyDeviceToHost));
+            AK_CUDA(cudaMemcpy(v + n, c->ff_der, n * sizeof(double), cudaMemcpyDeviceToHost));
+            AK_CUDA(cudaMemcpy(clock.data(), c->ff_clock, n * sizeof(long long), cudaMemcpyDeviceToHost));
+        }
+        for (long long k = 0; k < n; ++k) v[2 * n + k] = (double)clock[k];
+        const long long rows_n = (long long)c->nx * c->nz;
+        AK_CUDA(cudaMemcpy(v + 3 * n, c->ff_lo, rows_n * sizeof(double), cudaMemcpyDeviceToHost));
+        AK_CUDA(cudaMemcpy(v + 3 * n + rows_n, c->ff_hi, rows_n * sizeof(double), cudaMemcpyDeviceToHost));
+    } else if (c->farfield == AK_FARFIELD_LEGACY && c->n_out) {
+        AK_CUDA(cudaMemcpy(v, c->out_state, 2 * c->n_out * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    return AK_OK;
+}
+
+int ak_set_boundary_state(ak_case *c, const int32_t *rows, const double *values) {
+    AK_TRY(check_case(c));
+    if ((!rows && c->nouter) || !values) return fail(AK_ERR_INVALID, "null input");
+    AK_CUDA(cudaStreamSynchronize(c->stream));
+    std::vector<int32_t> r;
+    AK_TRY(boundary_rows(c, r));
+    if (!r.empty() && std::memcmp(rows, r.data(), r.size() * sizeof(int32_t)) != 0)
+        return fail(AK_ERR_INVALID, "boundary link geometry differs from this case's");
+    const double *v = values + 1;
+    const long long n = c->nouter;
+    if (c->farfield == AK_FARFIELD_CHARACTERISTIC) {
+        std::vector<long long> clock(n);
+        for (long long k = 0; k < n; ++k) {
+            const double t = v[2 * n + k];
+            if (!(t >= 0.0) || t != std::floor(t)) return fail(AK_ERR_INVALID, "invalid glancing clock");
+            clock[k] = (long long)t;
+        }
+        if (n) {
+            AK_CUDA(cudaMemcpy(c->ff_in, v, n * sizeof(double), cudaMemcpyHostToDevice));
+            AK_CUDA(cudaMemcpy(c->ff_der, v + n, n * sizeof(double), cudaMemcpyHostToDevice));
+            AK_CUDA(cudaMemcpy(c->ff_clock, clock.data(), n * sizeof(long long), cudaMemcpyHostToDevice));
+        }
+        const long long rows_n = (long long)c->nx * c->nz;
+        AK_CUDA(cudaMemcpy(c->ff_lo, v + 3 * n, rows_n * sizeof(double), cudaMemcpyHostToDevice));
+        AK_CUDA(cudaMemcpy(c->ff_hi, v + 3 * n + rows_n, rows_n * sizeof(double), cudaMemcpyHostToDevice));
+    } else if (c->farfield == AK_FARFIELD_LEGACY && c->n_out) {
+        AK_CUDA(cudaMemcpy(c->out_state, v, 2 * c->n_out * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    c->prepared = values[0] != 0.0;
+    return AK_OK;
+}
+
+int ak_set_steps_done(ak_case *c, int64_t steps) {
+    AK_TRY(check_case(c));
+    if (steps < 0) return fail(AK_ERR_INVALID, "steps must be >= 0");
+    c->steps = steps;
+    return AK_OK;
+}
+
 int ak_get_flags(ak_case *c, uint8_t *flags) {
     AK_TRY(check_case(c));
     if (!flags) return fail(AK_ERR_INVALID, "null output");
@@ -1534,6 +1636,20 @@ int ak_refined_outer_flux(ak_refined *R, double *out) {
     if (!R || !out) return fail(AK_ERR_INVALID, "a case and an output array are required");
     AK_CUDA(cudaStreamSynchronize(R->coarse->stream));
     AK_CUDA(cudaMemcpy(out, R->outer_out, 8 * sizeof(double), cudaMemcpyDeviceToHost));
+    return AK_OK;
+}
+
+int ak_refined_restore_counters(ak_refined *R, int64_t steps, const double *cumulative_loads,
+                                const double *cumulative_outer) {
+    if (!R || steps < 0 || !cumulative_loads || !cumulative_outer)
+        return fail(AK_ERR_INVALID, "a case, steps >= 0 and both arrays are required");
+    AK_CUDA(cudaStreamSynchronize(R->coarse->stream));
+    AK_CUDA(cudaMemcpy(R->cum_loads, cumulative_loads, 5 * std::max(1, R->fine->n_elements) * sizeof(double),
+                       cudaMemcpyHostToDevice));
+    AK_CUDA(cudaMemcpy(R->outer_out + 4, cumulative_outer, 4 * sizeof(double), cudaMemcpyHostToDevice));
+    R->steps = steps;
+    R->coarse->steps = steps;
+    R->fine->steps = 2 * steps;
     return AK_OK;
 }
 

@@ -13,7 +13,10 @@ from dataclasses import asdict
 import hashlib
 import json
 import math
+import os
 from pathlib import Path
+import shutil
+import uuid
 
 import numpy as np
 
@@ -21,7 +24,7 @@ from . import _native
 from ._native import check
 from .project import write_json
 from .refined_plan import RefinedPlan, RefinementSettings, refined_project_dict
-from .solver import _duration_steps, _leading_edge, _ptr
+from .solver import _duration_steps, _file_hash, _leading_edge, _ptr
 
 __all__ = ["RefinedSolver", "RefinementSettings", "RefinedPlan"]
 
@@ -352,42 +355,95 @@ class RefinedSolver:
         tmp.replace(path)
         return path
 
+    # ------------------------------------------------------------ checkpoints
+    def _padded_shape(self):
+        fx, fy, fz = self.fine_shape
+        return (fx + 2 * self.pad, fy + 2 * self.pad, fz)
+
+    def save_checkpoint(self, path, context=None):
+        from .checkpoint import save_refined_checkpoint
+        return save_refined_checkpoint(self, path, context)
+
+    @classmethod
+    def from_checkpoint(cls, path, progress=None):
+        from .checkpoint import restore_refined_checkpoint
+        return restore_refined_checkpoint(cls, path, progress)
+
+    @classmethod
+    def resume_run(cls, output, **kwargs):
+        """Continue an interrupted run from output/checkpoint.npz (refined_run.py:159-163)."""
+        output = Path(output)
+        solver = cls.from_checkpoint(output / "checkpoint.npz", progress=kwargs.pop("progress", None))
+        return solver.run(output, resume=True, **kwargs)
+
     def run(self, output, *, callback=None, stop_event=None, resume=False, residual_callback=None):
         """Run the project's RunSettings and write project.json, history.csv,
-        metadata.json, summary.json and frames (refined_run.py:19-156) for new
-        runs; checks, samples, frames, the callback/stop_event contract and the
-        failed-run report follow the reference."""
-        if resume:
-            raise NotImplementedError("resume needs the GPU checkpoint format, which this engine does not write yet")
+        metadata.json, summary.json, frames and checkpoint.npz
+        (refined_run.py:19-156): checks, samples, frames, checkpoints every
+        checkpoint_every steps and at the end, resume from the last checkpoint,
+        the callback/stop_event contract and the failed-run report."""
+        from .refined_plan import load_refined_project
         settings = self.project.run
-        requested = _duration_steps(settings.duration_convective, self.coarse_level.dt)
         output = Path(output)
-        if output.exists() and any(output.iterdir()):
+        if not resume and output.exists() and any(output.iterdir()):
             raise FileExistsError("Use a new/empty refined result directory")
         output.mkdir(parents=True, exist_ok=True)
-        (output / "frames").mkdir()
+        (output / "frames").mkdir(exist_ok=resume)
         history = output / "history.csv"
         columns = ["step", "t_star", "cl", "cd", "cm"]
         if self.plan.dt_seconds is not None:
             columns.append("time_s")
-        end_step = self.steps + requested
-        metadata = {"format": "aerokinetic_refined_run", "version": "aerokinetic_gb300",
-                    "case_fingerprint": self.case_fingerprint, "flow": asdict(self.flow),
-                    "grid": asdict(self.grid), "refinement": asdict(self.refinement),
-                    "plan": _jsonable(self.plan.as_dict()), "run": asdict(settings), "start_step": self.steps,
-                    "contours": [{"name": e.name, "xy": e.xy.tolist()} for e in self.section.elements],
-                    "coefficient_convention": "Cl up; Cd downstream; Cm nose-up about the chosen reference; area=c*periodic_span",
-                    "force_time": "average of both fine momentum-transfer intervals; timestamp at coarse interval midpoint",
-                    "experimental_validation": "not_performed", "resume_supported": False,
-                    "storage": self.storage, "reference_chord_input_units": self.section.chord,
-                    "moment_reference_input_units": self.section.moment_reference}
-        write_json(output / "project.json", refined_project_dict(self.project, self.refinement))
-        with history.open("w", newline="", encoding="utf-8") as handle:
-            csv.DictWriter(handle, fieldnames=columns).writeheader()
-        self.save_frame(output / "frames" / f"frame_{self.steps:09d}.npz")
+        end_step = self.steps + _duration_steps(settings.duration_convective, self.coarse_level.dt)
+        if resume:
+            metadata = json.loads((output / "metadata.json").read_text(encoding="utf-8"))
+            context = getattr(self, "_checkpoint_context", {})
+            metadata["resumed_with_version"] = "aerokinetic_gb300"
+            original, refinement = load_refined_project(output / "project.json")
+            if (original.case_fingerprint != self.project.case_fingerprint or refinement != self.refinement
+                    or original.run != settings or metadata["case_fingerprint"] != self.case_fingerprint
+                    or context.get("case_fingerprint") != self.case_fingerprint):
+                raise ValueError("Refined project/run settings changed; cannot mix histories")
+            if metadata["status"] == "completed":
+                raise ValueError("The requested refined run has already completed")
+            end_step = context["end_step"]
+            prefix = context["history_bytes"]
+            if _file_hash(history, prefix) != context["history_sha256"]:
+                raise ValueError("Refined history before checkpoint changed")
+            future = [p for p in (output / "frames").glob("frame_*.npz") if int(p.stem.split("_")[-1]) > self.steps]
+            if history.stat().st_size > prefix or future:
+                recovery = output / "recovery" / uuid.uuid4().hex
+                recovery.mkdir(parents=True)
+                shutil.copy2(history, recovery / "history_before_resume.csv")
+                with history.open("r+b") as handle:
+                    handle.truncate(prefix)
+                for path in future:
+                    shutil.move(str(path), str(recovery / path.name))
+        else:
+            metadata = {"format": "aerokinetic_refined_run", "version": "aerokinetic_gb300",
+                        "case_fingerprint": self.case_fingerprint, "flow": asdict(self.flow),
+                        "grid": asdict(self.grid), "refinement": asdict(self.refinement),
+                        "plan": _jsonable(self.plan.as_dict()), "run": asdict(settings), "start_step": self.steps,
+                        "contours": [{"name": e.name, "xy": e.xy.tolist()} for e in self.section.elements],
+                        "coefficient_convention": "Cl up; Cd downstream; Cm nose-up about the chosen reference; area=c*periodic_span",
+                        "force_time": "average of both fine momentum-transfer intervals; timestamp at coarse interval midpoint",
+                        "experimental_validation": "not_performed", "resume_supported": True,
+                        "storage": self.storage, "reference_chord_input_units": self.section.chord,
+                        "moment_reference_input_units": self.section.moment_reference}
+            write_json(output / "project.json", refined_project_dict(self.project, self.refinement))
+            with history.open("w", newline="", encoding="utf-8") as handle:
+                csv.DictWriter(handle, fieldnames=columns).writeheader()
+            self.save_frame(output / "frames" / f"frame_{self.steps:09d}.npz")
         metadata.update(status="running", target_steps=end_step)
         write_json(output / "metadata.json", metadata)
         status, error, reason = "completed", None, "duration_reached"
+
+        def checkpoint(handle):
+            handle.flush()
+            os.fsync(handle.fileno())
+            context = {"case_fingerprint": self.case_fingerprint, "end_step": end_step,
+                       "history_bytes": history.stat().st_size, "history_sha256": _file_hash(history)}
+            self.save_checkpoint(output / "checkpoint.npz", context)
+
         try:
             with history.open("a", newline="", encoding="utf-8") as handle:
                 writer = csv.DictWriter(handle, fieldnames=columns)
@@ -395,10 +451,12 @@ class RefinedSolver:
                     if stop_event is not None and stop_event.is_set():
                         status, reason = "stopped", "user_stopped"
                         break
-                    # steps up to the next one that checks, samples or writes a frame
+                    # steps up to the next one that checks, samples, writes a frame or a checkpoint
                     nxt = end_step
-                    for every in (settings.check_every, settings.sample_every, settings.frame_every):
-                        nxt = min(nxt, (self.steps // every + 1) * every)
+                    for every in (settings.check_every, settings.sample_every, settings.frame_every,
+                                  settings.checkpoint_every):
+                        if every:
+                            nxt = min(nxt, (self.steps // every + 1) * every)
                     record = self.advance(nxt - self.steps)
                     if self.steps % settings.check_every == 0:
                         self.diagnostics()
@@ -409,10 +467,13 @@ class RefinedSolver:
                             status, reason = "stopped", "user_stopped"
                     if self.steps % settings.frame_every == 0:
                         self.save_frame(output / "frames" / f"frame_{self.steps:09d}.npz")
+                    if settings.checkpoint_every and self.steps % settings.checkpoint_every == 0:
+                        checkpoint(handle)
                     if status == "stopped":
                         break
-            self.diagnostics()
-            self.save_frame(output / "frames" / f"frame_{self.steps:09d}.npz")
+                self.diagnostics()
+                self.save_frame(output / "frames" / f"frame_{self.steps:09d}.npz")
+                checkpoint(handle)
         except Exception as failure:
             status, error, reason = "failed", f"{type(failure).__name__}: {failure}", "failed"
         with history.open(newline="", encoding="utf-8") as handle:

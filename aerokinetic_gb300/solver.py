@@ -8,10 +8,14 @@ C ABI of include/aerokinetic_gb300.h.  There is no CPU path.
 import csv
 import ctypes
 from dataclasses import asdict
+import hashlib
 import json
 import math
+import os
 from pathlib import Path
+import shutil
 import time
+import uuid
 
 import numpy as np
 
@@ -194,31 +198,50 @@ class Solver:
                                 dx=self.plan.dx * stride, t_star=self.steps * self.plan.dt_convective)
         tmp.replace(path)
 
+    # --------------------------------------------------------------- checkpoints
+    def save_checkpoint(self, path, context=None):
+        from .checkpoint import save_checkpoint
+        return save_checkpoint(self, path, context)
+
+    @classmethod
+    def from_checkpoint(cls, path, progress=None):
+        from .checkpoint import restore_checkpoint
+        return restore_checkpoint(cls, path, progress)
+
+    @classmethod
+    def resume_run(cls, output, callback=None, stop_event=None, progress=None, residual_callback=None):
+        """Continue an interrupted run from output/checkpoint.npz (solver.py:345-351)."""
+        output = Path(output)
+        metadata = json.loads((output / "metadata.json").read_text(encoding="utf-8"))
+        solver = cls.from_checkpoint(output / "checkpoint.npz", progress)
+        run = dict(metadata["run"])
+        return solver.run(output=output, callback=callback, stop_event=stop_event, residual_callback=residual_callback,
+                          resume=True, **run)
+
     # --------------------------------------------------------------- run loop
     def run(self, duration_convective, output, sample_every=20, frame_every=200, average_after=0.0,
             check_every=100, callback=None, stop_event=None, checkpoint_every=1000, resume=False,
             termination=None, residual_callback=None):
-        """Advance t* = t U / c and write history.csv, metadata.json, summary.json and frames.
-
-        Mirrors solver.py:353-537 for new runs (sampling, guards, frames,
-        callback/stop_event contract and the failed-run report).  Steps between
-        samples are issued as one engine call.
+        """Advance t* = t U / c and write history.csv, metadata.json, summary.json,
+        frames and checkpoint.npz (solver.py:353-537): sampling, guards, frames,
+        the callback/stop_event contract, checkpoints every checkpoint_every
+        steps and at the end, resume from the last checkpoint (resume_run), and
+        the failed-run report.  Steps between samples are one engine call.
         """
-        if resume:
-            raise NotImplementedError("resume needs the GPU checkpoint format, which this engine does not write yet")
         from .project import StopCriteria
+        if isinstance(termination, dict):
+            termination = StopCriteria(**termination)
         settings = RunSettings(duration_convective, sample_every, frame_every, check_every, average_after,
                                checkpoint_every, termination or StopCriteria())
         project = Project(self.section, self.flow, self.grid, settings,
                           "+".join(e.name for e in self.section.elements))
         output = Path(output)
-        if output.exists() and any(output.iterdir()):
+        if not resume and output.exists() and any(output.iterdir()):
             raise FileExistsError("Use a new/empty output directory to avoid mixing histories")
         output.mkdir(parents=True, exist_ok=True)
-        (output / "frames").mkdir(exist_ok=True)
-        project.save(output / "project.json")
-        requested = _duration_steps(duration_convective, self.plan.dt_convective)
-        end_step = self.steps + requested
+        (output / "frames").mkdir(exist_ok=resume)
+        history = output / "history.csv"
+        end_step = self.steps + _duration_steps(duration_convective, self.plan.dt_convective)
         metadata = {"version": "aerokinetic_gb300", "flow": asdict(self.flow), "grid": asdict(self.grid),
                     "plan": self.plan.as_dict(), "reference_chord_input_units": self.section.chord,
                     "moment_reference_input_units": self.section.moment_reference,
@@ -226,26 +249,81 @@ class Solver:
                     "coefficient_convention": "Cl up; Cd downstream; Cm nose-up about moment_reference; area=c*periodic_span",
                     "force_time": "midpoint of boundary momentum-transfer interval", "status": "running",
                     "experimental_validation": "not_performed", "case_fingerprint": project.case_fingerprint,
-                    "run": asdict(settings), "start_step": self.steps, "storage": self.storage,
-                    "end_step": end_step}
-        write_json(output / "metadata.json", metadata)
+                    "run": asdict(settings), "start_step": self.steps,
+                    "start_t_star": self.steps * self.plan.dt_convective, "storage": self.storage,
+                    "resume_supported": True}
         names = ["step", "t_star", "time_s", "cl", "cd", "cm", "local_mach_max", "density_error_max"]
-        rows, state, reason = [], "completed", "duration_reached"
+        rows = []
+        if resume:
+            old = json.loads((output / "metadata.json").read_text(encoding="utf-8"))
+            metadata["start_step"] = old.get("start_step", 0)
+            metadata["start_t_star"] = metadata["start_step"] * self.plan.dt_convective
+            metadata["resumed_from_version"] = old.get("version")
+            context = getattr(self, "_checkpoint_context", {})
+            saved_project = Project.load(output / "project.json")
+            if (saved_project.case_fingerprint != project.case_fingerprint
+                    or asdict(saved_project.run) != asdict(settings)):
+                raise ValueError("Saved project or run settings changed; resume requires the original project")
+            if (old.get("case_fingerprint") != project.case_fingerprint
+                    or context.get("case_fingerprint") != project.case_fingerprint):
+                raise ValueError("Resume requires the original project, settings and checkpoint")
+            if old.get("status") == "completed":
+                raise ValueError("This run has already completed")
+            end_step = context["end_step"]
+            prefix = context["history_bytes"]
+            if _file_hash(history, prefix) != context["history_sha256"]:
+                raise ValueError("History before the checkpoint has changed; refusing to mix results")
+            # samples and frames written after the last durable checkpoint are
+            # kept aside, then the same timeline continues from the checkpoint
+            future = [p for p in (output / "frames").glob("frame_*.npz") if int(p.stem.split("_")[-1]) > self.steps]
+            if history.stat().st_size > prefix or future:
+                recovery = output / "recovery" / uuid.uuid4().hex
+                recovery.mkdir(parents=True)
+                shutil.copy2(history, recovery / "history_before_resume.csv")
+                with history.open("r+b") as handle:
+                    handle.truncate(prefix)
+                for path in future:
+                    shutil.move(str(path), str(recovery / path.name))
+            with history.open(newline="", encoding="utf-8") as handle:
+                rows = list(csv.DictReader(handle))
+            for row in rows:
+                row["step"] = int(row["step"])
+                for name in ("t_star", "cl", "cd", "cm"):
+                    row[name] = float(row[name])
+            if rows and rows[-1]["step"] > self.steps:
+                raise ValueError("History extends beyond the checkpoint")
+        else:
+            project.save(output / "project.json")
+        if self.steps > end_step:
+            raise ValueError("Checkpoint is past the requested end time")
+        metadata["end_step"] = end_step
+        write_json(output / "metadata.json", metadata)
+        state, reason = "completed", "duration_reached"
         start = time.monotonic()
         try:
             self.diagnostics()
             self.save_frame(output / "frames" / f"frame_{self.steps:010d}.npz")
-            with (output / "history.csv").open("w", newline="", encoding="utf-8") as handle:
+            with history.open("a" if resume else "w", newline="", encoding="utf-8") as handle:
                 writer = csv.DictWriter(handle, names)
-                writer.writeheader()
+                if not resume:
+                    writer.writeheader()
+
+                def checkpoint():
+                    handle.flush()
+                    os.fsync(handle.fileno())
+                    context = {"case_fingerprint": project.case_fingerprint, "end_step": end_step,
+                               "history_bytes": history.stat().st_size, "history_sha256": _file_hash(history)}
+                    self.save_checkpoint(output / "checkpoint.npz", context)
+
                 while self.steps < end_step:
                     if stop_event is not None and stop_event.is_set():
                         state, reason = "stopped", "user_stopped"
                         break
-                    # next step that samples, checks or writes a frame
+                    # next step that samples, checks, writes a frame or a checkpoint
                     nxt = end_step
-                    for every in (sample_every, check_every, frame_every):
-                        nxt = min(nxt, (self.steps // every + 1) * every)
+                    for every in (sample_every, check_every, frame_every, checkpoint_every):
+                        if every:
+                            nxt = min(nxt, (self.steps // every + 1) * every)
                     sample = nxt % sample_every == 0
                     record = self.advance(nxt - self.steps, sample_last=sample)
                     diagnostic = None
@@ -264,12 +342,18 @@ class Solver:
                         if callback is not None and callback(self, record) is False:
                             state, reason = "stopped", "user_stopped"
                             break
+                    if checkpoint_every and self.steps % checkpoint_every == 0:
+                        checkpoint()
+                self.diagnostics()
+                self.save_frame(output / "frames" / f"frame_{self.steps:010d}.npz")
+                checkpoint()
         except BaseException as error:
             state, reason = "failed", "failed"
             metadata["failure"] = f"{type(error).__name__}: {error}"
             raise
         finally:
-            selected = np.array([[r["cl"], r["cd"], r["cm"]] for r in rows if r["t_star"] >= average_after])
+            selected = np.array([[float(r["cl"]), float(r["cd"]), float(r["cm"])] for r in rows
+                                 if float(r["t_star"]) >= average_after])
             ok = len(selected) and state != "failed"
             summary = {"status": state, "steps": self.steps, "t_star": self.steps * self.plan.dt_convective,
                        "wall_clock_seconds": time.monotonic() - start, "samples": len(rows),
@@ -301,6 +385,21 @@ class Solver:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def _file_hash(path, limit=None):
+    """sha256 of a file's first `limit` bytes (all of it without a limit)."""
+    digest = hashlib.sha256()
+    remaining = None if limit is None else int(limit)
+    with Path(path).open("rb") as handle:
+        while remaining is None or remaining > 0:
+            block = handle.read(1 << 20 if remaining is None else min(1 << 20, remaining))
+            if not block:
+                break
+            digest.update(block)
+            if remaining is not None:
+                remaining -= len(block)
+    return digest.hexdigest()
 
 
 def _duration_steps(duration, dt):

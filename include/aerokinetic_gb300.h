@@ -138,6 +138,21 @@ int ak_macros(ak_case *c, double *rho, double *u);
 int ak_get_pdf(ak_case *c, double *pdf);
 int ak_set_pdf(ak_case *c, const double *pdf);
 
+/* History of the outer boundary for checkpoints (checkpoint.py:32-135 keeps
+ * lbmpy's boundary index arrays for the same reason): n_links outer links,
+ * rows[4 k .. 4 k + 3] = (x, y, z, direction) of link k in interior
+ * coordinates; values[0] = 1 once the boundary data are prepared, then for the
+ * characteristic farfield incoming[n], derivative[n], glancing clock[n],
+ * initial invariant rows lo[nx * nz], hi[nx * nz]; for the legacy boundary the
+ * ExtrapolationOutflow state (neighbour, boundary value) of each outflow link.
+ * ak_set_boundary_state refuses rows that differ from the case's own. */
+int ak_boundary_state_size(ak_case *c, int64_t *n_links, int64_t *n_values);
+int ak_get_boundary_state(ak_case *c, int32_t *rows, double *values);
+int ak_set_boundary_state(ak_case *c, const int32_t *rows, const double *values);
+/* Step counter of a restored case (Solver.steps after restore_checkpoint,
+ * checkpoint.py:113). */
+int ak_set_steps_done(ak_case *c, int64_t steps);
+
 /* Solid flags of the interior columns (nx*ny, x-major like the reference's
  * _solid_xy): 0 fluid, k+1 inside element k. */
 int ak_get_flags(ak_case *c, uint8_t *flags);
@@ -189,6 +204,11 @@ int ak_refined_outer_flux(ak_refined *r, double *out);
  * step since initialisation (cumulative_wall_impulse and
  * cumulative_wall_mass_exchange, refined_solver.py:340-341). */
 int ak_refined_cumulative_loads(ak_refined *r, double *out);
+/* Restores a checkpoint's step count and running sums (refined_checkpoint.py):
+ * cumulative_loads[n_elements * 5] as ak_refined_cumulative_loads returns
+ * them, cumulative_outer[4] as out[4..7] of ak_refined_outer_flux. */
+int ak_refined_restore_counters(ak_refined *r, int64_t steps, const double *cumulative_loads,
+                                const double *cumulative_outer);
 /* Per-level statistics for conserved_integrals and diagnostics
  * (refined_solver.py:291-299, 347-361): out[0..7] coarse cells outside the
  * fine box, out[8..15] fluid cells of the physical fine block, each
