@@ -19,6 +19,7 @@ from pathlib import Path
 import numpy as np
 
 from ._native import check
+from .convergence import restore_control, save_control
 from .project import Project
 
 FORMAT = "aerokinetic_gb300_checkpoint"
@@ -95,7 +96,9 @@ def save_checkpoint(solver, path, context=None):
     metadata = {"format": FORMAT, "schema_version": SCHEMA, "kind": "uniform", "project": project.as_dict(),
                 "case_fingerprint": project.case_fingerprint, "steps": solver.steps, "storage": solver.storage,
                 "wall_fallback_links": solver.wall_fallback_links, "context": context or {}}
-    return _write(path, {"pdf": solver.pdf(), "boundary_rows": rows, "boundary_values": values}, metadata)
+    arrays = {"pdf": solver.pdf(), "boundary_rows": rows, "boundary_values": values}
+    save_control(solver, arrays, metadata)
+    return _write(path, arrays, metadata)
 
 
 def restore_checkpoint(solver_type, path, progress=None):
@@ -116,6 +119,7 @@ def restore_checkpoint(solver_type, path, progress=None):
             solver.steps = meta["steps"]
             check(solver._lib.ak_set_steps_done(solver._case, solver.steps))
             solver._checkpoint_context = meta["context"]
+            restore_control(solver, saved, meta)
             solver.diagnostics()
         except Exception:
             solver.close()
@@ -145,6 +149,7 @@ def save_refined_checkpoint(solver, path, context=None):
                 "last_loads": solver.last_loads, "last_budget": solver.last_budget,
                 "initial_integrals": solver._initial_integrals, "wall_fallback_links": solver.wall_fallback_links,
                 "context": context or {}}
+    save_control(solver, arrays, metadata)
     return _write(path, arrays, metadata)
 
 
@@ -181,6 +186,7 @@ def restore_refined_checkpoint(solver_type, path, progress=None):
             solver._initial_integrals = meta["initial_integrals"]
             solver._integrals = None
             solver._checkpoint_context = meta["context"]
+            restore_control(solver, saved, meta)
             solver.diagnostics()
         except Exception:
             solver.close()

@@ -44,6 +44,8 @@ int fail(int code, const std::string &msg) {
     } while (0)
 
 long long blocks_for(long long n, int threads) { return (n + threads - 1) / threads; }
+// fixed grid of the per-case reductions whose results must not depend on the device
+constexpr int STATS_BLOCKS_CASE = 4 * 152;
 
 }  // namespace
 
@@ -99,6 +101,10 @@ struct ak_case {
     long long launches = 0;  // kernels issued by stepping since creation
     bool prepared = false;
     int device = 0;  // CUDA device current when the case was created
+    // stationarity residuals: the owned region (interior coordinates, an
+    // excluded rectangle) and the device snapshot of (rho, j / U) per cell
+    int res_region[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    double *res_snapshot = nullptr, *res_partials = nullptr, *res_out = nullptr;
     bool periodic_xy = false;  // the padded fine block of a refined case wraps in x and y
     // optional per-kernel timing: events recorded around each kernel group
     std::vector<cudaEvent_t> *timing = nullptr;
@@ -133,7 +139,8 @@ void release(ak_case *c) {
     void *ptrs[] = {c->pdf[0], c->pdf[1], c->flags, c->d_poly, c->d_start, c->d_count, c->keys, c->wall_q,
                     c->ox_, c->oy_, c->oz_, c->od, c->oobj, c->oedge, c->sel_ubb, c->sel_out, c->out_state,
                     c->ubb_cells, c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, c->partials, c->reduced,
-                    c->staging, c->d_ff, c->d_shift, c->ring_ru, c->ring_lr};
+                    c->staging, c->d_ff, c->d_shift, c->ring_ru, c->ring_lr, c->res_snapshot,
+                    c->res_partials, c->res_out};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -569,6 +576,8 @@ int create_lattice(const ak_case_desc *desc, int farfield, bool periodic_xy, ak_
     c->nx = desc->nx;
     c->ny = desc->ny;
     c->nz = desc->nz;
+    c->res_region[1] = desc->nx;
+    c->res_region[3] = desc->ny;
     c->origin_x = desc->origin_x;
     c->origin_y = desc->origin_y;
     c->dx = desc->dx;
@@ -1032,6 +1041,56 @@ int ak_set_steps_done(ak_case *c, int64_t steps) {
     return AK_OK;
 }
 
+// ---- stationarity residuals (convergence.py:58-176) on the device
+namespace {
+long long residual_cells(const ak_case *c) {
+    const int *r = c->res_region;
+    return (long long)(r[1] - r[0]) * (r[3] - r[2]) * c->nz;
+}
+int ensure_residual_buffers(ak_case *c) {
+    if (!c->res_snapshot) {
+        AK_TRY(dalloc(c, &c->res_snapshot, (size_t)(4 * residual_cells(c))));
+        AK_TRY(dalloc(c, &c->res_partials, (size_t)STATS_BLOCKS_CASE * 9));
+        AK_TRY(dalloc(c, &c->res_out, 9));
+    }
+    return AK_OK;
+}
+}  // namespace
+
+int ak_residuals(ak_case *c, double inv_speed, double inv_dt, int32_t reset, double *out) {
+    AK_TRY(check_case(c));
+    if (!out || !(inv_speed > 0) || !(inv_dt > 0)) return fail(AK_ERR_INVALID, "positive scales and an output are required");
+    AK_TRY(ensure_residual_buffers(c));
+    const int *g = c->res_region;
+    const Region region{g[0], g[1], g[2], g[3], g[4], g[5], g[6], g[7]};
+    AK_TRY(with_storage(c, [&](auto *tag) {
+        using S = std::remove_pointer_t<decltype(tag)>;
+        k_residuals<S><<<STATS_BLOCKS_CASE, 256, 0, c->stream>>>(src_of<S>(c), c->G, c->flags, region,
+                                                                  c->res_snapshot, inv_speed, inv_dt, reset ? 1 : 0,
+                                                                  c->res_partials);
+        k_residuals_final<<<1, 1, 0, c->stream>>>(c->res_partials, STATS_BLOCKS_CASE, c->res_out);
+        AK_CUDA(cudaGetLastError());
+        return AK_OK;
+    }));
+    AK_CUDA(cudaMemcpyAsync(out, c->res_out, 9 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    AK_CUDA(cudaStreamSynchronize(c->stream));
+    return AK_OK;
+}
+
+int ak_residual_snapshot(ak_case *c, int32_t write, double *data, int64_t *count) {
+    AK_TRY(check_case(c));
+    if (!count) return fail(AK_ERR_INVALID, "null count");
+    *count = 4 * residual_cells(c);
+    if (!data) return AK_OK;
+    AK_TRY(ensure_residual_buffers(c));
+    AK_CUDA(cudaStreamSynchronize(c->stream));
+    if (write)
+        AK_CUDA(cudaMemcpy(c->res_snapshot, data, *count * sizeof(double), cudaMemcpyHostToDevice));
+    else
+        AK_CUDA(cudaMemcpy(data, c->res_snapshot, *count * sizeof(double), cudaMemcpyDeviceToHost));
+    return AK_OK;
+}
+
 int ak_get_flags(ak_case *c, uint8_t *flags) {
     AK_TRY(check_case(c));
     if (!flags) return fail(AK_ERR_INVALID, "null output");
@@ -1477,6 +1536,11 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
                 r = fail(AK_ERR_INVALID, "A solid intersects the fluid donor band");
     }
     if (r == AK_OK) {
+        // owned regions: coarse cells outside the fine box, the physical fine block
+        const int cr[8] = {0, R->coarse->nx, 0, R->coarse->ny, B.lo[0], B.hi[0], B.lo[1], B.hi[1]};
+        const int fr[8] = {R->pad, R->fine->nx - R->pad, R->pad, R->fine->ny - R->pad, 0, 0, 0, 0};
+        std::copy(cr, cr + 8, R->coarse->res_region);
+        std::copy(fr, fr + 8, R->fine->res_region);
         free_populations(R->speed, R->free_g);
         r = ralloc(R, &R->d_free, Q);
         if (r == AK_OK) r = cudaMemcpy(R->d_free, R->free_g, sizeof R->free_g, cudaMemcpyHostToDevice) == cudaSuccess

@@ -858,4 +858,89 @@ __global__ void k_region_final(const double *__restrict__ partials, int nblocks,
     for (int k = 0; k < NSTAT; ++k) out[k] = a[k];
 }
 
+// ------------------------------------------------------------ stationarity residuals
+// d(rho, j / U)/dt over a region's fluid cells (convergence.py:58-96) against
+// a snapshot kept on the device: partials[block][9] = sum of squares (4),
+// max |.| (4), cells; the snapshot takes the current values.  With reset the
+// snapshot is only taken.
+template <typename S>
+__global__ void __launch_bounds__(256)
+    k_residuals(const S *__restrict__ pdf, Grid G, const uint8_t *__restrict__ flags, Region R,
+                double *__restrict__ snapshot, double inv_speed, double inv_dt, int reset,
+                double *__restrict__ partials) {
+    const int w = R.x1 - R.x0, h = R.y1 - R.y0;
+    const long long n = (long long)w * h * G.nz;
+    double sq[4] = {0, 0, 0, 0}, mx[4] = {0, 0, 0, 0}, cells = 0.0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = R.x0 + (int)(i % w);
+        const long long r = i / w;
+        const int y = R.y0 + (int)(r % h), z = (int)(r / h);
+        if (x >= R.ex0 && x < R.ex1 && y >= R.ey0 && y < R.ey1) continue;
+        if (flags[(y + 1) * G.nxp + (x + 1)] != FLAG_FLUID) continue;
+        double drho = 0.0, j[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const double v = load_g(pdf, G, q, x + 1, y + 1, z);
+            drho += v;
+            if (cx(q)) j[0] += cx(q) > 0 ? v : -v;
+            if (cy(q)) j[1] += cy(q) > 0 ? v : -v;
+            if (cz(q)) j[2] += cz(q) > 0 ? v : -v;
+        }
+        const double cur[4] = {drho + 1.0, j[0] * inv_speed, j[1] * inv_speed, j[2] * inv_speed};
+        double *s = snapshot + 4 * i;
+        if (!reset) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const double d = (cur[k] - s[k]) * inv_dt;
+                sq[k] += d * d;
+                mx[k] = fmax(mx[k], fabs(d));
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) s[k] = cur[k];
+        cells += 1.0;
+    }
+    __shared__ double red[8][9];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        for (int k = 0; k < 4; ++k) {
+            sq[k] += __shfl_down_sync(0xffffffffu, sq[k], o);
+            mx[k] = fmax(mx[k], __shfl_down_sync(0xffffffffu, mx[k], o));
+        }
+        cells += __shfl_down_sync(0xffffffffu, cells, o);
+    }
+    if (lane == 0) {
+        for (int k = 0; k < 4; ++k) {
+            red[warp][k] = sq[k];
+            red[warp][4 + k] = mx[k];
+        }
+        red[warp][8] = cells;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int wv = 1; wv < (int)(blockDim.x >> 5); ++wv) {
+            for (int k = 0; k < 4; ++k) {
+                red[0][k] += red[wv][k];
+                red[0][4 + k] = fmax(red[0][4 + k], red[wv][4 + k]);
+            }
+            red[0][8] += red[wv][8];
+        }
+        for (int k = 0; k < 9; ++k) partials[(long long)blockIdx.x * 9 + k] = red[0][k];
+    }
+}
+
+__global__ void k_residuals_final(const double *__restrict__ partials, int nblocks, double *__restrict__ out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double a[9];
+    for (int k = 0; k < 9; ++k) a[k] = partials[k];
+    for (int b = 1; b < nblocks; ++b) {
+        for (int k = 0; k < 4; ++k) {
+            a[k] += partials[b * 9 + k];
+            a[4 + k] = fmax(a[4 + k], partials[b * 9 + 4 + k]);
+        }
+        a[8] += partials[b * 9 + 8];
+    }
+    for (int k = 0; k < 9; ++k) out[k] = a[k];
+}
+
 }  // namespace ak

@@ -43,6 +43,10 @@ class StopCriteria:
             if type(getattr(self, name)) is not int or getattr(self, name) < minimum:
                 raise ValueError(f'{name} must be an integer >= {minimum}')
 
+    @property
+    def thresholds(self):
+        return (self.mass_tolerance, self.momentum_x_tolerance, self.momentum_y_tolerance, self.momentum_z_tolerance)
+
 
 @dataclass(frozen=True)
 class RunSettings:

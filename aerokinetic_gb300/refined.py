@@ -433,7 +433,12 @@ class RefinedSolver:
             with history.open("w", newline="", encoding="utf-8") as handle:
                 csv.DictWriter(handle, fieldnames=columns).writeheader()
             self.save_frame(output / "frames" / f"frame_{self.steps:09d}.npz")
+        from .convergence import RunControl
+        control = RunControl(self, settings, output, resume=resume, callback=residual_callback,
+                             start_step=metadata.get("start_step", self.steps))
         metadata.update(status="running", target_steps=end_step)
+        metadata["residual_definition"] = ("Volume-weighted L2/Linf of d(rho,j_common)/dt*, owned fluid only; "
+                                           "integral balance defects of the last coarse step are a separate diagnostic")
         write_json(output / "metadata.json", metadata)
         status, error, reason = "completed", None, "duration_reached"
 
@@ -442,6 +447,7 @@ class RefinedSolver:
             os.fsync(handle.fileno())
             context = {"case_fingerprint": self.case_fingerprint, "end_step": end_step,
                        "history_bytes": history.stat().st_size, "history_sha256": _file_hash(history)}
+            context.update(control.checkpoint_context())
             self.save_checkpoint(output / "checkpoint.npz", context)
 
         try:
@@ -457,9 +463,12 @@ class RefinedSolver:
                                   settings.checkpoint_every):
                         if every:
                             nxt = min(nxt, (self.steps // every + 1) * every)
+                    if settings.termination.max_steps:
+                        nxt = min(nxt, max(self.steps + 1, control.run_start_step + settings.termination.max_steps))
                     record = self.advance(nxt - self.steps)
                     if self.steps % settings.check_every == 0:
                         self.diagnostics()
+                        control.observe()
                     if self.steps % settings.sample_every == 0:
                         writer.writerow({k: record[k] for k in columns})
                         handle.flush()
@@ -470,6 +479,12 @@ class RefinedSolver:
                     if settings.checkpoint_every and self.steps % settings.checkpoint_every == 0:
                         checkpoint(handle)
                     if status == "stopped":
+                        break
+                    stop = control.stop_reason()
+                    if stop:
+                        reason = stop
+                        if stop == "wall_time_limit":
+                            status = "stopped"
                         break
                 self.diagnostics()
                 self.save_frame(output / "frames" / f"frame_{self.steps:09d}.npz")
@@ -492,7 +507,9 @@ class RefinedSolver:
                    "average_after_t_star": settings.average_after, "samples": len(rows),
                    "averaging_samples": len(selected), "mean": mean, "rms": rms,
                    "experimental_validation": "not_performed", "statistical_convergence": "not_established",
-                   "diagnostics": final, "termination_reason": reason}
+                   "diagnostics": final}
+        summary.update(control.summary(reason))
+        control.close()
         if error:
             summary["error"] = error
         metadata.update(status=status, completed_steps=self.steps, termination_reason=reason)

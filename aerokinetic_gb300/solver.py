@@ -296,7 +296,12 @@ class Solver:
             project.save(output / "project.json")
         if self.steps > end_step:
             raise ValueError("Checkpoint is past the requested end time")
+        from .convergence import RunControl
+        control = RunControl(self, settings, output, resume=resume, callback=residual_callback,
+                             start_step=metadata["start_step"])
         metadata["end_step"] = end_step
+        metadata["residual_definition"] = ("Volume-weighted L2/Linf of d(rho,j_common)/dt*, owned fluid only; "
+                                           "stationary-flow residual, not a turbulence-accuracy measure")
         write_json(output / "metadata.json", metadata)
         state, reason = "completed", "duration_reached"
         start = time.monotonic()
@@ -313,6 +318,7 @@ class Solver:
                     os.fsync(handle.fileno())
                     context = {"case_fingerprint": project.case_fingerprint, "end_step": end_step,
                                "history_bytes": history.stat().st_size, "history_sha256": _file_hash(history)}
+                    context.update(control.checkpoint_context())
                     self.save_checkpoint(output / "checkpoint.npz", context)
 
                 while self.steps < end_step:
@@ -324,11 +330,15 @@ class Solver:
                     for every in (sample_every, check_every, frame_every, checkpoint_every):
                         if every:
                             nxt = min(nxt, (self.steps // every + 1) * every)
+                    if settings.termination.max_steps:
+                        nxt = min(nxt, max(self.steps + 1, control.run_start_step + settings.termination.max_steps))
                     sample = nxt % sample_every == 0
                     record = self.advance(nxt - self.steps, sample_last=sample)
                     diagnostic = None
                     if self.steps % check_every == 0 or self.steps == end_step or sample:
                         diagnostic = self.diagnostics()
+                    if self.steps % check_every == 0:
+                        control.observe()
                     if self.steps % frame_every == 0 or self.steps == end_step:
                         self.save_frame(output / "frames" / f"frame_{self.steps:010d}.npz")
                     if record is not None:
@@ -342,6 +352,12 @@ class Solver:
                         if callback is not None and callback(self, record) is False:
                             state, reason = "stopped", "user_stopped"
                             break
+                    stop = control.stop_reason()
+                    if stop:
+                        reason = stop
+                        if stop == "wall_time_limit":
+                            state = "stopped"
+                        break
                     if checkpoint_every and self.steps % checkpoint_every == 0:
                         checkpoint()
                 self.diagnostics()
@@ -360,8 +376,9 @@ class Solver:
                        "averaging_samples": len(selected), "average_after_t_star": average_after,
                        "mean": dict(zip(("cl", "cd", "cm"), selected.mean(axis=0))) if ok else None,
                        "rms_fluctuation": dict(zip(("cl", "cd", "cm"), selected.std(axis=0))) if ok else None,
-                       "wall_fallback_links": self.wall_fallback_links, "experimental_validation": "not_performed",
-                       "termination_reason": reason}
+                       "wall_fallback_links": self.wall_fallback_links, "experimental_validation": "not_performed"}
+            summary.update(control.summary(reason))
+            control.close()
             metadata["status"] = state
             metadata["termination_reason"] = reason
             write_json(output / "metadata.json", metadata)

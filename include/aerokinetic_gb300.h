@@ -153,6 +153,18 @@ int ak_set_boundary_state(ak_case *c, const int32_t *rows, const double *values)
  * checkpoint.py:113). */
 int ak_set_steps_done(ak_case *c, int64_t steps);
 
+/* Stationarity residuals (convergence.py:58-96) without a host gather: over
+ * the case's owned fluid cells (the whole interior of a uniform case; for a
+ * two-level case's levels, the coarse cells outside the fine box and the
+ * physical fine block), with a device snapshot of (rho, j * inv_speed) per
+ * cell, out[9] = sum over cells of ((current - snapshot) * inv_dt)^2 for the
+ * four components, their max |.|, and the number of cells; the snapshot then
+ * takes the current values.  reset != 0 only takes the snapshot. */
+int ak_residuals(ak_case *c, double inv_speed, double inv_dt, int32_t reset, double *out);
+/* The snapshot as 4 doubles per owned cell (count returned; data may be null):
+ * write = 0 copies it out, write != 0 replaces it (checkpoints). */
+int ak_residual_snapshot(ak_case *c, int32_t write, double *data, int64_t *count);
+
 /* Solid flags of the interior columns (nx*ny, x-major like the reference's
  * _solid_xy): 0 fluid, k+1 inside element k. */
 int ak_get_flags(ak_case *c, uint8_t *flags);
