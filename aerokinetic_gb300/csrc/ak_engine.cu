@@ -869,7 +869,7 @@ int ak_diagnostics(ak_case *c, double *diag) {
         AK_CUDA(cudaGetLastError());
         return AK_OK;
     }));
-    k_diagnostics_final<<<1, 32, 0, c->stream>>>(c->partials, nb, c->reduced);
+    k_diagnostics_final<<<1, REDUCE_THREADS, 0, c->stream>>>(c->partials, nb, c->reduced);
     AK_CUDA(cudaGetLastError());
     double r[6];
     AK_CUDA(cudaMemcpyAsync(r, c->reduced, sizeof r, cudaMemcpyDeviceToHost, c->stream));
@@ -1068,7 +1068,7 @@ int ak_residuals(ak_case *c, double inv_speed, double inv_dt, int32_t reset, dou
         k_residuals<S><<<STATS_BLOCKS_CASE, 256, 0, c->stream>>>(src_of<S>(c), c->G, c->flags, region,
                                                                   c->res_snapshot, inv_speed, inv_dt, reset ? 1 : 0,
                                                                   c->res_partials);
-        k_residuals_final<<<1, 1, 0, c->stream>>>(c->res_partials, STATS_BLOCKS_CASE, c->res_out);
+        k_residuals_final<<<1, REDUCE_THREADS, 0, c->stream>>>(c->res_partials, STATS_BLOCKS_CASE, c->res_out);
         AK_CUDA(cudaGetLastError());
         return AK_OK;
     }));
@@ -1336,7 +1336,7 @@ int refined_step(ak_refined *R, bool fork = false) {
         if (R->track_budget) {
             k_outer_flux<S><<<dim3((unsigned)R->outer_blocks, 4), 256, 0, st>>>(
                 src_of<S>(C), C->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_outer, 4, R->outer_partials);
-            k_outer_final<<<1, 1, 0, st>>>(R->outer_partials, R->d_outer, 4, R->outer_blocks,
+            k_outer_final<<<1, REDUCE_THREADS, 0, st>>>(R->outer_partials, R->d_outer, 4, R->outer_blocks,
                                            R->dx_c * R->dx_c * R->dx_c, R->outer_out);
             C->launches += 2;
         }
@@ -1735,9 +1735,9 @@ int ak_refined_integrals(ak_refined *R, double *out) {
     int r = with_storage(C, [&](auto *tag) {
         using S = std::remove_pointer_t<decltype(tag)>;
         k_region_stats<S><<<STATS_BLOCKS, 256, 0, st>>>(src_of<S>(C), C->G, C->flags, rc, R->stats_partials);
-        k_region_final<<<1, 1, 0, st>>>(R->stats_partials, STATS_BLOCKS, R->stats_out);
+        k_region_final<<<1, REDUCE_THREADS, 0, st>>>(R->stats_partials, STATS_BLOCKS, R->stats_out);
         k_region_stats<S><<<STATS_BLOCKS, 256, 0, st>>>(src_of<S>(F), F->G, F->flags, rf, R->stats_partials);
-        k_region_final<<<1, 1, 0, st>>>(R->stats_partials, STATS_BLOCKS, R->stats_out + NSTAT);
+        k_region_final<<<1, REDUCE_THREADS, 0, st>>>(R->stats_partials, STATS_BLOCKS, R->stats_out + NSTAT);
         C->launches += 4;
         AK_CUDA(cudaGetLastError());
         return AK_OK;

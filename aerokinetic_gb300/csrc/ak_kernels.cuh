@@ -746,18 +746,43 @@ __global__ void __launch_bounds__(256) k_diagnostics(const S *__restrict__ pdf, 
     }
 }
 
-__global__ void k_diagnostics_final(const double *__restrict__ partials, int nblocks, double *__restrict__ out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double a[6] = {partials[0], partials[1], partials[2], partials[3], partials[4], partials[5]};
-    for (int b = 1; b < nblocks; ++b) {
-        a[0] = fmax(a[0], partials[6 * b]);
-        a[1] = fmax(a[1], partials[6 * b + 1]);
-        a[2] = fmax(a[2], partials[6 * b + 2]);
-        a[3] += partials[6 * b + 3];
-        a[4] += partials[6 * b + 4];
-        a[5] += partials[6 * b + 5];
+// Reduction of nrows rows of NV partial values (column k a maximum when bit k
+// of max_mask is set, else a sum) by one block of REDUCE_THREADS threads: a
+// fixed strided accumulation, then a fixed shared-memory tree, so the result
+// does not depend on scheduling.  Thread 0 returns the reduced row.
+constexpr int REDUCE_THREADS = 256;
+template <int NV>
+__device__ void reduce_rows(const double *__restrict__ rows, long long nrows, unsigned max_mask, double (&acc)[NV]) {
+    __shared__ double red[NV][REDUCE_THREADS];
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = ((max_mask >> k) & 1) ? -INFINITY : 0.0;
+    for (long long b = t; b < nrows; b += REDUCE_THREADS)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const double v = rows[b * NV + k];
+            acc[k] = ((max_mask >> k) & 1) ? fmax(acc[k], v) : acc[k] + v;
+        }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) red[k][t] = acc[k];
+    __syncthreads();
+    for (int stride = REDUCE_THREADS / 2; stride > 0; stride >>= 1) {
+        if (t < stride)
+#pragma unroll
+            for (int k = 0; k < NV; ++k)
+                red[k][t] = ((max_mask >> k) & 1) ? fmax(red[k][t], red[k][t + stride]) : red[k][t] + red[k][t + stride];
+        __syncthreads();
     }
-    for (int k = 0; k < 6; ++k) out[k] = a[k];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = red[k][0];
+}
+
+__global__ void __launch_bounds__(REDUCE_THREADS)
+    k_diagnostics_final(const double *__restrict__ partials, int nblocks, double *__restrict__ out) {
+    double a[6];
+    reduce_rows<6>(partials, nblocks, 0x7u, a);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 6; ++k) out[k] = a[k];
 }
 
 }  // namespace ak

@@ -758,20 +758,21 @@ __global__ void __launch_bounds__(256)
 
 // out[k] = sum over faces (in order) of -side * dx^3 * sum over blocks, for
 // this step; out[4 + k] accumulates it over the tracked steps
-__global__ void k_outer_final(const double *__restrict__ partials, const Face *__restrict__ faces, int nfaces,
-                              int nblocks, double volume, double *__restrict__ out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__global__ void __launch_bounds__(REDUCE_THREADS)
+    k_outer_final(const double *__restrict__ partials, const Face *__restrict__ faces, int nfaces, int nblocks,
+                  double volume, double *__restrict__ out) {
     double total[4] = {0, 0, 0, 0};
     for (int f = 0; f < nfaces; ++f) {
-        double s[4] = {0, 0, 0, 0};
-        for (int b = 0; b < nblocks; ++b)
-            for (int k = 0; k < 4; ++k) s[k] += partials[((long long)f * nblocks + b) * 4 + k];
+        double s[4];
+        reduce_rows<4>(partials + (long long)f * nblocks * 4, nblocks, 0u, s);
         for (int k = 0; k < 4; ++k) total[k] -= faces[f].side * s[k] * volume;
+        __syncthreads();
     }
-    for (int k = 0; k < 4; ++k) {
-        out[k] = total[k];
-        out[4 + k] += total[k];
-    }
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 4; ++k) {
+            out[k] = total[k];
+            out[4 + k] += total[k];
+        }
 }
 
 // running sums of the wall loads over coarse steps: cum[k] += both fine steps
@@ -810,8 +811,8 @@ __global__ void __launch_bounds__(256)
             if (cy(q)) j[1] += cy(q) > 0 ? v : -v;
             if (cz(q)) j[2] += cz(q) > 0 ? v : -v;
         }
-        const double rho = drho + 1.0;
-        const double u[3] = {j[0] / rho, j[1] / rho, j[2] / rho};
+        const double rho = drho + 1.0, inv = 1.0 / rho;
+        const double u[3] = {j[0] * inv, j[1] * inv, j[2] * inv};
         const double u2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
         if (!isfinite(rho) || !isfinite(u2)) {
             a[7] += 1.0;
@@ -846,16 +847,12 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-__global__ void k_region_final(const double *__restrict__ partials, int nblocks, double *__restrict__ out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__global__ void __launch_bounds__(REDUCE_THREADS)
+    k_region_final(const double *__restrict__ partials, int nblocks, double *__restrict__ out) {
     double a[NSTAT];
-    for (int k = 0; k < NSTAT; ++k) a[k] = partials[k];
-    for (int b = 1; b < nblocks; ++b) {
-        a[0] = fmax(a[0], partials[b * NSTAT]);
-        a[1] = fmax(a[1], partials[b * NSTAT + 1]);
-        for (int k = 2; k < NSTAT; ++k) a[k] += partials[b * NSTAT + k];
-    }
-    for (int k = 0; k < NSTAT; ++k) out[k] = a[k];
+    reduce_rows<NSTAT>(partials, nblocks, 0x3u, a);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < NSTAT; ++k) out[k] = a[k];
 }
 
 // ------------------------------------------------------------ stationarity residuals
@@ -929,18 +926,12 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-__global__ void k_residuals_final(const double *__restrict__ partials, int nblocks, double *__restrict__ out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__global__ void __launch_bounds__(REDUCE_THREADS)
+    k_residuals_final(const double *__restrict__ partials, int nblocks, double *__restrict__ out) {
     double a[9];
-    for (int k = 0; k < 9; ++k) a[k] = partials[k];
-    for (int b = 1; b < nblocks; ++b) {
-        for (int k = 0; k < 4; ++k) {
-            a[k] += partials[b * 9 + k];
-            a[4 + k] = fmax(a[4 + k], partials[b * 9 + 4 + k]);
-        }
-        a[8] += partials[b * 9 + 8];
-    }
-    for (int k = 0; k < 9; ++k) out[k] = a[k];
+    reduce_rows<9>(partials, nblocks, 0xF0u, a);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 9; ++k) out[k] = a[k];
 }
 
 }  // namespace ak
