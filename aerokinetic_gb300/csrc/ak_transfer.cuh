@@ -41,10 +41,13 @@ __device__ __forceinline__ void static_for(F &&f) {
     }
 }
 
+// The transfer algebra runs in the storage form's arithmetic type T: FP64 for
+// the plain form, FP32 for the FP32-compute forms.
+
 // running sums of one cell: drho, j (3), second moments (xx, yy, zz, xy, xz, yz);
 // the zero products of the lattice velocities are skipped
-template <int q>
-__device__ __forceinline__ void add_moments(double s[10], double v) {
+template <int q, typename T>
+__device__ __forceinline__ void add_moments(T s[10], T v) {
     constexpr int c[3] = {cx(q), cy(q), cz(q)};
     s[0] += v;
 #pragma unroll
@@ -62,11 +65,12 @@ __device__ __forceinline__ void add_moments(double s[10], double v) {
 // The Mach test compares |j|^2 with (0.3 c_s rho)^2 (same decision up to the
 // rounding of the threshold) and the stress divides by rho through one
 // reciprocal: the FP64 pipe is the limit of these kernels.
-__device__ __forceinline__ void finish_moments(const double s[10], double m[10], int *flag, bool report) {
-    const double drho = s[0], rho = drho + 1.0, inv = 1.0 / rho;
+template <typename T>
+__device__ __forceinline__ void finish_moments(const T s[10], T m[10], int *flag, bool report) {
+    const T drho = s[0], rho = drho + T(1), inv = T(1) / rho;
     if (report) {
-        if (!(rho > 0.0)) atomicOr(flag, XF_DENSITY);
-        if (s[1] * s[1] + s[2] * s[2] + s[3] * s[3] > 0.09 * TCS2 * rho * rho) atomicOr(flag, XF_MACH);
+        if (!(rho > T(0))) atomicOr(flag, XF_DENSITY);
+        if (s[1] * s[1] + s[2] * s[2] + s[3] * s[3] > T(0.09 * TCS2) * rho * rho) atomicOr(flag, XF_MACH);
     }
     m[0] = rho;
     m[1] = s[1];
@@ -74,74 +78,52 @@ __device__ __forceinline__ void finish_moments(const double s[10], double m[10],
     m[3] = s[3];
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-        double p = s[4 + k];
-        if (k < 3) p -= drho * TCS2;
+        T p = s[4 + k];
+        if (k < 3) p -= drho * T(TCS2);
         m[4 + k] = p - s[1 + sa(k)] * s[1 + sb(k)] * inv;
     }
 }
 
-__device__ __forceinline__ void transfer_moments(const double g[Q], double m[10], int *flag) {
-    double s[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    bool negative = false;
-    static_for<0, Q>([&](auto qc) {
-        constexpr int q = decltype(qc)::value;
-        add_moments<q>(s, g[q]);
-        negative |= g[q] < -weight(q);
-    });
-    if (negative) atomicOr(flag, XF_NEGATIVE);
-    finish_moments(s, m, flag, true);
-}
-
 // checks of a moment set before populations are built from it
-__device__ __forceinline__ void check_fields(const double m[10], int *flag) {
-    const double rho = m[0];
-    if (!(rho > 0.0)) atomicOr(flag, XF_DENSITY);
-    if (m[1] * m[1] + m[2] * m[2] + m[3] * m[3] > 0.09 * TCS2 * rho * rho) atomicOr(flag, XF_MACH);
+template <typename T>
+__device__ __forceinline__ void check_fields(const T m[10], int *flag) {
+    const T rho = m[0];
+    if (!(rho > T(0))) atomicOr(flag, XF_DENSITY);
+    if (m[1] * m[1] + m[2] * m[2] + m[3] * m[3] > T(0.09 * TCS2) * rho * rho) atomicOr(flag, XF_MACH);
 }
 
 // per-axis factors of the tensor-product equilibrium, fac[a][c + 1]:
 // 2/3 - u^2 for c = 0, (1/3 + u^2 + c u) / 2 otherwise
-__device__ __forceinline__ void axis_factors(const double m[10], double fac[9]) {
-    const double inv = 1.0 / m[0];
+template <typename T>
+__device__ __forceinline__ void axis_factors(const T m[10], T fac[9]) {
+    const T inv = T(1) / m[0];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        const double u = m[1 + a] * inv, uu = u * u;
-        fac[3 * a + 0] = (TCS2 + uu - u) / 2.0;
-        fac[3 * a + 1] = 2.0 / 3.0 - uu;
-        fac[3 * a + 2] = (TCS2 + uu + u) / 2.0;
+        const T u = m[1 + a] * inv, uu = u * u;
+        fac[3 * a + 0] = (T(TCS2) + uu - u) / T(2);
+        fac[3 * a + 1] = T(2.0 / 3.0) - uu;
+        fac[3 * a + 2] = (T(TCS2) + uu + u) / T(2);
     }
 }
 
 // zero-centred population q of (rho, j, Pi_neq) (refinement.py:177-203):
 // tensor-product equilibrium + second-order Hermite stress term
-template <int q>
-__device__ __forceinline__ double population(const double m[10], const double fac[9], bool &bad) {
+template <int q, typename T>
+__device__ __forceinline__ T population(const T m[10], const T fac[9], bool &bad) {
     constexpr int c[3] = {cx(q), cy(q), cz(q)};
-    double eq = fac[c[0] + 1] * fac[3 + c[1] + 1];
+    T eq = fac[c[0] + 1] * fac[3 + c[1] + 1];
     eq *= fac[6 + c[2] + 1];
     eq *= m[0];
-    double neq = 0.0;
+    T neq = 0;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
         double h = (double)(c[sa(k)] * c[sb(k)]) - (k < 3 ? TCS2 : 0.0);
         if (k >= 3) h *= 2.0;
-        if (h != 0.0) neq += weight(q) * h / (2.0 * TCS2 * TCS2) * m[4 + k];
+        if (h != 0.0) neq += T(weight(q) * h / (2.0 * TCS2 * TCS2)) * m[4 + k];
     }
-    const double f = eq + neq;
-    bad |= !isfinite(f) || f < 0.0;
-    return f - weight(q);
-}
-
-__device__ __forceinline__ void transfer_populations(const double m[10], double g[Q], int *flag) {
-    check_fields(m, flag);
-    double fac[9];
-    axis_factors(m, fac);
-    bool bad = false;
-    static_for<0, Q>([&](auto qc) {
-        constexpr int q = decltype(qc)::value;
-        g[q] = population<q>(m, fac, bad);
-    });
-    if (bad) atomicOr(flag, XF_NEGATIVE);
+    const T f = eq + neq;
+    bad |= !isfinite(f) || f < T(0);
+    return f - T(weight(q));
 }
 
 // ------------------------------------------------------------ direction-split blocks
@@ -178,24 +160,27 @@ __device__ __forceinline__ void owned(F &&f) {
 // shared state of a direction-split block: per-warp partial sums and the
 // per-cell fields (moments + equilibrium factors) that warp 0 prepares
 constexpr int NFIELD = 19;  // m[10], fac[9]
+template <typename T>
 struct SplitShared {
-    double part[SPLIT_WARPS][10][SPLIT_CELLS];
+    T part[SPLIT_WARPS][10][SPLIT_CELLS];
     int neg[SPLIT_WARPS][SPLIT_CELLS];
-    double field[2][NFIELD][SPLIT_CELLS];
+    T field[2][NFIELD][SPLIT_CELLS];
 };
 
-__device__ __forceinline__ void put_partial(SplitShared &sh, const double s[10], bool neg) {
+template <typename T>
+__device__ __forceinline__ void put_partial(SplitShared<T> &sh, const T s[10], bool neg) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < 10; ++k) sh.part[w][k][lane] = s[k];
     sh.neg[w][lane] = neg;
 }
 // block-wide sums of the cell slot, warps 0..7 in order (after a barrier)
-__device__ __forceinline__ void sum_partials(const SplitShared &sh, double t[10], bool &any_neg) {
+template <typename T>
+__device__ __forceinline__ void sum_partials(const SplitShared<T> &sh, T t[10], bool &any_neg) {
     const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int k = 0; k < 10; ++k) {
-        double v = sh.part[0][k][lane];
+        T v = sh.part[0][k][lane];
 #pragma unroll
         for (int j = 1; j < SPLIT_WARPS; ++j) v += sh.part[j][k][lane];
         t[k] = v;
@@ -204,21 +189,35 @@ __device__ __forceinline__ void sum_partials(const SplitShared &sh, double t[10]
 #pragma unroll
     for (int j = 0; j < SPLIT_WARPS; ++j) any_neg |= sh.neg[j][lane] != 0;
 }
-__device__ __forceinline__ void put_fields(SplitShared &sh, int set, const double m[10]) {
+template <typename T>
+__device__ __forceinline__ void put_fields(SplitShared<T> &sh, int set, const T m[10]) {
     const int lane = threadIdx.x & 31;
-    double fac[9];
+    T fac[9];
     axis_factors(m, fac);
 #pragma unroll
     for (int k = 0; k < 10; ++k) sh.field[set][k][lane] = m[k];
 #pragma unroll
     for (int k = 0; k < 9; ++k) sh.field[set][10 + k][lane] = fac[k];
 }
-__device__ __forceinline__ void get_fields(const SplitShared &sh, int set, double m[10], double fac[9]) {
+template <typename T>
+__device__ __forceinline__ void get_fields(const SplitShared<T> &sh, int set, T m[10], T fac[9]) {
     const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int k = 0; k < 10; ++k) m[k] = sh.field[set][k][lane];
 #pragma unroll
     for (int k = 0; k < 9; ++k) fac[k] = sh.field[set][10 + k][lane];
+}
+
+// a population in the arithmetic type T of its storage form
+template <typename T, typename S>
+__device__ __forceinline__ T load_as(const S *pdf, const Grid &G, int q, int x, int y, int z) {
+    if (!AK_CHECK(G, q, x, y, z, 1)) return T(0);
+    return (T)Store<S>::load(pdf + q * G.qs + G.cell(x, y, z), q, G.shift[q]);
+}
+template <typename T, typename S>
+__device__ __forceinline__ void store_as(S *pdf, const Grid &G, int q, int x, int y, int z, T v) {
+    if (!AK_CHECK(G, q, x, y, z, 2)) return;
+    Store<S>::store(pdf + q * G.qs + G.cell(x, y, z), q, (typename Store<S>::T)v, G.shift[q]);
 }
 
 // cells of an nx x ny rectangle outside its interior [wx, nx - wx) x
@@ -250,12 +249,13 @@ __device__ __forceinline__ void ring_cell(long long b, int nx, int ny, int wx, i
 struct Rescale {
     double shear, bulk;  // target tau dt / source tau dt
 };
-__device__ __forceinline__ void rescale_stress(double m[10], Rescale r) {
-    const double iso = (m[4] + m[5] + m[6]) / 3.0;
+template <typename T>
+__device__ __forceinline__ void rescale_stress(T m[10], Rescale r) {
+    const T iso = (m[4] + m[5] + m[6]) / T(3);
 #pragma unroll
-    for (int k = 4; k < 10; ++k) m[k] *= r.shear;
+    for (int k = 4; k < 10; ++k) m[k] *= T(r.shear);
 #pragma unroll
-    for (int k = 4; k < 7; ++k) m[k] += (r.bulk - r.shear) * iso;
+    for (int k = 4; k < 7; ++k) m[k] += T(r.bulk - r.shear) * iso;
 }
 
 // ------------------------------------------------------------ split step
@@ -433,7 +433,8 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
     k_block_moments(const S *__restrict__ pdf, Grid G, BoxSpec B, const double *__restrict__ free_g,
                     double *__restrict__ out, const double *__restrict__ mix_from, double *__restrict__ half,
                     int *__restrict__ flag) {
-    __shared__ SplitShared sh;
+    using T = typename Store<S>::T;
+    __shared__ SplitShared<T> sh;
     const long long nring = ring_count(B.dnx, B.dny, DONOR_RING, DONOR_RING), nr = nring * G.nz;
     if ((long long)blockIdx.x * SPLIT_CELLS >= nr) return;
     const int lane = threadIdx.x & 31;
@@ -448,21 +449,21 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
         cyi = ((B.dy0 + by) % G.ny + G.ny) % G.ny;
         core = in_core(B, cxi, cyi);
     }
-    double s[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    T s[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     bool neg = false;
     by_warp([&](auto wc) {
         owned<decltype(wc)::value>([&](auto qc, int) {
             constexpr int q = decltype(qc)::value;
-            double v = 0.0;
-            if (valid) v = core ? free_g[q] : load_g(pdf, G, q, cxi + 1, cyi + 1, z);
+            T v = 0;
+            if (valid) v = core ? T(free_g[q]) : load_as<T>(pdf, G, q, cxi + 1, cyi + 1, z);
             add_moments<q>(s, v);
-            neg |= v < -weight(q);
+            neg |= v < T(-weight(q));
         });
     });
     put_partial(sh, s, neg);
     __syncthreads();
     if ((threadIdx.x >> 5) != 0 || !valid) return;
-    double t[10], m[10];
+    T t[10], m[10];
     bool any_neg;
     sum_partials(sh, t, any_neg);
     if (any_neg) atomicOr(flag, XF_NEGATIVE);
@@ -471,7 +472,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
 #pragma unroll
     for (int k = 0; k < 10; ++k) {
         out[k * n + j] = m[k];
-        if (mix_from) half[k * n + j] = 0.5 * mix_from[k * n + j] + 0.5 * m[k];
+        if (mix_from) half[k * n + j] = 0.5 * mix_from[k * n + j] + 0.5 * (double)m[k];
     }
 }
 
@@ -529,7 +530,8 @@ template <typename S>
 __global__ void __launch_bounds__(SPLIT_THREADS)
     k_donors(S *__restrict__ fine, Grid F, int nzc, const double *__restrict__ pxy, Rescale r, int pad,
              int *__restrict__ flag) {
-    __shared__ SplitShared sh;
+    using T = typename Store<S>::T;
+    __shared__ SplitShared<T> sh;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const long long nring = ring_count(F.nx, F.ny, pad, pad), n = nring * F.nz;
     if ((long long)blockIdx.x * SPLIT_CELLS >= n) return;
@@ -549,11 +551,11 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
             const int zz = ((pz + j - 2) % nzc + nzc) % nzc;
             a[j] = valid ? pxy[k * nxy + zz * plane + cell] : (k == 0 ? 1.0 : 0.0);
         }
-        sh.field[0][k][lane] = prolong_child(a[0], a[1], a[2], a[3], a[4], fz & 1);
+        sh.field[0][k][lane] = T(prolong_child(a[0], a[1], a[2], a[3], a[4], fz & 1));
     }
     __syncthreads();
     if (w == 0) {
-        double m[10];
+        T m[10];
 #pragma unroll
         for (int k = 0; k < 10; ++k) m[k] = sh.field[0][k][lane];
         rescale_stress(m, r);
@@ -561,14 +563,14 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
         put_fields(sh, 1, m);
     }
     __syncthreads();
-    double m[10], fac[9];
+    T m[10], fac[9];
     get_fields(sh, 1, m, fac);
     bool bad = false;
     by_warp([&](auto wc) {
         owned<decltype(wc)::value>([&](auto qc, int) {
             constexpr int q = decltype(qc)::value;
-            const double g = population<q>(m, fac, bad);
-            if (valid) store_g(fine, F, q, fx + 1, fy + 1, fz, g);
+            const T g = population<q>(m, fac, bad);
+            if (valid) store_as<T>(fine, F, q, fx + 1, fy + 1, fz, g);
         });
     });
     if (bad && valid) atomicOr(flag, XF_NEGATIVE);
@@ -582,7 +584,8 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
     k_reflux(S *__restrict__ pdf, Grid G, const Face *__restrict__ faces, int nfaces,
              const long long *__restrict__ offsets, const double *__restrict__ reg_c,
              const double *__restrict__ reg_f, double inv_volume, int *__restrict__ flag) {
-    __shared__ SplitShared sh;
+    using T = typename Store<S>::T;
+    __shared__ SplitShared<T> sh;
     const int f = blockIdx.y;
     if (f >= nfaces) return;
     const Face F = faces[f];
@@ -599,31 +602,31 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
     c3[F.axis] = F.side < 0 ? F.coarse_index : F.coarse_index + 1;  // the cell outside the box
     c3[a1] = F.lo1 + t1;
     c3[a2] = F.lo2 + t2;
-    double g[4] = {0, 0, 0, 0}, s[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    T g[4] = {0, 0, 0, 0}, s[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     bool neg = false;
     by_warp([&](auto wc) {
         owned<decltype(wc)::value>([&](auto qc, int slot) {
             constexpr int q = decltype(qc)::value;
-            g[slot] = valid ? load_g(pdf, G, q, c3[0] + 1, c3[1] + 1, c3[2]) : 0.0;
+            g[slot] = valid ? load_as<T>(pdf, G, q, c3[0] + 1, c3[1] + 1, c3[2]) : T(0);
             add_moments<q>(s, g[slot]);
-            neg |= g[slot] < -weight(q);
+            neg |= g[slot] < T(-weight(q));
         });
     });
     put_partial(sh, s, neg);
     __syncthreads();
     if (lead) {
-        double t[10], m_old[10], m_new[10];
+        T t[10], m_old[10], m_new[10];
         bool any_neg;
         sum_partials(sh, t, any_neg);
         if (valid && any_neg) atomicOr(flag, XF_NEGATIVE);
         finish_moments(t, m_old, flag, valid);
         const double *rc = reg_c + offsets[f] + 4 * e, *rf = reg_f + offsets[f] + 4 * e;
 #pragma unroll
-        for (int k = 4; k < 10; ++k) m_old[k] = 0.0;
+        for (int k = 4; k < 10; ++k) m_old[k] = T(0);
 #pragma unroll
         for (int k = 0; k < 10; ++k) m_new[k] = m_old[k];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) m_new[k] += F.side * (rf[k] - rc[k]) * inv_volume;
+        for (int k = 0; k < 4; ++k) m_new[k] += T(F.side * (rf[k] - rc[k]) * inv_volume);
         if (valid) {
             check_fields(m_new, flag);
             check_fields(m_old, flag);
@@ -632,18 +635,18 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
         put_fields(sh, 1, m_old);
     }
     __syncthreads();
-    double m_new[10], f_new[9], m_old[10], f_old[9];
+    T m_new[10], f_new[9], m_old[10], f_old[9];
     get_fields(sh, 0, m_new, f_new);
     get_fields(sh, 1, m_old, f_old);
     bool bad = false, neg2 = false;
-    double s2[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    T s2[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     by_warp([&](auto wc) {
         owned<decltype(wc)::value>([&](auto qc, int slot) {
             constexpr int q = decltype(qc)::value;
             g[slot] += population<q>(m_new, f_new, bad) - population<q>(m_old, f_old, bad);
             add_moments<q>(s2, g[slot]);
-            neg2 |= g[slot] < -weight(q);
-            if (valid) store_g(pdf, G, q, c3[0] + 1, c3[1] + 1, c3[2], g[slot]);
+            neg2 |= g[slot] < T(-weight(q));
+            if (valid) store_as<T>(pdf, G, q, c3[0] + 1, c3[1] + 1, c3[2], g[slot]);
         });
     });
     if (bad && valid) atomicOr(flag, XF_NEGATIVE);
@@ -652,7 +655,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
     put_partial(sh, s2, neg2);
     __syncthreads();
     if (lead && valid) {
-        double t[10], chk[10];
+        T t[10], chk[10];
         bool any_neg;
         sum_partials(sh, t, any_neg);
         if (any_neg) atomicOr(flag, XF_NEGATIVE);
@@ -669,7 +672,8 @@ template <typename Sc, typename Sf>
 __global__ void __launch_bounds__(SPLIT_THREADS)
     k_restrict(Sc *__restrict__ coarse, Grid G, const Sf *__restrict__ fine, Grid F, BoxSpec B, int pad,
                const double *__restrict__ free_g, Rescale r, int *__restrict__ flag) {
-    __shared__ SplitShared sh;
+    using T = typename Store<Sc>::T;
+    __shared__ SplitShared<T> sh;
     if (blockIdx.y == 1) {
         const int cx0 = B.bx - 6, cy0 = B.by - 6;
         if (cx0 <= 0 || cy0 <= 0) return;
@@ -694,39 +698,39 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
         ring_cell(i - z * nring, B.bx, B.by, 3, 3, bx, by);
     }
     const int fx = pad + 2 * bx + (w & 1), fy = pad + 2 * by + ((w >> 1) & 1), fz = 2 * z + (w >> 2);
-    double s[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    T s[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     bool neg = false;
     static_for<0, Q>([&](auto qc) {
         constexpr int q = decltype(qc)::value;
-        const double v = valid ? load_g(fine, F, q, fx + 1, fy + 1, fz) : 0.0;
+        const T v = valid ? load_as<T>(fine, F, q, fx + 1, fy + 1, fz) : T(0);
         add_moments<q>(s, v);
-        neg |= v < -weight(q);
+        neg |= v < T(-weight(q));
     });
-    double mc[10];
+    T mc[10];
     finish_moments(s, mc, flag, valid);
     put_partial(sh, mc, neg);
     __syncthreads();
     if (w == 0) {
-        double m[10];
+        T m[10];
         bool any_neg;
         sum_partials(sh, m, any_neg);
         if (valid && any_neg) atomicOr(flag, XF_NEGATIVE);
 #pragma unroll
-        for (int k = 0; k < 10; ++k) m[k] *= 0.125;
+        for (int k = 0; k < 10; ++k) m[k] *= T(0.125);
         rescale_stress(m, r);
         if (valid) check_fields(m, flag);
         put_fields(sh, 0, m);
     }
     __syncthreads();
-    double m[10], fac[9];
+    T m[10], fac[9];
     get_fields(sh, 0, m, fac);
     const int cxi = B.lo[0] + bx, cyi = B.lo[1] + by, czi = B.lo[2] + z;
     bool bad = false;
     by_warp([&](auto wc) {
         owned<decltype(wc)::value>([&](auto qc, int) {
             constexpr int q = decltype(qc)::value;
-            const double g = population<q>(m, fac, bad);
-            if (valid) store_g(coarse, G, q, cxi + 1, cyi + 1, czi, g);
+            const T g = population<q>(m, fac, bad);
+            if (valid) store_as<T>(coarse, G, q, cxi + 1, cyi + 1, czi, g);
         });
     });
     if (bad && valid) atomicOr(flag, XF_NEGATIVE);

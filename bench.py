@@ -278,6 +278,38 @@ def stream_ms(lib, stream_handle, fn):
     return float(a.elapsed_time(b))
 
 
+def form_errors(project, refinement, steps=400):
+    """The two-level case's FP32 and FP16 storage forms against the FP64 form
+    after the same number of coarse steps from the same initial state: Cl, Cd,
+    Cm (relative, floor 0.05), mean density over the owned cells and the
+    velocity field's relative L2 over both levels."""
+    from aerokinetic_gb300.refined import RefinedSolver
+    runs = {}
+    for storage in ("f64", "f32", "f16"):
+        solver = RefinedSolver(project, refinement, storage=storage)
+        record = solver.advance(steps)
+        integrals = solver.conserved_integrals()
+        volume = (solver.coarse_owned_cells * solver.coarse_level.dx ** 3
+                  + solver.fine_fluid_cells * solver.fine_level.dx ** 3)
+        (rc, uc), (rf, uf) = solver.level_macros()
+        box = solver.plan.box
+        owned = np.ones(rc.shape, bool)
+        owned[box.lower[0]:box.upper[0], box.lower[1]:box.upper[1]] = False
+        fluid = np.broadcast_to(~solver._fine_solid_xy()[:, :, None], rf.shape)
+        runs[storage] = (record, integrals["mass"] / volume, uc[owned], uf[fluid])
+        solver.close()
+    ref = runs["f64"]
+    out = {"coarse_steps": steps}
+    for storage in ("f32", "f16"):
+        rec, mean_rho, uc, uf = runs[storage]
+        du = np.sum((uc - ref[2]) ** 2) + np.sum((uf - ref[3]) ** 2)
+        norm = np.sum(ref[2] ** 2) + np.sum(ref[3] ** 2)
+        out[storage] = {**{k: abs(rec[k] - ref[0][k]) / max(abs(ref[0][k]), 0.05) for k in ("cl", "cd", "cm")},
+                        "mean_rho_abs": abs(mean_rho - ref[1]), "u_l2_rel": float(np.sqrt(du / norm))}
+    out["f64_values"] = {"cl": ref[0]["cl"], "cd": ref[0]["cd"], "cm": ref[0]["cm"], "mean_rho": ref[1]}
+    return out
+
+
 def run_batch(steps, n_cases=64, solve_steps=5000):
     """Batched polar sweep (64 uneven cases) against the same cases solved one
     after another in the plain FP64 form.  Throughputs are measured over
@@ -481,6 +513,7 @@ def run_engine(args, rank, world, local_rank):
                             "kernel_mlups": m["cells"] / (m["bulk_ms"] / 1e3) / 1e6,
                             "stream_collide_ms": m["bulk_ms"], "achieved_gbs": a, "frac_of_" + peak_kind: a / hbm}
 
+    forms["error_vs_f64"] = form_errors(project, refinement, steps=min(args.steps, 400))
     batch = run_batch(steps=min(args.steps, 100))
     serving = run_serving()
 

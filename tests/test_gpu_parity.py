@@ -354,3 +354,23 @@ def test_refined_run_writes_history_frames_and_summary(golden, tmp_path):
             solver.run(tmp_path / "out")
     finally:
         solver.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage,tol", [("f32", 1e-3), ("f16", 2e-2)])
+def test_refined_precision_forms_track_fp64(golden, storage, tol):
+    """The two-level case in the FP32-compute forms (FP32 or FP16 storage, FP32
+    transfer arithmetic) stays within the stated relative error of the FP64
+    form on Cl, Cd and Cm (floor 0.05) over 60 coarse steps."""
+    from aerokinetic_gb300.refined import RefinedSolver
+    from aerokinetic_gb300.refined_plan import load_refined_project
+    project, refinement = load_refined_project(golden["histories"]["refined_startup"]["project"])
+    plain, low = RefinedSolver(project, refinement), RefinedSolver(project, refinement, storage=storage)
+    try:
+        for _ in range(6):
+            a, b = plain.advance(10), low.advance(10)
+            for k in ("cl", "cd", "cm"):
+                assert abs(a[k] - b[k]) <= tol * max(abs(a[k]), 0.05), (a["step"], k, a[k], b[k])
+    finally:
+        plain.close()
+        low.close()
