@@ -91,10 +91,7 @@ __device__ __forceinline__ void stream_collide_cell(const S *__restrict__ src, S
                    ? Store<S>::load(src + q * G.qs + G.cell(x - cx(q), y - cy(q), zs), q, shift_at(shift, q))
                    : T(0);
     }
-    if constexpr (sizeof(T) == 8)
-        collide_full<T>(g, T(1) - omega_s, omega_b);
-    else
-        collide<T>(g, omega_s, omega_b);
+    collide_stored<S>(g, omega_s, omega_b);
     if (!fluid) return;
     const long long c = G.cell(x, y, z);
 #pragma unroll

@@ -296,4 +296,19 @@ __host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b) 
     }
 }
 
+// The collision form of a storage type: the chimera form (fewest operations)
+// for FP64 and for FP16 storage, whose quantisation (~1e-5 of a population)
+// dominates the FP32 rounding of populations near their rest weight; the
+// deviation form for FP32 storage, which keeps FP32's relative accuracy on
+// the small deviations it stores.
+template <typename S>
+__host__ __device__ __forceinline__ void collide_stored(typename Store<S>::T g[Q], typename Store<S>::T omega_s,
+                                                        typename Store<S>::T omega_b) {
+    using T = typename Store<S>::T;
+    if constexpr (sizeof(S) == sizeof(float))
+        collide<T>(g, omega_s, omega_b);
+    else
+        collide_full<T>(g, T(1) - omega_s, omega_b);
+}
+
 }  // namespace ak

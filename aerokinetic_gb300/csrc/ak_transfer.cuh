@@ -273,10 +273,7 @@ __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
     T g[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) g[q] = Store<S>::load(pdf + q * G.qs + c, q, shift.v[q]);
-    if constexpr (sizeof(T) == 8)
-        collide_full<T>(g, T(1) - omega_s, omega_b);
-    else
-        collide<T>(g, omega_s, omega_b);
+    collide_stored<S>(g, omega_s, omega_b);
 #pragma unroll
     for (int q = 0; q < Q; ++q) Store<S>::store(pdf + q * G.qs + c, q, g[q], shift.v[q]);
 }
