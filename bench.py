@@ -363,6 +363,58 @@ def run_batch(steps, n_cases=64, solve_steps=5000):
     return out
 
 
+def large_parts():
+    """The large two-level case: NACA0012 main element (chord 64 coarse, 128
+    fine cells) with a NACA0012 flap of 0.3c deflected 20 deg, 0.02c gap and
+    0.01c overlap at the main trailing edge; Re 1e5, lattice Mach 0.1, AoA 6,
+    span 32 coarse cells; coarse 3281 x 2195 x 32 and fine 866 x 422 x 64
+    (254 M cells, 277 M cell updates per coarse step)."""
+    from aerokinetic_gb300 import Flow, Grid, Project
+    from aerokinetic_gb300.refined_plan import RefinementSettings
+    from aerokinetic_gb300.serve import flapped_section
+    section = flapped_section(0.0, 0.0, 0.12, 20.0, n_side=161)
+    flow = Flow(reynolds=1e5, alpha_deg=6.0, lattice_speed=0.1 / math.sqrt(3))
+    grid = Grid(cells_per_chord=64, upstream_chords=16.0, downstream_chords=34.0, transverse_chords=17.0,
+                span_chords=0.5, memory_limit_gib=250)
+    return Project(section, flow, grid), RefinementSettings(upstream_chords=1.5, downstream_chords=4.0,
+                                                            transverse_chords=1.5)
+
+
+def run_large(steps=8):
+    """The large two-element two-level case in the plain FP64 form and the FP16
+    storage form: graph-replayed coarse steps timed by CUDA events."""
+    import torch
+    from aerokinetic_gb300 import _native
+    from aerokinetic_gb300.refined import RefinedSolver
+    project, refinement = large_parts()
+    out = {"workload": "two-element NACA0012 + 0.3c flap at 20 deg, chord 64/128, Re 1e5, AoA 6, span 32, "
+                       "legacy farfield"}
+    lib = _native.load()
+    for storage in ("f64", "f16"):
+        t0 = time.perf_counter()
+        solver = RefinedSolver(project, refinement, storage=storage, budget=False)
+        setup_s = time.perf_counter() - t0
+        cells = refined_cells(solver.plan)
+        fine_padded = math.prod((2 * solver.plan.box.shape[0] + 4, 2 * solver.plan.box.shape[1] + 4,
+                                 2 * solver.plan.box.shape[2]))
+        _native.check(lib.ak_refined_step(solver._handle, 2, None))
+        ms = stream_ms(lib, lib.ak_case_stream(solver._coarse),
+                       lambda: _native.check(lib.ak_refined_step(solver._handle, steps, None)))
+        groups = np.zeros(6)
+        _native.check(lib.ak_refined_step_timed(solver._handle, 2, groups.ctypes.data_as(ctypes.c_void_p)))
+        collide_ms = (groups[1] + groups[3]) / 2
+        collide_bytes = (math.prod(solver.plan.shape) + 2 * fine_padded) * BYTES_PER_CELL[storage]
+        out.setdefault("coarse_shape", list(solver.plan.shape))
+        out.setdefault("fine_shape", list(solver.fine_shape))
+        out.setdefault("cell_updates_per_step", cells)
+        out[storage] = {"mlups": cells * steps / (ms / 1e3) / 1e6, "ms_per_step": ms / steps,
+                        "collide_achieved_gbs": collide_bytes / (collide_ms / 1e3) / 1e9,
+                        "setup_s": setup_s, "device_gib": solver.plan.estimated_memory_gib, "steps": steps}
+        solver.close()
+        torch.cuda.synchronize()
+    return out
+
+
 def run_serving(n_requests=16, rate_per_s=20.0, seed=7):
     """Continuous batching of NACA 4-digit solves (optionally flapped) with
     Poisson arrivals; latencies and solves per hour against the same requests
@@ -516,6 +568,7 @@ def run_engine(args, rank, world, local_rank):
     forms["error_vs_f64"] = form_errors(project, refinement, steps=min(args.steps, 400))
     batch = run_batch(steps=min(args.steps, 100))
     serving = run_serving()
+    large = run_large()
 
     traffic = None
     summary = ROOT / "profiles" / "collide_f64_refined_512x384x8.txt"
@@ -547,6 +600,7 @@ def run_engine(args, rank, world, local_rank):
                                 "closes the mass/momentum budget (RefinedSolver.step)"},
             "batch": batch,
             "serving": serving,
+            "large": large,
             "gpu_launches": int(launches),
             "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)
