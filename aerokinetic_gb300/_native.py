@@ -20,7 +20,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 AK_OK, AK_ERR_INVALID, AK_ERR_CUDA, AK_ERR_NOMEM, AK_ERR_NONFINITE, AK_ERR_GUARD, AK_ERR_GEOMETRY = range(7)
 FARFIELD = {"legacy": 0, "characteristic_transport_v1": 1}
-STORAGE = {"f64": 0, "f32": 1, "f16": 2}
+STORAGE = {"f64": 0, "f32": 1, "f16": 2, "df64": 3}
 
 
 class EngineError(RuntimeError):

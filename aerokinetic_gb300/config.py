@@ -13,7 +13,7 @@ import numpy as np
 EXTERIOR_FARFIELD = "exterior_regularized_fd_v1"
 CHARACTERISTIC_FARFIELD = "characteristic_transport_v1"
 FARFIELDS = ("legacy", CHARACTERISTIC_FARFIELD, EXTERIOR_FARFIELD)
-STORAGE_MODES = ("f64", "f32", "f16")
+STORAGE_MODES = ("f64", "f32", "f16", "df64")
 
 
 @dataclass(frozen=True)
@@ -115,7 +115,7 @@ class Grid:
 def device_bytes_per_cell(storage="f64"):
     """Bytes of HBM one lattice cell occupies in this engine (two population
     copies plus the per-column flag byte amortised over the span)."""
-    size = {"f64": 8, "f32": 4, "f16": 2}[storage]
+    size = {"f64": 8, "f32": 4, "f16": 2, "df64": 8}[storage]
     return 2 * 27 * size
 
 

@@ -177,6 +177,7 @@ int with_storage(ak_case *c, F &&f) {
     case AK_STORAGE_F64: return f((double *)nullptr);
     case AK_STORAGE_F32: return f((float *)nullptr);
     case AK_STORAGE_F16: return f((__half *)nullptr);
+    case AK_STORAGE_DF64: return f((df2 *)nullptr);
     }
     return fail(AK_ERR_INVALID, "unknown storage");
 }
@@ -438,7 +439,7 @@ int prepare_boundaries(ak_case *c) {
                 src, c->G, c->outer(), c->ff(), c->ring(), c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, 1);
             AK_CUDA(cudaGetLastError());
         }
-        k_glancing_rows<typename Store<S>::T><<<(unsigned)blocks_for((long long)c->nx * c->nz, T), T, 0, c->stream>>>(c->G, c->ff(), c->ring(),
+        k_glancing_rows<typename Store<S>::A><<<(unsigned)blocks_for((long long)c->nx * c->nz, T), T, 0, c->stream>>>(c->G, c->ff(), c->ring(),
                                                                                                c->ff_lo, c->ff_hi);
         AK_CUDA(cudaGetLastError());
     }
@@ -606,7 +607,7 @@ int create_lattice(const ak_case_desc *desc, int farfield, bool periodic_xy, ak_
             delete c;
             return fail(AK_ERR_INVALID, "polygon vertices must be finite");
         }
-    c->esize = c->storage == AK_STORAGE_F64 ? 8 : (c->storage == AK_STORAGE_F32 ? 4 : 2);
+    c->esize = (c->storage == AK_STORAGE_F64 || c->storage == AK_STORAGE_DF64) ? 8 : (c->storage == AK_STORAGE_F32 ? 4 : 2);
     Grid &G = c->G;
     G.nx = c->nx;
     G.ny = c->ny;
@@ -663,7 +664,7 @@ int validate_desc(const ak_case_desc *desc, bool need_elements) {
         return fail(AK_ERR_INVALID, "freestream speed must be subsonic");
     if (desc->farfield != AK_FARFIELD_LEGACY && desc->farfield != AK_FARFIELD_CHARACTERISTIC)
         return fail(AK_ERR_INVALID, "unknown farfield");
-    if (desc->storage < AK_STORAGE_F64 || desc->storage > AK_STORAGE_F16) return fail(AK_ERR_INVALID, "unknown storage");
+    if (desc->storage < AK_STORAGE_F64 || desc->storage > AK_STORAGE_DF64) return fail(AK_ERR_INVALID, "unknown storage");
     if ((need_elements && desc->n_elements < 1) || desc->n_elements > MAX_ELEMENTS ||
         (desc->n_elements && (!desc->element_sizes || !desc->polygon_xy)))
         return fail(AK_ERR_INVALID, "between 1 and 8 polygons are required");
@@ -2007,6 +2008,7 @@ int batch_dispatch(ak_batch *B, F &&f) {
     case AK_STORAGE_F64: return f((double *)nullptr);
     case AK_STORAGE_F32: return f((float *)nullptr);
     case AK_STORAGE_F16: return f((__half *)nullptr);
+    case AK_STORAGE_DF64: return f((df2 *)nullptr);
     }
     return fail(AK_ERR_INVALID, "unknown storage");
 }

@@ -344,9 +344,9 @@ __device__ __forceinline__ void macro_at(const S *pdf, const Grid &G, int x, int
 // arithmetic type (FP64 for the plain form, FP32 for the others)
 template <typename S>
 __device__ __forceinline__ void macro_lr(const S *pdf, const Grid &G, int x, int y, int z,
-                                         typename Store<S>::T &rho, typename Store<S>::T u[3],
-                                         typename Store<S>::T &lr) {
-    using T = typename Store<S>::T;
+                                         typename Store<S>::A &rho, typename Store<S>::A u[3],
+                                         typename Store<S>::A &lr) {
+    using T = typename Store<S>::A;
     if constexpr (sizeof(T) == 8) {
         macro_at(pdf, G, x, y, z, rho, u);
         lr = log(rho);
@@ -406,7 +406,7 @@ __device__ __forceinline__ void ring_cell(const Grid &G, long long r, int &x, in
 
 template <typename S>
 __device__ __forceinline__ void ring_macro_item(const S *__restrict__ pdf, const Grid &G, const Ring &R, long long i) {
-    using T = typename Store<S>::T;
+    using T = typename Store<S>::A;
     const int z = (int)(i / R.n);
     const long long r = i - (long long)z * R.n;
     int x, y;
@@ -495,7 +495,7 @@ __device__ __forceinline__ void farfield_link(S *__restrict__ pdf, const Grid &G
                                               double *__restrict__ derivative, long long *__restrict__ clock,
                                               const double *__restrict__ init_lo, const double *__restrict__ init_hi,
                                               int prepare, long long i) {
-    using T = typename Store<S>::T;
+    using T = typename Store<S>::A;
     const int x = L.x[i], y = L.y[i], z = L.z[i], d = L.d[i], di = inv(d);
 #ifdef AK_CHECKED
     if (L.obj[i] < 0 || L.obj[i] >= P.nobj) {

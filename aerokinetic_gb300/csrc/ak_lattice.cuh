@@ -28,6 +28,8 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include "ak_df64.cuh"
+
 namespace ak {
 
 constexpr int Q = 27;
@@ -70,26 +72,45 @@ __host__ __device__ constexpr double weight(int q) {
 // departures from it) and scaled by 1/w_q into the same range for every
 // direction.  With a zero freestream a_q = 0 and the shift is plain f - w.
 template <typename S> struct Store;
+// T: the collision's arithmetic; A: the arithmetic of the boundaries and
+// the refinement transfers.
 template <> struct Store<double> {
     using T = double;
+    using A = double;
     static constexpr int MIN_BLOCKS = 4;
     __device__ static __forceinline__ double load(const double *p, int, float) { return __ldg(p); }
     __device__ static __forceinline__ void store(double *p, int, double v, float) { *p = v; }
 };
 template <> struct Store<float> {
     using T = float;
+    using A = float;
     static constexpr int MIN_BLOCKS = 8;
     __device__ static __forceinline__ float load(const float *p, int, float) { return __ldg(p); }
     __device__ static __forceinline__ void store(float *p, int, float v, float) { *p = v; }
 };
 template <> struct Store<__half> {
     using T = float;
+    using A = float;
     static constexpr int MIN_BLOCKS = 8;
     __device__ static __forceinline__ float load(const __half *p, int q, float shift) {
         return fmaf(__half2float(__ldg(p)), (float)weight(q), shift);
     }
     __device__ static __forceinline__ void store(__half *p, int q, float v, float shift) {
         *p = __float2half_rn((v - shift) * (float)(1.0 / weight(q)));
+    }
+};
+// df64 form: FP64-sized storage as (hi, lo) float pairs, the collision in
+// double-float arithmetic on the FP32 pipe, boundaries and transfers in FP64
+template <> struct Store<df2> {
+    using T = df64;
+    using A = double;
+    static constexpr int MIN_BLOCKS = 4;
+    __device__ static __forceinline__ df64 load(const df2 *p, int, float) {
+        const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+        return df64(v.x, v.y);
+    }
+    __device__ static __forceinline__ void store(df2 *p, int, df64 v, float) {
+        *reinterpret_cast<float2 *>(p) = make_float2(v.hi, v.lo);
     }
 };
 // the FP16 shift by value, for kernels that index it with compile-time q
@@ -235,7 +256,7 @@ __host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b) 
     const T kdx = M200 - jx * ux, kdy = M020 - jy * uy, kdz = M002 - jz * uz;
     const T P1 = om1 * (kdx - kdy), P2 = om1 * (kdx - kdz);
     const T S = kdx + kdy + kdz;
-    const T third = T(1) / T(3);
+    const T third = T(1.0 / 3.0);
     const T kx = (P1 + P2 + (S + omega_b * (drho - S))) * third;
     // normalised covariance: s_aa = (1/3 + k_a) / rho; t_a = u_a^2 + s_aa
     const T r3 = third * rinv;

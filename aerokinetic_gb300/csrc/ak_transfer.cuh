@@ -430,7 +430,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
     k_block_moments(const S *__restrict__ pdf, Grid G, BoxSpec B, const double *__restrict__ free_g,
                     double *__restrict__ out, const double *__restrict__ mix_from, double *__restrict__ half,
                     int *__restrict__ flag) {
-    using T = typename Store<S>::T;
+    using T = typename Store<S>::A;
     __shared__ SplitShared<T> sh;
     const long long nring = ring_count(B.dnx, B.dny, DONOR_RING, DONOR_RING), nr = nring * G.nz;
     if ((long long)blockIdx.x * SPLIT_CELLS >= nr) return;
@@ -527,7 +527,7 @@ template <typename S>
 __global__ void __launch_bounds__(SPLIT_THREADS)
     k_donors(S *__restrict__ fine, Grid F, int nzc, const double *__restrict__ pxy, Rescale r, int pad,
              int *__restrict__ flag) {
-    using T = typename Store<S>::T;
+    using T = typename Store<S>::A;
     __shared__ SplitShared<T> sh;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const long long nring = ring_count(F.nx, F.ny, pad, pad), n = nring * F.nz;
@@ -581,7 +581,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
     k_reflux(S *__restrict__ pdf, Grid G, const Face *__restrict__ faces, int nfaces,
              const long long *__restrict__ offsets, const double *__restrict__ reg_c,
              const double *__restrict__ reg_f, double inv_volume, int *__restrict__ flag) {
-    using T = typename Store<S>::T;
+    using T = typename Store<S>::A;
     __shared__ SplitShared<T> sh;
     const int f = blockIdx.y;
     if (f >= nfaces) return;
@@ -669,7 +669,7 @@ template <typename Sc, typename Sf>
 __global__ void __launch_bounds__(SPLIT_THREADS)
     k_restrict(Sc *__restrict__ coarse, Grid G, const Sf *__restrict__ fine, Grid F, BoxSpec B, int pad,
                const double *__restrict__ free_g, Rescale r, int *__restrict__ flag) {
-    using T = typename Store<Sc>::T;
+    using T = typename Store<Sc>::A;
     __shared__ SplitShared<T> sh;
     if (blockIdx.y == 1) {
         const int cx0 = B.bx - 6, cy0 = B.by - 6;

@@ -41,7 +41,7 @@ CELLS_PER_CHORD = 32
 WORKLOAD = ("two-level NACA0012, coarse 512x384x8 (chord 32) + fine 160x76x16 (chord 64) over "
             "x in [-0.5c, 2c], y in [-0.6c, 0.6c], AoA 8, Re 3e4, Ma 0.1, legacy farfield")
 UNIFORM = "uniform NACA0012 384x256x8, chord 32, AoA 4, Re 3e4, Ma 0.1, characteristic farfield"
-BYTES_PER_CELL = {"f64": 27 * 2 * 8, "f32": 27 * 2 * 4, "f16": 27 * 2 * 2}
+BYTES_PER_CELL = {"f64": 27 * 2 * 8, "f32": 27 * 2 * 4, "f16": 27 * 2 * 2, "df64": 27 * 2 * 8}
 
 
 def case_parts():
@@ -285,7 +285,7 @@ def form_errors(project, refinement, steps=400):
     velocity field's relative L2 over both levels."""
     from aerokinetic_gb300.refined import RefinedSolver
     runs = {}
-    for storage in ("f64", "f32", "f16"):
+    for storage in ("f64", "df64", "f32", "f16"):
         solver = RefinedSolver(project, refinement, storage=storage)
         record = solver.advance(steps)
         integrals = solver.conserved_integrals()
@@ -300,7 +300,7 @@ def form_errors(project, refinement, steps=400):
         solver.close()
     ref = runs["f64"]
     out = {"coarse_steps": steps}
-    for storage in ("f32", "f16"):
+    for storage in ("df64", "f32", "f16"):
         rec, mean_rho, uc, uf = runs[storage]
         du = np.sum((uc - ref[2]) ** 2) + np.sum((uf - ref[3]) ** 2)
         norm = np.sum(ref[2] ** 2) + np.sum(ref[3] ** 2)
@@ -532,7 +532,7 @@ def run_engine(args, rank, world, local_rank):
 
     # ---- reduced-precision forms of the two-level case
     forms = {}
-    for storage in ("f32", "f16"):
+    for storage in ("df64", "f32", "f16"):
         r = RefinedSolver(project, refinement, storage=storage, budget=False)
         fst = torch.cuda.ExternalStream(lib.ak_case_stream(r._coarse))
         _native.check(lib.ak_refined_step(r._handle, max(3, args.warmup), None))
@@ -557,7 +557,7 @@ def run_engine(args, rank, world, local_rank):
 
     # ---- the uniform case (the reference's CPU-runnable configuration)
     uniform = {}
-    for storage in ("f64", "f32", "f16"):
+    for storage in ("f64", "df64", "f32", "f16"):
         m = measure_form(storage, steps=min(args.steps, 100), warmup=args.warmup, flush=True)
         bytes_launch = m["fluid_cells"] * BYTES_PER_CELL[storage]
         a = bytes_launch / (m["bulk_ms"] / 1e3) / 1e9

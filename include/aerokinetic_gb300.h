@@ -57,6 +57,8 @@ extern "C" {
 #define AK_STORAGE_F64 0  /* plain form: FP64 storage and arithmetic */
 #define AK_STORAGE_F32 1  /* FP32 arithmetic, FP32 (f - w) storage */
 #define AK_STORAGE_F16 2  /* FP32 arithmetic, FP16 storage of (f - f_eq(1, U)) / w */
+#define AK_STORAGE_DF64 3 /* 8-byte storage as FP32 pairs, collision in double-float (48-bit) arithmetic,
+                             boundaries and refinement transfers in FP64 */
 
 typedef struct ak_case ak_case;
 

@@ -74,10 +74,12 @@ def test_flags_links_and_fractions_bit_exact(golden, name):
         solver.close()
 
 
-def compare_run(project, steps, sample_every, pdf_tol=2e-12, load_tol=2e-10):
-    solver, oracle = solver_for(project), oracle_for(project)
+def compare_run(project, steps, sample_every, pdf_tol=2e-12, load_tol=2e-10, storage="f64"):
+    solver, oracle = solver_for(project, storage), oracle_for(project)
     try:
-        np.testing.assert_allclose(solver.pdf(), oracle.lattice.interior(), rtol=0, atol=1e-15)
+        # df64 storage holds 48 bits: ~2^-48 of a population near its rest weight
+        np.testing.assert_allclose(solver.pdf(), oracle.lattice.interior(), rtol=0,
+                                   atol=1e-15 if storage == "f64" else 5e-15)
         fluid = oracle.lattice.fluid
         worst = 0.0
         for s in range(1, steps + 1):
@@ -104,6 +106,26 @@ def test_legacy_case_matches_oracle():
 
 def test_characteristic_case_matches_oracle():
     compare_run(kat_project("characteristic_transport_v1"), steps=40, sample_every=8)
+
+
+@pytest.mark.parametrize("farfield", ["legacy", "characteristic_transport_v1"])
+def test_df64_form_meets_the_plain_tolerances(farfield):
+    """The df64 form (FP64-sized storage, double-float collision, FP64
+    boundaries) against the FP64 oracle at the plain form's own bars:
+    2e-12 per population per step and 2e-10 on the loads."""
+    compare_run(kat_project(farfield), steps=40, sample_every=8, storage="df64")
+
+
+def test_df64_known_answer_272_steps(golden):
+    kat = golden["kat272"]
+    solver = solver_for(kat_project("legacy"), "df64")
+    try:
+        solver.advance(kat["steps"] - 1)
+        loads = solver.step(sample=True)
+        for k, v in kat["last_sample"].items():
+            assert loads[k] == pytest.approx(v, rel=1e-10)
+    finally:
+        solver.close()
 
 
 def test_known_answer_272_steps_on_gpu(golden):
@@ -211,12 +233,12 @@ def test_precision_forms_track_fp64(storage, inst_tol, mean_tol):
 
 
 # ---------------------------------------------------------------- two levels
-def refined_pair(record, steps_needed=0):
+def refined_pair(record, steps_needed=0, storage="f64"):
     from aerokinetic_gb300.refined import RefinedSolver
     from aerokinetic_gb300.refined_plan import load_refined_project
     from oracle.refined import RefinedCase
     project, refinement = load_refined_project(record["project"])
-    solver = RefinedSolver(project, refinement)
+    solver = RefinedSolver(project, refinement, storage=storage)
     plan = solver.plan
     sec, flow = project.section, project.flow
     lead = O.leading_edge([e.xy for e in sec.elements], sec.moment_reference, sec.chord, flow.alpha_deg)
@@ -227,9 +249,11 @@ def refined_pair(record, steps_needed=0):
     return solver, oracle
 
 
-def test_refined_levels_match_oracle(golden):
-    """Both levels' populations and the loads after each of 3 coarse steps."""
-    solver, oracle = refined_pair(golden["histories"]["refined_startup"])
+@pytest.mark.parametrize("storage", ["f64", "df64"])
+def test_refined_levels_match_oracle(golden, storage):
+    """Both levels' populations and the loads after each of 3 coarse steps, in
+    the plain form and the df64 form, at the plain form's tolerances."""
+    solver, oracle = refined_pair(golden["histories"]["refined_startup"], storage=storage)
     try:
         pad = oracle.pad
         coarse, fine = solver.states()
