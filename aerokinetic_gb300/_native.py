@@ -110,6 +110,7 @@ SIGNATURES = {
     "ak_get_boundary_state": ([_P, _P, _P], ctypes.c_int),
     "ak_set_boundary_state": ([_P, _P, _P], ctypes.c_int),
     "ak_set_steps_done": ([_P, ctypes.c_int64], ctypes.c_int),
+    "ak_case_buffers": ([_P, _P, _P, _P, _P], ctypes.c_int),
     "ak_residuals": ([_P, _D, _D, ctypes.c_int32, _P], ctypes.c_int),
     "ak_residual_snapshot": ([_P, ctypes.c_int32, _P, _P], ctypes.c_int),
     "ak_refined_restore_counters": ([_P, ctypes.c_int64, _P, _P], ctypes.c_int),

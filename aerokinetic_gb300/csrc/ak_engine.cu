@@ -1035,6 +1035,20 @@ int ak_set_boundary_state(ak_case *c, const int32_t *rows, const double *values)
     return AK_OK;
 }
 
+int ak_case_buffers(ak_case *c, void **current, void **other, int64_t *dims, int32_t *element_bytes) {
+    AK_TRY(check_case(c));
+    if (!current || !other || !dims || !element_bytes) return fail(AK_ERR_INVALID, "null output");
+    AK_CUDA(cudaStreamSynchronize(c->stream));
+    *current = c->pdf[c->cur];
+    *other = c->pdf[1 - c->cur];
+    dims[0] = Q;
+    dims[1] = c->nz;
+    dims[2] = c->G.nyp;
+    dims[3] = c->G.sx;
+    *element_bytes = (int32_t)c->esize;
+    return AK_OK;
+}
+
 int ak_set_steps_done(ak_case *c, int64_t steps) {
     AK_TRY(check_case(c));
     if (steps < 0) return fail(AK_ERR_INVALID, "steps must be >= 0");

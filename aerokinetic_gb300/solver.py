@@ -157,6 +157,13 @@ class Solver:
         check(self._lib.ak_macros(self._case, _ptr(rho), _ptr(u)))
         return rho, u
 
+    def population_tensor(self):
+        """The current population array as a torch tensor viewing the engine's
+        device memory (no copy): shape (27, nz, ny + 2, pitch) in the storage's
+        dtype (df64: a trailing (hi, lo) axis of float32), x and y offset by one
+        ghost layer.  Valid until the next step swaps the two copies."""
+        return population_view(self._lib, self._case, self.storage)
+
     def pdf(self):
         """Interior populations g = f - w as (nx, ny, nz, 27) doubles."""
         out = np.empty(self.plan.shape + (27,))
@@ -402,6 +409,28 @@ class Solver:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class _DeviceArray:
+    """__cuda_array_interface__ of engine-owned device memory."""
+
+    def __init__(self, pointer, shape, typestr, owner):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (pointer, False),
+                                         "version": 3, "strides": None}
+        self._owner = owner
+
+
+def population_view(lib, handle, storage):
+    import torch
+    current, other = ctypes.c_void_p(), ctypes.c_void_p()
+    dims = (ctypes.c_int64 * 4)()
+    size = ctypes.c_int32()
+    check(lib.ak_case_buffers(handle, ctypes.byref(current), ctypes.byref(other), dims, ctypes.byref(size)))
+    shape = list(dims)
+    typestr = {"f64": "<f8", "f32": "<f4", "f16": "<f2", "df64": "<f4"}[storage]
+    if storage == "df64":
+        shape.append(2)
+    return torch.as_tensor(_DeviceArray(current.value, shape, typestr, handle), device="cuda")
 
 
 def _file_hash(path, limit=None):

@@ -151,6 +151,13 @@ int ak_set_pdf(ak_case *c, const double *pdf);
 int ak_boundary_state_size(ak_case *c, int64_t *n_links, int64_t *n_values);
 int ak_get_boundary_state(ak_case *c, int32_t *rows, double *values);
 int ak_set_boundary_state(ak_case *c, const int32_t *rows, const double *values);
+/* The case's two population arrays in device memory, for zero-copy views
+ * (e.g. torch tensors through __cuda_array_interface__): current holds the
+ * state ak_get_pdf returns, other the second copy.  Layout [q][z][y][x] with
+ * dims = (27, nz, ny + 2, row pitch), x and y offset by one ghost layer;
+ * element_bytes 8 (f64 doubles, df64 (hi, lo) float pairs), 4 (f32) or 2
+ * (f16, (f - f_eq(1, U)) / w).  Valid until the next step swaps the copies. */
+int ak_case_buffers(ak_case *c, void **current, void **other, int64_t *dims, int32_t *element_bytes);
 /* Step counter of a restored case (Solver.steps after restore_checkpoint,
  * checkpoint.py:113). */
 int ak_set_steps_done(ak_case *c, int64_t steps);

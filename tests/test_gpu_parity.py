@@ -398,3 +398,27 @@ def test_refined_precision_forms_track_fp64(golden, storage, tol):
     finally:
         plain.close()
         low.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage", ["f64", "f32", "df64"])
+def test_population_tensor_views_the_engine_state(storage):
+    """Solver.population_tensor is a torch view of the engine's current copy:
+    its interior equals ak_get_pdf without any copy by the engine."""
+    import torch
+    solver = solver_for(kat_project("characteristic_transport_v1"), storage)
+    try:
+        solver.advance(3)
+        view = solver.population_tensor()
+        assert view.is_cuda and view.shape[:3] == (27, solver.plan.shape[2], solver.plan.shape[1] + 2)
+        nx, ny, nz = solver.plan.shape
+        interior = view[:, :, 1:ny + 1, 1:nx + 1].double()
+        if storage == "df64":
+            interior = interior[..., 0] + interior[..., 1]
+        got = interior.permute(3, 2, 1, 0).cpu().numpy()
+        assert np.array_equal(got, solver.pdf())
+        before = view.clone()
+        solver.advance(1)
+        assert not torch.equal(solver.population_tensor(), before)
+    finally:
+        solver.close()
