@@ -157,9 +157,14 @@ class Plan:
             if min(grid.upstream_chords, grid.downstream_chords, grid.transverse_chords) * n < 2:
                 raise ValueError("Characteristic farfield needs at least two fluid cells between body bounds and exterior")
             if grid.farfield == EXTERIOR_FARFIELD:
-                raise ValueError("exterior_regularized_fd_v1 is not provided by this engine")
-            notes.append("Experimental characteristic_transport_v1 farfield with linearized transverse transport; "
-                         "not full viscous NSCBC or validated airfoil accuracy.")
+                if flow.sgs != "none":
+                    raise ValueError("Exterior FD currently supports molecular viscosity with sgs=none only")
+                notes.append("Research exterior_regularized_fd_v1; physical shape unchanged, auxiliary ring of one "
+                             "cell in x and y; explicit exterior source. Uniform grids only; no validated airfoil "
+                             "accuracy or full viscous NSCBC.")
+            else:
+                notes.append("Experimental characteristic_transport_v1 farfield with linearized transverse "
+                             "transport; not full viscous NSCBC or validated airfoil accuracy.")
         if n < 256:
             notes.append("Fewer than 256 cells/chord: use for development; do not assume a resolved boundary layer.")
         if tau < 0.501:

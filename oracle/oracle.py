@@ -434,6 +434,12 @@ class AirfoilCase:
                 lat.set_boundary(Boundary("farfield", 0, normal=normal, velocity=freestream, density=1.0), outside)
         else:
             raise ValueError(f"unsupported farfield {farfield}")
+        self._install_walls()
+
+    def _install_walls(self):
+        lat = self.lattice
+        nx, ny, nz = self.shape
+        x, y, z = lat.midpoints()
         self.walls = []
         xx = x[:, :, 0] * self.dx + self.origin[0]
         yy = y[:, :, 0] * self.dx + self.origin[1]

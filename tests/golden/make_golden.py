@@ -38,7 +38,10 @@ HISTORIES = {
     "characteristic_down3": ("docs/verification_farfield_20261107/airfoil/characteristic_down3", 120),
     "legacy_corrected32": ("docs/verification_stage1_20261106/corrected32_t12", 120),
     "legacy_down6": ("docs/verification_farfield_20261107/airfoil/legacy_down6", 120),
+    "exterior_down3": ("docs/verification_exterior_library_20261108/raw/matched_airfoils/airfoil_down3", 60),
 }
+EXTERIOR_COLUMNS = ("wall_mass_exchange_lattice", "wall_mass_exchange_accumulated", "exterior_source_mass_lattice",
+                    "exterior_source_mass_accumulated")
 
 # Geometry cases: (name, project kwargs) built with the reference's classes.
 GEOMETRY_CASES = {
@@ -67,6 +70,7 @@ def read_history(path, limit):
         rows = list(csv.DictReader(handle))
     rows = rows if limit is None else rows[:limit]
     keep = ("step", "cl", "cd", "cm", "local_mach_max", "density_error_max")
+    keep += tuple(k for k in EXTERIOR_COLUMNS if rows and k in rows[0])
     return [{k: (int(r[k]) if k == "step" else float(r[k])) for k in keep} for r in rows]
 
 

@@ -6,7 +6,7 @@ down: plane-wave probe records for its UBB and ExtrapolationOutflow
 (docs/verification_stage1_20261106/acoustics/), a nonlinear start-up with the
 Mach/density guards (docs/verification_failure_capture_20261107/), the 272-step
 known answer (tools/profile_stage1.py) and the first samples of full Cl/Cd/Cm
-histories with both farfields.  Tolerances: the reference's own thread-count
+histories with the three farfields.  Tolerances: the reference's own thread-count
 variation is 2e-14 in Cl after 272 steps (RESOURCE_CHECK.json:14-18); every
 bound below is a few hundred times that and far below any modelling change.
 """
@@ -123,6 +123,44 @@ def test_history_first_samples(golden, name, samples):
             loads = case.step(sample=(case.steps + 1) % every == 0)
         for k in ("cl", "cd", "cm"):
             assert loads[k] == pytest.approx(row[k], abs=2e-12)
+
+
+def _exterior(project, threads=None):
+    from oracle.exterior import ExteriorCase
+    plan = Plan.create(project.section, project.flow, project.grid)
+    contours = [c.xy for c in project.section.normalized(project.flow.alpha_deg)]
+    lead = O.leading_edge([e.xy for e in project.section.elements], project.section.moment_reference,
+                          project.section.chord, project.flow.alpha_deg)
+    case = ExteriorCase(contours, plan.shape, plan.origin, plan.dx, plan.span, plan.relaxation_rate,
+                        project.flow.lattice_speed, project.grid.cells_per_chord, project.flow.perturbation,
+                        project.flow.seed, lead, threads or oracle_threads())
+    return plan, case
+
+
+def test_exterior_history_first_samples(golden):
+    """exterior_regularized_fd_v1 on the 176x101x16 NACA0012 case: loads, wall
+    mass, exterior source and guards of the first 12 samples (96 steps).  The
+    source is the sum of rebuilt-minus-streamed populations over ~2.4e5 ring
+    values of order 1e-3 each, so its rounding (summation order) is ~1e-13
+    while Cl/Cd/Cm agree to ~1e-14."""
+    record = golden["histories"]["exterior_down3"]
+    project = Project.from_dict(record["project"])
+    plan, case = _exterior(project)
+    assert plan.shape == (176, 101, 16)
+    every = project.run.sample_every
+    for row in record["history"][:12]:
+        while case.steps < row["step"]:
+            loads = case.step(sample=(case.steps + 1) % every == 0)
+        for k in ("cl", "cd", "cm"):
+            assert loads[k] == pytest.approx(row[k], abs=2e-12)
+        for k in ("wall_mass_exchange_lattice", "wall_mass_exchange_accumulated"):
+            assert loads[k] == pytest.approx(row[k], abs=2e-12)
+        assert loads["exterior_source_mass_lattice"] == pytest.approx(row["exterior_source_mass_lattice"], abs=5e-12)
+        assert loads["exterior_source_mass_accumulated"] == pytest.approx(row["exterior_source_mass_accumulated"],
+                                                                          abs=5e-11)
+        diag = case.diagnostics()
+        for k in ("local_mach_max", "density_error_max"):
+            assert diag[k] == pytest.approx(row[k], abs=1e-12)
 
 
 # ---------------------------------------------------------------- collision
