@@ -19,7 +19,7 @@ LIBRARY = PACKAGE / "_build" / "libaerokinetic_gb300.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 AK_OK, AK_ERR_INVALID, AK_ERR_CUDA, AK_ERR_NOMEM, AK_ERR_NONFINITE, AK_ERR_GUARD, AK_ERR_GEOMETRY = range(7)
-FARFIELD = {"legacy": 0, "characteristic_transport_v1": 1}
+FARFIELD = {"legacy": 0, "characteristic_transport_v1": 1, "exterior_regularized_fd_v1": 2}
 STORAGE = {"f64": 0, "f32": 1, "f16": 2, "df64": 3}
 
 
@@ -111,6 +111,7 @@ SIGNATURES = {
     "ak_set_boundary_state": ([_P, _P, _P], ctypes.c_int),
     "ak_set_steps_done": ([_P, ctypes.c_int64], ctypes.c_int),
     "ak_case_buffers": ([_P, _P, _P, _P, _P], ctypes.c_int),
+    "ak_exterior_report": ([_P, _P], ctypes.c_int),
     "ak_residuals": ([_P, _D, _D, ctypes.c_int32, _P], ctypes.c_int),
     "ak_residual_snapshot": ([_P, ctypes.c_int32, _P, _P], ctypes.c_int),
     "ak_refined_restore_counters": ([_P, ctypes.c_int64, _P, _P], ctypes.c_int),

@@ -17,6 +17,7 @@
 #include "ak_geometry.cuh"
 #include "ak_transfer.cuh"
 #include "ak_batch.cuh"
+#include "ak_exterior.cuh"
 
 using namespace ak;
 
@@ -106,6 +107,16 @@ struct ak_case {
     int res_region[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     double *res_snapshot = nullptr, *res_partials = nullptr, *res_out = nullptr;
     bool periodic_xy = false;  // the padded fine block of a refined case wraps in x and y
+    // exterior farfield: the ghost layer is the auxiliary ring; band states
+    // (log rho, u) of the cells within two of the edge (current and next), the
+    // predictor's three stages, the initial incoming invariant of the glancing
+    // rows, the source partials and out[10] (source, wall mass, running sums)
+    ExtGeom ext{};
+    double *ext_band[2] = {nullptr, nullptr};
+    int ext_cur = 0;
+    double *ext_stage[3] = {nullptr, nullptr, nullptr};
+    double *ext_inc0 = nullptr, *ext_partials = nullptr, *ext_out = nullptr;
+    long long ext_blocks = 0, wall_blocks = 0;
     // optional per-kernel timing: events recorded around each kernel group
     std::vector<cudaEvent_t> *timing = nullptr;
     cudaStream_t stream = nullptr;
@@ -140,7 +151,8 @@ void release(ak_case *c) {
                     c->ox_, c->oy_, c->oz_, c->od, c->oobj, c->oedge, c->sel_ubb, c->sel_out, c->out_state,
                     c->ubb_cells, c->ff_in, c->ff_der, c->ff_clock, c->ff_lo, c->ff_hi, c->partials, c->reduced,
                     c->staging, c->d_ff, c->d_shift, c->ring_ru, c->ring_lr, c->res_snapshot,
-                    c->res_partials, c->res_out};
+                    c->res_partials, c->res_out, c->ext_band[0], c->ext_band[1], c->ext_stage[0],
+                    c->ext_stage[1], c->ext_stage[2], c->ext_inc0, c->ext_partials, c->ext_out};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -456,8 +468,12 @@ void mark(ak_case *c) {
 }
 
 template <typename S>
+int exterior_step(ak_case *c, double *fixed_partials, long long fixed_capacity);
+
+template <typename S>
 int one_step(ak_case *c, bool sample, double *fixed_partials = nullptr, long long fixed_capacity = 0) {
     using T = typename Store<S>::T;
+    if (c->farfield == AK_FARFIELD_EXTERIOR) return exterior_step<S>(c, fixed_partials, fixed_capacity);
     const bool first = !c->prepared;
     if (first) AK_TRY(prepare_boundaries<S>(c));
     S *src = src_of<S>(c);
@@ -534,6 +550,121 @@ int one_step(ak_case *c, bool sample, double *fixed_partials = nullptr, long lon
     mark(c);
     c->cur = 1 - c->cur;
     c->steps += 1;
+    return AK_OK;
+}
+
+// One step of the exterior farfield (exterior.py:173-200 around solver.py:
+// 262-271): the ring predictor from the current band state, the walls with
+// their loads and wall mass (every step: the wall mass accumulates), the
+// streamed band macros, the rebuilt and collided ring, the fused bulk
+// stream-collide, and the step's source and wall-mass sums.
+template <typename S>
+int exterior_step(ak_case *c, double *fixed_partials, long long fixed_capacity) {
+    using T = typename Store<S>::T;
+    if (!c->prepared) return fail(AK_ERR_INVALID, "the exterior case needs an initial state first");
+    S *src = src_of<S>(c), *dst = dst_of<S>(c);
+    const ExtGeom &E = c->ext;
+    double *band = c->ext_band[c->ext_cur], *next = c->ext_band[1 - c->ext_cur];
+    const long long nr = (long long)E.nring * E.nz;
+    const unsigned rb = (unsigned)blocks_for(nr, 128);
+    const double step = (double)c->steps;
+    mark(c);
+    double *moment_error = c->ext_out + 10;
+    k_ext_stage<<<rb, 128, 0, c->stream>>>(E, band, nullptr, c->ext_stage[0], 1, step, c->ext_inc0, moment_error);
+    k_ext_stage<<<rb, 128, 0, c->stream>>>(E, band, c->ext_stage[0], c->ext_stage[1], 2, step, c->ext_inc0,
+                                           moment_error);
+    k_ext_stage<<<rb, 128, 0, c->stream>>>(E, band, c->ext_stage[1], c->ext_stage[2], 3, step, c->ext_inc0,
+                                           moment_error);
+    AK_CUDA(cudaGetLastError());
+    c->launches += 3;
+    mark(c);
+    const long long nlinks = c->nkeys * c->nz * 3;
+    if (nlinks) {
+        const long long nb = c->wall_blocks;
+        double *partials = c->partials;
+        if (fixed_partials) {
+            if (nb * 5 * c->n_elements > fixed_capacity)
+                return fail(AK_ERR_INVALID, "wall links need more partial sums than the static scratch holds");
+            partials = fixed_partials;
+        }
+        k_walls<S><<<(unsigned)nb, 256, 0, c->stream>>>(src, c->G, c->keys, c->wall_q, c->nkeys, 1, c->n_elements,
+                                                        c->ox, c->oy, partials);
+        k_sum_partials<<<5 * c->n_elements, 32, 0, c->stream>>>(partials, (int)nb, 5 * c->n_elements, c->reduced);
+        AK_CUDA(cudaGetLastError());
+        c->launches += 2;
+    } else {
+        AK_CUDA(cudaMemsetAsync(c->reduced, 0, sizeof(double) * 5 * c->n_elements, c->stream));
+    }
+    mark(c);
+    k_ext_band_pull<S><<<(unsigned)blocks_for((long long)E.nband * E.nz, 128), 128, 0, c->stream>>>(src, c->G, E,
+                                                                                                    next);
+    k_ext_ring<S><<<rb, 128, 0, c->stream>>>(src, dst, c->G, E, next, c->ext_stage[2], c->shift_host, (T)c->omega_s,
+                                             (T)c->omega_b, c->omega_s, c->ext_partials, moment_error);
+    AK_CUDA(cudaGetLastError());
+    c->launches += 2;
+    mark(c);
+    dim3 grid((unsigned)blocks_for(c->nx, 128), (unsigned)c->ny, (unsigned)c->nz);
+    k_stream_collide<S><<<grid, 128, 0, c->stream>>>(src, dst, c->flags, c->G, c->shift_host, (T)c->omega_s,
+                                                     (T)c->omega_b);
+    AK_CUDA(cudaGetLastError());
+    mark(c);
+    k_ext_final<<<1, REDUCE_THREADS, 0, c->stream>>>(c->ext_partials, rb, c->reduced, c->n_elements, c->ext_out);
+    AK_CUDA(cudaGetLastError());
+    c->launches += 2;
+    c->cur = 1 - c->cur;
+    c->ext_cur = 1 - c->ext_cur;
+    c->steps += 1;
+    return AK_OK;
+}
+
+// The initial exterior state: the ring at the freestream equilibrium, the
+// band state and the glancing rows' invariant of these pre-collision
+// populations, then their collision into the stored (post-collision) form.
+template <typename S>
+int exterior_prepare(ak_case *c) {
+    using T = typename Store<S>::T;
+    S *pdf = src_of<S>(c);
+    const ExtGeom &E = c->ext;
+    const long long nr = (long long)E.nring * E.nz;
+    k_ext_fill_ring<S><<<(unsigned)blocks_for(nr, 128), 128, 0, c->stream>>>(pdf, c->G, E);
+    k_ext_band_direct<S><<<(unsigned)blocks_for((long long)E.nband * E.nz, 128), 128, 0, c->stream>>>(
+        pdf, c->G, E, c->ext_band[0], c->ext_inc0);
+    dim3 grid((unsigned)blocks_for(c->nx, 128), (unsigned)c->ny, (unsigned)c->nz);
+    k_collide<S><<<grid, 128, 0, c->stream>>>(pdf, c->flags, c->G, c->shift_host, (T)c->omega_s, (T)c->omega_b);
+    k_ext_collide_ring<S><<<(unsigned)blocks_for(nr, 128), 128, 0, c->stream>>>(pdf, c->G, E, c->shift_host,
+                                                                                (T)c->omega_s, (T)c->omega_b);
+    AK_CUDA(cudaGetLastError());
+    AK_CUDA(cudaMemsetAsync(c->ext_out, 0, 11 * sizeof(double), c->stream));
+    c->ext_cur = 0;
+    c->prepared = true;
+    return AK_OK;
+}
+
+// the two layers inside the ring must be fluid (the plan keeps two fluid
+// cells between the body and the physical edge; the ring itself is the ghost
+// layer, flagged outer and free of solids by build_geometry); the buffers of
+// the ring work
+int build_exterior(ak_case *c, const std::vector<uint8_t> &hflags) {
+    c->ext = make_ext_geom(c->nx, c->ny, c->nz, c->speed);
+    const ExtGeom &E = c->ext;
+    if (E.NX < 6 || E.NY < 6) return fail(AK_ERR_INVALID, "the exterior farfield needs at least 4 cells in x and y");
+    for (int y = 0; y < E.NY; ++y)
+        for (int x = 0; x < E.NX; ++x) {
+            const int layer = std::min(std::min(x, y), std::min(E.NX - 1 - x, E.NY - 1 - y));
+            if (layer >= 1 && layer <= 2 && hflags[(size_t)y * c->G.nxp + x] != FLAG_FLUID)
+                return fail(AK_ERR_INVALID, "the two layers inside the exterior ring must be fluid");
+        }
+    const long long nr = (long long)E.nring * E.nz, nb = (long long)E.nband * E.nz;
+    for (int k = 0; k < 2; ++k) AK_TRY(dalloc(c, &c->ext_band[k], 4 * nb));
+    for (int k = 0; k < 3; ++k) AK_TRY(dalloc(c, &c->ext_stage[k], 4 * nr));
+    AK_TRY(dalloc(c, &c->ext_inc0, 2LL * E.nz * E.NX));
+    c->ext_blocks = blocks_for(nr, 128);
+    AK_TRY(dalloc(c, &c->ext_partials, 4 * c->ext_blocks));
+    AK_TRY(dalloc(c, &c->ext_out, 11));
+    AK_CUDA(cudaMemsetAsync(c->ext_out, 0, 11 * sizeof(double), c->stream));
+    // the walls reduce their loads every step: size the partials once
+    c->wall_blocks = blocks_for(c->nkeys * c->nz * 3, 256);
+    if (c->wall_blocks) AK_TRY(ensure_partials(c, c->wall_blocks * 5 * c->n_elements));
     return AK_OK;
 }
 
@@ -638,7 +769,8 @@ int create_lattice(const ak_case_desc *desc, int farfield, bool periodic_xy, ak_
     std::vector<uint8_t> hflags;
     if (r == AK_OK && c->farfield == AK_FARFIELD_CHARACTERISTIC) build_farfield_objects(c);
     if (r == AK_OK) r = build_geometry(c, hflags);
-    if (r == AK_OK && c->farfield >= 0) r = build_outer(c, hflags);
+    if (r == AK_OK && c->farfield == AK_FARFIELD_EXTERIOR) r = build_exterior(c, hflags);
+    else if (r == AK_OK && c->farfield >= 0) r = build_outer(c, hflags);
     if (r == AK_OK) r = dalloc(c, &c->reduced, 64);
     if (r == AK_OK) r = with_storage(c, [&](auto *tag) { return allocate_populations<std::remove_pointer_t<decltype(tag)>>(c); });
     if (r == AK_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) r = fail(AK_ERR_CUDA, "case set-up failed");
@@ -662,7 +794,8 @@ int validate_desc(const ak_case_desc *desc, bool need_elements) {
         return fail(AK_ERR_INVALID, "relaxation rates must lie in (0, 2)");
     if (!std::isfinite(desc->speed) || std::fabs(desc->speed) >= 1.0 / std::sqrt(3.0))
         return fail(AK_ERR_INVALID, "freestream speed must be subsonic");
-    if (desc->farfield != AK_FARFIELD_LEGACY && desc->farfield != AK_FARFIELD_CHARACTERISTIC)
+    if (desc->farfield != AK_FARFIELD_LEGACY && desc->farfield != AK_FARFIELD_CHARACTERISTIC &&
+        desc->farfield != AK_FARFIELD_EXTERIOR)
         return fail(AK_ERR_INVALID, "unknown farfield");
     if (desc->storage < AK_STORAGE_F64 || desc->storage > AK_STORAGE_DF64) return fail(AK_ERR_INVALID, "unknown storage");
     if ((need_elements && desc->n_elements < 1) || desc->n_elements > MAX_ELEMENTS ||
@@ -718,10 +851,12 @@ int ak_init_perturbed(ak_case *c, double amp, double phase_y, double phase_z, do
             src_of<S>(c), c->G, c->flags, c->speed, amp, phase_y, phase_z, lead_x, lead_y, c->origin_x, c->origin_y,
             c->dx, ky, kz);
         AK_CUDA(cudaGetLastError());
+        if (c->farfield == AK_FARFIELD_EXTERIOR) return exterior_prepare<S>(c);
         return AK_OK;
     }));
     AK_CUDA(cudaStreamSynchronize(c->stream));
-    c->prepared = false;
+    c->prepared = c->farfield == AK_FARFIELD_EXTERIOR;
+    c->steps = 0;
     return AK_OK;
 }
 
@@ -737,10 +872,12 @@ int ak_init_fields(ak_case *c, const double *rho, const double *u) {
         k_init_fields<S><<<(unsigned)blocks_for(n, 256), 256, 0, c->stream>>>(src_of<S>(c), c->G, c->staging,
                                                                                c->staging + n);
         AK_CUDA(cudaGetLastError());
+        if (c->farfield == AK_FARFIELD_EXTERIOR) return exterior_prepare<S>(c);
         return AK_OK;
     }));
     AK_CUDA(cudaStreamSynchronize(c->stream));
-    c->prepared = false;
+    c->prepared = c->farfield == AK_FARFIELD_EXTERIOR;
+    c->steps = 0;
     return AK_OK;
 }
 
@@ -863,14 +1000,18 @@ int ak_diagnostics(ak_case *c, double *diag) {
     AK_TRY(check_case(c));
     if (!diag) return fail(AK_ERR_INVALID, "null output");
     const int nb = 152 * 4;
-    AK_TRY(ensure_partials(c, (long long)nb * 6));
+    const int ring_rows = c->farfield == AK_FARFIELD_EXTERIOR ? 64 : 0;
+    AK_TRY(ensure_partials(c, (long long)(nb + ring_rows) * 6));
     AK_TRY(with_storage(c, [&](auto *tag) {
         using S = std::remove_pointer_t<decltype(tag)>;
         k_diagnostics<S><<<nb, 256, 0, c->stream>>>(src_of<S>(c), c->G, c->flags, c->partials);
+        if (ring_rows)
+            k_ext_ring_diagnostics<S><<<ring_rows, 256, 0, c->stream>>>(src_of<S>(c), c->G, c->ext,
+                                                                         c->partials + (long long)nb * 6);
         AK_CUDA(cudaGetLastError());
         return AK_OK;
     }));
-    k_diagnostics_final<<<1, REDUCE_THREADS, 0, c->stream>>>(c->partials, nb, c->reduced);
+    k_diagnostics_final<<<1, REDUCE_THREADS, 0, c->stream>>>(c->partials, nb + ring_rows, c->reduced);
     AK_CUDA(cudaGetLastError());
     double r[6];
     AK_CUDA(cudaMemcpyAsync(r, c->reduced, sizeof r, cudaMemcpyDeviceToHost, c->stream));
@@ -942,9 +1083,52 @@ int ak_set_pdf(ak_case *c, const double *pdf) {
 
 // ---- outer-boundary history for checkpoints
 namespace {
+// exterior state: ring populations (ring cell, z, 27), the current band state,
+// the glancing rows' initial invariant and the running sums
+long long exterior_values(const ak_case *c) {
+    const ExtGeom &E = c->ext;
+    return (long long)E.nring * E.nz * Q + 4LL * E.nband * E.nz + 2LL * E.NX * E.nz + 10;
+}
+int exterior_state(ak_case *c, double *v, bool write) {
+    const ExtGeom &E = c->ext;
+    const long long nr = (long long)E.nring * E.nz, nb = 4LL * E.nband * E.nz, ni = 2LL * E.NX * E.nz;
+    AK_TRY(ensure_staging(c, (size_t)(nr * Q)));
+    if (write) {
+        for (long long k = 0; k < exterior_values(c); ++k)
+            if (!std::isfinite(v[k])) return fail(AK_ERR_INVALID, "exterior state is not finite");
+        AK_CUDA(cudaMemcpyAsync(c->staging, v, nr * Q * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    }
+    AK_TRY(with_storage(c, [&](auto *tag) {
+        using S = std::remove_pointer_t<decltype(tag)>;
+        if (write)
+            k_ext_ring_import<S><<<(unsigned)blocks_for(nr, 128), 128, 0, c->stream>>>(src_of<S>(c), c->G, E,
+                                                                                      c->staging);
+        else
+            k_ext_ring_export<S><<<(unsigned)blocks_for(nr, 128), 128, 0, c->stream>>>(src_of<S>(c), c->G, E,
+                                                                                      c->staging);
+        AK_CUDA(cudaGetLastError());
+        return AK_OK;
+    }));
+    const cudaMemcpyKind kind = write ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+    double *band = c->ext_band[c->ext_cur];
+    if (write) {
+        AK_CUDA(cudaMemcpyAsync(band, v + nr * Q, nb * sizeof(double), kind, c->stream));
+        AK_CUDA(cudaMemcpyAsync(c->ext_inc0, v + nr * Q + nb, ni * sizeof(double), kind, c->stream));
+        AK_CUDA(cudaMemcpyAsync(c->ext_out, v + nr * Q + nb + ni, 10 * sizeof(double), kind, c->stream));
+    } else {
+        AK_CUDA(cudaMemcpyAsync(v, c->staging, nr * Q * sizeof(double), kind, c->stream));
+        AK_CUDA(cudaMemcpyAsync(v + nr * Q, band, nb * sizeof(double), kind, c->stream));
+        AK_CUDA(cudaMemcpyAsync(v + nr * Q + nb, c->ext_inc0, ni * sizeof(double), kind, c->stream));
+        AK_CUDA(cudaMemcpyAsync(v + nr * Q + nb + ni, c->ext_out, 10 * sizeof(double), kind, c->stream));
+    }
+    AK_CUDA(cudaStreamSynchronize(c->stream));
+    return AK_OK;
+}
+
 long long boundary_values(const ak_case *c) {
     if (c->farfield == AK_FARFIELD_CHARACTERISTIC) return 1 + 3 * c->nouter + 2LL * c->nx * c->nz;
     if (c->farfield == AK_FARFIELD_LEGACY) return 1 + 2 * c->n_out;
+    if (c->farfield == AK_FARFIELD_EXTERIOR) return 1 + exterior_values(c);
     return 1;
 }
 int boundary_rows(ak_case *c, std::vector<int32_t> &rows) {
@@ -999,6 +1183,8 @@ int ak_get_boundary_state(ak_case *c, int32_t *rows, double *values) {
         AK_CUDA(cudaMemcpy(v + 3 * n + rows_n, c->ff_hi, rows_n * sizeof(double), cudaMemcpyDeviceToHost));
     } else if (c->farfield == AK_FARFIELD_LEGACY && c->n_out) {
         AK_CUDA(cudaMemcpy(v, c->out_state, 2 * c->n_out * sizeof(double), cudaMemcpyDeviceToHost));
+    } else if (c->farfield == AK_FARFIELD_EXTERIOR) {
+        AK_TRY(exterior_state(c, v, false));
     }
     return AK_OK;
 }
@@ -1030,8 +1216,20 @@ int ak_set_boundary_state(ak_case *c, const int32_t *rows, const double *values)
         AK_CUDA(cudaMemcpy(c->ff_hi, v + 3 * n + rows_n, rows_n * sizeof(double), cudaMemcpyHostToDevice));
     } else if (c->farfield == AK_FARFIELD_LEGACY && c->n_out) {
         AK_CUDA(cudaMemcpy(c->out_state, v, 2 * c->n_out * sizeof(double), cudaMemcpyHostToDevice));
+    } else if (c->farfield == AK_FARFIELD_EXTERIOR) {
+        if (values[0] == 0.0) return fail(AK_ERR_INVALID, "an exterior checkpoint holds a prepared state");
+        AK_TRY(exterior_state(c, const_cast<double *>(v), true));
     }
     c->prepared = values[0] != 0.0;
+    return AK_OK;
+}
+
+int ak_exterior_report(ak_case *c, double *out) {
+    AK_TRY(check_case(c));
+    if (!out) return fail(AK_ERR_INVALID, "null output");
+    if (c->farfield != AK_FARFIELD_EXTERIOR) return fail(AK_ERR_INVALID, "not an exterior case");
+    AK_CUDA(cudaMemcpyAsync(out, c->ext_out, 11 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    AK_CUDA(cudaStreamSynchronize(c->stream));
     return AK_OK;
 }
 

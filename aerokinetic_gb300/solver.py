@@ -21,7 +21,7 @@ import numpy as np
 
 from . import _native
 from ._native import NumericalFailure, check
-from .config import Flow, Grid, Plan
+from .config import EXTERIOR_FARFIELD, Flow, Grid, Plan
 from .geometry import Section
 from .project import Project, RunSettings, write_json
 
@@ -70,6 +70,16 @@ class Solver:
         self._progress("Building the D3Q27 cumulant case on the GPU")
         self._lib = _native.load()
         self._case = None
+        # exterior_regularized_fd_v1 pads the physical core by one auxiliary
+        # cell in x and y, the engine's ghost layer (solver.py:36-41)
+        self._exterior = grid.farfield == EXTERIOR_FARFIELD
+        self._padding = (1, 1, 0) if self._exterior else (0, 0, 0)
+        self._storage_shape = tuple(n + 2 * p for n, p in zip(self.plan.shape, self._padding))
+        self._storage_origin = tuple(x - p * self.plan.dx for x, p in zip(self.plan.origin, self._padding[:2]))
+        self._wall_mass_exchange = 0.0
+        self._wall_mass_total = 0.0
+        self._exterior_report = None
+        self._exterior_source_total = np.zeros(4)
         self._build()
         self.steps = 0
         self.last_loads = None
@@ -126,10 +136,46 @@ class Solver:
         out = np.zeros((len(self.contours), 5)) if sample_last else None
         check(self._lib.ak_step(self._case, int(nsteps), _ptr(out) if out is not None else None))
         self.steps += int(nsteps)
+        if self._exterior:
+            self._read_exterior()
         if out is None:
             return None
         self.last_loads = self._record(out)
+        if self._exterior:
+            # solver.py:264-271: the wall mass of every step accumulates
+            self.last_loads.update(wall_mass_exchange_lattice=self._wall_mass_exchange,
+                                   wall_mass_exchange_accumulated=self._wall_mass_total,
+                                   exterior_source_mass_lattice=self._exterior_report["exterior_source_mass_momentum"][0],
+                                   exterior_source_mass_accumulated=float(self._exterior_source_total[0]))
         return self.last_loads
+
+    def _read_exterior(self):
+        """The exterior boundary's bookkeeping after the last step (exterior.py:186-200)."""
+        out = np.zeros(11)
+        check(self._lib.ak_exterior_report(self._case, _ptr(out)))
+        self._exterior_source_total = out[4:8].copy()
+        self._wall_mass_exchange = float(out[8])
+        self._wall_mass_total = float(out[9])
+        self._exterior_report = {"step": self.steps, "reconstruction_moment_error": float(out[10]),
+                                 "exterior_source_mass_momentum": out[0:4].tolist()} if self.steps else None
+
+    def boundary_diagnostics(self):
+        """Numerical exchanges of the exterior farfield, in lattice mass per step
+        (solver.py:299-310); None for the other outer boundaries.  The engine
+        stores post-collision populations, so pdf_stage differs from the
+        reference's pre-collision storage."""
+        if not self._exterior:
+            return None
+        self._read_exterior()
+        return {"model": EXTERIOR_FARFIELD, "pdf_stage": "post_collision",
+                "physical_shape": tuple(self.plan.shape), "storage_shape": self._storage_shape,
+                "storage_origin": self._storage_origin,
+                "wall_mass_exchange_lattice": self._wall_mass_exchange,
+                "wall_mass_exchange_accumulated": self._wall_mass_total,
+                "exterior_source_mass_momentum_accumulated": self._exterior_source_total.tolist(),
+                "last_exterior_step": self._exterior_report,
+                "definition": "Wall incoming-minus-outgoing mass and explicit auxiliary PDF source; a closed "
+                              "bookkeeping budget does not prove zero wall mass flux or accuracy."}
 
     def _record(self, per_element):
         """The sample-step record of solver.py:262-279 from per-element lattice loads."""
@@ -260,6 +306,10 @@ class Solver:
                     "start_t_star": self.steps * self.plan.dt_convective, "storage": self.storage,
                     "resume_supported": True}
         names = ["step", "t_star", "time_s", "cl", "cd", "cm", "local_mach_max", "density_error_max"]
+        if self._exterior:
+            names.extend(("wall_mass_exchange_lattice", "wall_mass_exchange_accumulated",
+                          "exterior_source_mass_lattice", "exterior_source_mass_accumulated"))
+            metadata["boundary_model"] = self.boundary_diagnostics()
         rows = []
         if resume:
             old = json.loads((output / "metadata.json").read_text(encoding="utf-8"))
@@ -386,6 +436,11 @@ class Solver:
                        "wall_fallback_links": self.wall_fallback_links, "experimental_validation": "not_performed"}
             summary.update(control.summary(reason))
             control.close()
+            if self._exterior:
+                boundary = json.loads(json.dumps(self.boundary_diagnostics(), allow_nan=True),
+                                      parse_constant=lambda value: None)
+                summary["boundary_diagnostics"] = boundary
+                metadata["boundary_model"] = boundary
             metadata["status"] = state
             metadata["termination_reason"] = reason
             write_json(output / "metadata.json", metadata)

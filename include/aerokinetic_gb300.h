@@ -53,6 +53,8 @@ extern "C" {
 
 #define AK_FARFIELD_LEGACY 0          /* UBB + ExtrapolationOutflow (solver.py:130-135) */
 #define AK_FARFIELD_CHARACTERISTIC 1  /* characteristic_transport_v1 (farfield.py) */
+#define AK_FARFIELD_EXTERIOR 2        /* exterior_regularized_fd_v1 (exterior.py): the ghost layer is an
+                                         auxiliary ring rebuilt each step from a predicted state */
 
 #define AK_STORAGE_F64 0  /* plain form: FP64 storage and arithmetic */
 #define AK_STORAGE_F32 1  /* FP32 arithmetic, FP32 (f - w) storage */
@@ -151,6 +153,20 @@ int ak_set_pdf(ak_case *c, const double *pdf);
 int ak_boundary_state_size(ak_case *c, int64_t *n_links, int64_t *n_values);
 int ak_get_boundary_state(ak_case *c, int32_t *rows, double *values);
 int ak_set_boundary_state(ak_case *c, const int32_t *rows, const double *values);
+/* exterior_regularized_fd_v1 bookkeeping (solver.py:262-271, 299-309):
+ * out[0..3] = the last step's exterior source (mass, momentum x/y/z: the
+ * rebuilt ring populations minus the streamed ones, exterior.py:195-200),
+ * out[4..7] their running sums, out[8] the last step's wall mass exchange
+ * (incoming minus outgoing over all wall links), out[9] its running sum,
+ * out[10] the last step's reconstruction moment error (the largest departure
+ * of a rebuilt ring cell's mass or momentum from its predicted rho, rho u,
+ * exterior.py:168-170).  out holds 11 doubles.
+ * An exterior case stores post-collision populations (ak_get_pdf returns
+ * them); its initial state is prepared by ak_init_perturbed/ak_init_fields,
+ * and its checkpoint state (ring populations, ring-band macros, the initial
+ * incoming invariant of the glancing rows, these sums) travels through
+ * ak_get/set_boundary_state with no link rows. */
+int ak_exterior_report(ak_case *c, double *out);
 /* The case's two population arrays in device memory, for zero-copy views
  * (e.g. torch tensors through __cuda_array_interface__): current holds the
  * state ak_get_pdf returns, other the second copy.  Layout [q][z][y][x] with

@@ -32,7 +32,9 @@ def test_checkpoint_files_are_validated(tmp_path):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("farfield,storage", [("characteristic_transport_v1", "f64"), ("legacy", "f64"),
-                                              ("characteristic_transport_v1", "f16")])
+                                              ("characteristic_transport_v1", "f16"),
+                                              ("exterior_regularized_fd_v1", "f64"),
+                                              ("exterior_regularized_fd_v1", "f16")])
 def test_uniform_checkpoint_continues_bit_for_bit(tmp_path, farfield, storage):
     from aerokinetic_gb300.solver import Solver
     straight = Solver(*_parts(farfield), storage=storage)
@@ -50,6 +52,11 @@ def test_uniform_checkpoint_continues_bit_for_bit(tmp_path, farfield, storage):
             # cell pulls from a solid cell is rewritten by the walls first)
             fluid = ~straight._solid_xy
             assert np.array_equal(restored.pdf()[fluid], straight.pdf()[fluid])
+            if farfield == "exterior_regularized_fd_v1":
+                # the ring, its band state and the running sums continue too
+                for k in ("wall_mass_exchange_accumulated", "exterior_source_mass_accumulated"):
+                    assert got[k] == ref[k], k
+                assert restored.boundary_diagnostics() == straight.boundary_diagnostics()
         finally:
             restored.close()
     finally:
