@@ -61,7 +61,8 @@ class CaseDesc(ctypes.Structure):
                 ("origin_x", ctypes.c_double), ("origin_y", ctypes.c_double), ("dx", ctypes.c_double),
                 ("omega_shear", ctypes.c_double), ("omega_bulk", ctypes.c_double), ("speed", ctypes.c_double),
                 ("farfield", ctypes.c_int32), ("storage", ctypes.c_int32), ("n_elements", ctypes.c_int32),
-                ("element_sizes", ctypes.POINTER(ctypes.c_int32)), ("polygon_xy", ctypes.POINTER(ctypes.c_double))]
+                ("element_sizes", ctypes.POINTER(ctypes.c_int32)), ("polygon_xy", ctypes.POINTER(ctypes.c_double)),
+                ("smagorinsky", ctypes.c_double)]
 
 
 class RefinedDesc(ctypes.Structure):

@@ -22,6 +22,7 @@ struct BatchCase {
     const uint8_t *flags;
     Grid G;
     typename Store<S>::T omega_s, omega_b;
+    Sgs<typename Store<S>::T> sgs;  // Smagorinsky constants (c18 = 0: molecular viscosity)
     int cur0;  // copy holding the case's state at batch parity 0
     int n_elements;
     double ox, oy;
@@ -113,7 +114,7 @@ __global__ void __launch_bounds__(TB, Store<S>::MIN_BLOCKS * 128 / TB)
         const int x = bx * TB + threadIdx.x + 1;
         if (x <= G.nx)
             stream_collide_cell(c.pdf[c.cur0 ^ parity], c.pdf[c.cur0 ^ parity ^ 1], c.flags, G, G.shift, c.omega_s,
-                                c.omega_b, x, y, z);
+                                c.omega_b, x, y, z, c.sgs);
     }
 }
 

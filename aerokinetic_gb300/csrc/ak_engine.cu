@@ -54,6 +54,7 @@ struct ak_case {
     // description
     int nx = 0, ny = 0, nz = 0;
     double origin_x = 0, origin_y = 0, dx = 0, omega_s = 0, omega_b = 1, speed = 0;
+    double smagorinsky = 0;  // subgrid constant C of the bulk collision (0: molecular viscosity)
     double ox = 0, oy = 0;  // origin / dx, the lever-arm offset of solver.py:239-240
     int farfield = 0, storage = 0, n_elements = 0;
     std::vector<int> poly_start, poly_count;
@@ -467,6 +468,18 @@ void mark(ak_case *c) {
     c->timing->push_back(e);
 }
 
+// the bulk collision's subgrid constants: tau0 = 1/omega and 18 C^2
+template <typename S>
+Sgs<typename Store<S>::T> sgs_of(const ak_case *c) {
+    Sgs<typename Store<S>::T> m;
+    if (c->smagorinsky > 0.0) {
+        using R = typename SgsReal<typename Store<S>::T>::type;
+        m.tau0 = R(1.0 / c->omega_s);
+        m.c18 = R(18.0 * c->smagorinsky * c->smagorinsky);
+    }
+    return m;
+}
+
 template <typename S>
 int exterior_step(ak_case *c, double *fixed_partials, long long fixed_capacity);
 
@@ -544,7 +557,7 @@ int one_step(ak_case *c, bool sample, double *fixed_partials = nullptr, long lon
     mark(c);
     dim3 grid((unsigned)blocks_for(c->nx, 128), (unsigned)c->ny, (unsigned)c->nz);
     k_stream_collide<S><<<grid, 128, 0, c->stream>>>(src, dst_of<S>(c), c->flags, c->G, c->shift_host,
-                                                     (T)c->omega_s, (T)c->omega_b);
+                                                     (T)c->omega_s, (T)c->omega_b, sgs_of<S>(c));
     AK_CUDA(cudaGetLastError());
     ++c->launches;
     mark(c);
@@ -605,7 +618,7 @@ int exterior_step(ak_case *c, double *fixed_partials, long long fixed_capacity) 
     mark(c);
     dim3 grid((unsigned)blocks_for(c->nx, 128), (unsigned)c->ny, (unsigned)c->nz);
     k_stream_collide<S><<<grid, 128, 0, c->stream>>>(src, dst, c->flags, c->G, c->shift_host, (T)c->omega_s,
-                                                     (T)c->omega_b);
+                                                     (T)c->omega_b, Sgs<T>{});
     AK_CUDA(cudaGetLastError());
     mark(c);
     k_ext_final<<<1, REDUCE_THREADS, 0, c->stream>>>(c->ext_partials, rb, c->reduced, c->n_elements, c->ext_out);
@@ -717,6 +730,7 @@ int create_lattice(const ak_case_desc *desc, int farfield, bool periodic_xy, ak_
     c->oy = desc->origin_y / desc->dx;
     c->omega_s = desc->omega_shear;
     c->omega_b = desc->omega_bulk;
+    c->smagorinsky = desc->smagorinsky;
     c->speed = desc->speed;
     c->farfield = farfield;
     c->periodic_xy = periodic_xy;
@@ -798,6 +812,10 @@ int validate_desc(const ak_case_desc *desc, bool need_elements) {
         desc->farfield != AK_FARFIELD_EXTERIOR)
         return fail(AK_ERR_INVALID, "unknown farfield");
     if (desc->storage < AK_STORAGE_F64 || desc->storage > AK_STORAGE_DF64) return fail(AK_ERR_INVALID, "unknown storage");
+    if (!(desc->smagorinsky >= 0.0 && desc->smagorinsky < 0.3))
+        return fail(AK_ERR_INVALID, "the Smagorinsky constant must lie in [0, 0.3)");
+    if (desc->smagorinsky > 0.0 && desc->farfield == AK_FARFIELD_EXTERIOR)
+        return fail(AK_ERR_INVALID, "Exterior FD currently supports molecular viscosity with sgs=none only");
     if ((need_elements && desc->n_elements < 1) || desc->n_elements > MAX_ELEMENTS ||
         (desc->n_elements && (!desc->element_sizes || !desc->polygon_xy)))
         return fail(AK_ERR_INVALID, "between 1 and 8 polygons are required");
@@ -1686,6 +1704,7 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
     const ak_case_desc &cd = desc->coarse;
     AK_TRY(validate_desc(&cd, true));
     if (cd.farfield != AK_FARFIELD_LEGACY) return fail(AK_ERR_INVALID, "the refined solver uses the legacy outer boundary");
+    if (cd.smagorinsky != 0.0) return fail(AK_ERR_INVALID, "Refined SGS is not implemented; select sgs=none explicitly");
     for (int a = 0; a < 3; ++a)
         if (desc->box_lower[a] < 0 || desc->box_upper[a] <= desc->box_lower[a])
             return fail(AK_ERR_INVALID, "fine-box bounds must have 0 <= lower < upper");
@@ -2141,6 +2160,7 @@ int batch_build(ak_batch *B) {
         d.flags = c->flags;
         d.G = c->G;
         d.omega_s = (typename Store<S>::T)c->omega_s;
+        d.sgs = sgs_of<S>(c);
         d.omega_b = (typename Store<S>::T)c->omega_b;
         d.cur0 = B->cur0[i];
         d.n_elements = c->n_elements;

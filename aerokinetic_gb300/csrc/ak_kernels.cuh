@@ -79,7 +79,8 @@ template <typename S, typename Shift>
 __device__ __forceinline__ void stream_collide_cell(const S *__restrict__ src, S *__restrict__ dst,
                                                     const uint8_t *__restrict__ flags, const Grid &G,
                                                     const Shift &shift, typename Store<S>::T omega_s,
-                                                    typename Store<S>::T omega_b, int x, int y, int z) {
+                                                    typename Store<S>::T omega_b, int x, int y, int z,
+                                                    const Sgs<typename Store<S>::T> &sgs) {
     using T = typename Store<S>::T;
     // the column flag only gates the stores, so the 27 loads issue at once
     const bool fluid = __ldg(flags + y * G.nxp + x) == FLAG_FLUID;
@@ -91,7 +92,7 @@ __device__ __forceinline__ void stream_collide_cell(const S *__restrict__ src, S
                    ? Store<S>::load(src + q * G.qs + G.cell(x - cx(q), y - cy(q), zs), q, shift_at(shift, q))
                    : T(0);
     }
-    collide_stored<S>(g, omega_s, omega_b);
+    collide_stored<S>(g, omega_s, omega_b, sgs);
     if (!fluid) return;
     const long long c = G.cell(x, y, z);
 #pragma unroll
@@ -101,12 +102,13 @@ __device__ __forceinline__ void stream_collide_cell(const S *__restrict__ src, S
 template <typename S>
 __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
     k_stream_collide(const S *__restrict__ src, S *__restrict__ dst, const uint8_t *__restrict__ flags, Grid G,
-                     Shift27 shift, typename Store<S>::T omega_s, typename Store<S>::T omega_b) {
+                     Shift27 shift, typename Store<S>::T omega_s, typename Store<S>::T omega_b,
+                     Sgs<typename Store<S>::T> sgs) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int y = blockIdx.y + 1;
     const int z = blockIdx.z;
     if (x > G.nx) return;
-    stream_collide_cell(src, dst, flags, G, shift, omega_s, omega_b, x, y, z);
+    stream_collide_cell(src, dst, flags, G, shift, omega_s, omega_b, x, y, z, sgs);
 }
 
 // ------------------------------------------------------------ walls

@@ -119,8 +119,31 @@ struct Shift27 {
 };
 
 // ---------------------------------------------------------------- collision
+// Smagorinsky subgrid model (sgs="smagorinsky", solver.py:74-77; Hou,
+// Sterling, Chen & Doolen 1996 in lattice units): with the non-equilibrium
+// second moments Pi_ab = K_ab - rho/3 delta_ab (K the central moments) and
+// |Pi| = sqrt(2 Pi:Pi) / rho, the cell's shear rate is
+// 2 / (tau0 + sqrt(tau0^2 + 18 C^2 |Pi|)), tau0 = 1/omega the molecular
+// relaxation time.  c18 = 18 C^2; c18 = 0 keeps the molecular rate.  The
+// double-float form evaluates the rate in FP64 (a few operations per cell).
+template <typename T> struct SgsReal { using type = T; };
+template <> struct SgsReal<df64> { using type = double; };
 template <typename T>
-__host__ __device__ __forceinline__ void collide(T g[Q], T omega_s, T omega_b) {
+struct Sgs {
+    typename SgsReal<T>::type tau0 = 0, c18 = 0;
+};
+template <typename T>
+__host__ __device__ __forceinline__ T smagorinsky_rate(const Sgs<T> &m, T rinv, T pxx, T pyy, T pzz, T pxy, T pxz,
+                                                      T pyz) {
+    using R = typename SgsReal<T>::type;
+    const R a = R(pxx), b = R(pyy), c = R(pzz), d = R(pxy), e = R(pxz), f = R(pyz);
+    const R ss = (a * a + b * b + c * c) + R(2) * (d * d + e * e + f * f);
+    const R norm = sqrt(R(2) * ss) * R(rinv);
+    return T(R(2) / (m.tau0 + sqrt(m.c18 * norm + m.tau0 * m.tau0)));
+}
+
+template <typename T>
+__host__ __device__ __forceinline__ void collide(T g[Q], T omega_s, T omega_b, const Sgs<T> &sgs = Sgs<T>{}) {
     // raw moments of g up to second order through partial line sums
     T Z0[3][3], Z1[3][3], Z2[3][3];
 #pragma unroll
@@ -159,14 +182,15 @@ __host__ __device__ __forceinline__ void collide(T g[Q], T omega_s, T omega_b) {
     // second-order central moments minus their rest value 1/3
     const T kdx = M200 - jx * ux, kdy = M020 - jy * uy, kdz = M002 - jz * uz;
     const T kxy = M110 - jx * uy, kxz = M101 - jx * uz, kyz = M011 - jy * uz;
-    const T om1 = T(1) - omega_s;
+    const T third = T(1) / T(3);
+    const T d3 = drho * third;
+    const T om1 = T(1) - (sgs.c18 > 0 ? smagorinsky_rate(sgs, rinv, kdx - d3, kdy - d3, kdz - d3, kxy, kxz, kyz)
+                                      : omega_s);
     const T P1 = om1 * (kdx - kdy), P2 = om1 * (kdx - kdz);
     const T S = kdx + kdy + kdz;
     const T tr = S + omega_b * (drho - S);
-    const T third = T(1) / T(3);
     const T kx = (P1 + P2 + tr) * third;
     const T ky = kx - P1, kz = kx - P2;
-    const T d3 = drho * third;
     const T sig[3] = {(kx - d3) * rinv, (ky - d3) * rinv, (kz - d3) * rinv};
     const T sxy = om1 * kxy * rinv, sxz = om1 * kxz * rinv, syz = om1 * kyz * rinv;
     const T u[3] = {ux, uy, uz};
@@ -217,7 +241,7 @@ __host__ __device__ __forceinline__ void collide(T g[Q], T omega_s, T omega_b) {
 // first along x for A, B, C of every c_y, then along z with rho folded into
 // the z-functions.  About 370 FP64 operations per cell.
 template <typename T>
-__host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b) {
+__host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b, const Sgs<T> &sgs = Sgs<T>{}) {
     T Z0[3][3], Z1[3][3], Z2[3][3];
 #pragma unroll
     for (int ix = 0; ix < 3; ++ix)
@@ -254,9 +278,14 @@ __host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b) 
     const T ux = jx * rinv, uy = jy * rinv, uz = jz * rinv;
     // second-order central moments minus 1/3, relaxed
     const T kdx = M200 - jx * ux, kdy = M020 - jy * uy, kdz = M002 - jz * uz;
+    const T third = T(1.0 / 3.0);
+    if (sgs.c18 > 0) {
+        const T d3 = drho * third;
+        om1 = T(1) - smagorinsky_rate(sgs, rinv, kdx - d3, kdy - d3, kdz - d3, M110 - jx * uy, M101 - jx * uz,
+                                      M011 - jy * uz);
+    }
     const T P1 = om1 * (kdx - kdy), P2 = om1 * (kdx - kdz);
     const T S = kdx + kdy + kdz;
-    const T third = T(1.0 / 3.0);
     const T kx = (P1 + P2 + (S + omega_b * (drho - S))) * third;
     // normalised covariance: s_aa = (1/3 + k_a) / rho; t_a = u_a^2 + s_aa
     const T r3 = third * rinv;
@@ -324,12 +353,13 @@ __host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b) 
 // the small deviations it stores.
 template <typename S>
 __host__ __device__ __forceinline__ void collide_stored(typename Store<S>::T g[Q], typename Store<S>::T omega_s,
-                                                        typename Store<S>::T omega_b) {
+                                                        typename Store<S>::T omega_b,
+                                                        const Sgs<typename Store<S>::T> &sgs = {}) {
     using T = typename Store<S>::T;
     if constexpr (sizeof(S) == sizeof(float))
-        collide<T>(g, omega_s, omega_b);
+        collide<T>(g, omega_s, omega_b, sgs);
     else
-        collide_full<T>(g, T(1) - omega_s, omega_b);
+        collide_full<T>(g, T(1) - omega_s, omega_b, sgs);
 }
 
 }  // namespace ak

@@ -95,7 +95,8 @@ class Solver:
                                 self.plan.relaxation_rate, 1.0, self.flow.lattice_speed,
                                 _native.FARFIELD[self.grid.farfield], _native.STORAGE[self.storage],
                                 len(self.contours), sizes.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
-                                xy.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+                                xy.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                self.flow.smagorinsky_constant if self.flow.sgs == "smagorinsky" else 0.0)
         handle = ctypes.c_void_p()
         check(self._lib.ak_case_create(ctypes.byref(desc), ctypes.byref(handle)))
         self._case = handle

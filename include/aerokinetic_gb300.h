@@ -76,6 +76,8 @@ typedef struct {
     int32_t n_elements;          /* number of polygons (wall elements) */
     const int32_t *element_sizes;/* vertices per polygon */
     const double *polygon_xy;    /* all vertices, (x, y) pairs, normalised frame */
+    double smagorinsky;          /* Smagorinsky constant C of sgs="smagorinsky" (solver.py:74-77), 0 for
+                                    molecular viscosity; uniform legacy/characteristic cases only */
 } ak_case_desc;
 
 typedef struct {

@@ -24,7 +24,8 @@
  *   - compressible UBB (solver.py:131) and ExtrapolationOutflow after Geier
  *     et al. 2015 appendix F (solver.py:133-135);
  *   - the characteristic farfield of farfield.py:144-206;
- *   - momentum-exchange loads of solver.py:204-250.
+ *   - momentum-exchange loads of solver.py:204-250;
+ *   - the Smagorinsky shear rate of sgs="smagorinsky" (solver.py:74-77).
  *
  * Layout: every population array is (NX, NY, NZ, 27) C-order doubles with one
  * ghost layer, NX = nx+2 etc., exactly the reference's pdf[x, y, z, d] view
@@ -98,8 +99,24 @@ static inline void backward_line(double *m, double u) {
     m[0] = 0.5 * (m0 * (u * u - u) + m1 * (2.0 * u - 1.0) + m2);
 }
 
-/* Cumulant collision of one cell, in place on zero-centred populations g. */
-static void collide_cell(double *g, double omega_s, double omega_b) {
+/* Smagorinsky shear rate of one cell (solver.py:74-77 selects lbmpy's
+ * SMAGORINSKY subgrid model for sgs="smagorinsky"; the model is Hou, Sterling,
+ * Chen & Doolen 1996 in its lattice form): with the non-equilibrium second
+ * moments Pi_ab = K_ab - rho/3 delta_ab (K the central moments) and
+ * |Pi| = sqrt(2 Pi:Pi) / rho, the effective relaxation time is
+ * tau = (tau0 + sqrt(tau0^2 + 18 C^2 |Pi|)) / 2 with tau0 = 1/omega, the
+ * molecular value.  c18 = 18 C^2; 0 keeps the molecular rate. */
+static double smagorinsky_rate(double omega, double c18, double rho, double pxx, double pyy, double pzz,
+                               double pxy, double pxz, double pyz) {
+    const double tau0 = 1.0 / omega;
+    const double norm = sqrt(2.0 * (pxx * pxx + pyy * pyy + pzz * pzz + 2.0 * (pxy * pxy + pxz * pxz + pyz * pyz))) /
+                        rho;
+    return 2.0 / (tau0 + sqrt(c18 * norm + tau0 * tau0));
+}
+
+/* Cumulant collision of one cell, in place on zero-centred populations g;
+ * c18 > 0 replaces omega_s by the cell's Smagorinsky rate. */
+static void collide_cell_sgs(double *g, double omega_s, double omega_b, double c18) {
     double K[3][3][3];
     double drho = 0.0, j[3] = {0.0, 0.0, 0.0};
     for (int q = 0; q < Q; ++q) {
@@ -132,6 +149,9 @@ static void collide_cell(double *g, double omega_s, double omega_b) {
      * deviatoric combinations with omega_s and the trace with omega_b towards
      * rho*cs^2 per diagonal entry */
     double kxx = K[2][0][0], kyy = K[0][2][0], kzz = K[0][0][2];
+    if (c18 > 0.0)
+        omega_s = smagorinsky_rate(omega_s, c18, rho, kxx - rho / 3.0, kyy - rho / 3.0, kzz - rho / 3.0, K[1][1][0],
+                                   K[1][0][1], K[0][1][1]);
     double d1 = (1.0 - omega_s) * (kxx - kyy);
     double d2 = (1.0 - omega_s) * (kxx - kzz);
     double tr = kxx + kyy + kzz;
@@ -186,9 +206,16 @@ static void collide_cell(double *g, double omega_s, double omega_b) {
     for (int q = 0; q < Q; ++q) g[q] = K[CV[q][0] + 1][CV[q][1] + 1][CV[q][2] + 1] - W[q];
 }
 
+static void collide_cell(double *g, double omega_s, double omega_b) { collide_cell_sgs(g, omega_s, omega_b, 0.0); }
+
 void ako_collide_cells(double *g, int64_t n, double omega_s, double omega_b) {
     init_tables();
     for (int64_t i = 0; i < n; ++i) collide_cell(g + Q * i, omega_s, omega_b);
+}
+
+void ako_collide_cells_sgs(double *g, int64_t n, double omega_s, double omega_b, double c18) {
+    init_tables();
+    for (int64_t i = 0; i < n; ++i) collide_cell_sgs(g + Q * i, omega_s, omega_b, c18);
 }
 
 #define IDX(x, y, z) ((((int64_t)(x) * NY + (y)) * NZ + (z)) * Q)
@@ -196,8 +223,8 @@ void ako_collide_cells(double *g, int64_t n, double omega_s, double omega_b) {
 /* Pull-stream every interior cell from src, collide, write dst (the reference's
  * "stream_collide" kernel; solid cells are updated too, as the generated kernel
  * does, and their values are never read by the fluid). */
-void ako_stream_collide(const double *src, double *dst, int nx, int ny, int nz, double omega_s,
-                        double omega_b, int threads) {
+void ako_stream_collide_sgs(const double *src, double *dst, int nx, int ny, int nz, double omega_s,
+                            double omega_b, double c18, int threads) {
     init_tables();
     const int NY = ny + 2, NZ = nz + 2;
 #ifdef _OPENMP
@@ -209,9 +236,14 @@ void ako_stream_collide(const double *src, double *dst, int nx, int ny, int nz, 
             for (int z = 1; z <= nz; ++z) {
                 double g[Q];
                 for (int q = 0; q < Q; ++q) g[q] = src[IDX(x - CV[q][0], y - CV[q][1], z - CV[q][2]) + q];
-                collide_cell(g, omega_s, omega_b);
+                collide_cell_sgs(g, omega_s, omega_b, c18);
                 memcpy(dst + IDX(x, y, z), g, sizeof g);
             }
+}
+
+void ako_stream_collide(const double *src, double *dst, int nx, int ny, int nz, double omega_s,
+                        double omega_b, int threads) {
+    ako_stream_collide_sgs(src, dst, nx, ny, nz, omega_s, omega_b, 0.0, threads);
 }
 
 /* Only the "collide" half, in place (refined levels order collide, stream). */

@@ -39,7 +39,9 @@ _D = ctypes.c_double
 _SIGNATURES = {
     "ako_stencil": [_P, _P, _P],
     "ako_collide_cells": [_P, _L, _D, _D],
+    "ako_collide_cells_sgs": [_P, _L, _D, _D, _D],
     "ako_stream_collide": [_P, _P, _I, _I, _I, _D, _D, _I],
+    "ako_stream_collide_sgs": [_P, _P, _I, _I, _I, _D, _D, _D, _I],
     "ako_collide": [_P, _I, _I, _I, _D, _D, _I],
     "ako_stream": [_P, _P, _I, _I, _I],
     "ako_sync_periodic": [_P, _I, _I, _I, _I, _I, _I],
@@ -119,11 +121,20 @@ def macros(g):
     return rho, u
 
 
-def collide(g, omega_s, omega_b=1.0):
-    """Cumulant collision of independent cells (...,27), returning a new array."""
+def collide(g, omega_s, omega_b=1.0, smagorinsky=0.0):
+    """Cumulant collision of independent cells (...,27), returning a new array;
+    smagorinsky > 0 (the constant C) uses each cell's Smagorinsky shear rate."""
     out = np.array(g, dtype=np.float64, order="C", copy=True)
-    lib().ako_collide_cells(_p(out), out.size // 27, omega_s, omega_b)
+    if smagorinsky > 0:
+        lib().ako_collide_cells_sgs(_p(out), out.size // 27, omega_s, omega_b, sgs_c18(smagorinsky))
+    else:
+        lib().ako_collide_cells(_p(out), out.size // 27, omega_s, omega_b)
     return out
+
+
+def sgs_c18(constant):
+    """18 C^2 of the Smagorinsky rate, 0 for molecular viscosity."""
+    return 18.0 * float(constant) ** 2 if constant else 0.0
 
 
 # ---------------------------------------------------------------- geometry
@@ -185,6 +196,7 @@ class Lattice:
         self.flags = np.zeros((nx + 2, ny + 2, nz + 2), np.int16)
         self.boundaries = []
         self.steps = 0
+        self.smagorinsky = 0.0  # Smagorinsky constant C of the bulk collision (0: molecular viscosity)
 
     def midpoints(self):
         nx, ny, nz = self.shape
@@ -248,8 +260,8 @@ class Lattice:
 
     def stream_collide(self):
         nx, ny, nz = self.shape
-        lib().ako_stream_collide(_p(self.pdf), _p(self.tmp), nx, ny, nz, self.omega_s, self.omega_b,
-                                 self.threads)
+        lib().ako_stream_collide_sgs(_p(self.pdf), _p(self.tmp), nx, ny, nz, self.omega_s, self.omega_b,
+                                     sgs_c18(self.smagorinsky), self.threads)
         self.pdf, self.tmp = self.tmp, self.pdf
 
     def step(self, before_stream=None):
@@ -394,7 +406,7 @@ class AirfoilCase:
     """
 
     def __init__(self, contours, shape, origin, dx, span, omega, speed, chord_cells, farfield="legacy",
-                 perturbation=1e-4, seed=31, leading=(0.0, 0.0), threads=0):
+                 perturbation=1e-4, seed=31, leading=(0.0, 0.0), threads=0, smagorinsky=0.0):
         self.contours = [np.asarray(cn, dtype=np.float64) for cn in contours]
         self.shape = tuple(shape)
         self.origin = tuple(origin)
@@ -404,6 +416,7 @@ class AirfoilCase:
         self.chord_cells = int(chord_cells)
         self.farfield = farfield
         self.lattice = Lattice(shape, (False, False, True), omega, 1.0, threads)
+        self.lattice.smagorinsky = float(smagorinsky)
         self.wall_fallback_links = 0
         self._install(farfield)
         self._initialise(perturbation, seed, leading)

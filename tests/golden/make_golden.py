@@ -182,6 +182,11 @@ def main():
         histories[name] = {"project": project, "source": path,
                            "history": [{k: (int(r[k]) if k == "step" else float(r[k]))
                                         for k in ("step", "cl", "cd", "cm")} for r in rows]}
+    # the recorded Smagorinsky (sgs="smagorinsky") run: demo_wake/ was written
+    # from examples/naca0012_wake_demo.json (demo_wake/README_RU.md)
+    project = json.loads((ref / "examples/naca0012_wake_demo.json").read_text())
+    histories["smagorinsky_wake"] = {"project": project, "source": "demo_wake; examples/naca0012_wake_demo.json",
+                                     "history": read_history(ref / "demo_wake/history.csv", None)}
     (HERE / "histories.json").write_text(json.dumps(histories) + "\n")
 
     profile = json.loads((ref / "docs/verification_stage1_20261106/profile_threads1.json").read_text())

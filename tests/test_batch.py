@@ -5,9 +5,9 @@ import pytest
 from aerokinetic_gb300 import Flow, Grid, Section, naca4
 
 
-def _parts(chord, alpha, reynolds, seed, farfield="characteristic_transport_v1"):
+def _parts(chord, alpha, reynolds, seed, farfield="characteristic_transport_v1", sgs="none"):
     section = Section((naca4("0012", 41),))
-    flow = Flow(reynolds=reynolds, alpha_deg=alpha, lattice_speed=0.05, seed=seed)
+    flow = Flow(reynolds=reynolds, alpha_deg=alpha, lattice_speed=0.05, seed=seed, sgs=sgs)
     grid = Grid(cells_per_chord=chord, upstream_chords=2.0, downstream_chords=3.0, transverse_chords=1.5,
                 span_chords=0.25, farfield=farfield, memory_limit_gib=8)
     return section, flow, grid
@@ -46,6 +46,31 @@ def test_batch_matches_cases_stepped_alone(storage):
             assert a.diagnostics() == b.diagnostics()
     finally:
         for s in alone + mixed:
+            s.close()
+
+
+@pytest.mark.gpu
+def test_batch_mixes_subgrid_and_molecular_cases():
+    """Cases with sgs="smagorinsky" keep their own subgrid rate inside a batch
+    beside molecular-viscosity cases: each ends bit-identical to itself alone."""
+    from aerokinetic_gb300.batch import Batch
+    from aerokinetic_gb300.solver import Solver
+    specs = [(16, 4.0, 2e4, 1, "characteristic_transport_v1", "smagorinsky"), (20, 6.0, 3e4, 4),
+             (24, -2.0, 5e4, 2, "characteristic_transport_v1", "smagorinsky")]
+    alone = [Solver(*_parts(*c), storage="f32") for c in specs]
+    mixed = [Solver(*_parts(*c), storage="f32") for c in specs]
+    plain = Solver(*_parts(*specs[0][:4]), storage="f32")
+    try:
+        with Batch(mixed) as batch:
+            records = batch.advance(12)
+        for solver, record in zip(alone, records):
+            assert solver.advance(12, sample_last=True)["cl"] == record["cl"]
+        for a, b in zip(alone, mixed):
+            assert np.array_equal(a.pdf(), b.pdf())
+        plain.advance(12)
+        assert not np.array_equal(plain.pdf(), alone[0].pdf())
+    finally:
+        for s in alone + mixed + [plain]:
             s.close()
 
 

@@ -22,8 +22,10 @@ PROGRAM = r'''
 #include <cmath>
 #include <random>
 #include "ak_lattice.cuh"
-extern "C" void ako_collide_cells(double *g, long long n, double ws, double wb);
-int main() {
+#include <cstdlib>
+extern "C" void ako_collide_cells_sgs(double *g, long long n, double ws, double wb, double c18);
+int main(int argc, char **argv) {
+    const double C = argc > 1 ? atof(argv[1]) : 0.0, c18 = 18.0 * C * C;
     std::mt19937_64 rng(5);
     std::normal_distribution<double> N(0, 1);
     double worst_full = 0, worst_dev = 0, worst_f32 = 0, worst_df = 0;
@@ -42,11 +44,20 @@ int main() {
             h[q] = ak::df64(g[q]);
         }
         double ws = 1.0 + 0.999 * (t % 100) / 100.0, wb = (t % 3 == 0) ? 1.0 : 0.7;
-        ak::collide_full<double>(a, 1.0 - ws, wb);
-        ak::collide<double>(b, ws, wb);
-        ak::collide<float>(f, (float)ws, (float)wb);
-        ak::collide_full<ak::df64>(h, ak::df64(1.0 - ws), ak::df64(wb));
-        ako_collide_cells(c, 1, ws, wb);
+        ak::Sgs<double> md;
+        ak::Sgs<float> mf;
+        ak::Sgs<ak::df64> mh;
+        if (c18 > 0) {
+            md.tau0 = mh.tau0 = 1.0 / ws;
+            md.c18 = mh.c18 = c18;
+            mf.tau0 = (float)(1.0 / ws);
+            mf.c18 = (float)c18;
+        }
+        ak::collide_full<double>(a, 1.0 - ws, wb, md);
+        ak::collide<double>(b, ws, wb, md);
+        ak::collide<float>(f, (float)ws, (float)wb, mf);
+        ak::collide_full<ak::df64>(h, ak::df64(1.0 - ws), ak::df64(wb), mh);
+        ako_collide_cells_sgs(c, 1, ws, wb, c18);
         for (int q = 0; q < 27; ++q) {
             worst_full = fmax(worst_full, fabs(a[q] - c[q]));
             worst_dev = fmax(worst_dev, fabs(b[q] - c[q]));
@@ -60,7 +71,9 @@ int main() {
 '''
 
 
-def test_device_collision_forms_match_oracle_on_host():
+@pytest.mark.parametrize("smagorinsky", [0.0, 0.1, 0.25])
+def test_device_collision_forms_match_oracle_on_host(smagorinsky):
+    """Molecular viscosity and the Smagorinsky shear rate (C = 0.1, 0.25)."""
     nvcc = _native.nvcc()
     with tempfile.TemporaryDirectory() as tmp:
         tmp = Path(tmp)
@@ -71,7 +84,7 @@ def test_device_collision_forms_match_oracle_on_host():
         subprocess.run([nvcc, "-std=c++17", "-O2", "-I", str(_native.PACKAGE / "csrc"), "-o", str(exe),
                         str(tmp / "main.cu"), str(obj), "-Xcompiler", "-fopenmp", "-lgomp", "-lm"],
                        check=True, capture_output=True)
-        out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+        out = subprocess.run([str(exe), repr(smagorinsky)], check=True, capture_output=True, text=True).stdout.split()
     full, dev, f32, df = map(float, out)
     assert full < 2e-15 and dev < 2e-15
     assert f32 < 2e-6

@@ -36,9 +36,11 @@ def oracle_for(project):
     contours = [c.xy for c in project.section.normalized(project.flow.alpha_deg)]
     lead = O.leading_edge([e.xy for e in project.section.elements], project.section.moment_reference,
                           project.section.chord, project.flow.alpha_deg)
+    smagorinsky = project.flow.smagorinsky_constant if project.flow.sgs == "smagorinsky" else 0.0
     return O.AirfoilCase(contours, plan.shape, plan.origin, plan.dx, plan.span, plan.relaxation_rate,
                          project.flow.lattice_speed, project.grid.cells_per_chord, project.grid.farfield,
-                         project.flow.perturbation, project.flow.seed, lead, oracle_threads())
+                         project.flow.perturbation, project.flow.seed, lead, oracle_threads(),
+                         smagorinsky=smagorinsky)
 
 
 def kat_project(farfield="legacy"):

@@ -69,10 +69,42 @@ def _airfoil(project, threads=None):
     contours = [c.xy for c in project.section.normalized(project.flow.alpha_deg)]
     lead = O.leading_edge([e.xy for e in project.section.elements], project.section.moment_reference,
                           project.section.chord, project.flow.alpha_deg)
+    smagorinsky = project.flow.smagorinsky_constant if project.flow.sgs == "smagorinsky" else 0.0
     case = O.AirfoilCase(contours, plan.shape, plan.origin, plan.dx, plan.span, plan.relaxation_rate,
                          project.flow.lattice_speed, project.grid.cells_per_chord, project.grid.farfield,
-                         project.flow.perturbation, project.flow.seed, lead, threads or oracle_threads())
+                         project.flow.perturbation, project.flow.seed, lead, threads or oracle_threads(),
+                         smagorinsky=smagorinsky)
     return plan, case
+
+
+def test_smagorinsky_history_first_samples(golden):
+    """The reference's recorded sgs="smagorinsky" run (demo_wake/history.csv,
+    written from examples/naca0012_wake_demo.json: 176x102x16, Re 1e4, AoA 8,
+    C = 0.1, legacy outer boundary): Cl/Cd/Cm of the first 12 samples (480
+    steps) within 2e-10, the reference's own load gate.  This record was
+    written by the reference's 0.1.0 release; its loads sit ~1e-10 from the
+    oracle's without growing, while the same run with molecular viscosity
+    departs by 6e-2 at the first sample, so the record pins the subgrid rate."""
+    record = golden["histories"]["smagorinsky_wake"]
+    project = Project.from_dict(record["project"])
+    assert project.flow.sgs == "smagorinsky" and project.flow.smagorinsky_constant == 0.1
+    plan, case = _airfoil(project)
+    assert list(plan.shape) == [176, 102, 16]
+    every = project.run.sample_every
+    for row in record["history"][:12]:
+        while case.steps < row["step"]:
+            loads = case.step(sample=(case.steps + 1) % every == 0)
+        for k in ("cl", "cd", "cm"):
+            assert loads[k] == pytest.approx(row[k], abs=2e-10), (row["step"], k)
+    lead = O.leading_edge([e.xy for e in project.section.elements], project.section.moment_reference,
+                          project.section.chord, project.flow.alpha_deg)
+    plain = O.AirfoilCase([c.xy for c in project.section.normalized(project.flow.alpha_deg)], plan.shape,
+                          plan.origin, plan.dx, plan.span, plan.relaxation_rate, project.flow.lattice_speed,
+                          project.grid.cells_per_chord, project.grid.farfield, project.flow.perturbation,
+                          project.flow.seed, lead, oracle_threads())
+    while plain.steps < every:
+        loads = plain.step(sample=plain.steps + 1 == every)
+    assert abs(loads["cl"] - record["history"][0]["cl"]) > 1e-2
 
 
 def test_failure_capture_nonlinear_startup(golden):
