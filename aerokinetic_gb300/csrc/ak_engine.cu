@@ -985,8 +985,11 @@ void *ak_case_stream(const ak_case *c) { return c ? (void *)c->stream : nullptr;
 int ak_step_timed(ak_case *c, int32_t nsteps, double *ms) {
     AK_TRY(check_case(c));
     if (nsteps < 1 || !ms) return fail(AK_ERR_INVALID, "nsteps >= 1 and an output array are required");
+    // events per step: outer boundary | walls | stream-collide; the exterior
+    // step has a fourth interval (the ring rebuild, part of its outer boundary)
+    const int marks = c->farfield == AK_FARFIELD_EXTERIOR ? 5 : 4;
     std::vector<cudaEvent_t> events;
-    events.reserve((size_t)4 * nsteps);
+    events.reserve((size_t)marks * nsteps);
     c->timing = &events;
     int r = AK_OK;
     for (int s = 0; s < nsteps && r == AK_OK; ++s)
@@ -994,17 +997,21 @@ int ak_step_timed(ak_case *c, int32_t nsteps, double *ms) {
     c->timing = nullptr;
     cudaError_t e = cudaStreamSynchronize(c->stream);
     for (int k = 0; k < 4; ++k) ms[k] = 0.0;
-    if (r == AK_OK && e == cudaSuccess && events.size() == (size_t)4 * nsteps) {
+    if (r == AK_OK && e == cudaSuccess && events.size() == (size_t)marks * nsteps) {
         float t = 0.0f;
         cudaEventElapsedTime(&t, events.front(), events.back());
         ms[0] = t;
         for (int s = 0; s < nsteps; ++s) {
-            cudaEvent_t *ev = events.data() + 4 * s;
-            cudaEventElapsedTime(&t, ev[0], ev[1]);  // outer boundary
+            cudaEvent_t *ev = events.data() + marks * s;
+            cudaEventElapsedTime(&t, ev[0], ev[1]);  // outer boundary (exterior: the predictor)
             ms[3] += t;
             cudaEventElapsedTime(&t, ev[1], ev[2]);  // walls
             ms[2] += t;
-            cudaEventElapsedTime(&t, ev[2], ev[3]);  // stream-collide
+            if (marks == 5) {
+                cudaEventElapsedTime(&t, ev[2], ev[3]);  // exterior: band state and ring rebuild
+                ms[3] += t;
+            }
+            cudaEventElapsedTime(&t, ev[marks - 2], ev[marks - 1]);  // stream-collide
             ms[1] += t;
         }
     }

@@ -44,13 +44,12 @@ UNIFORM = "uniform NACA0012 384x256x8, chord 32, AoA 4, Re 3e4, Ma 0.1, characte
 BYTES_PER_CELL = {"f64": 27 * 2 * 8, "f32": 27 * 2 * 4, "f16": 27 * 2 * 2, "df64": 27 * 2 * 8}
 
 
-def case_parts():
+def case_parts(farfield="characteristic_transport_v1", sgs="none"):
     from aerokinetic_gb300 import Flow, Grid, Section, naca0012
     section = Section((naca0012(),))
-    flow = Flow(reynolds=30000, alpha_deg=4, lattice_speed=0.1 / math.sqrt(3))
+    flow = Flow(reynolds=30000, alpha_deg=4, lattice_speed=0.1 / math.sqrt(3), sgs=sgs)
     grid = Grid(cells_per_chord=CELLS_PER_CHORD, upstream_chords=4.0, downstream_chords=6.9867,
-                transverse_chords=3.9266, span_chords=0.125, farfield="characteristic_transport_v1",
-                memory_limit_gib=64)
+                transverse_chords=3.9266, span_chords=0.125, farfield=farfield, memory_limit_gib=64)
     return section, flow, grid
 
 
@@ -223,18 +222,18 @@ def flush_l2(buf, stream):
         buf.add_(1)
 
 
-def measure_form(storage, steps, warmup, flush):
+def measure_form(storage, steps, warmup, flush, farfield="characteristic_transport_v1", sgs="none"):
     """Per-step timing of the uniform case's stream-collide kernel in one storage form."""
     import torch
     from aerokinetic_gb300.solver import Solver
-    section, flow, grid = case_parts()
+    section, flow, grid = case_parts(farfield, sgs)
     solver = Solver(section, flow, grid, storage=storage)
     lib = solver._lib
     stream = torch.cuda.ExternalStream(lib.ak_case_stream(solver._case))
     buf = torch.zeros(128 * 2**20, dtype=torch.float32, device="cuda")
     ms = np.zeros(4)
     lib.ak_step_timed(solver._case, max(1, warmup), ms.ctypes.data_as(ctypes.c_void_p))
-    bulk = total = 0.0
+    bulk = total = outer = 0.0
     for _ in range(steps):
         if flush:
             flush_l2(buf, stream)
@@ -244,10 +243,11 @@ def measure_form(storage, steps, warmup, flush):
             raise RuntimeError(lib.ak_last_error())
         total += ms[0]
         bulk += ms[1]
+        outer += ms[3]
     info = solver.info
     solver.close()
     return {"cells": info["cells"], "fluid_cells": info["fluid_cells"], "bulk_ms": bulk / steps,
-            "step_ms": total / steps}
+            "step_ms": total / steps, "outer_ms": outer / steps}
 
 
 def batch_case_parts(i, base_seed=2026):
@@ -564,6 +564,19 @@ def run_engine(args, rank, world, local_rank):
         uniform[storage] = {"mlups": m["cells"] / (m["step_ms"] / 1e3) / 1e6,
                             "kernel_mlups": m["cells"] / (m["bulk_ms"] / 1e3) / 1e6,
                             "stream_collide_ms": m["bulk_ms"], "achieved_gbs": a, "frac_of_" + peak_kind: a / hbm}
+    # the same case with the other outer boundaries and with the Smagorinsky
+    # subgrid rate (FP64 and the FP32 form)
+    for label, farfield, sgs in (("exterior", "exterior_regularized_fd_v1", "none"),
+                                 ("legacy", "legacy", "none"),
+                                 ("smagorinsky", "characteristic_transport_v1", "smagorinsky")):
+        for storage in ("f64", "f32"):
+            m = measure_form(storage, steps=min(args.steps, 50), warmup=args.warmup, flush=True, farfield=farfield,
+                             sgs=sgs)
+            a = m["fluid_cells"] * BYTES_PER_CELL[storage] / (m["bulk_ms"] / 1e3) / 1e9
+            uniform[f"{label}_{storage}"] = {"mlups": m["cells"] / (m["step_ms"] / 1e3) / 1e6,
+                                             "kernel_mlups": m["cells"] / (m["bulk_ms"] / 1e3) / 1e6,
+                                             "stream_collide_ms": m["bulk_ms"], "outer_boundary_ms": m["outer_ms"],
+                                             "achieved_gbs": a, "frac_of_" + peak_kind: a / hbm}
 
     forms["error_vs_f64"] = form_errors(project, refinement, steps=min(args.steps, 400))
     batch = run_batch(steps=min(args.steps, 100))
