@@ -84,12 +84,17 @@ __device__ __forceinline__ void stream_collide_cell(const S *__restrict__ src, S
     using T = typename Store<S>::T;
     // the column flag only gates the stores, so the 27 loads issue at once
     const bool fluid = __ldg(flags + y * G.nxp + x) == FLAG_FLUID;
+    // the cell's column in the three z planes it pulls from; a direction adds
+    // q * qs - cy * sx - cx, so each load costs one address add
+    const S *row[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) row[c] = src + (long long)G.wrapz(z - (c - 1)) * G.plane + (long long)y * G.sx + x;
     T g[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
-        const int zs = G.wrapz(z - cz(q));
-        g[q] = AK_CHECK(G, q, x - cx(q), y - cy(q), zs, 3)
-                   ? Store<S>::load(src + q * G.qs + G.cell(x - cx(q), y - cy(q), zs), q, shift_at(shift, q))
+        const long long off = (long long)q * G.qs - (long long)cy(q) * G.sx - cx(q);
+        g[q] = AK_CHECK(G, q, x - cx(q), y - cy(q), G.wrapz(z - cz(q)), 3)
+                   ? Store<S>::load(row[cz(q) + 1] + off, q, shift_at(shift, q))
                    : T(0);
     }
     collide_stored<S>(g, omega_s, omega_b, sgs);

@@ -34,29 +34,52 @@ namespace ak {
 
 constexpr int Q = 27;
 
-// lbmpy D3Q27 order
+// lbmpy D3Q27 order.  The tables are packed into 64-bit words at compile
+// time (2 bits per velocity component, 5 bits per direction index, 12
+// entries per word), so a direction known only at run time (a link's
+// direction, a loop that is not unrolled) costs a shift and a mask; a plain
+// constexpr array indexed at run time is materialised in local memory.
+struct Packed27 {
+    uint64_t w[3] = {0, 0, 0};
+    int bits = 0;
+    __host__ __device__ constexpr int get(int i) const {
+        const uint64_t word = i < 12 ? w[0] : (i < 24 ? w[1] : w[2]);
+        return (int)((word >> (bits * (i % 12))) & ((1ull << bits) - 1));
+    }
+};
+__host__ __device__ constexpr Packed27 pack27(const int8_t (&t)[27], int offset, int bits) {
+    Packed27 p;
+    p.bits = bits;
+    for (int i = 0; i < 27; ++i) p.w[i / 12] |= (uint64_t)(t[i] + offset) << (bits * (i % 12));
+    return p;
+}
 __host__ __device__ constexpr int cx(int q) {
     constexpr int8_t t[Q] = {0, 0, 0, -1, 1, 0, 0, -1, 1, -1, 1, 0, 0, -1, 1, 0, 0, -1, 1, 1, -1, 1, -1, 1, -1, 1, -1};
-    return t[q];
+    constexpr Packed27 p = pack27(t, 1, 2);
+    return p.get(q) - 1;
 }
 __host__ __device__ constexpr int cy(int q) {
     constexpr int8_t t[Q] = {0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, -1, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1};
-    return t[q];
+    constexpr Packed27 p = pack27(t, 1, 2);
+    return p.get(q) - 1;
 }
 __host__ __device__ constexpr int cz(int q) {
     constexpr int8_t t[Q] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, 1, 1, -1, -1, -1, -1, 1, 1, 1, 1, -1, -1, -1, -1};
-    return t[q];
+    constexpr Packed27 p = pack27(t, 1, 2);
+    return p.get(q) - 1;
 }
 // direction index of (cx, cy, cz) given as (ix, iy, iz) = c + 1
 __host__ __device__ constexpr int qof(int ix, int iy, int iz) {
     constexpr int8_t t[27] = {26, 9, 22, 17, 3, 13, 24, 7, 20,   // cx = -1
                               16, 2, 12, 6, 0, 5, 15, 1, 11,     // cx = 0
                               25, 10, 21, 18, 4, 14, 23, 8, 19}; // cx = +1
-    return t[(ix * 3 + iy) * 3 + iz];
+    constexpr Packed27 p = pack27(t, 0, 5);
+    return p.get((ix * 3 + iy) * 3 + iz);
 }
 __host__ __device__ constexpr int inv(int q) {
     constexpr int8_t t[Q] = {0, 2, 1, 4, 3, 6, 5, 10, 9, 8, 7, 16, 15, 18, 17, 12, 11, 14, 13, 26, 25, 24, 23, 22, 21, 20, 19};
-    return t[q];
+    constexpr Packed27 p = pack27(t, 0, 5);
+    return p.get(q);
 }
 __host__ __device__ constexpr double w1(int i) { return i == 1 ? 2.0 / 3.0 : 1.0 / 6.0; }  // i = c + 1
 __host__ __device__ constexpr double weight(int q) {
