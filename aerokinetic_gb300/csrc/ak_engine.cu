@@ -1396,6 +1396,11 @@ struct ak_refined {
     long long launches_per_step = 0;
     cudaStream_t side = nullptr;  // the first fine step's stream inside the captured graphs
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // the face-flux registers' branch inside the captured graphs: the coarse
+    // and both fine face fluxes run in order on their own stream beside the
+    // boundaries, walls and streaming, and join before the reflux
+    cudaStream_t flux = nullptr;
+    cudaEvent_t ev_flux_in[3] = {nullptr, nullptr, nullptr}, ev_flux_f0 = nullptr, ev_flux_done = nullptr;
     // budget support: inflow through the outer x/y faces of each tracked step,
     // and the per-level statistics of the conserved integrals / validity check
     bool track_budget = false;
@@ -1431,6 +1436,9 @@ void refined_release(ak_refined *R) {
     if (R->ev_fork) cudaEventDestroy(R->ev_fork);
     if (R->ev_join) cudaEventDestroy(R->ev_join);
     if (R->side) cudaStreamDestroy(R->side);
+    for (cudaEvent_t e : {R->ev_flux_in[0], R->ev_flux_in[1], R->ev_flux_in[2], R->ev_flux_f0, R->ev_flux_done})
+        if (e) cudaEventDestroy(e);
+    if (R->flux) cudaStreamDestroy(R->flux);
     if (R->coarse) {
         release(R->coarse);
         delete R->coarse;
@@ -1556,13 +1564,26 @@ int refined_step(ak_refined *R, bool fork = false) {
     const long long nlinks = F->nkeys * F->nz * 3;
     const long long nb = blocks_for(nlinks, 256);
 
+    // the stream a face flux runs on: in the captured graph the flux branch,
+    // entered after the collision on stream s (slot: 0 coarse, 1 + sub fine)
+    auto flux_stream = [&](cudaStream_t s, int slot) -> cudaStream_t {
+        if (!fork) return s;
+        if (cudaEventRecord(R->ev_flux_in[slot], s) != cudaSuccess ||
+            cudaStreamWaitEvent(R->flux, R->ev_flux_in[slot], 0) != cudaSuccess)
+            return nullptr;
+        return R->flux;
+    };
     // coarse collide, face fluxes, outer boundary, stream, donors after the step
     auto coarse_part = [&]() -> int {
         mark(C);
         k_collide<S><<<gc, 128, 0, st>>>(src_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s,
                                          (T)C->omega_b);
         mark(C);
-        k_face_flux_coarse<S><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, st>>>(
+        cudaStream_t fs = flux_stream(st, 0);
+        if (!fs) return fail(AK_ERR_CUDA, "face-flux branch could not be forked");
+        // reads the post-collision coarse copy, which nothing in this step
+        // writes afterwards (streaming writes the other copy)
+        k_face_flux_coarse<S><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, fs>>>(
             src_of<S>(C), C->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs,
             R->dx_c * R->dx_c * R->dx_c, R->reg_c);
         if (C->n_ubb)
@@ -1600,9 +1621,12 @@ int refined_step(ak_refined *R, bool fork = false) {
         mark(C);
         k_collide<S><<<gf, 128, 0, s>>>(src_of<S>(F), F->flags, F->G, F->shift_host, (T)F->omega_s, (T)F->omega_b);
         mark(C);
-        k_face_flux_fine<S><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, s>>>(
+        cudaStream_t fs = flux_stream(s, 1 + sub);
+        if (!fs) return fail(AK_ERR_CUDA, "face-flux branch could not be forked");
+        k_face_flux_fine<S><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, fs>>>(
             src_of<S>(F), F->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs, R->pad,
             R->dx_f * R->dx_f * R->dx_f, R->reg_f);
+        if (fork && sub == 0) AK_CUDA(cudaEventRecord(R->ev_flux_f0, R->flux));
         if (nlinks) {
             k_walls<S><<<(unsigned)nb, 256, 0, s>>>(src_of<S>(F), F->G, F->keys, F->wall_q, F->nkeys, 1,
                                                     F->n_elements, F->ox, F->oy, F->partials);
@@ -1610,6 +1634,8 @@ int refined_step(ak_refined *R, bool fork = false) {
                                                              R->d_loads + sub * 5 * F->n_elements);
         }
         mark(C);
+        // the second fine step streams into the copy the first step's flux reads
+        if (fork && sub == 1) AK_CUDA(cudaStreamWaitEvent(s, R->ev_flux_f0, 0));
         k_stream<S><<<gf, 128, 0, s>>>(src_of<S>(F), dst_of<S>(F), F->flags, F->G, 1);
         mark(C);
         AK_CUDA(cudaGetLastError());
@@ -1640,6 +1666,10 @@ int refined_step(ak_refined *R, bool fork = false) {
     if (nlinks) {
         k_accumulate_loads<<<1, 128, 0, st>>>(R->d_loads, 5 * F->n_elements, R->cum_loads);
         C->launches += 1;
+    }
+    if (fork) {
+        AK_CUDA(cudaEventRecord(R->ev_flux_done, R->flux));
+        AK_CUDA(cudaStreamWaitEvent(st, R->ev_flux_done, 0));
     }
     k_reflux<S><<<dim3((unsigned)split_blocks(R->max_face), R->nfaces), SPLIT_THREADS, 0, st>>>(
         src_of<S>(C), C->G, R->d_faces, R->nfaces, R->d_offs, R->reg_c, R->reg_f,
@@ -1858,8 +1888,14 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
             r = fail(AK_ERR_CUDA, "memset failed");
     }
     if (r == AK_OK && (cudaStreamCreateWithFlags(&R->side, cudaStreamNonBlocking) != cudaSuccess ||
+                       cudaStreamCreateWithFlags(&R->flux, cudaStreamNonBlocking) != cudaSuccess ||
                        cudaEventCreateWithFlags(&R->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-                       cudaEventCreateWithFlags(&R->ev_join, cudaEventDisableTiming) != cudaSuccess))
+                       cudaEventCreateWithFlags(&R->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&R->ev_flux_in[0], cudaEventDisableTiming) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&R->ev_flux_in[1], cudaEventDisableTiming) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&R->ev_flux_in[2], cudaEventDisableTiming) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&R->ev_flux_f0, cudaEventDisableTiming) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&R->ev_flux_done, cudaEventDisableTiming) != cudaSuccess))
         r = fail(AK_ERR_CUDA, "stream or event creation failed");
     if (r == AK_OK) r = ralloc(R, &R->d_flag, 1);
     if (r == AK_OK) r = ralloc(R, &R->d_loads, (size_t)2 * 5 * std::max(1, cd.n_elements));
