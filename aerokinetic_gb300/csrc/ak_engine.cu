@@ -122,6 +122,14 @@ struct ak_case {
     std::vector<cudaEvent_t> *timing = nullptr;
     cudaStream_t stream = nullptr;
     size_t device_bytes = 0;
+    // ak_step replays the step from CUDA graphs, one per (copy parity,
+    // sample), with the walls on a side stream beside the outer boundary; a
+    // graph is captured again when the loads' partial sums have moved
+    cudaGraphExec_t step_graph[4] = {nullptr, nullptr, nullptr, nullptr};
+    double *graph_partials[4] = {nullptr, nullptr, nullptr, nullptr};
+    long long graph_launches[4] = {0, 0, 0, 0};
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 
     OuterLinks outer() const { return OuterLinks{ox_, oy_, oz_, od, oobj, oedge, nouter}; }
 };
@@ -156,6 +164,11 @@ void release(ak_case *c) {
                     c->ext_stage[1], c->ext_stage[2], c->ext_inc0, c->ext_partials, c->ext_out};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    for (cudaGraphExec_t g : c->step_graph)
+        if (g) cudaGraphExecDestroy(g);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->side) cudaStreamDestroy(c->side);
     if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -483,14 +496,25 @@ Sgs<typename Store<S>::T> sgs_of(const ak_case *c) {
 template <typename S>
 int exterior_step(ak_case *c, double *fixed_partials, long long fixed_capacity);
 
+// One step.  branch: the walls run on the case's side stream, forked before
+// the outer boundary and joined before the bulk (the walls write only solid
+// cells, the outer boundary only ghost cells, and each reads fluid cells the
+// other does not write); used when the step is captured into a graph.
 template <typename S>
-int one_step(ak_case *c, bool sample, double *fixed_partials = nullptr, long long fixed_capacity = 0) {
+int one_step(ak_case *c, bool sample, double *fixed_partials = nullptr, long long fixed_capacity = 0,
+             bool branch = false) {
     using T = typename Store<S>::T;
     if (c->farfield == AK_FARFIELD_EXTERIOR) return exterior_step<S>(c, fixed_partials, fixed_capacity);
     const bool first = !c->prepared;
     if (first) AK_TRY(prepare_boundaries<S>(c));
     S *src = src_of<S>(c);
     const int TB = 256;
+    cudaStream_t ws = c->stream;
+    if (branch) {
+        AK_CUDA(cudaEventRecord(c->ev_fork, c->stream));
+        AK_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+        ws = c->side;
+    }
     mark(c);
     // outer boundary: the reference applies its boundary objects in
     // installation order; the outflow reads ghost values the UBB just wrote
@@ -541,17 +565,21 @@ int one_step(ak_case *c, bool sample, double *fixed_partials = nullptr, long lon
             AK_TRY(ensure_partials(c, nb * 5 * c->n_elements));
             partials = c->partials;
         }
-        k_walls<S><<<(unsigned)nb, 256, 0, c->stream>>>(src, c->G, c->keys, c->wall_q, c->nkeys, sample ? 1 : 0,
-                                                        c->n_elements, c->ox, c->oy, partials);
+        k_walls<S><<<(unsigned)nb, 256, 0, ws>>>(src, c->G, c->keys, c->wall_q, c->nkeys, sample ? 1 : 0,
+                                                 c->n_elements, c->ox, c->oy, partials);
         AK_CUDA(cudaGetLastError());
         ++c->launches;
         if (sample) {
-            k_sum_partials<<<5 * c->n_elements, 32, 0, c->stream>>>(partials, (int)nb, 5 * c->n_elements, c->reduced);
+            k_sum_partials<<<5 * c->n_elements, 32, 0, ws>>>(partials, (int)nb, 5 * c->n_elements, c->reduced);
             AK_CUDA(cudaGetLastError());
             ++c->launches;
         }
     } else if (sample) {
-        AK_CUDA(cudaMemsetAsync(c->reduced, 0, sizeof(double) * 5 * c->n_elements, c->stream));
+        AK_CUDA(cudaMemsetAsync(c->reduced, 0, sizeof(double) * 5 * c->n_elements, ws));
+    }
+    if (branch) {
+        AK_CUDA(cudaEventRecord(c->ev_join, c->side));
+        AK_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
     }
     // bulk
     mark(c);
@@ -563,6 +591,54 @@ int one_step(ak_case *c, bool sample, double *fixed_partials = nullptr, long lon
     mark(c);
     c->cur = 1 - c->cur;
     c->steps += 1;
+    return AK_OK;
+}
+
+// One step replayed from the captured graph of its (copy parity, sample) slot.
+template <typename S>
+int step_graphed(ak_case *c, bool sample) {
+    const long long nlinks = c->nkeys * c->nz * 3;
+    if (sample && nlinks) AK_TRY(ensure_partials(c, blocks_for(nlinks, 256) * 5 * c->n_elements));
+    if (!c->side) {
+        if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess)
+            return fail(AK_ERR_CUDA, "stream or event creation failed");
+    }
+    const int slot = c->cur | (sample ? 2 : 0);
+    if (c->step_graph[slot] && c->graph_partials[slot] != c->partials) {
+        cudaGraphExecDestroy(c->step_graph[slot]);
+        c->step_graph[slot] = nullptr;
+    }
+    if (!c->step_graph[slot]) {
+        const int cur = c->cur;
+        const long long steps = c->steps, launches = c->launches;
+        AK_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        const int r = one_step<S>(c, sample, nullptr, 0, true);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        const long long per = c->launches - launches;
+        c->cur = cur;
+        c->steps = steps;
+        c->launches = launches;
+        if (r != AK_OK || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            return r != AK_OK ? r : fail(AK_ERR_CUDA, std::string("step capture failed: ") + cudaGetErrorString(e));
+        }
+        const cudaError_t ei = cudaGraphInstantiate(&c->step_graph[slot], g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) {
+            c->step_graph[slot] = nullptr;
+            return fail(AK_ERR_CUDA, std::string("step graph instantiation failed: ") + cudaGetErrorString(ei));
+        }
+        c->graph_partials[slot] = c->partials;
+        c->graph_launches[slot] = per;
+    }
+    AK_CUDA(cudaGraphLaunch(c->step_graph[slot], c->stream));
+    c->cur = 1 - c->cur;
+    c->steps += 1;
+    c->launches += c->graph_launches[slot];
     return AK_OK;
 }
 
@@ -904,7 +980,13 @@ int ak_step(ak_case *c, int32_t nsteps, double *loads) {
     if (nsteps < 1) return fail(AK_ERR_INVALID, "nsteps must be >= 1");
     for (int s = 0; s < nsteps; ++s) {
         const bool sample = loads != nullptr && s == nsteps - 1;
-        AK_TRY(with_storage(c, [&](auto *tag) { return one_step<std::remove_pointer_t<decltype(tag)>>(c, sample); }));
+        AK_TRY(with_storage(c, [&](auto *tag) {
+            using S = std::remove_pointer_t<decltype(tag)>;
+            // the first step prepares the boundaries eagerly; the exterior
+            // step and timed steps stay eager
+            if (c->prepared && c->farfield != AK_FARFIELD_EXTERIOR && !c->timing) return step_graphed<S>(c, sample);
+            return one_step<S>(c, sample);
+        }));
     }
     if (loads) {
         AK_CUDA(cudaMemcpyAsync(loads, c->reduced, sizeof(double) * 5 * c->n_elements, cudaMemcpyDeviceToHost,

@@ -102,6 +102,33 @@ def compare_run(project, steps, sample_every, pdf_tol=2e-12, load_tol=2e-10, sto
         solver.close()
 
 
+@pytest.mark.parametrize("farfield,storage", [("characteristic_transport_v1", "f64"), ("legacy", "f16"),
+                                              ("characteristic_transport_v1", "f32")])
+def test_graph_replayed_steps_equal_eager_steps(farfield, storage):
+    """ak_step replays captured graphs (walls beside the outer boundary);
+    ak_step_timed runs the same kernels eagerly in one stream: same bits,
+    including after the loads' partial sums move (diagnostics in between)."""
+    import ctypes
+    project = kat_project(farfield)
+    graphed, eager = solver_for(project, storage), solver_for(project, storage)
+    try:
+        ms = np.zeros(4)
+        for chunk in (1, 5, 3):
+            loads = graphed.advance(chunk, sample_last=True)
+            graphed.diagnostics()
+            for _ in range(chunk):
+                assert eager._lib.ak_step_timed(eager._case, 1, ms.ctypes.data_as(ctypes.c_void_p)) == 0
+            eager.steps += chunk
+        assert np.array_equal(graphed.pdf(), eager.pdf())
+        ref = eager.step(sample=True)
+        got = graphed.step(sample=True)
+        assert (got["cl"], got["cd"], got["cm"]) == (ref["cl"], ref["cd"], ref["cm"])
+        assert loads["step"] == 9
+    finally:
+        graphed.close()
+        eager.close()
+
+
 def test_legacy_case_matches_oracle():
     compare_run(kat_project("legacy"), steps=40, sample_every=8)
 
