@@ -102,6 +102,7 @@ SIGNATURES = {
     "ak_refined_destroy": ([_P], ctypes.c_int),
     "ak_refined_init_perturbed": ([_P, _D, _D, _D, _D, _D], ctypes.c_int),
     "ak_refined_step": ([_P, ctypes.c_int32, _P], ctypes.c_int),
+    "ak_refined_step_budget": ([_P, ctypes.c_int32, _P, _P, _P], ctypes.c_int),
     "ak_refined_steps_done": ([_P], ctypes.c_int64),
     "ak_refined_track_budget": ([_P, ctypes.c_int32], ctypes.c_int),
     "ak_refined_outer_flux": ([_P, _P], ctypes.c_int),

@@ -495,6 +495,7 @@ Sgs<typename Store<S>::T> sgs_of(const ak_case *c) {
 
 template <typename S>
 int exterior_step(ak_case *c, double *fixed_partials, long long fixed_capacity);
+constexpr int EXT_THREADS = 64;  // block width of the exterior ring kernels
 
 // One step.  branch: the walls run on the case's side stream, forked before
 // the outer boundary and joined before the bulk (the walls write only solid
@@ -655,14 +656,17 @@ int exterior_step(ak_case *c, double *fixed_partials, long long fixed_capacity) 
     const ExtGeom &E = c->ext;
     double *band = c->ext_band[c->ext_cur], *next = c->ext_band[1 - c->ext_cur];
     const long long nr = (long long)E.nring * E.nz;
-    const unsigned rb = (unsigned)blocks_for(nr, 128);
+    // 64-thread blocks over the ~2 (nx + ny) nz ring cells: the FP64 ring
+    // arithmetic spreads over every SM
+    const unsigned rb = (unsigned)blocks_for(nr, EXT_THREADS);
     const double step = (double)c->steps;
     mark(c);
     double *moment_error = c->ext_out + 10;
-    k_ext_stage<<<rb, 128, 0, c->stream>>>(E, band, nullptr, c->ext_stage[0], 1, step, c->ext_inc0, moment_error);
-    k_ext_stage<<<rb, 128, 0, c->stream>>>(E, band, c->ext_stage[0], c->ext_stage[1], 2, step, c->ext_inc0,
+    k_ext_stage<<<rb, EXT_THREADS, 0, c->stream>>>(E, band, nullptr, c->ext_stage[0], 1, step, c->ext_inc0,
+                                                   moment_error);
+    k_ext_stage<<<rb, EXT_THREADS, 0, c->stream>>>(E, band, c->ext_stage[0], c->ext_stage[1], 2, step, c->ext_inc0,
                                            moment_error);
-    k_ext_stage<<<rb, 128, 0, c->stream>>>(E, band, c->ext_stage[1], c->ext_stage[2], 3, step, c->ext_inc0,
+    k_ext_stage<<<rb, EXT_THREADS, 0, c->stream>>>(E, band, c->ext_stage[1], c->ext_stage[2], 3, step, c->ext_inc0,
                                            moment_error);
     AK_CUDA(cudaGetLastError());
     c->launches += 3;
@@ -687,8 +691,9 @@ int exterior_step(ak_case *c, double *fixed_partials, long long fixed_capacity) 
     mark(c);
     k_ext_band_pull<S><<<(unsigned)blocks_for((long long)E.nband * E.nz, 128), 128, 0, c->stream>>>(src, c->G, E,
                                                                                                     next);
-    k_ext_ring<S><<<rb, 128, 0, c->stream>>>(src, dst, c->G, E, next, c->ext_stage[2], c->shift_host, (T)c->omega_s,
-                                             (T)c->omega_b, c->omega_s, c->ext_partials, moment_error);
+    k_ext_ring<S><<<rb, EXT_THREADS, 0, c->stream>>>(src, dst, c->G, E, next, c->ext_stage[2], c->shift_host,
+                                                     (T)c->omega_s, (T)c->omega_b, c->omega_s, c->ext_partials,
+                                                     moment_error);
     AK_CUDA(cudaGetLastError());
     c->launches += 2;
     mark(c);
@@ -747,7 +752,7 @@ int build_exterior(ak_case *c, const std::vector<uint8_t> &hflags) {
     for (int k = 0; k < 2; ++k) AK_TRY(dalloc(c, &c->ext_band[k], 4 * nb));
     for (int k = 0; k < 3; ++k) AK_TRY(dalloc(c, &c->ext_stage[k], 4 * nr));
     AK_TRY(dalloc(c, &c->ext_inc0, 2LL * E.nz * E.NX));
-    c->ext_blocks = blocks_for(nr, 128);
+    c->ext_blocks = blocks_for(nr, EXT_THREADS);
     AK_TRY(dalloc(c, &c->ext_partials, 4 * c->ext_blocks));
     AK_TRY(dalloc(c, &c->ext_out, 11));
     AK_CUDA(cudaMemsetAsync(c->ext_out, 0, 11 * sizeof(double), c->stream));
@@ -1474,7 +1479,8 @@ struct ak_refined {
     std::vector<void *> owned;  // device buffers of the driver
     // one captured coarse step per (coarse, fine) buffer parity, replayed by
     // ak_refined_step; launches_per_step counts the kernels of one replay
-    cudaGraphExec_t graph[8] = {};
+    cudaGraphExec_t graph[16] = {};  // (coarse copy, fine copy, budget, step integrals)
+    bool step_stats = false;         // the step ends with the budget's integrals
     long long launches_per_step = 0;
     cudaStream_t side = nullptr;  // the first fine step's stream inside the captured graphs
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -1629,6 +1635,24 @@ int refined_init(ak_refined *R, double amp, double phase_y, double phase_z, doub
     return AK_OK;
 }
 
+// Mass, momentum and validity statistics of the coarse cells outside the
+// fine box and the fine block's physical cells, into stats_out[2][NSTAT]
+// (refined_solver.py:291-299, 347-361).
+template <typename S>
+int enqueue_region_stats(ak_refined *R, cudaStream_t st) {
+    ak_case *C = R->coarse, *F = R->fine;
+    const BoxSpec &B = R->B;
+    const Region rc{0, C->nx, 0, C->ny, B.lo[0], B.hi[0], B.lo[1], B.hi[1]};
+    const Region rf{R->pad, F->nx - R->pad, R->pad, F->ny - R->pad, 0, 0, 0, 0};
+    k_region_stats<S><<<STATS_BLOCKS, 256, 0, st>>>(src_of<S>(C), C->G, C->flags, rc, R->stats_partials);
+    k_region_final<<<1, REDUCE_THREADS, 0, st>>>(R->stats_partials, STATS_BLOCKS, R->stats_out);
+    k_region_stats<S><<<STATS_BLOCKS, 256, 0, st>>>(src_of<S>(F), F->G, F->flags, rf, R->stats_partials);
+    k_region_final<<<1, REDUCE_THREADS, 0, st>>>(R->stats_partials, STATS_BLOCKS, R->stats_out + NSTAT);
+    C->launches += 4;
+    AK_CUDA(cudaGetLastError());
+    return AK_OK;
+}
+
 template <typename S>
 int refined_step(ak_refined *R, bool fork = false) {
     using T = typename Store<S>::T;
@@ -1758,6 +1782,8 @@ int refined_step(ak_refined *R, bool fork = false) {
         1.0 / (R->dx_c * R->dx_c * R->dx_c), R->d_flag);
     launch_restrict<S>(R, f2c, st);
     AK_CUDA(cudaGetLastError());
+    // a tracked budget closes on the integrals of the state the step leaves
+    if (R->track_budget && R->step_stats) AK_TRY(enqueue_region_stats<S>(R, st));
     mark(C);  // step end
     C->launches += 6 + 8 * 2 + (C->n_ubb ? 1 : 0) + (C->n_out ? 1 : 0) + (nlinks ? 0 : -4) + 1;
     C->steps += 1;
@@ -1773,7 +1799,7 @@ int refined_step(ak_refined *R, bool fork = false) {
 template <typename S>
 int refined_step_graphed(ak_refined *R) {
     ak_case *C = R->coarse, *F = R->fine;
-    const int slot = C->cur | (F->cur << 1) | (R->track_budget ? 4 : 0);
+    const int slot = C->cur | (F->cur << 1) | (R->track_budget ? 4 : 0) | (R->step_stats ? 8 : 0);
     if (!R->graph[slot]) {
         const int ccur = C->cur, fcur = F->cur;
         const long long cs = C->steps, fs = F->steps, rs = R->steps, cl = C->launches;
@@ -2021,19 +2047,32 @@ int ak_refined_init_perturbed(ak_refined *R, double amp, double phase_y, double 
 }
 
 int ak_refined_step(ak_refined *R, int32_t nsteps, double *loads) {
+    return ak_refined_step_budget(R, nsteps, loads, nullptr, nullptr);
+}
+
+int ak_refined_step_budget(ak_refined *R, int32_t nsteps, double *loads, double *outer, double *stats) {
     if (!R) return fail(AK_ERR_INVALID, "null case");
     if (nsteps < 1) return fail(AK_ERR_INVALID, "nsteps must be >= 1");
+    if ((outer || stats) && !R->track_budget)
+        return fail(AK_ERR_INVALID, "the outer flux and the integrals of a step need budget tracking");
     cudaStream_t st = R->coarse->stream;
     AK_CUDA(cudaMemsetAsync(R->d_flag, 0, sizeof(int), st));
-    for (int s = 0; s < nsteps; ++s)
-        AK_TRY(with_storage(R->coarse, [&](auto *tag) {
+    for (int s = 0; s < nsteps; ++s) {
+        // only the last step computes the integrals a caller asked for
+        R->step_stats = stats != nullptr && s == nsteps - 1;
+        const int r = with_storage(R->coarse, [&](auto *tag) {
             return refined_step_graphed<std::remove_pointer_t<decltype(tag)>>(R);
-        }));
+        });
+        R->step_stats = false;
+        if (r != AK_OK) return r;
+    }
     int flag = 0;
     AK_CUDA(cudaMemcpyAsync(&flag, R->d_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
     const int n = R->fine->n_elements;
     std::vector<double> two((size_t)10 * std::max(1, n));
     if (loads) AK_CUDA(cudaMemcpyAsync(two.data(), R->d_loads, sizeof(double) * 10 * n, cudaMemcpyDeviceToHost, st));
+    if (outer) AK_CUDA(cudaMemcpyAsync(outer, R->outer_out, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (stats) AK_CUDA(cudaMemcpyAsync(stats, R->stats_out, 2 * NSTAT * sizeof(double), cudaMemcpyDeviceToHost, st));
     AK_CUDA(cudaStreamSynchronize(st));
     if (flag) {
         std::string why = (flag & XF_NEGATIVE) ? "negative physical populations" :
@@ -2084,21 +2123,9 @@ int ak_refined_cumulative_loads(ak_refined *R, double *out) {
 
 int ak_refined_integrals(ak_refined *R, double *out) {
     if (!R || !out) return fail(AK_ERR_INVALID, "a case and an output array are required");
-    ak_case *C = R->coarse, *F = R->fine;
+    ak_case *C = R->coarse;
     cudaStream_t st = C->stream;
-    const BoxSpec &B = R->B;
-    const Region rc{0, C->nx, 0, C->ny, B.lo[0], B.hi[0], B.lo[1], B.hi[1]};
-    const Region rf{R->pad, F->nx - R->pad, R->pad, F->ny - R->pad, 0, 0, 0, 0};
-    int r = with_storage(C, [&](auto *tag) {
-        using S = std::remove_pointer_t<decltype(tag)>;
-        k_region_stats<S><<<STATS_BLOCKS, 256, 0, st>>>(src_of<S>(C), C->G, C->flags, rc, R->stats_partials);
-        k_region_final<<<1, REDUCE_THREADS, 0, st>>>(R->stats_partials, STATS_BLOCKS, R->stats_out);
-        k_region_stats<S><<<STATS_BLOCKS, 256, 0, st>>>(src_of<S>(F), F->G, F->flags, rf, R->stats_partials);
-        k_region_final<<<1, REDUCE_THREADS, 0, st>>>(R->stats_partials, STATS_BLOCKS, R->stats_out + NSTAT);
-        C->launches += 4;
-        AK_CUDA(cudaGetLastError());
-        return AK_OK;
-    });
+    const int r = with_storage(C, [&](auto *tag) { return enqueue_region_stats<std::remove_pointer_t<decltype(tag)>>(R, st); });
     if (r != AK_OK) return r;
     AK_CUDA(cudaMemcpyAsync(out, R->stats_out, 2 * NSTAT * sizeof(double), cudaMemcpyDeviceToHost, st));
     AK_CUDA(cudaStreamSynchronize(st));
@@ -2163,6 +2190,9 @@ struct ak_batch {
     // grid, table order (0 case-major, 1 interleaved)
     int tb = 128, per_sm = 4, order = 0;
     cudaGraphExec_t graph[4] = {};  // (parity, sample)
+    // inside the graphs the walls run on a side stream beside the farfield
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 namespace {
@@ -2181,6 +2211,9 @@ void batch_release(ak_batch *B) {
     for (void *p : {(void *)B->d_cases, (void *)B->w_ring, (void *)B->w_ff, (void *)B->w_walls, (void *)B->w_bulk,
                     (void *)B->loads})
         if (p) cudaFree(p);
+    if (B->ev_fork) cudaEventDestroy(B->ev_fork);
+    if (B->ev_join) cudaEventDestroy(B->ev_join);
+    if (B->side) cudaStreamDestroy(B->side);
     if (B->stream) cudaStreamDestroy(B->stream);
 }
 
@@ -2245,9 +2278,18 @@ int bulk_occupancy(int tb, int *blocks) {
     return AK_OK;
 }
 
+// branch: the walls (and their load sums) on the side stream, forked before
+// the farfield and joined before the stream-collide; they touch disjoint
+// cells (solid cells against ghost cells), as in the single-case step
 template <typename S>
-int batch_enqueue(ak_batch *B, int parity, bool sample) {
+int batch_enqueue(ak_batch *B, int parity, bool sample, bool branch = false) {
     const BatchCase<S> *cases = (const BatchCase<S> *)B->d_cases;
+    cudaStream_t ws = B->stream;
+    if (branch) {
+        AK_CUDA(cudaEventRecord(B->ev_fork, B->stream));
+        AK_CUDA(cudaStreamWaitEvent(B->side, B->ev_fork, 0));
+        ws = B->side;
+    }
     if (B->n_ring) {
         k_batch_ring_macros<S><<<(unsigned)B->n_ring, 256, 0, B->stream>>>(cases, B->w_ring, parity);
         AK_CUDA(cudaGetLastError());
@@ -2257,13 +2299,17 @@ int batch_enqueue(ak_batch *B, int parity, bool sample) {
         AK_CUDA(cudaGetLastError());
     }
     if (B->n_walls) {
-        k_batch_walls<S><<<(unsigned)B->n_walls, 256, 0, B->stream>>>(cases, B->w_walls, parity, sample ? 1 : 0);
+        k_batch_walls<S><<<(unsigned)B->n_walls, 256, 0, ws>>>(cases, B->w_walls, parity, sample ? 1 : 0);
         AK_CUDA(cudaGetLastError());
     }
     if (sample) {
-        k_batch_sum_partials<S><<<dim3(5 * MAX_ELEMENTS, (unsigned)B->cases.size()), 32, 0, B->stream>>>(cases,
-                                                                                                      B->loads);
+        k_batch_sum_partials<S><<<dim3(5 * MAX_ELEMENTS, (unsigned)B->cases.size()), 32, 0, ws>>>(cases,
+                                                                                              B->loads);
         AK_CUDA(cudaGetLastError());
+    }
+    if (branch) {
+        AK_CUDA(cudaEventRecord(B->ev_join, B->side));
+        AK_CUDA(cudaStreamWaitEvent(B->stream, B->ev_join, 0));
     }
     AK_TRY(bulk_launch<S>(B, B->tb, B->per_sm * B->sms, parity));
     return AK_OK;
@@ -2335,9 +2381,15 @@ int batch_build(ak_batch *B) {
 template <typename S>
 int batch_step_graphed(ak_batch *B, bool sample) {
     const int slot = B->parity | (sample ? 2 : 0);
+    if (!B->side) {
+        if (cudaStreamCreateWithFlags(&B->side, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&B->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&B->ev_join, cudaEventDisableTiming) != cudaSuccess)
+            return fail(AK_ERR_CUDA, "stream or event creation failed");
+    }
     if (!B->graph[slot]) {
         AK_CUDA(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
-        const int r = batch_enqueue<S>(B, B->parity, sample);
+        const int r = batch_enqueue<S>(B, B->parity, sample, true);
         cudaGraph_t g = nullptr;
         const cudaError_t e = cudaStreamEndCapture(B->stream, &g);
         if (r != AK_OK || e != cudaSuccess) {

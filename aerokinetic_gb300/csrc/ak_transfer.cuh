@@ -795,18 +795,19 @@ __global__ void __launch_bounds__(256)
     k_region_stats(const S *__restrict__ pdf, Grid G, const uint8_t *__restrict__ flags, Region R,
                    double *__restrict__ partials) {
     const int w = R.x1 - R.x0, h = R.y1 - R.y0;
-    const long long n = (long long)w * h * G.nz;
+    const long long nrows = (long long)h * G.nz;
     double a[NSTAT] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int x = R.x0 + (int)(i % w);
-        const long long r = i / w;
-        const int y = R.y0 + (int)(r % h), z = (int)(r / h);
+    // blocks walk the region's (y, z) rows, threads its x
+    for (long long row = blockIdx.x; row < nrows; row += gridDim.x)
+    for (int xx = threadIdx.x; xx < w; xx += blockDim.x) {
+        const int z = (int)(row / h), y = R.y0 + (int)(row - (long long)z * h), x = R.x0 + xx;
         if (x >= R.ex0 && x < R.ex1 && y >= R.ey0 && y < R.ey1) continue;
         if (flags[(y + 1) * G.nxp + (x + 1)] != FLAG_FLUID) continue;
         double drho = 0.0, j[3] = {0.0, 0.0, 0.0};
+        const S *cell = pdf + G.cell(x + 1, y + 1, z);
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
-            const double v = load_g(pdf, G, q, x + 1, y + 1, z);
+            const double v = (double)Store<S>::load(cell + q * G.qs, q, G.shift[q]);
             drho += v;
             if (cx(q)) j[0] += cx(q) > 0 ? v : -v;
             if (cy(q)) j[1] += cy(q) > 0 ? v : -v;
@@ -867,18 +868,21 @@ __global__ void __launch_bounds__(256)
                 double *__restrict__ snapshot, double inv_speed, double inv_dt, int reset,
                 double *__restrict__ partials) {
     const int w = R.x1 - R.x0, h = R.y1 - R.y0;
-    const long long n = (long long)w * h * G.nz;
+    const long long nrows = (long long)h * G.nz;
     double sq[4] = {0, 0, 0, 0}, mx[4] = {0, 0, 0, 0}, cells = 0.0;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int x = R.x0 + (int)(i % w);
-        const long long r = i / w;
-        const int y = R.y0 + (int)(r % h), z = (int)(r / h);
+    // blocks walk the region's (y, z) rows, threads its x; the snapshot is
+    // indexed by the cell's place in the region, (z h + y - y0) w + x - x0
+    for (long long row = blockIdx.x; row < nrows; row += gridDim.x)
+    for (int xx = threadIdx.x; xx < w; xx += blockDim.x) {
+        const int z = (int)(row / h), y = R.y0 + (int)(row - (long long)z * h), x = R.x0 + xx;
+        const long long i = row * w + xx;
         if (x >= R.ex0 && x < R.ex1 && y >= R.ey0 && y < R.ey1) continue;
         if (flags[(y + 1) * G.nxp + (x + 1)] != FLAG_FLUID) continue;
         double drho = 0.0, j[3] = {0.0, 0.0, 0.0};
+        const S *cell = pdf + G.cell(x + 1, y + 1, z);
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
-            const double v = load_g(pdf, G, q, x + 1, y + 1, z);
+            const double v = (double)Store<S>::load(cell + q * G.qs, q, G.shift[q]);
             drho += v;
             if (cx(q)) j[0] += cx(q) > 0 ? v : -v;
             if (cy(q)) j[1] += cy(q) > 0 ? v : -v;

@@ -56,6 +56,39 @@ def segments_intersect(a, b, c, d):
     return -1e-12 <= t <= 1 + 1e-12 and -1e-12 <= u <= 1 + 1e-12
 
 
+def _any_segments_intersect(p, nxt, chunk=1 << 16):
+    """segments_intersect over every pair of non-adjacent edges (i, j), j >= i + 2,
+    except the closing pair (0, n - 1): the same tests, evaluated with numpy
+    over blocks of pairs instead of one Python call per pair."""
+    n = len(p)
+    ii, jj = np.triu_indices(n, k=2)
+    keep = ~((ii == 0) & (jj == n - 1))
+    ii, jj = ii[keep], jj[keep]
+    for start in range(0, len(ii), chunk):
+        i, j = ii[start:start + chunk], jj[start:start + chunk]
+        a, b, c, d = p[i], nxt[i], p[j], nxt[j]
+        ab, cd, ca = b - a, d - c, c - a
+        den = cross2(ab, cd)
+        norm_ab = np.sqrt(np.einsum("ij,ij->i", ab, ab))
+        norm_cd = np.sqrt(np.einsum("ij,ij->i", cd, cd))
+        tol = 1e-12 * np.maximum(norm_ab * norm_cd, 1e-30)
+        parallel = np.abs(den) <= tol
+        # parallel pairs: collinear and overlapping along the edge's main axis
+        axis = np.argmax(np.abs(ab), axis=1)
+        rows = np.arange(len(i))
+        a_ax, b_ax, c_ax, d_ax = a[rows, axis], b[rows, axis], c[rows, axis], d[rows, axis]
+        lo = np.maximum(np.minimum(a_ax, b_ax), np.minimum(c_ax, d_ax))
+        hi = np.minimum(np.maximum(a_ax, b_ax), np.maximum(c_ax, d_ax))
+        collinear = (np.abs(cross2(ca, ab)) <= tol) & (lo <= hi + 1e-12)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            t = cross2(ca, cd) / den
+            u = cross2(ca, ab) / den
+        crossing = (-1e-12 <= t) & (t <= 1 + 1e-12) & (-1e-12 <= u) & (u <= 1 + 1e-12)
+        if np.any(np.where(parallel, collinear, crossing)):
+            return True
+    return False
+
+
 @dataclass(frozen=True)
 class Contour:
     """Closed polygon in a common frame (geometry.py:10-85); any length scale."""
@@ -76,13 +109,8 @@ class Contour:
         nxt = np.roll(p, -1, axis=0)
         if abs(np.sum(cross2(p, nxt))) / 2 <= 1e-12 * np.ptp(p, axis=0).max() ** 2:
             raise ValueError("Contour has zero enclosed area")
-        n = len(p)
-        for i in range(n):
-            for j in range(i + 2, n):
-                if i == 0 and j == n - 1:
-                    continue
-                if segments_intersect(p[i], nxt[i], p[j], nxt[j]):
-                    raise ValueError(f"Self-intersection in contour {self.name}")
+        if _any_segments_intersect(p, nxt):
+            raise ValueError(f"Self-intersection in contour {self.name}")
         p.setflags(write=False)
         object.__setattr__(self, "xy", p)
 

@@ -141,26 +141,29 @@ class RefinedSolver:
             before = self._integrals if self._integrals is not None else (
                 self.conserved_integrals() if self.budget else None)
             raw = np.zeros((len(self.contours), 5))
-            check(self._lib.ak_refined_step(self._handle, 1, _ptr(raw)))
+            flux = stats = None
+            if self.budget:
+                # the step returns its loads, outer-face flux and integrals at once
+                flux, stats = np.zeros(8), np.zeros(16)
+                check(self._lib.ak_refined_step_budget(self._handle, 1, _ptr(raw), _ptr(flux), _ptr(stats)))
+            else:
+                check(self._lib.ak_refined_step(self._handle, 1, _ptr(raw)))
             self.steps += 1
         except Exception:
             self.initialized = False
             raise
         record = self._record(raw)
         if self.budget:
-            self._close_budget(before, raw)
+            self._close_budget(before, raw, flux, self._integrals_of(stats[:8], stats[8:]))
         self.last_loads = record
         return record
 
     def step(self):
         return self.advance(1)
 
-    def _close_budget(self, before, raw):
+    def _close_budget(self, before, raw, flux, after):
         """refined_solver.py:329-339 from the engine's integrals and outer-face flux."""
         f = self.fine_level
-        flux = np.zeros(8)
-        check(self._lib.ak_refined_outer_flux(self._handle, _ptr(flux)))
-        after = self.conserved_integrals()
         self._integrals = after
         unit = f.lattice_velocity_unit
         external = flux[:4].copy()
@@ -184,8 +187,11 @@ class RefinedSolver:
     def conserved_integrals(self):
         """Mass and momentum of the coarse cells outside the fine box and the
         fine fluid cells (refined_solver.py:291-299), common units."""
+        return self._integrals_of(*self._stats())
+
+    def _integrals_of(self, coarse, fine):
         mass, impulse = 0.0, np.zeros(3)
-        for st, level in zip(self._stats(), (self.coarse_level, self.fine_level)):
+        for st, level in zip((coarse, fine), (self.coarse_level, self.fine_level)):
             if st[7]:
                 return {"mass": float("nan"), "momentum": [float("nan")] * 3}
             volume = level.dx ** 3

@@ -228,6 +228,12 @@ int ak_refined_init_perturbed(ak_refined *r, double amp, double phase_y, double 
  * normalised frame's origin in fine lattice units.  The step's kernels are
  * captured once per buffer parity into CUDA graphs and replayed. */
 int ak_refined_step(ak_refined *r, int32_t nsteps, double *loads);
+/* ak_refined_step that also returns, with one synchronisation, what the
+ * budget of the last step needs (refined_solver.py:329-339): outer[8] as
+ * ak_refined_outer_flux, stats[16] as ak_refined_integrals of the state the
+ * step leaves (computed inside the step).  Needs ak_refined_track_budget on;
+ * outer or stats may be NULL. */
+int ak_refined_step_budget(ak_refined *r, int32_t nsteps, double *loads, double *outer, double *stats);
 int64_t ak_refined_steps_done(const ak_refined *r);
 /* With enable != 0, every following step also measures the inflow through
  * the outer x and y faces of the coarse lattice after its boundaries
