@@ -56,37 +56,46 @@ def segments_intersect(a, b, c, d):
     return -1e-12 <= t <= 1 + 1e-12 and -1e-12 <= u <= 1 + 1e-12
 
 
-def _any_segments_intersect(p, nxt, chunk=1 << 16):
-    """segments_intersect over every pair of non-adjacent edges (i, j), j >= i + 2,
-    except the closing pair (0, n - 1): the same tests, evaluated with numpy
-    over blocks of pairs instead of one Python call per pair."""
-    n = len(p)
-    ii, jj = np.triu_indices(n, k=2)
-    keep = ~((ii == 0) & (jj == n - 1))
-    ii, jj = ii[keep], jj[keep]
-    for start in range(0, len(ii), chunk):
-        i, j = ii[start:start + chunk], jj[start:start + chunk]
-        a, b, c, d = p[i], nxt[i], p[j], nxt[j]
-        ab, cd, ca = b - a, d - c, c - a
-        den = cross2(ab, cd)
-        norm_ab = np.sqrt(np.einsum("ij,ij->i", ab, ab))
-        norm_cd = np.sqrt(np.einsum("ij,ij->i", cd, cd))
-        tol = 1e-12 * np.maximum(norm_ab * norm_cd, 1e-30)
-        parallel = np.abs(den) <= tol
-        # parallel pairs: collinear and overlapping along the edge's main axis
-        axis = np.argmax(np.abs(ab), axis=1)
-        rows = np.arange(len(i))
-        a_ax, b_ax, c_ax, d_ax = a[rows, axis], b[rows, axis], c[rows, axis], d[rows, axis]
-        lo = np.maximum(np.minimum(a_ax, b_ax), np.minimum(c_ax, d_ax))
-        hi = np.minimum(np.maximum(a_ax, b_ax), np.maximum(c_ax, d_ax))
-        collinear = (np.abs(cross2(ca, ab)) <= tol) & (lo <= hi + 1e-12)
-        with np.errstate(divide="ignore", invalid="ignore"):
-            t = cross2(ca, cd) / den
-            u = cross2(ca, ab) / den
-        crossing = (-1e-12 <= t) & (t <= 1 + 1e-12) & (-1e-12 <= u) & (u <= 1 + 1e-12)
-        if np.any(np.where(parallel, collinear, crossing)):
+def _pairs_intersect(a, b, c, d):
+    """segments_intersect for arrays of segment pairs (a, b) x (c, d), (k, 2) each:
+    the same tests and tolerances, evaluated with numpy."""
+    ab, cd, ca = b - a, d - c, c - a
+    den = cross2(ab, cd)
+    norm_ab = np.sqrt(np.einsum("ij,ij->i", ab, ab))
+    norm_cd = np.sqrt(np.einsum("ij,ij->i", cd, cd))
+    tol = 1e-12 * np.maximum(norm_ab * norm_cd, 1e-30)
+    parallel = np.abs(den) <= tol
+    # parallel pairs: collinear and overlapping along the first edge's main axis
+    axis = np.argmax(np.abs(ab), axis=1)
+    rows = np.arange(len(a))
+    a_ax, b_ax, c_ax, d_ax = a[rows, axis], b[rows, axis], c[rows, axis], d[rows, axis]
+    lo = np.maximum(np.minimum(a_ax, b_ax), np.minimum(c_ax, d_ax))
+    hi = np.minimum(np.maximum(a_ax, b_ax), np.maximum(c_ax, d_ax))
+    collinear = (np.abs(cross2(ca, ab)) <= tol) & (lo <= hi + 1e-12)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        t = cross2(ca, cd) / den
+        u = cross2(ca, ab) / den
+    crossing = (-1e-12 <= t) & (t <= 1 + 1e-12) & (-1e-12 <= u) & (u <= 1 + 1e-12)
+    return np.where(parallel, collinear, crossing)
+
+
+def _any_intersection(starts1, ends1, starts2, ends2, i, j, chunk=1 << 16):
+    """Whether edge i of the first list meets edge j of the second for any
+    listed pair (i, j), in blocks of pairs."""
+    for k in range(0, len(i), chunk):
+        ii, jj = i[k:k + chunk], j[k:k + chunk]
+        if np.any(_pairs_intersect(starts1[ii], ends1[ii], starts2[jj], ends2[jj])):
             return True
     return False
+
+
+def _any_segments_intersect(p, nxt):
+    """segments_intersect over every pair of non-adjacent edges (i, j), j >= i + 2,
+    of one closed polygon, except the closing pair (0, n - 1)."""
+    n = len(p)
+    i, j = np.triu_indices(n, k=2)
+    keep = ~((i == 0) & (j == n - 1))
+    return _any_intersection(p, nxt, p, nxt, i[keep], j[keep])
 
 
 @dataclass(frozen=True)
@@ -198,8 +207,9 @@ class Section:
             for f in elements[i + 1:]:
                 touching = bool(e.contains(*f.xy[0]) or f.contains(*e.xy[0]))
                 if not touching:
-                    touching = any(segments_intersect(a, b, c, d)
-                                   for a, b in zip(*e.edges()) for c, d in zip(*f.edges()))
+                    (a, b), (c, d) = e.edges(), f.edges()
+                    i, j = np.meshgrid(np.arange(len(a)), np.arange(len(c)), indexing="ij")
+                    touching = _any_intersection(a, b, c, d, i.ravel(), j.ravel())
                 if touching:
                     raise ValueError(f"Elements touch or overlap: {e.name}, {f.name}")
 
