@@ -494,7 +494,7 @@ Sgs<typename Store<S>::T> sgs_of(const ak_case *c) {
 }
 
 template <typename S>
-int exterior_step(ak_case *c, double *fixed_partials, long long fixed_capacity);
+int exterior_step(ak_case *c, double *fixed_partials, long long fixed_capacity, bool branch);
 constexpr int EXT_THREADS = 64;  // block width of the exterior ring kernels
 
 // One step.  branch: the walls run on the case's side stream, forked before
@@ -505,7 +505,7 @@ template <typename S>
 int one_step(ak_case *c, bool sample, double *fixed_partials = nullptr, long long fixed_capacity = 0,
              bool branch = false) {
     using T = typename Store<S>::T;
-    if (c->farfield == AK_FARFIELD_EXTERIOR) return exterior_step<S>(c, fixed_partials, fixed_capacity);
+    if (c->farfield == AK_FARFIELD_EXTERIOR) return exterior_step<S>(c, fixed_partials, fixed_capacity, branch);
     const bool first = !c->prepared;
     if (first) AK_TRY(prepare_boundaries<S>(c));
     S *src = src_of<S>(c);
@@ -606,13 +606,15 @@ int step_graphed(ak_case *c, bool sample) {
             cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess)
             return fail(AK_ERR_CUDA, "stream or event creation failed");
     }
-    const int slot = c->cur | (sample ? 2 : 0);
+    // the exterior step samples its loads every step and flips its band
+    // buffers with the population copies: its slot is the two parities
+    const int slot = c->farfield == AK_FARFIELD_EXTERIOR ? (c->cur | (c->ext_cur << 1)) : (c->cur | (sample ? 2 : 0));
     if (c->step_graph[slot] && c->graph_partials[slot] != c->partials) {
         cudaGraphExecDestroy(c->step_graph[slot]);
         c->step_graph[slot] = nullptr;
     }
     if (!c->step_graph[slot]) {
-        const int cur = c->cur;
+        const int cur = c->cur, ext_cur = c->ext_cur;
         const long long steps = c->steps, launches = c->launches;
         AK_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         const int r = one_step<S>(c, sample, nullptr, 0, true);
@@ -620,6 +622,7 @@ int step_graphed(ak_case *c, bool sample) {
         const cudaError_t e = cudaStreamEndCapture(c->stream, &g);
         const long long per = c->launches - launches;
         c->cur = cur;
+        c->ext_cur = ext_cur;
         c->steps = steps;
         c->launches = launches;
         if (r != AK_OK || e != cudaSuccess) {
@@ -638,6 +641,7 @@ int step_graphed(ak_case *c, bool sample) {
     }
     AK_CUDA(cudaGraphLaunch(c->step_graph[slot], c->stream));
     c->cur = 1 - c->cur;
+    if (c->farfield == AK_FARFIELD_EXTERIOR) c->ext_cur = 1 - c->ext_cur;
     c->steps += 1;
     c->launches += c->graph_launches[slot];
     return AK_OK;
@@ -649,9 +653,12 @@ int step_graphed(ak_case *c, bool sample) {
 // streamed band macros, the rebuilt and collided ring, the fused bulk
 // stream-collide, and the step's source and wall-mass sums.
 template <typename S>
-int exterior_step(ak_case *c, double *fixed_partials, long long fixed_capacity) {
+int exterior_step(ak_case *c, double *fixed_partials, long long fixed_capacity, bool branch) {
     using T = typename Store<S>::T;
     if (!c->prepared) return fail(AK_ERR_INVALID, "the exterior case needs an initial state first");
+    // branch (captured graphs): the walls on the side stream beside the
+    // predictor, joined before the band pull (which may read a solid cell of
+    // the third layer) -- the step's clock lives on the device (ext_out[11])
     S *src = src_of<S>(c), *dst = dst_of<S>(c);
     const ExtGeom &E = c->ext;
     double *band = c->ext_band[c->ext_cur], *next = c->ext_band[1 - c->ext_cur];
@@ -659,15 +666,21 @@ int exterior_step(ak_case *c, double *fixed_partials, long long fixed_capacity) 
     // 64-thread blocks over the ~2 (nx + ny) nz ring cells: the FP64 ring
     // arithmetic spreads over every SM
     const unsigned rb = (unsigned)blocks_for(nr, EXT_THREADS);
-    const double step = (double)c->steps;
+    const double *clock = c->ext_out + 11;
+    cudaStream_t ws = c->stream;
+    if (branch) {
+        AK_CUDA(cudaEventRecord(c->ev_fork, c->stream));
+        AK_CUDA(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+        ws = c->side;
+    }
     mark(c);
     double *moment_error = c->ext_out + 10;
-    k_ext_stage<<<rb, EXT_THREADS, 0, c->stream>>>(E, band, nullptr, c->ext_stage[0], 1, step, c->ext_inc0,
+    k_ext_stage<<<rb, EXT_THREADS, 0, c->stream>>>(E, band, nullptr, c->ext_stage[0], 1, clock, c->ext_inc0,
                                                    moment_error);
-    k_ext_stage<<<rb, EXT_THREADS, 0, c->stream>>>(E, band, c->ext_stage[0], c->ext_stage[1], 2, step, c->ext_inc0,
-                                           moment_error);
-    k_ext_stage<<<rb, EXT_THREADS, 0, c->stream>>>(E, band, c->ext_stage[1], c->ext_stage[2], 3, step, c->ext_inc0,
-                                           moment_error);
+    k_ext_stage<<<rb, EXT_THREADS, 0, c->stream>>>(E, band, c->ext_stage[0], c->ext_stage[1], 2, clock,
+                                                   c->ext_inc0, moment_error);
+    k_ext_stage<<<rb, EXT_THREADS, 0, c->stream>>>(E, band, c->ext_stage[1], c->ext_stage[2], 3, clock,
+                                                   c->ext_inc0, moment_error);
     AK_CUDA(cudaGetLastError());
     c->launches += 3;
     mark(c);
@@ -680,13 +693,17 @@ int exterior_step(ak_case *c, double *fixed_partials, long long fixed_capacity) 
                 return fail(AK_ERR_INVALID, "wall links need more partial sums than the static scratch holds");
             partials = fixed_partials;
         }
-        k_walls<S><<<(unsigned)nb, 256, 0, c->stream>>>(src, c->G, c->keys, c->wall_q, c->nkeys, 1, c->n_elements,
-                                                        c->ox, c->oy, partials);
-        k_sum_partials<<<5 * c->n_elements, 32, 0, c->stream>>>(partials, (int)nb, 5 * c->n_elements, c->reduced);
+        k_walls<S><<<(unsigned)nb, 256, 0, ws>>>(src, c->G, c->keys, c->wall_q, c->nkeys, 1, c->n_elements, c->ox,
+                                                 c->oy, partials);
+        k_sum_partials<<<5 * c->n_elements, 32, 0, ws>>>(partials, (int)nb, 5 * c->n_elements, c->reduced);
         AK_CUDA(cudaGetLastError());
         c->launches += 2;
     } else {
-        AK_CUDA(cudaMemsetAsync(c->reduced, 0, sizeof(double) * 5 * c->n_elements, c->stream));
+        AK_CUDA(cudaMemsetAsync(c->reduced, 0, sizeof(double) * 5 * c->n_elements, ws));
+    }
+    if (branch) {
+        AK_CUDA(cudaEventRecord(c->ev_join, c->side));
+        AK_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
     }
     mark(c);
     k_ext_band_pull<S><<<(unsigned)blocks_for((long long)E.nband * E.nz, 128), 128, 0, c->stream>>>(src, c->G, E,
@@ -728,7 +745,7 @@ int exterior_prepare(ak_case *c) {
     k_ext_collide_ring<S><<<(unsigned)blocks_for(nr, 128), 128, 0, c->stream>>>(pdf, c->G, E, c->shift_host,
                                                                                 (T)c->omega_s, (T)c->omega_b);
     AK_CUDA(cudaGetLastError());
-    AK_CUDA(cudaMemsetAsync(c->ext_out, 0, 11 * sizeof(double), c->stream));
+    AK_CUDA(cudaMemsetAsync(c->ext_out, 0, 12 * sizeof(double), c->stream));
     c->ext_cur = 0;
     c->prepared = true;
     return AK_OK;
@@ -754,8 +771,8 @@ int build_exterior(ak_case *c, const std::vector<uint8_t> &hflags) {
     AK_TRY(dalloc(c, &c->ext_inc0, 2LL * E.nz * E.NX));
     c->ext_blocks = blocks_for(nr, EXT_THREADS);
     AK_TRY(dalloc(c, &c->ext_partials, 4 * c->ext_blocks));
-    AK_TRY(dalloc(c, &c->ext_out, 11));
-    AK_CUDA(cudaMemsetAsync(c->ext_out, 0, 11 * sizeof(double), c->stream));
+    AK_TRY(dalloc(c, &c->ext_out, 12));
+    AK_CUDA(cudaMemsetAsync(c->ext_out, 0, 12 * sizeof(double), c->stream));
     // the walls reduce their loads every step: size the partials once
     c->wall_blocks = blocks_for(c->nkeys * c->nz * 3, 256);
     if (c->wall_blocks) AK_TRY(ensure_partials(c, c->wall_blocks * 5 * c->n_elements));
@@ -987,9 +1004,9 @@ int ak_step(ak_case *c, int32_t nsteps, double *loads) {
         const bool sample = loads != nullptr && s == nsteps - 1;
         AK_TRY(with_storage(c, [&](auto *tag) {
             using S = std::remove_pointer_t<decltype(tag)>;
-            // the first step prepares the boundaries eagerly; the exterior
-            // step and timed steps stay eager
-            if (c->prepared && c->farfield != AK_FARFIELD_EXTERIOR && !c->timing) return step_graphed<S>(c, sample);
+            // the first step prepares the boundaries eagerly; timed steps
+            // stay eager
+            if (c->prepared && !c->timing) return step_graphed<S>(c, sample);
             return one_step<S>(c, sample);
         }));
     }
@@ -1363,6 +1380,12 @@ int ak_set_steps_done(ak_case *c, int64_t steps) {
     AK_TRY(check_case(c));
     if (steps < 0) return fail(AK_ERR_INVALID, "steps must be >= 0");
     c->steps = steps;
+    if (c->farfield == AK_FARFIELD_EXTERIOR) {
+        // the exterior step's clock (the traced incoming invariant's time)
+        const double clock = (double)steps;
+        AK_CUDA(cudaMemcpyAsync(c->ext_out + 11, &clock, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        AK_CUDA(cudaStreamSynchronize(c->stream));
+    }
     return AK_OK;
 }
 

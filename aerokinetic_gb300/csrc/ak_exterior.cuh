@@ -285,9 +285,10 @@ __global__ void k_ext_band_pull(const S *__restrict__ src, Grid G, ExtGeom E, do
 // band's ring values y0, stage 2 and 3 from the previous stage's values;
 // stage 1 also clears the step's reconstruction moment error
 __global__ void k_ext_stage(ExtGeom E, const double *__restrict__ band, const double *__restrict__ prev,
-                            double *__restrict__ out, int stage, double step, const double *__restrict__ inc0,
-                            double *__restrict__ moment_error) {
+                            double *__restrict__ out, int stage, const double *__restrict__ clock,
+                            const double *__restrict__ inc0, double *__restrict__ moment_error) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const double step = *clock;  // steps done before this one
     if (stage == 1 && i == 0) *moment_error = 0.0;  // the ring kernel of this step takes its maximum
     if (i >= (long long)E.nring * E.nz) return;
     const int z = (int)(i / E.nring), r = (int)(i - (long long)z * E.nring);
@@ -564,7 +565,9 @@ __global__ void __launch_bounds__(256) k_ext_ring_diagnostics(const S *__restric
 // the step's exterior source and wall mass, and their running sums:
 // out[0..3] source (mass, momentum) of the step, out[4..7] accumulated,
 // out[8] wall mass exchange of the step (sum over elements of the wall
-// kernel's incoming-minus-outgoing column), out[9] accumulated
+// kernel's incoming-minus-outgoing column), out[9] accumulated; out[10] is
+// the step's reconstruction moment error (k_ext_ring), out[11] the number of
+// steps done (the predictor's clock)
 __global__ void __launch_bounds__(REDUCE_THREADS)
     k_ext_final(const double *__restrict__ partials, long long nblocks, const double *__restrict__ walls,
                 int n_elements, double *__restrict__ out) {
@@ -579,6 +582,7 @@ __global__ void __launch_bounds__(REDUCE_THREADS)
         for (int e = 0; e < n_elements; ++e) wall += walls[5 * e + 4];
         out[8] = wall;
         out[9] += wall;
+        out[11] += 1.0;  // the step clock
     }
 }
 
