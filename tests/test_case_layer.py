@@ -82,3 +82,35 @@ def test_project_round_trip_and_fingerprint(golden, tmp_path):
     assert json.loads(path.read_text())["format"] == "aerokinetic_project"
     with pytest.raises(ValueError):
         Project.from_dict({"format": "other"})
+
+
+def test_vectorised_intersection_tests_agree_with_the_pairwise_test():
+    """Contour and Section validation evaluate segments_intersect (the
+    reference's closed-segment test, geometry.py:112-123) over all edge pairs
+    with numpy; on random polygons, including collinear and touching edges on
+    a half-integer lattice, the outcome equals the pair-by-pair loop."""
+    from aerokinetic_gb300.geometry import _any_segments_intersect, _pairs_intersect, segments_intersect
+    rng = np.random.default_rng(7)
+    for trial in range(200):
+        n = int(rng.integers(3, 12))
+        p = rng.normal(size=(n, 2))
+        q = rng.normal(size=(5, 2))
+        if trial % 3 == 0:
+            p, q = np.round(p * 2) / 2, np.round(q * 2) / 2
+        pn, qn = np.roll(p, -1, axis=0), np.roll(q, -1, axis=0)
+        self_ref = any(segments_intersect(p[i], pn[i], p[j], pn[j])
+                       for i in range(n) for j in range(i + 2, n) if not (i == 0 and j == n - 1))
+        assert _any_segments_intersect(p, pn) == self_ref
+        i, j = np.meshgrid(np.arange(n), np.arange(5), indexing="ij")
+        pair_ref = [segments_intersect(p[a], pn[a], q[b], qn[b]) for a, b in zip(i.ravel(), j.ravel())]
+        assert list(_pairs_intersect(p[i.ravel()], pn[i.ravel()], q[j.ravel()], qn[j.ravel()])) == pair_ref
+
+
+def test_validation_errors_match_the_reference_messages():
+    square = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], dtype=float)
+    bowtie = np.array([[0, 0], [2, 2], [2, 0], [0, 1]], dtype=float)
+    with pytest.raises(ValueError, match="Self-intersection"):
+        Contour(bowtie, "bowtie")
+    with pytest.raises(ValueError, match="touch or overlap"):
+        Section((Contour(square, "a"), Contour(square + [0.5, 0.0], "b")))
+    Section((Contour(square, "a"), Contour(square + [2.0, 0.0], "b")))
