@@ -1800,10 +1800,22 @@ int refined_step(ak_refined *R, bool fork = false) {
         AK_CUDA(cudaEventRecord(R->ev_flux_done, R->flux));
         AK_CUDA(cudaStreamWaitEvent(st, R->ev_flux_done, 0));
     }
+    // the restriction (coarse cells inside the box) and the reflux (coarse
+    // cells just outside its faces) write disjoint cells: in the graph the
+    // restriction runs on the side stream beside the reflux
+    if (fork) {
+        AK_CUDA(cudaEventRecord(R->ev_fork, st));
+        AK_CUDA(cudaStreamWaitEvent(R->side, R->ev_fork, 0));
+        launch_restrict<S>(R, f2c, R->side);
+        AK_CUDA(cudaEventRecord(R->ev_join, R->side));
+    }
     k_reflux<S><<<dim3((unsigned)split_blocks(R->max_face), R->nfaces), SPLIT_THREADS, 0, st>>>(
         src_of<S>(C), C->G, R->d_faces, R->nfaces, R->d_offs, R->reg_c, R->reg_f,
         1.0 / (R->dx_c * R->dx_c * R->dx_c), R->d_flag);
-    launch_restrict<S>(R, f2c, st);
+    if (fork)
+        AK_CUDA(cudaStreamWaitEvent(st, R->ev_join, 0));
+    else
+        launch_restrict<S>(R, f2c, st);
     AK_CUDA(cudaGetLastError());
     // a tracked budget closes on the integrals of the state the step leaves
     if (R->track_budget && R->step_stats) AK_TRY(enqueue_region_stats<S>(R, st));
