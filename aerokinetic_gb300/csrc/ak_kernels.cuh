@@ -211,7 +211,7 @@ __device__ __forceinline__ void wall_block_sums(const double acc[5], int element
 // mass = sum g_in - g_out.  Partials: [element][block][5].
 constexpr int MAX_ELEMENTS = 8;
 template <typename S>
-__global__ void __launch_bounds__(256) k_walls(S *__restrict__ pdf, Grid G, const WallKey *__restrict__ keys,
+__global__ void __launch_bounds__(256, 2) k_walls(S *__restrict__ pdf, Grid G, const WallKey *__restrict__ keys,
                                                const double *__restrict__ qs, long long nkeys, int sample,
                                                int n_elements, double ox, double oy,
                                                double *__restrict__ partials) {

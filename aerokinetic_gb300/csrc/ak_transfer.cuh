@@ -288,13 +288,22 @@ __global__ void k_stream(const S *__restrict__ src, S *__restrict__ dst, const u
     if (x > G.nx) return;
     if (__ldg(flags + y * G.nxp + x) != FLAG_FLUID) return;
     const long long c = G.cell(x, y, z);
+    if (!periodic_xy) {
+        // the cell's column in the three z planes it pulls from: one address
+        // add per population
+        const S *row[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) row[k] = src + (long long)G.wrapz(z - (k - 1)) * G.plane + (long long)y * G.sx + x;
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+            dst[q * G.qs + c] = row[cz(q) + 1][(long long)q * G.qs - (long long)cy(q) * G.sx - cx(q)];
+        return;
+    }
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         int xs = x - cx(q), ys = y - cy(q);
-        if (periodic_xy) {
-            xs = xs < 1 ? xs + G.nx : (xs > G.nx ? xs - G.nx : xs);
-            ys = ys < 1 ? ys + G.ny : (ys > G.ny ? ys - G.ny : ys);
-        }
+        xs = xs < 1 ? xs + G.nx : (xs > G.nx ? xs - G.nx : xs);
+        ys = ys < 1 ? ys + G.ny : (ys > G.ny ? ys - G.ny : ys);
         dst[q * G.qs + c] = src[q * G.qs + G.cell(xs, ys, G.wrapz(z - cz(q)))];
     }
 }
