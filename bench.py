@@ -216,6 +216,22 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def reduce_max(value, dist):
+    """The largest of every rank's value (the slowest replica's time): on the
+    GPU for NCCL, on the host for gloo."""
+    import torch
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_mlups(cells, steps, elapsed_ms, world):
+    """Whole-job MLUPS of `world` replicas that each advanced `cells` cell
+    updates per step for `steps` steps in `elapsed_ms` (the slowest rank's)."""
+    return world * cells * steps / (elapsed_ms / 1e3) / 1e6
+
+
 def flush_l2(buf, stream):
     import torch
     with torch.cuda.stream(stream):
@@ -516,10 +532,8 @@ def run_engine(args, rank, world, local_rank):
               "fine_collide_ms": ms[3] / group_steps, "fine_stream_ms": ms[4] / group_steps,
               "interface_and_boundaries_ms": ms[5] / group_steps, "eager_step_ms": ms[0] / group_steps}
     if dist:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
-    value = world * cells * args.steps / (elapsed_ms / 1e3) / 1e6
+        elapsed_ms = reduce_max(elapsed_ms, dist)
+    value = replica_mlups(cells, args.steps, elapsed_ms, world)
     fine_padded = math.prod(n for n in (2 * plan.box.shape[0] + 4, 2 * plan.box.shape[1] + 4, 2 * plan.box.shape[2]))
     coarse_cells = math.prod(plan.shape)
     solver.close()
