@@ -740,8 +740,8 @@ int exterior_prepare(ak_case *c) {
     k_ext_fill_ring<S><<<(unsigned)blocks_for(nr, 128), 128, 0, c->stream>>>(pdf, c->G, E);
     k_ext_band_direct<S><<<(unsigned)blocks_for((long long)E.nband * E.nz, 128), 128, 0, c->stream>>>(
         pdf, c->G, E, c->ext_band[0], c->ext_inc0);
-    dim3 grid((unsigned)blocks_for(c->nx, 128), (unsigned)c->ny, (unsigned)c->nz);
-    k_collide<S><<<grid, 128, 0, c->stream>>>(pdf, c->flags, c->G, c->shift_host, (T)c->omega_s, (T)c->omega_b);
+    k_collide<S><<<(unsigned)blocks_for((long long)c->nx * c->ny * c->nz, 128), 128, 0, c->stream>>>(
+        pdf, c->flags, c->G, c->shift_host, (T)c->omega_s, (T)c->omega_b);
     k_ext_collide_ring<S><<<(unsigned)blocks_for(nr, 128), 128, 0, c->stream>>>(pdf, c->G, E, c->shift_host,
                                                                                 (T)c->omega_s, (T)c->omega_b);
     AK_CUDA(cudaGetLastError());
@@ -1685,6 +1685,9 @@ int refined_step(ak_refined *R, bool fork = false) {
     const long long nring_block = ring_count(B.dnx, B.dny, DONOR_RING, DONOR_RING) * C->nz;
     dim3 gc((unsigned)blocks_for(C->nx, 128), (unsigned)C->ny, (unsigned)C->nz);
     dim3 gf((unsigned)blocks_for(F->nx, 128), (unsigned)F->ny, (unsigned)F->nz);
+    // the collisions number their cells across rows (1-D grids)
+    const unsigned gc1 = (unsigned)blocks_for((long long)C->nx * C->ny * C->nz, 128);
+    const unsigned gf1 = (unsigned)blocks_for((long long)F->nx * F->ny * F->nz, 128);
     const Rescale c2f{R->tau_s_f * R->dt_f / (R->tau_s_c * R->dt_c), R->tau_b_f * R->dt_f / (R->tau_b_c * R->dt_c)};
     const Rescale f2c{R->tau_s_c * R->dt_c / (R->tau_s_f * R->dt_f), R->tau_b_c * R->dt_c / (R->tau_b_f * R->dt_f)};
     const long long nband = ring_count(F->nx, F->ny, R->pad, R->pad) * F->nz;
@@ -1705,7 +1708,7 @@ int refined_step(ak_refined *R, bool fork = false) {
     // coarse collide, face fluxes, outer boundary, stream, donors after the step
     auto coarse_part = [&]() -> int {
         mark(C);
-        k_collide<S><<<gc, 128, 0, st>>>(src_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s,
+        k_collide<S><<<gc1, 128, 0, st>>>(src_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s,
                                          (T)C->omega_b);
         mark(C);
         cudaStream_t fs = flux_stream(st, 0);
@@ -1748,7 +1751,8 @@ int refined_step(ak_refined *R, bool fork = false) {
         k_donors<S><<<(unsigned)split_blocks(nband), SPLIT_THREADS, 0, s>>>(src_of<S>(F), F->G, C->nz, R->pro_xy,
                                                                             c2f, R->pad, R->d_flag);
         mark(C);
-        k_collide<S><<<gf, 128, 0, s>>>(src_of<S>(F), F->flags, F->G, F->shift_host, (T)F->omega_s, (T)F->omega_b);
+        k_collide<S><<<gf1, 128, 0, s>>>(src_of<S>(F), F->flags, F->G, F->shift_host, (T)F->omega_s,
+                                          (T)F->omega_b);
         mark(C);
         cudaStream_t fs = flux_stream(s, 1 + sub);
         if (!fs) return fail(AK_ERR_CUDA, "face-flux branch could not be forked");

@@ -264,10 +264,15 @@ __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
     k_collide(S *__restrict__ pdf, const uint8_t *__restrict__ flags, Grid G, Shift27 shift,
               typename Store<S>::T omega_s, typename Store<S>::T omega_b) {
     using T = typename Store<S>::T;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int y = blockIdx.y + 1;
-    const int z = blockIdx.z;
-    if (x > G.nx) return;
+    // one thread per interior cell, x fastest, numbered across rows: warps
+    // stay full whatever nx is (this kernel is bound by the FP64 pipe in the
+    // plain form, where a warp with a few live lanes costs a full one)
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned nxy = (unsigned)G.nx * (unsigned)G.ny;
+    if (i >= nxy * (unsigned)G.nz) return;
+    const unsigned z = i / nxy, r = i - z * nxy;
+    const unsigned yr = r / (unsigned)G.nx;
+    const int x = (int)(r - yr * (unsigned)G.nx) + 1, y = (int)yr + 1;
     if (__ldg(flags + y * G.nxp + x) != FLAG_FLUID) return;
     const long long c = G.cell(x, y, z);
     T g[Q];
