@@ -584,7 +584,7 @@ int one_step(ak_case *c, bool sample, double *fixed_partials = nullptr, long lon
     }
     // bulk
     mark(c);
-    dim3 grid((unsigned)blocks_for(c->nx, 128), (unsigned)c->ny, (unsigned)c->nz);
+    const unsigned grid = (unsigned)blocks_for((long long)c->nx * c->ny * c->nz, 128);
     k_stream_collide<S><<<grid, 128, 0, c->stream>>>(src, dst_of<S>(c), c->flags, c->G, c->shift_host,
                                                      (T)c->omega_s, (T)c->omega_b, sgs_of<S>(c));
     AK_CUDA(cudaGetLastError());
@@ -714,7 +714,7 @@ int exterior_step(ak_case *c, double *fixed_partials, long long fixed_capacity, 
     AK_CUDA(cudaGetLastError());
     c->launches += 2;
     mark(c);
-    dim3 grid((unsigned)blocks_for(c->nx, 128), (unsigned)c->ny, (unsigned)c->nz);
+    const unsigned grid = (unsigned)blocks_for((long long)c->nx * c->ny * c->nz, 128);
     k_stream_collide<S><<<grid, 128, 0, c->stream>>>(src, dst, c->flags, c->G, c->shift_host, (T)c->omega_s,
                                                      (T)c->omega_b, Sgs<T>{});
     AK_CUDA(cudaGetLastError());

@@ -109,11 +109,16 @@ __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
     k_stream_collide(const S *__restrict__ src, S *__restrict__ dst, const uint8_t *__restrict__ flags, Grid G,
                      Shift27 shift, typename Store<S>::T omega_s, typename Store<S>::T omega_b,
                      Sgs<typename Store<S>::T> sgs) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int y = blockIdx.y + 1;
-    const int z = blockIdx.z;
-    if (x > G.nx) return;
-    stream_collide_cell(src, dst, flags, G, shift, omega_s, omega_b, x, y, z, sgs);
+    // one thread per interior cell, x fastest, numbered across rows: warps
+    // stay full whatever nx is (the plain form is bound by the FP64 pipe,
+    // where a warp with a few live lanes costs as much as a full one)
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned nxy = (unsigned)G.nx * (unsigned)G.ny;
+    if (i >= nxy * (unsigned)G.nz) return;
+    const unsigned z = i / nxy, r = i - z * nxy;
+    const unsigned yr = r / (unsigned)G.nx;
+    stream_collide_cell(src, dst, flags, G, shift, omega_s, omega_b, (int)(r - yr * (unsigned)G.nx) + 1, (int)yr + 1,
+                        (int)z, sgs);
 }
 
 // ------------------------------------------------------------ walls
