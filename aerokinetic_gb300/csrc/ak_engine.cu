@@ -1486,7 +1486,7 @@ struct ak_refined {
     double free_g[Q];
     double *d_free = nullptr;
     double *mom_old = nullptr, *mom_new = nullptr, *mom_half = nullptr;
-    double *pro_x = nullptr, *pro_xy = nullptr;  // donor moments after the x and the y prolongation pass
+    double *pro_x = nullptr;  // donor moments after the x prolongation pass
     Face faces[4];
     int nfaces = 0;
     long long offs[4] = {0, 0, 0, 0};
@@ -1692,7 +1692,6 @@ int refined_step(ak_refined *R, bool fork = false) {
     const Rescale f2c{R->tau_s_c * R->dt_c / (R->tau_s_f * R->dt_f), R->tau_b_c * R->dt_c / (R->tau_b_f * R->dt_f)};
     const long long nband = ring_count(F->nx, F->ny, R->pad, R->pad) * F->nz;
     const long long nprox = ring_count(F->nx, B.dny, R->pad, DONOR_RING) * C->nz;
-    const long long nproxy = ring_count(F->nx, F->ny, R->pad, R->pad) * C->nz;
     const long long nlinks = F->nkeys * F->nz * 3;
     const long long nb = blocks_for(nlinks, 256);
 
@@ -1747,8 +1746,7 @@ int refined_step(ak_refined *R, bool fork = false) {
         // half-way (1 - 1/2) old + 1/2 new (refined_solver.py:311-318)
         k_prolong_x<<<(unsigned)blocks3(nprox), 256, 0, s>>>(B, C->nz, R->pad, sub ? R->mom_half : R->mom_old,
                                                               R->pro_x);
-        k_prolong_y<<<(unsigned)blocks3(nproxy), 256, 0, s>>>(B, C->nz, R->pad, R->pro_x, R->pro_xy);
-        k_donors<S><<<(unsigned)split_blocks(nband), SPLIT_THREADS, 0, s>>>(src_of<S>(F), F->G, C->nz, R->pro_xy,
+        k_donors<S><<<(unsigned)split_blocks(nband), SPLIT_THREADS, 0, s>>>(src_of<S>(F), F->G, C->nz, R->pro_x, B.dny,
                                                                             c2f, R->pad, R->d_flag);
         mark(C);
         k_collide<S><<<gf1, 128, 0, s>>>(src_of<S>(F), F->flags, F->G, F->shift_host, (T)F->omega_s,
@@ -1824,7 +1822,7 @@ int refined_step(ak_refined *R, bool fork = false) {
     // a tracked budget closes on the integrals of the state the step leaves
     if (R->track_budget && R->step_stats) AK_TRY(enqueue_region_stats<S>(R, st));
     mark(C);  // step end
-    C->launches += 6 + 8 * 2 + (C->n_ubb ? 1 : 0) + (C->n_out ? 1 : 0) + (nlinks ? 0 : -4) + 1;
+    C->launches += 6 + 7 * 2 + (C->n_ubb ? 1 : 0) + (C->n_out ? 1 : 0) + (nlinks ? 0 : -4) + 1;
     C->steps += 1;
     F->steps += 2;
     R->steps += 1;
@@ -1967,7 +1965,6 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
     if (r == AK_OK) r = ralloc(R, &R->mom_new, (size_t)nblock * 10);
     if (r == AK_OK) r = ralloc(R, &R->mom_half, (size_t)nblock * 10);
     if (r == AK_OK) r = ralloc(R, &R->pro_x, (size_t)(2 * B.bx + 2 * R->pad) * B.dny * cd.nz * 10);
-    if (r == AK_OK) r = ralloc(R, &R->pro_xy, (size_t)(2 * B.bx + 2 * R->pad) * (2 * B.by + 2 * R->pad) * cd.nz * 10);
     if (r == AK_OK) {
         R->nfaces = 0;
         long long off = 0;

@@ -515,31 +515,15 @@ __global__ void k_prolong_x(BoxSpec B, int nz, int pad, const double *__restrict
     }
 }
 
-// y pass on the band: out[k][z][fy][fx] (fy in [0, nfy = 2 (by + 2)))
-__global__ void k_prolong_y(BoxSpec B, int nz, int pad, const double *__restrict__ in, double *__restrict__ out) {
-    const int nfx = 2 * (B.bx + 2), nfy = 2 * (B.by + 2);
-    const long long nring = ring_count(nfx, nfy, pad, pad);
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nring * nz) return;
-    const int z = (int)(i / nring);
-    int fx, fy;
-    ring_cell(i - z * nring, nfx, nfy, pad, pad, fx, fy);
-    const long long n = (long long)nfx * nfy * nz, nin = (long long)nfx * B.dny * nz;
-    const long long o = ((long long)z * nfy + fy) * nfx + fx, base = ((long long)z * B.dny + (fy >> 1)) * nfx + fx;
-#pragma unroll
-    for (int k = 0; k < 10; ++k) {
-        const double *a = in + k * nin + base;
-        out[k * n + o] = prolong_child(a[0], a[nfx], a[2 * nfx], a[3 * nfx], a[4 * nfx], fy & 1);
-    }
-}
-
-// z pass on the padding band (pad fine cells around the physical block in x
-// and y, every z), stress rescaled coarse -> fine, populations.  Warp w
-// prolongs moments w and w + 8, warp 0 rescales and prepares the fields,
-// every warp writes its own directions.
+// y and z passes on the padding band (pad fine cells around the physical
+// block in x and y, every z), stress rescaled coarse -> fine, populations.
+// Warp w prolongs moments w and w + 8: each of the five coarse z planes the
+// z pass reads is first prolonged in y from the x pass's rows, so the y pass
+// needs no launch of its own (the same operations on the same values).  Warp
+// 0 rescales and prepares the fields, every warp writes its own directions.
 template <typename S>
 __global__ void __launch_bounds__(SPLIT_THREADS)
-    k_donors(S *__restrict__ fine, Grid F, int nzc, const double *__restrict__ pxy, Rescale r, int pad,
+    k_donors(S *__restrict__ fine, Grid F, int nzc, const double *__restrict__ px, int dny, Rescale r, int pad,
              int *__restrict__ flag) {
     using T = typename Store<S>::A;
     __shared__ SplitShared<T> sh;
@@ -553,14 +537,20 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
         fz = (int)(i / nring);
         ring_cell(i - fz * nring, F.nx, F.ny, pad, pad, fx, fy);
     }
-    const long long plane = (long long)F.nx * F.ny, nxy = plane * nzc, cell = (long long)fy * F.nx + fx;
+    // x-pass rows: px[k][z][by][fx], fx in [0, F.nx), by in [0, dny)
+    const long long nin = (long long)F.nx * dny * nzc, row0 = (long long)(fy >> 1) * F.nx + fx;
     const int pz = fz >> 1;
     for (int k = w; k < 10; k += SPLIT_WARPS) {
         double a[5];
 #pragma unroll
         for (int j = 0; j < 5; ++j) {
             const int zz = ((pz + j - 2) % nzc + nzc) % nzc;
-            a[j] = valid ? pxy[k * nxy + zz * plane + cell] : (k == 0 ? 1.0 : 0.0);
+            if (valid) {
+                const double *b = px + k * nin + (long long)zz * dny * F.nx + row0;
+                a[j] = prolong_child(b[0], b[F.nx], b[2 * F.nx], b[3 * F.nx], b[4 * F.nx], fy & 1);
+            } else {
+                a[j] = k == 0 ? 1.0 : 0.0;
+            }
         }
         sh.field[0][k][lane] = T(prolong_child(a[0], a[1], a[2], a[3], a[4], fz & 1));
     }
