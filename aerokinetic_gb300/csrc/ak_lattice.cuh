@@ -142,6 +142,17 @@ struct Shift27 {
 };
 
 // ---------------------------------------------------------------- collision
+// a * s for a power of two s (0.5, 2, -2, 4, -1): exact in every form, so the
+// double-float form scales both of its words instead of a full product
+template <typename T>
+__host__ __device__ __forceinline__ T mul_pow2(T a, double s) {
+    return a * T(s);
+}
+template <>
+__host__ __device__ __forceinline__ df64 mul_pow2<df64>(df64 a, double s) {
+    return df64(a.hi * (float)s, a.lo * (float)s);
+}
+
 // Smagorinsky subgrid model (sgs="smagorinsky", solver.py:74-77; Hou,
 // Sterling, Chen & Doolen 1996 in lattice units): with the non-equilibrium
 // second moments Pi_ab = K_ab - rho/3 delta_ab (K the central moments) and
@@ -318,42 +329,42 @@ __host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b, 
     const T omr = om1 * rinv;
     const T sxy = (M110 - jx * uy) * omr, sxz = (M101 - jx * uz) * omr, syz = (M011 - jy * uz) * omr;
     // coefficient products
-    const T s2xy = T(2) * sxy, s2xz = T(2) * sxz, s2yz = T(2) * syz;
+    const T s2xy = mul_pow2(sxy, 2.0), s2xz = mul_pow2(sxz, 2.0), s2yz = mul_pow2(syz, 2.0);
     const T kAchi = s2xy * sxy;        // 2 sxy^2
     const T kBpsi = s2xy * syz;        // 2 sxy syz
     const T kBchi = s2xy * sxz;        // 2 sxy sxz
     const T kCphi = s2yz * syz;        // 2 syz^2
     const T kCpsi = s2xz * syz;        // 2 sxz syz
     const T kCchi = s2xz * sxz;        // 2 sxz^2
-    const T k8 = T(4) * kBchi * syz;   // 8 sxy sxz syz
+    const T k8 = mul_pow2(kBchi, 4.0) * syz;   // 8 sxy sxz syz
     // y-functions
-    const T phy[3] = {T(0.5) * (ty - uy), T(1) - ty, T(0.5) * (ty + uy)};
-    const T psy[3] = {uy - T(0.5), T(-2) * uy, uy + T(0.5)};
-    const T chy[3] = {T(0.5), T(-1), T(0.5)};
+    const T phy[3] = {mul_pow2(ty - uy, 0.5), T(1) - ty, mul_pow2(ty + uy, 0.5)};
+    const T psy[3] = {uy - T(0.5), mul_pow2(uy, -2.0), uy + T(0.5)};
+    constexpr double chy[3] = {0.5, -1.0, 0.5};
     // x-functions: phi_x(+-1) = (t_x +- u_x) / 2, psi_x(+-1) = u_x +- 1/2
-    const T htx = T(0.5) * tx, hux = T(0.5) * ux, omtx = T(1) - tx, m2ux = T(-2) * ux;
+    const T htx = mul_pow2(tx, 0.5), hux = mul_pow2(ux, 0.5), omtx = T(1) - tx, m2ux = mul_pow2(ux, -2.0);
     const T px2 = htx + hux, px0 = htx - hux, sx2 = ux + T(0.5), sx0 = ux - T(0.5);
     // rho-scaled z-functions, the c_z = +1 and -1 rows as sums and differences
-    const T rhtz = T(0.5) * rho * tz, rhuz = T(0.5) * rho * uz, rh = T(0.5) * rho;
-    const T r0z = rho * (T(1) - tz), rm2uz = T(-2) * rho * uz, ruz = rho * uz;
+    const T rh = mul_pow2(rho, 0.5), rhtz = rh * tz, rhuz = rh * uz;
+    const T r0z = rho * (T(1) - tz), rm2uz = mul_pow2(rho, -2.0) * uz, ruz = rho * uz;
     const T pz2 = rhtz + rhuz, pz0 = rhtz - rhuz, qz2 = ruz + rh, qz0 = ruz - rh;
 #pragma unroll
     for (int iy = 0; iy < 3; ++iy) {
         // coefficients of phi_x, psi_x, chi_x in A, B, C for this c_y
-        const T Ap = phy[iy], As = sxy * psy[iy], Ac = kAchi * chy[iy];
-        const T Bp = syz * psy[iy], Bs = sxz * phy[iy] + kBpsi * chy[iy], Bc = kBchi * psy[iy];
-        const T Cp = kCphi * chy[iy], Cs = kCpsi * psy[iy], Cc = kCchi * phy[iy] + k8 * chy[iy];
+        const T Ap = phy[iy], As = sxy * psy[iy], Ac = mul_pow2(kAchi, chy[iy]);
+        const T Bp = syz * psy[iy], Bs = sxz * phy[iy] + mul_pow2(kBpsi, chy[iy]), Bc = kBchi * psy[iy];
+        const T Cp = mul_pow2(kCphi, chy[iy]), Cs = kCpsi * psy[iy], Cc = kCchi * phy[iy] + mul_pow2(k8, chy[iy]);
         T A[3], B[3], C[3];
         {
-            const T hc = T(0.5) * Ac;
+            const T hc = mul_pow2(Ac, 0.5);
             A[2] = px2 * Ap + (sx2 * As + hc); A[0] = px0 * Ap + (sx0 * As + hc); A[1] = omtx * Ap + (m2ux * As - Ac);
         }
         {
-            const T hc = T(0.5) * Bc;
+            const T hc = mul_pow2(Bc, 0.5);
             B[2] = px2 * Bp + (sx2 * Bs + hc); B[0] = px0 * Bp + (sx0 * Bs + hc); B[1] = omtx * Bp + (m2ux * Bs - Bc);
         }
         {
-            const T hc = T(0.5) * Cc;
+            const T hc = mul_pow2(Cc, 0.5);
             C[2] = px2 * Cp + (sx2 * Cs + hc); C[0] = px0 * Cp + (sx0 * Cs + hc); C[1] = omtx * Cp + (m2ux * Cs - Cc);
         }
         // the rest weights (equal for c_z = -1 and +1) enter the fused
