@@ -1,7 +1,7 @@
 """Pins of the CPU oracle against the reference's own recorded outputs.
 
 The oracle (oracle/) restates the reference's lbmpy-generated step.  Before it
-may judge the CUDA engine it has to reproduce what the reference itself wrote
+may check the CUDA engine it has to reproduce what the reference itself wrote
 down: plane-wave probe records for its UBB and ExtrapolationOutflow
 (docs/verification_stage1_20261106/acoustics/), a nonlinear start-up with the
 Mach/density guards (docs/verification_failure_capture_20261107/), the 272-step
