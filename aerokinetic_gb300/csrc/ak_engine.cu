@@ -1499,7 +1499,7 @@ struct ak_refined {
     int *d_flag = nullptr;
     double *d_loads = nullptr;
     long long steps = 0;
-    std::vector<void *> owned;  // device buffers of the driver
+    std::vector<void *> owned;  // device buffers the two-level case owns
     // one captured coarse step per (coarse, fine) buffer parity, replayed by
     // ak_refined_step; launches_per_step counts the kernels of one replay
     cudaGraphExec_t graph[16] = {};  // (coarse copy, fine copy, budget, step integrals)
