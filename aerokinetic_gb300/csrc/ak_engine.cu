@@ -1481,6 +1481,15 @@ struct ak_refined {
     ak_case *coarse = nullptr, *fine = nullptr;
     BoxSpec B{};
     int pad = 2;
+    // The coarse level keeps post-collision populations outside the transfer
+    // block (the box and three coarse cells around it, padded coordinates
+    // x [xfer.x, xfer.y) by y [xfer.z, xfer.w)), whose cells the donors read
+    // and the reflux and restriction write as pre-collision populations
+    // there: the coarse streaming of one step then fuses with the next
+    // step's collision everywhere else.  Used when the block lies inside the
+    // lattice (the donor block does not wrap).
+    bool fused = false;
+    int4 xfer{0, 0, 0, 0};
     double dx_c = 0, dt_c = 0, dx_f = 0, dt_f = 0, span = 0, speed = 0;
     double tau_s_c = 0, tau_b_c = 0, tau_s_f = 0, tau_b_f = 0;
     double free_g[Q];
@@ -1647,6 +1656,14 @@ int refined_init(ak_refined *R, double amp, double phase_y, double phase_z, doub
             src_of<S>(C), C->G, C->outer(), C->sel_out, C->n_out, C->out_state, 1, 0, 0, 1.0, C->speed, 0.0, 0.0);
         AK_CUDA(cudaGetLastError());
     }
+    if (R->fused) {
+        // outside the transfer block the coarse level stores post-collision
+        using T = typename Store<S>::T;
+        k_collide<S><<<(unsigned)blocks_for((long long)C->nx * C->ny * C->nz, 128), 128, 0, st>>>(
+            src_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s, (T)C->omega_b,
+            make_int4(0, 1 << 30, 0, 1 << 30), R->xfer);
+        AK_CUDA(cudaGetLastError());
+    }
     C->prepared = F->prepared = true;
     R->steps = 0;
     AK_CUDA(cudaMemsetAsync(R->outer_out, 0, 8 * sizeof(double), st));
@@ -1707,8 +1724,9 @@ int refined_step(ak_refined *R, bool fork = false) {
     // coarse collide, face fluxes, outer boundary, stream, donors after the step
     auto coarse_part = [&]() -> int {
         mark(C);
+        // fused: only the transfer block holds pre-collision populations
         k_collide<S><<<gc1, 128, 0, st>>>(src_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s,
-                                         (T)C->omega_b);
+                                          (T)C->omega_b, R->fused ? R->xfer : make_int4(0, 1 << 30, 0, 1 << 30));
         mark(C);
         cudaStream_t fs = flux_stream(st, 0);
         if (!fs) return fail(AK_ERR_CUDA, "face-flux branch could not be forked");
@@ -1731,7 +1749,13 @@ int refined_step(ak_refined *R, bool fork = false) {
             C->launches += 2;
         }
         mark(C);
-        k_stream<S><<<gc, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, 0);
+        if (R->fused)
+            // streaming fused with the next step's collision, the transfer
+            // block streamed only
+            k_stream_collide<S><<<gc1, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, C->shift_host,
+                                                      (T)C->omega_s, (T)C->omega_b, Sgs<T>{}, R->xfer);
+        else
+            k_stream<S><<<gc, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, 0);
         mark(C);
         AK_CUDA(cudaGetLastError());
         C->cur = 1 - C->cur;
@@ -1919,6 +1943,8 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
     B.dy0 = B.lo[1] - 3;
     B.dnx = B.bx + 6;
     B.dny = B.by + 6;
+    R->fused = B.lo[0] >= 3 && B.hi[0] + 3 <= cd.nx && B.lo[1] >= 3 && B.hi[1] + 3 <= cd.ny;
+    R->xfer = make_int4(B.lo[0] - 2, B.hi[0] + 4, B.lo[1] - 2, B.hi[1] + 4);
     int r = AK_OK;
     // coarse lattice: no walls (they live on the fine level)
     ak_case_desc coarse = cd;

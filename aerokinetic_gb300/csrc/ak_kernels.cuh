@@ -74,13 +74,15 @@ __device__ __forceinline__ float shift_at(const Shift27 &s, int q) { return s.v[
 __device__ __forceinline__ float shift_at(const float *s, int q) { return __ldg(s + q); }
 
 // pull the 27 populations of interior cell (x, y, z) (padded x, y), collide,
-// store into dst if the column is fluid
+// store into dst if the column is fluid; stream_only: store the pulled values
+// as they are (bit copies, no collision)
 template <typename S, typename Shift>
 __device__ __forceinline__ void stream_collide_cell(const S *__restrict__ src, S *__restrict__ dst,
                                                     const uint8_t *__restrict__ flags, const Grid &G,
                                                     const Shift &shift, typename Store<S>::T omega_s,
                                                     typename Store<S>::T omega_b, int x, int y, int z,
-                                                    const Sgs<typename Store<S>::T> &sgs) {
+                                                    const Sgs<typename Store<S>::T> &sgs,
+                                                    bool stream_only = false) {
     using T = typename Store<S>::T;
     // the column flag only gates the stores, so the 27 loads issue at once
     const bool fluid = __ldg(flags + y * G.nxp + x) == FLAG_FLUID;
@@ -89,6 +91,14 @@ __device__ __forceinline__ void stream_collide_cell(const S *__restrict__ src, S
     const S *row[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) row[c] = src + (long long)G.wrapz(z - (c - 1)) * G.plane + (long long)y * G.sx + x;
+    if (stream_only) {
+        if (!fluid) return;
+        const long long c = G.cell(x, y, z);
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+            dst[q * G.qs + c] = row[cz(q) + 1][(long long)q * G.qs - (long long)cy(q) * G.sx - cx(q)];
+        return;
+    }
     T g[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -108,7 +118,7 @@ template <typename S>
 __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
     k_stream_collide(const S *__restrict__ src, S *__restrict__ dst, const uint8_t *__restrict__ flags, Grid G,
                      Shift27 shift, typename Store<S>::T omega_s, typename Store<S>::T omega_b,
-                     Sgs<typename Store<S>::T> sgs) {
+                     Sgs<typename Store<S>::T> sgs, int4 raw = make_int4(0, 0, 0, 0)) {
     // one thread per interior cell, x fastest, numbered across rows: warps
     // stay full whatever nx is (the plain form is bound by the FP64 pipe,
     // where a warp with a few live lanes costs as much as a full one)
@@ -117,8 +127,11 @@ __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
     if (i >= nxy * (unsigned)G.nz) return;
     const unsigned z = i / nxy, r = i - z * nxy;
     const unsigned yr = r / (unsigned)G.nx;
-    stream_collide_cell(src, dst, flags, G, shift, omega_s, omega_b, (int)(r - yr * (unsigned)G.nx) + 1, (int)yr + 1,
-                        (int)z, sgs);
+    const int x = (int)(r - yr * (unsigned)G.nx) + 1, y = (int)yr + 1;
+    // raw: the padded x [raw.x, raw.y) by y [raw.z, raw.w) columns are only
+    // streamed (they keep pre-collision populations)
+    const bool stream_only = x >= raw.x && x < raw.y && y >= raw.z && y < raw.w;
+    stream_collide_cell(src, dst, flags, G, shift, omega_s, omega_b, x, y, (int)z, sgs, stream_only);
 }
 
 // ------------------------------------------------------------ walls

@@ -262,7 +262,8 @@ __device__ __forceinline__ void rescale_stress(T m[10], Rescale r) {
 template <typename S>
 __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
     k_collide(S *__restrict__ pdf, const uint8_t *__restrict__ flags, Grid G, Shift27 shift,
-              typename Store<S>::T omega_s, typename Store<S>::T omega_b) {
+              typename Store<S>::T omega_s, typename Store<S>::T omega_b,
+              int4 keep = make_int4(0, 1 << 30, 0, 1 << 30), int4 skip = make_int4(0, 0, 0, 0)) {
     using T = typename Store<S>::T;
     // one thread per interior cell, x fastest, numbered across rows: warps
     // stay full whatever nx is (this kernel is bound by the FP64 pipe in the
@@ -273,6 +274,10 @@ __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
     const unsigned z = i / nxy, r = i - z * nxy;
     const unsigned yr = r / (unsigned)G.nx;
     const int x = (int)(r - yr * (unsigned)G.nx) + 1, y = (int)yr + 1;
+    // only the padded columns inside keep = x [keep.x, keep.y) by y [keep.z,
+    // keep.w) and outside skip (same layout)
+    if (x < keep.x || x >= keep.y || y < keep.z || y >= keep.w) return;
+    if (x >= skip.x && x < skip.y && y >= skip.z && y < skip.w) return;
     if (__ldg(flags + y * G.nxp + x) != FLAG_FLUID) return;
     const long long c = G.cell(x, y, z);
     T g[Q];

@@ -261,8 +261,24 @@ class RefinedSolver:
         data = {"project_case": self.project.case_fingerprint, "refinement": asdict(self.refinement)}
         return hashlib.sha256(json.dumps(data, sort_keys=True, separators=(",", ":")).encode()).hexdigest()
 
+    def coarse_post_collision(self):
+        """(nx, ny) columns where states() holds post-collision coarse
+        populations: outside the transfer block (the fine box and three coarse
+        cells around it), whose coarse streaming is fused with the next step's
+        collision, when that block lies inside the lattice.  The reference
+        stores pre-collision populations everywhere; collision conserves mass
+        and momentum, so macroscopic fields and integrals agree."""
+        nx, ny, _ = self.plan.shape
+        lo, hi = self.plan.box.lower, self.plan.box.upper
+        mask = np.zeros((nx, ny), dtype=bool)
+        if lo[0] >= 3 and hi[0] + 3 <= nx and lo[1] >= 3 and hi[1] + 3 <= ny:
+            mask[:, :] = True
+            mask[lo[0] - 3:hi[0] + 3, lo[1] - 3:hi[1] + 3] = False
+        return mask
+
     def states(self):
-        """Coarse populations (covered cells virtual) and the physical fine block, (x, y, z, 27)."""
+        """Coarse populations (covered cells virtual; post-collision where
+        coarse_post_collision() is set) and the physical fine block, (x, y, z, 27)."""
         nx, ny, nz = self.plan.shape
         coarse = np.empty((nx, ny, nz, 27))
         check(self._lib.ak_get_pdf(self._coarse, _ptr(coarse)))
