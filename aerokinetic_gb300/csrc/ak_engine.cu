@@ -1660,8 +1660,8 @@ int refined_init(ak_refined *R, double amp, double phase_y, double phase_z, doub
         // outside the transfer block the coarse level stores post-collision
         using T = typename Store<S>::T;
         k_collide<S><<<(unsigned)blocks_for((long long)C->nx * C->ny * C->nz, 128), 128, 0, st>>>(
-            src_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s, (T)C->omega_b,
-            make_int4(0, 1 << 30, 0, 1 << 30), R->xfer);
+            src_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s, (T)C->omega_b, make_int4(0, 0, 0, 0),
+            R->xfer);
         AK_CUDA(cudaGetLastError());
     }
     C->prepared = F->prepared = true;
@@ -1704,6 +1704,7 @@ int refined_step(ak_refined *R, bool fork = false) {
     dim3 gf((unsigned)blocks_for(F->nx, 128), (unsigned)F->ny, (unsigned)F->nz);
     // the collisions number their cells across rows (1-D grids)
     const unsigned gc1 = (unsigned)blocks_for((long long)C->nx * C->ny * C->nz, 128);
+    const unsigned gx1 = (unsigned)blocks_for((long long)(R->xfer.y - R->xfer.x) * (R->xfer.w - R->xfer.z) * C->nz, 128);
     const unsigned gf1 = (unsigned)blocks_for((long long)F->nx * F->ny * F->nz, 128);
     const Rescale c2f{R->tau_s_f * R->dt_f / (R->tau_s_c * R->dt_c), R->tau_b_f * R->dt_f / (R->tau_b_c * R->dt_c)};
     const Rescale f2c{R->tau_s_c * R->dt_c / (R->tau_s_f * R->dt_f), R->tau_b_c * R->dt_c / (R->tau_b_f * R->dt_f)};
@@ -1724,9 +1725,14 @@ int refined_step(ak_refined *R, bool fork = false) {
     // coarse collide, face fluxes, outer boundary, stream, donors after the step
     auto coarse_part = [&]() -> int {
         mark(C);
-        // fused: only the transfer block holds pre-collision populations
-        k_collide<S><<<gc1, 128, 0, st>>>(src_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s,
-                                          (T)C->omega_b, R->fused ? R->xfer : make_int4(0, 1 << 30, 0, 1 << 30));
+        // fused: only the transfer block holds pre-collision populations (a
+        // grid over its cells alone)
+        if (R->fused)
+            k_collide<S><<<gx1, 128, 0, st>>>(src_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s,
+                                              (T)C->omega_b, R->xfer);
+        else
+            k_collide<S><<<gc1, 128, 0, st>>>(src_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s,
+                                              (T)C->omega_b);
         mark(C);
         cudaStream_t fs = flux_stream(st, 0);
         if (!fs) return fail(AK_ERR_CUDA, "face-flux branch could not be forked");
@@ -2213,9 +2219,9 @@ int ak_refined_step_timed(ak_refined *R, int32_t nsteps, double *ms) {
             cudaEventElapsedTime(&t, ev[0], ev[13]);
             ms[0] += t;
             cudaEventElapsedTime(&t, ev[1], ev[2]);
-            ms[1] += t;  // coarse collide
+            ms[1] += t;  // coarse collide (the transfer block alone when fused)
             cudaEventElapsedTime(&t, ev[3], ev[4]);
-            ms[2] += t;  // coarse stream
+            ms[2] += t;  // coarse stream (fused with the next collision)
             for (int sub = 0; sub < 2; ++sub) {
                 cudaEventElapsedTime(&t, ev[5 + 4 * sub], ev[6 + 4 * sub]);
                 ms[3] += t;  // fine collide

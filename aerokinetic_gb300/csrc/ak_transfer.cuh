@@ -263,20 +263,21 @@ template <typename S>
 __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
     k_collide(S *__restrict__ pdf, const uint8_t *__restrict__ flags, Grid G, Shift27 shift,
               typename Store<S>::T omega_s, typename Store<S>::T omega_b,
-              int4 keep = make_int4(0, 1 << 30, 0, 1 << 30), int4 skip = make_int4(0, 0, 0, 0)) {
+              int4 rect = make_int4(0, 0, 0, 0), int4 skip = make_int4(0, 0, 0, 0)) {
     using T = typename Store<S>::T;
-    // one thread per interior cell, x fastest, numbered across rows: warps
-    // stay full whatever nx is (this kernel is bound by the FP64 pipe in the
-    // plain form, where a warp with a few live lanes costs a full one)
+    // one thread per cell of the padded columns x [rect.x, rect.y) by y
+    // [rect.z, rect.w) (rect.y == 0: the whole interior), every z, x fastest,
+    // numbered across rows: warps stay full whatever the width (this kernel is
+    // bound by the FP64 pipe in the plain form, where a warp with a few live
+    // lanes costs a full one); columns inside skip are left as they are
+    if (rect.y == 0) rect = make_int4(1, G.nx + 1, 1, G.ny + 1);
+    const unsigned w = (unsigned)(rect.y - rect.x), h = (unsigned)(rect.w - rect.z);
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned nxy = (unsigned)G.nx * (unsigned)G.ny;
+    const unsigned nxy = w * h;
     if (i >= nxy * (unsigned)G.nz) return;
     const unsigned z = i / nxy, r = i - z * nxy;
-    const unsigned yr = r / (unsigned)G.nx;
-    const int x = (int)(r - yr * (unsigned)G.nx) + 1, y = (int)yr + 1;
-    // only the padded columns inside keep = x [keep.x, keep.y) by y [keep.z,
-    // keep.w) and outside skip (same layout)
-    if (x < keep.x || x >= keep.y || y < keep.z || y >= keep.w) return;
+    const unsigned yr = r / w;
+    const int x = rect.x + (int)(r - yr * w), y = rect.z + (int)yr;
     if (x >= skip.x && x < skip.y && y >= skip.z && y < skip.w) return;
     if (__ldg(flags + y * G.nxp + x) != FLAG_FLUID) return;
     const long long c = G.cell(x, y, z);

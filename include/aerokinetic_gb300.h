@@ -263,11 +263,18 @@ int ak_refined_integrals(ak_refined *r, double *out);
 /* ak_refined_step without loads, timed with CUDA events on the case's stream:
  * ms[0] whole interval, ms[1] coarse collide, ms[2] coarse stream, ms[3] fine
  * collides, ms[4] fine streams, ms[5] the rest (interface transfers, face
- * fluxes, boundaries, walls), milliseconds summed over the steps.  No
- * counterpart in the reference; it exists for measurement. */
+ * fluxes, boundaries, walls), milliseconds summed over the steps.  When the
+ * fine box lies three coarse cells inside the lattice the coarse streaming is
+ * fused with the next step's collision: ms[1] then covers the collision of
+ * the transfer block (the box and three cells around it) alone and ms[2] the
+ * fused pass.  No counterpart in the reference; it exists for measurement. */
 int ak_refined_step_timed(ak_refined *r, int32_t nsteps, double *ms);
 /* The level's lattice (0 coarse, 1 fine block) for ak_get_pdf / ak_macros /
- * ak_get_wall_links; owned by the refined case. */
+ * ak_get_wall_links; owned by the refined case.  When the fine box lies three
+ * coarse cells inside the lattice, the coarse level holds post-collision
+ * populations outside the box and three cells around it (the coarse
+ * streaming is fused with the next step's collision); mass and momentum, and
+ * so ak_macros, are those of the pre-collision state. */
 ak_case *ak_refined_level(ak_refined *r, int32_t level);
 
 /* ---- batches of independent uniform cases --------------------------------
