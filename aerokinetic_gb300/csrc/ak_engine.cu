@@ -1490,6 +1490,13 @@ struct ak_refined {
     // lattice (the donor block does not wrap).
     bool fused = false;
     int4 xfer{0, 0, 0, 0};
+    // the outer boundaries' branch inside the captured graphs (fused form,
+    // transfer block at least three columns from every outer face): UBB,
+    // outflow and the budget's outer flux run beside the transfer-block
+    // collision, whose cells they neither read nor write
+    bool bnd_branch = false;
+    cudaStream_t bnd = nullptr;
+    cudaEvent_t ev_bnd_in = nullptr, ev_bnd_out = nullptr;
     double dx_c = 0, dt_c = 0, dx_f = 0, dt_f = 0, span = 0, speed = 0;
     double tau_s_c = 0, tau_b_c = 0, tau_s_f = 0, tau_b_f = 0;
     double free_g[Q];
@@ -1559,6 +1566,9 @@ void refined_release(ak_refined *R) {
     for (cudaEvent_t e : {R->ev_flux_in[0], R->ev_flux_in[1], R->ev_flux_in[2], R->ev_flux_f0, R->ev_flux_done})
         if (e) cudaEventDestroy(e);
     if (R->flux) cudaStreamDestroy(R->flux);
+    if (R->ev_bnd_in) cudaEventDestroy(R->ev_bnd_in);
+    if (R->ev_bnd_out) cudaEventDestroy(R->ev_bnd_out);
+    if (R->bnd) cudaStreamDestroy(R->bnd);
     if (R->coarse) {
         release(R->coarse);
         delete R->coarse;
@@ -1722,8 +1732,34 @@ int refined_step(ak_refined *R, bool fork = false) {
             return nullptr;
         return R->flux;
     };
+    // the outer boundaries of the coarse level on stream s: UBB, outflow and
+    // the budget's flux through the outer faces
+    auto outer_part = [&](cudaStream_t s) -> int {
+        if (C->n_ubb)
+            k_ubb<S><<<(unsigned)blocks3(C->n_ubb_cells * C->nz), 256, 0, s>>>(src_of<S>(C), C->G, C->ubb_cells,
+                                                                               C->n_ubb_cells, C->speed, 0.0, 0.0);
+        if (C->n_out)
+            k_outflow<S><<<(unsigned)blocks3(C->n_out), 256, 0, s>>>(src_of<S>(C), C->G, C->outer(), C->sel_out,
+                                                                     C->n_out, C->out_state, 1, 0, 0);
+        if (R->track_budget) {
+            k_outer_flux<S><<<dim3((unsigned)R->outer_blocks, 4), 256, 0, s>>>(
+                src_of<S>(C), C->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_outer, 4, R->outer_partials);
+            k_outer_final<<<1, REDUCE_THREADS, 0, s>>>(R->outer_partials, R->d_outer, 4, R->outer_blocks,
+                                                      R->dx_c * R->dx_c * R->dx_c, R->outer_out);
+            C->launches += 2;
+        }
+        AK_CUDA(cudaGetLastError());
+        return AK_OK;
+    };
     // coarse collide, face fluxes, outer boundary, stream, donors after the step
     auto coarse_part = [&]() -> int {
+        const bool bnd = fork && R->fused && R->bnd_branch;
+        if (bnd) {
+            AK_CUDA(cudaEventRecord(R->ev_bnd_in, st));
+            AK_CUDA(cudaStreamWaitEvent(R->bnd, R->ev_bnd_in, 0));
+            AK_TRY(outer_part(R->bnd));
+            AK_CUDA(cudaEventRecord(R->ev_bnd_out, R->bnd));
+        }
         mark(C);
         // fused: only the transfer block holds pre-collision populations (a
         // grid over its cells alone)
@@ -1741,19 +1777,10 @@ int refined_step(ak_refined *R, bool fork = false) {
         k_face_flux_coarse<S><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, fs>>>(
             src_of<S>(C), C->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs,
             R->dx_c * R->dx_c * R->dx_c, R->reg_c);
-        if (C->n_ubb)
-            k_ubb<S><<<(unsigned)blocks3(C->n_ubb_cells * C->nz), 256, 0, st>>>(src_of<S>(C), C->G, C->ubb_cells,
-                                                                                C->n_ubb_cells, C->speed, 0.0, 0.0);
-        if (C->n_out)
-            k_outflow<S><<<(unsigned)blocks3(C->n_out), 256, 0, st>>>(src_of<S>(C), C->G, C->outer(), C->sel_out,
-                                                                      C->n_out, C->out_state, 1, 0, 0);
-        if (R->track_budget) {
-            k_outer_flux<S><<<dim3((unsigned)R->outer_blocks, 4), 256, 0, st>>>(
-                src_of<S>(C), C->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_outer, 4, R->outer_partials);
-            k_outer_final<<<1, REDUCE_THREADS, 0, st>>>(R->outer_partials, R->d_outer, 4, R->outer_blocks,
-                                           R->dx_c * R->dx_c * R->dx_c, R->outer_out);
-            C->launches += 2;
-        }
+        if (bnd)
+            AK_CUDA(cudaStreamWaitEvent(st, R->ev_bnd_out, 0));
+        else
+            AK_TRY(outer_part(st));
         mark(C);
         if (R->fused)
             // streaming fused with the next step's collision, the transfer
@@ -1951,6 +1978,7 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
     B.dny = B.by + 6;
     R->fused = B.lo[0] >= 3 && B.hi[0] + 3 <= cd.nx && B.lo[1] >= 3 && B.hi[1] + 3 <= cd.ny;
     R->xfer = make_int4(B.lo[0] - 2, B.hi[0] + 4, B.lo[1] - 2, B.hi[1] + 4);
+    R->bnd_branch = B.lo[0] >= 6 && B.hi[0] + 6 <= cd.nx && B.lo[1] >= 6 && B.hi[1] + 6 <= cd.ny;
     int r = AK_OK;
     // coarse lattice: no walls (they live on the fine level)
     ak_case_desc coarse = cd;
@@ -2071,7 +2099,10 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
                        cudaEventCreateWithFlags(&R->ev_flux_in[1], cudaEventDisableTiming) != cudaSuccess ||
                        cudaEventCreateWithFlags(&R->ev_flux_in[2], cudaEventDisableTiming) != cudaSuccess ||
                        cudaEventCreateWithFlags(&R->ev_flux_f0, cudaEventDisableTiming) != cudaSuccess ||
-                       cudaEventCreateWithFlags(&R->ev_flux_done, cudaEventDisableTiming) != cudaSuccess))
+                       cudaEventCreateWithFlags(&R->ev_flux_done, cudaEventDisableTiming) != cudaSuccess ||
+                       cudaStreamCreateWithFlags(&R->bnd, cudaStreamNonBlocking) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&R->ev_bnd_in, cudaEventDisableTiming) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&R->ev_bnd_out, cudaEventDisableTiming) != cudaSuccess))
         r = fail(AK_ERR_CUDA, "stream or event creation failed");
     if (r == AK_OK) r = ralloc(R, &R->d_flag, 1);
     if (r == AK_OK) r = ralloc(R, &R->d_loads, (size_t)2 * 5 * std::max(1, cd.n_elements));

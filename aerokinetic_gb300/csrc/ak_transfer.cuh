@@ -60,6 +60,45 @@ __device__ __forceinline__ void add_moments(T s[10], T v) {
     }
 }
 
+// the same sums of one cell from all 27 of its populations, reduced axis by
+// axis (x moments of each (cy, cz) line, then y, then z): 68 additions
+// instead of the 171 of add_moments over every direction
+template <typename T>
+__host__ __device__ __forceinline__ void cell_moments(const T g[Q], T s[10]) {
+    T a0[3][3], a1[3][3], a2[3][3];  // [cy + 1][cz + 1]: sum, sum cx, sum cx^2
+#pragma unroll
+    for (int iy = 0; iy < 3; ++iy)
+#pragma unroll
+        for (int iz = 0; iz < 3; ++iz) {
+            const T m = g[qof(0, iy, iz)], o = g[qof(1, iy, iz)], p = g[qof(2, iy, iz)];
+            a2[iy][iz] = p + m;
+            a1[iy][iz] = p - m;
+            a0[iy][iz] = a2[iy][iz] + o;
+        }
+    // per cz: sum, sum cy, sum cy^2 of a0; sum, sum cy of a1; sum of a2
+    T b00[3], b01[3], b02[3], b10[3], b11[3], b20[3];
+#pragma unroll
+    for (int iz = 0; iz < 3; ++iz) {
+        b02[iz] = a0[2][iz] + a0[0][iz];
+        b01[iz] = a0[2][iz] - a0[0][iz];
+        b00[iz] = b02[iz] + a0[1][iz];
+        b11[iz] = a1[2][iz] - a1[0][iz];
+        b10[iz] = (a1[2][iz] + a1[0][iz]) + a1[1][iz];
+        b20[iz] = (a2[2][iz] + a2[0][iz]) + a2[1][iz];
+    }
+    const T zz = b00[2] + b00[0];
+    s[0] = zz + b00[1];
+    s[1] = (b10[2] + b10[0]) + b10[1];
+    s[2] = (b01[2] + b01[0]) + b01[1];
+    s[3] = b00[2] - b00[0];
+    s[4] = (b20[2] + b20[0]) + b20[1];  // xx
+    s[5] = (b02[2] + b02[0]) + b02[1];  // yy
+    s[6] = zz;                          // zz
+    s[7] = (b11[2] + b11[0]) + b11[1];  // xy
+    s[8] = b10[2] - b10[0];             // xz
+    s[9] = b01[2] - b01[0];             // yz
+}
+
 // (rho, j, Pi_neq) from the running sums, with the reference's density and
 // Mach <= 0.3 checks (refinement.py:140-173); report = 0 skips the checks.
 // The Mach test compares |j|^2 with (0.3 c_s rho)^2 (same decision up to the
@@ -676,7 +715,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
 // w), warp 0 averages the eight children and prepares the fields, every warp
 // writes its own directions.  blockIdx.y == 1: core cells take the free stream.
 template <typename Sc, typename Sf>
-__global__ void __launch_bounds__(SPLIT_THREADS)
+__global__ void __launch_bounds__(SPLIT_THREADS, 2)
     k_restrict(Sc *__restrict__ coarse, Grid G, const Sf *__restrict__ fine, Grid F, BoxSpec B, int pad,
                const double *__restrict__ free_g, Rescale r, int *__restrict__ flag) {
     using T = typename Store<Sc>::A;
@@ -705,14 +744,14 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
         ring_cell(i - z * nring, B.bx, B.by, 3, 3, bx, by);
     }
     const int fx = pad + 2 * bx + (w & 1), fy = pad + 2 * by + ((w >> 1) & 1), fz = 2 * z + (w >> 2);
-    T s[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    T v[Q], s[10];
     bool neg = false;
     static_for<0, Q>([&](auto qc) {
         constexpr int q = decltype(qc)::value;
-        const T v = valid ? load_as<T>(fine, F, q, fx + 1, fy + 1, fz) : T(0);
-        add_moments<q>(s, v);
-        neg |= v < T(-weight(q));
+        v[q] = valid ? load_as<T>(fine, F, q, fx + 1, fy + 1, fz) : T(0);
+        neg |= v[q] < T(-weight(q));
     });
+    cell_moments(v, s);
     T mc[10];
     finish_moments(s, mc, flag, valid);
     put_partial(sh, mc, neg);
