@@ -1494,7 +1494,14 @@ struct ak_refined {
     // transfer block at least three columns from every outer face): UBB,
     // outflow and the budget's outer flux run beside the transfer-block
     // collision, whose cells they neither read nor write
+    // The same branch then streams and collides the coarse cells outside
+    // near (the transfer block and one cell around it, padded coordinates):
+    // they pull only from cells outside the block, which nothing in the step
+    // writes, so the pass runs beside the rest of the step (the second fine
+    // step, restriction, reflux) at the least priority, and the step's own
+    // stream takes the cells of near alone.
     bool bnd_branch = false;
+    int4 near{0, 0, 0, 0};
     cudaStream_t bnd = nullptr;
     cudaEvent_t ev_bnd_in = nullptr, ev_bnd_out = nullptr;
     double dx_c = 0, dt_c = 0, dx_f = 0, dt_f = 0, span = 0, speed = 0;
@@ -1715,6 +1722,10 @@ int refined_step(ak_refined *R, bool fork = false) {
     // the collisions number their cells across rows (1-D grids)
     const unsigned gc1 = (unsigned)blocks_for((long long)C->nx * C->ny * C->nz, 128);
     const unsigned gx1 = (unsigned)blocks_for((long long)(R->xfer.y - R->xfer.x) * (R->xfer.w - R->xfer.z) * C->nz, 128);
+    const unsigned gn1 = (unsigned)blocks_for((long long)(R->near.y - R->near.x) * (R->near.w - R->near.z) * C->nz, 128);
+    // fork mode, fused form, transfer block away from the outer faces: the
+    // boundaries and the far coarse pass on their own branch
+    const bool bnd = fork && R->fused && R->bnd_branch;
     const unsigned gf1 = (unsigned)blocks_for((long long)F->nx * F->ny * F->nz, 128);
     const Rescale c2f{R->tau_s_f * R->dt_f / (R->tau_s_c * R->dt_c), R->tau_b_f * R->dt_f / (R->tau_b_c * R->dt_c)};
     const Rescale f2c{R->tau_s_c * R->dt_c / (R->tau_s_f * R->dt_f), R->tau_b_c * R->dt_c / (R->tau_b_f * R->dt_f)};
@@ -1753,11 +1764,13 @@ int refined_step(ak_refined *R, bool fork = false) {
     };
     // coarse collide, face fluxes, outer boundary, stream, donors after the step
     auto coarse_part = [&]() -> int {
-        const bool bnd = fork && R->fused && R->bnd_branch;
         if (bnd) {
             AK_CUDA(cudaEventRecord(R->ev_bnd_in, st));
             AK_CUDA(cudaStreamWaitEvent(R->bnd, R->ev_bnd_in, 0));
             AK_TRY(outer_part(R->bnd));
+            k_stream_collide<S><<<gc1, 128, 0, R->bnd>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, C->shift_host,
+                                                          (T)C->omega_s, (T)C->omega_b, Sgs<T>{}, R->xfer,
+                                                          make_int4(0, 0, 0, 0), R->near);
             AK_CUDA(cudaEventRecord(R->ev_bnd_out, R->bnd));
         }
         mark(C);
@@ -1777,12 +1790,13 @@ int refined_step(ak_refined *R, bool fork = false) {
         k_face_flux_coarse<S><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, fs>>>(
             src_of<S>(C), C->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs,
             R->dx_c * R->dx_c * R->dx_c, R->reg_c);
-        if (bnd)
-            AK_CUDA(cudaStreamWaitEvent(st, R->ev_bnd_out, 0));
-        else
-            AK_TRY(outer_part(st));
+        if (!bnd) AK_TRY(outer_part(st));
         mark(C);
-        if (R->fused)
+        if (bnd)
+            // the cells of near; the rest runs on the boundaries' branch
+            k_stream_collide<S><<<gn1, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, C->shift_host,
+                                                      (T)C->omega_s, (T)C->omega_b, Sgs<T>{}, R->xfer, R->near);
+        else if (R->fused)
             // streaming fused with the next step's collision, the transfer
             // block streamed only
             k_stream_collide<S><<<gc1, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, C->shift_host,
@@ -1876,13 +1890,43 @@ int refined_step(ak_refined *R, bool fork = false) {
     else
         launch_restrict<S>(R, f2c, st);
     AK_CUDA(cudaGetLastError());
+    if (bnd) AK_CUDA(cudaStreamWaitEvent(st, R->ev_bnd_out, 0));
     // a tracked budget closes on the integrals of the state the step leaves
     if (R->track_budget && R->step_stats) AK_TRY(enqueue_region_stats<S>(R, st));
     mark(C);  // step end
-    C->launches += 6 + 7 * 2 + (C->n_ubb ? 1 : 0) + (C->n_out ? 1 : 0) + (nlinks ? 0 : -4) + 1;
+    C->launches += 6 + 7 * 2 + (C->n_ubb ? 1 : 0) + (C->n_out ? 1 : 0) + (nlinks ? 0 : -4) + 1 + (bnd ? 1 : 0);
     C->steps += 1;
     F->steps += 2;
     R->steps += 1;
+    return AK_OK;
+}
+
+// Kernel priorities of a captured refined step: the coarse pass outside the
+// transfer block (the full-lattice grid of k_stream_collide on the
+// boundaries' branch) takes the device's least priority, every other kernel
+// the greatest, so the short kernels of the interface chain are scheduled
+// ahead of the long pass's remaining blocks as SMs free up.
+template <typename S>
+int graph_priorities(ak_refined *R, cudaGraph_t g) {
+    ak_case *C = R->coarse;
+    const unsigned far_grid = (unsigned)blocks_for((long long)C->nx * C->ny * C->nz, 128);
+    int least = 0, greatest = 0;
+    AK_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    size_t n = 0;
+    AK_CUDA(cudaGraphGetNodes(g, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    AK_CUDA(cudaGraphGetNodes(g, nodes.data(), &n));
+    const void *pass = (const void *)k_stream_collide<S>;
+    for (size_t k = 0; k < n; ++k) {
+        cudaGraphNodeType type;
+        AK_CUDA(cudaGraphNodeGetType(nodes[k], &type));
+        if (type != cudaGraphNodeTypeKernel) continue;
+        cudaKernelNodeParams p{};
+        AK_CUDA(cudaGraphKernelNodeGetParams(nodes[k], &p));
+        cudaKernelNodeAttrValue v{};
+        v.priority = p.func == pass && p.gridDim.x == far_grid ? least : greatest;
+        AK_CUDA(cudaGraphKernelNodeSetAttribute(nodes[k], cudaKernelNodeAttributePriority, &v));
+    }
     return AK_OK;
 }
 
@@ -1916,7 +1960,15 @@ int refined_step_graphed(ak_refined *R) {
             cudaGetLastError();
             return r != AK_OK ? r : fail(AK_ERR_CUDA, std::string("step capture failed: ") + cudaGetErrorString(e));
         }
-        const cudaError_t ei = cudaGraphInstantiate(&R->graph[slot], g, 0);
+        const bool prio = R->fused && R->bnd_branch;
+        const int rp = prio ? graph_priorities<S>(R, g) : AK_OK;
+        if (rp != AK_OK) {
+            cudaGraphDestroy(g);
+            return rp;
+        }
+        // the nodes' own priorities apply only with this flag
+        const cudaError_t ei =
+            cudaGraphInstantiate(&R->graph[slot], g, prio ? cudaGraphInstantiateFlagUseNodePriority : 0);
         cudaGraphDestroy(g);
         if (ei != cudaSuccess) {
             R->graph[slot] = nullptr;
@@ -1979,6 +2031,7 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
     R->fused = B.lo[0] >= 3 && B.hi[0] + 3 <= cd.nx && B.lo[1] >= 3 && B.hi[1] + 3 <= cd.ny;
     R->xfer = make_int4(B.lo[0] - 2, B.hi[0] + 4, B.lo[1] - 2, B.hi[1] + 4);
     R->bnd_branch = B.lo[0] >= 6 && B.hi[0] + 6 <= cd.nx && B.lo[1] >= 6 && B.hi[1] + 6 <= cd.ny;
+    R->near = make_int4(R->xfer.x - 1, R->xfer.y + 1, R->xfer.z - 1, R->xfer.w + 1);
     int r = AK_OK;
     // coarse lattice: no walls (they live on the fine level)
     ak_case_desc coarse = cd;

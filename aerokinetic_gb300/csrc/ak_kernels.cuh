@@ -118,16 +118,23 @@ template <typename S>
 __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
     k_stream_collide(const S *__restrict__ src, S *__restrict__ dst, const uint8_t *__restrict__ flags, Grid G,
                      Shift27 shift, typename Store<S>::T omega_s, typename Store<S>::T omega_b,
-                     Sgs<typename Store<S>::T> sgs, int4 raw = make_int4(0, 0, 0, 0)) {
-    // one thread per interior cell, x fastest, numbered across rows: warps
-    // stay full whatever nx is (the plain form is bound by the FP64 pipe,
-    // where a warp with a few live lanes costs as much as a full one)
+                     Sgs<typename Store<S>::T> sgs, int4 raw = make_int4(0, 0, 0, 0),
+                     int4 rect = make_int4(0, 0, 0, 0), int4 skip = make_int4(0, 0, 0, 0)) {
+    // one thread per cell of the padded columns x [rect.x, rect.y) by y
+    // [rect.z, rect.w) (rect.y == 0: the whole interior), every z, x fastest,
+    // numbered across rows: warps stay full whatever the width (the plain
+    // form is bound by the FP64 pipe, where a warp with a few live lanes
+    // costs as much as a full one); columns inside skip are left to another
+    // launch
+    if (rect.y == 0) rect = make_int4(1, G.nx + 1, 1, G.ny + 1);
+    const unsigned w = (unsigned)(rect.y - rect.x), h = (unsigned)(rect.w - rect.z);
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned nxy = (unsigned)G.nx * (unsigned)G.ny;
+    const unsigned nxy = w * h;
     if (i >= nxy * (unsigned)G.nz) return;
     const unsigned z = i / nxy, r = i - z * nxy;
-    const unsigned yr = r / (unsigned)G.nx;
-    const int x = (int)(r - yr * (unsigned)G.nx) + 1, y = (int)yr + 1;
+    const unsigned yr = r / w;
+    const int x = rect.x + (int)(r - yr * w), y = rect.z + (int)yr;
+    if (x >= skip.x && x < skip.y && y >= skip.z && y < skip.w) return;
     // raw: the padded x [raw.x, raw.y) by y [raw.z, raw.w) columns are only
     // streamed (they keep pre-collision populations)
     const bool stream_only = x >= raw.x && x < raw.y && y >= raw.z && y < raw.w;
