@@ -40,6 +40,19 @@ def _jsonable(value):
     return value
 
 
+def post_collision_columns(plan):
+    """(nx, ny) coarse columns whose populations the engine stores
+    post-collision: all but the transfer block (the fine box and three coarse
+    cells around it) when that block lies inside the lattice, else none."""
+    nx, ny, _ = plan.shape
+    lo, hi = plan.box.lower, plan.box.upper
+    mask = np.zeros((nx, ny), dtype=bool)
+    if lo[0] >= 3 and hi[0] + 3 <= nx and lo[1] >= 3 and hi[1] + 3 <= ny:
+        mask[:, :] = True
+        mask[lo[0] - 3:hi[0] + 3, lo[1] - 3:hi[1] + 3] = False
+    return mask
+
+
 class RefinedSolver:
     """Two-level solver.  budget=True (the reference's behaviour) closes the
     mass and momentum budget of every step() (refined_solver.py:311-343);
@@ -268,13 +281,7 @@ class RefinedSolver:
         collision, when that block lies inside the lattice.  The reference
         stores pre-collision populations everywhere; collision conserves mass
         and momentum, so macroscopic fields and integrals agree."""
-        nx, ny, _ = self.plan.shape
-        lo, hi = self.plan.box.lower, self.plan.box.upper
-        mask = np.zeros((nx, ny), dtype=bool)
-        if lo[0] >= 3 and hi[0] + 3 <= nx and lo[1] >= 3 and hi[1] + 3 <= ny:
-            mask[:, :] = True
-            mask[lo[0] - 3:hi[0] + 3, lo[1] - 3:hi[1] + 3] = False
-        return mask
+        return post_collision_columns(self.plan)
 
     def states(self):
         """Coarse populations (covered cells virtual; post-collision where

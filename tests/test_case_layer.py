@@ -114,3 +114,22 @@ def test_validation_errors_match_the_reference_messages():
     with pytest.raises(ValueError, match="touch or overlap"):
         Section((Contour(square, "a"), Contour(square + [0.5, 0.0], "b")))
     Section((Contour(square, "a"), Contour(square + [2.0, 0.0], "b")))
+
+
+def test_post_collision_columns_follow_the_transfer_block(golden):
+    """The coarse columns whose populations the engine stores post-collision:
+    all but the fine box and three coarse cells around it, and none when that
+    block reaches the lattice's edge (the unfused form)."""
+    from types import SimpleNamespace
+
+    from aerokinetic_gb300.refined import post_collision_columns
+    from aerokinetic_gb300.refined_plan import RefinedPlan, load_refined_project
+    project, refinement = load_refined_project(golden["histories"]["refined_startup"]["project"])
+    plan = RefinedPlan.create(project, refinement)
+    lo, hi = plan.box.lower, plan.box.upper
+    mask = post_collision_columns(plan)
+    assert mask.shape == tuple(plan.shape[:2])
+    assert not mask[lo[0] - 3:hi[0] + 3, lo[1] - 3:hi[1] + 3].any()
+    assert mask.sum() == mask.size - (hi[0] - lo[0] + 6) * (hi[1] - lo[1] + 6)
+    edge = SimpleNamespace(shape=plan.shape, box=SimpleNamespace(lower=(2, lo[1], lo[2]), upper=hi))
+    assert not post_collision_columns(edge).any()
