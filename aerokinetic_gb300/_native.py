@@ -126,6 +126,9 @@ SIGNATURES = {
     "ak_batch_stream": ([_P], _P),
     "ak_refined_step_timed": ([_P, ctypes.c_int32, _P], ctypes.c_int),
     "ak_refined_level": ([_P, ctypes.c_int32], _P),
+    "ak_refined_probe": ([_P, ctypes.c_int32, _P, _P], ctypes.c_int),
+    "ak_fma_peak": ([ctypes.c_int32, _P], ctypes.c_int),
+    "ak_collision_flops": ([ctypes.c_int32, _P], ctypes.c_int),
     "ak_last_error": ([], ctypes.c_char_p),
     "ak_version": ([], ctypes.c_char_p),
 }

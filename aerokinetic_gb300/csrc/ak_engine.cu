@@ -18,6 +18,7 @@
 #include "ak_transfer.cuh"
 #include "ak_batch.cuh"
 #include "ak_exterior.cuh"
+#include "ak_peaks.cuh"
 
 using namespace ak;
 
@@ -798,6 +799,68 @@ const char *ak_version(void) {
 #endif
 }
 
+int ak_fma_peak(int32_t precision, double *tflops) {
+    if ((precision != 0 && precision != 1) || !tflops)
+        return fail(AK_ERR_INVALID, "precision 0 (FP64) or 1 (FP32) and an output are required");
+    int dev = 0, sms = 0;
+    AK_CUDA(cudaGetDevice(&dev));
+    AK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int threads = 256, blocks = 8 * sms;
+    // about 30 ms per launch on GB300 for either pipe
+    const int iters = precision == 0 ? 8192 : 262144;
+    cudaStream_t st = nullptr;
+    cudaEvent_t a = nullptr, b = nullptr;
+    void *out = nullptr;
+    AK_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    int r = AK_OK;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess ||
+        cudaMalloc(&out, (size_t)blocks * threads * 8) != cudaSuccess)
+        r = fail(AK_ERR_CUDA, "peak measurement set-up failed");
+    double best = 0.0;
+    for (int rep = 0; rep < 4 && r == AK_OK; ++rep) {
+        cudaEventRecord(a, st);
+        if (precision == 0)
+            k_fma_peak<double><<<blocks, threads, 0, st>>>((double *)out, iters, 0.999999, 1e-6);
+        else
+            k_fma_peak<float><<<blocks, threads, 0, st>>>((float *)out, iters, 0.999999f, 1e-6f);
+        cudaEventRecord(b, st);
+        if (cudaEventSynchronize(b) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+            r = fail(AK_ERR_CUDA, "peak measurement kernel failed");
+            break;
+        }
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, a, b);
+        const double flops = 2.0 * 8.0 * (double)iters * blocks * threads;
+        if (rep > 0) best = std::max(best, flops / (ms * 1e-3) / 1e12);  // the first launch warms up
+    }
+    if (out) cudaFree(out);
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    cudaStreamDestroy(st);
+    if (r != AK_OK) return r;
+    *tflops = best;
+    return AK_OK;
+}
+
+int ak_collision_flops(int32_t storage, double *counts) {
+    if (storage < AK_STORAGE_F64 || storage > AK_STORAGE_F16 || !counts)
+        return fail(AK_ERR_INVALID, "storage f64, f32 or f16 and an output are required");
+    // any non-degenerate cell: the operation count does not depend on the values
+    Counted g[Q];
+    for (int q = 0; q < Q; ++q) g[q] = Counted(1e-3 * ((q * 7) % 11 - 5) * weight(q));
+    Counted::reset();
+    // the collision form each storage type uses (collide_stored)
+    if (storage == AK_STORAGE_F32)
+        collide<Counted>(g, Counted(1.9), Counted(1.0));
+    else
+        collide_full<Counted>(g, Counted(1.0 - 1.9), Counted(1.0));
+    counts[0] = (double)Counted::adds;
+    counts[1] = (double)Counted::muls;
+    counts[2] = (double)Counted::divs;
+    counts[3] = (double)(Counted::adds + Counted::muls + Counted::divs);
+    return AK_OK;
+}
+
 #ifdef AK_CHECKED
 unsigned long long ak_debug_status(void) {
     unsigned long long v = 0, zero = 0;
@@ -1021,13 +1084,17 @@ int ak_step(ak_case *c, int32_t nsteps, double *loads) {
 }  // extern "C"
 
 // ---- allocation-free loads
-// Callers that run where device allocation is not allowed or not wanted (a
-// host thread inside CUDA stream capture, a real-time control loop on a
-// pre-sized device budget, a plugin host that forbids driver allocations
-// after start-up) cannot use ak_step's loads path, which allocates its
-// per-block partial sums on the first sampled step.  ak_step_loads_static
-// keeps those partial sums in this file-scope array instead: 131072 doubles
-// (1 MiB) that every GPU loading the library holds until the process exits.
+// Some callers cannot allocate device memory once they run: a host
+// application whose memory pool has already reserved the GPU's free memory
+// (a cudaMalloc would fail or fragment its pool), a control loop on a fixed
+// device budget that cannot afford the implicit synchronisation of an
+// allocation, or a plugin host that forbids driver allocations after
+// start-up.  ak_step's loads path allocates its per-block partial sums on
+// the first sampled step; ak_step_loads_static keeps them in this file-scope
+// array instead: 131072 doubles (1 MiB) that every GPU loading the library
+// holds until the process exits.  It steps eagerly (one launch per kernel,
+// no graph replay), so each step costs the launch latencies ak_step's
+// replayed graphs hide.
 namespace {
 constexpr long long STATIC_LOADS_DOUBLES = 131072;
 constexpr int STATIC_MAX_DEVICES = 64;
@@ -1066,6 +1133,17 @@ int ak_step_loads_static(ak_case *c, int32_t nsteps, double *loads) {
     AK_CUDA(cudaGetDevice(&dev));
     if (dev != c->device)
         return fail(AK_ERR_INVALID, "make the case's device current before ak_step_loads_static");
+    // every check before the first launch: a rejected call leaves the case,
+    // its boundary history and its step count as they were
+    if (c->farfield == AK_FARFIELD_EXTERIOR && !c->prepared)
+        return fail(AK_ERR_INVALID, "the exterior case needs an initial state first");
+    const long long blocks =
+        c->farfield == AK_FARFIELD_EXTERIOR ? c->wall_blocks : blocks_for(c->nkeys * c->nz * 3, 256);
+    const long long needed = blocks * 5 * c->n_elements;
+    if (needed > STATIC_LOADS_DOUBLES)
+        return fail(AK_ERR_INVALID, "wall links need " + std::to_string(needed) +
+                                        " partial sums; the static scratch holds " +
+                                        std::to_string(STATIC_LOADS_DOUBLES));
     double *scratch = nullptr;
     AK_TRY(static_loads_scratch(&scratch));
     for (int s = 0; s < nsteps; ++s) {
@@ -2318,6 +2396,61 @@ int ak_refined_step_timed(ak_refined *R, int32_t nsteps, double *ms) {
     for (cudaEvent_t ev : events) cudaEventDestroy(ev);
     if (r != AK_OK) return r;
     AK_CUDA(e);
+    return AK_OK;
+}
+
+int ak_refined_probe(ak_refined *R, int32_t op, double *out, int64_t *n_out) {
+    if (!R || op < 0 || op > 3) return fail(AK_ERR_INVALID, "a case and an operation 0..3 are required");
+    if (n_out) *n_out = op == 2 ? 2 * R->reg_doubles : 0;
+    if (op == 2 && !out) return AK_OK;
+    ak_case *C = R->coarse, *F = R->fine;
+    cudaStream_t st = C->stream;
+    const BoxSpec &B = R->B;
+    AK_CUDA(cudaStreamSynchronize(st));
+    AK_CUDA(cudaMemsetAsync(R->d_flag, 0, sizeof(int), st));
+    const int r = with_storage(C, [&](auto *tag) -> int {
+        using S = std::remove_pointer_t<decltype(tag)>;
+        if (op == 0) {
+            const long long nring_block = ring_count(B.dnx, B.dny, DONOR_RING, DONOR_RING) * C->nz;
+            const long long nprox = ring_count(F->nx, B.dny, R->pad, DONOR_RING) * C->nz;
+            const long long nband = ring_count(F->nx, F->ny, R->pad, R->pad) * F->nz;
+            const Rescale c2f{R->tau_s_f * R->dt_f / (R->tau_s_c * R->dt_c),
+                              R->tau_b_f * R->dt_f / (R->tau_b_c * R->dt_c)};
+            k_block_moments<S><<<(unsigned)split_blocks(nring_block), SPLIT_THREADS, 0, st>>>(
+                src_of<S>(C), C->G, B, R->d_free, R->mom_old, nullptr, nullptr, R->d_flag);
+            k_prolong_x<<<(unsigned)blocks3(nprox), 256, 0, st>>>(B, C->nz, R->pad, R->mom_old, R->pro_x);
+            k_donors<S><<<(unsigned)split_blocks(nband), SPLIT_THREADS, 0, st>>>(src_of<S>(F), F->G, C->nz, R->pro_x,
+                                                                                 B.dny, c2f, R->pad, R->d_flag);
+        } else if (op == 1) {
+            const Rescale f2c{R->tau_s_c * R->dt_c / (R->tau_s_f * R->dt_f),
+                              R->tau_b_c * R->dt_c / (R->tau_b_f * R->dt_f)};
+            launch_restrict<S>(R, f2c, st);
+        } else if (op == 2) {
+            AK_CUDA(cudaMemsetAsync(R->reg_f, 0, sizeof(double) * R->reg_doubles, st));
+            k_face_flux_coarse<S><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, st>>>(
+                src_of<S>(C), C->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs,
+                R->dx_c * R->dx_c * R->dx_c, R->reg_c);
+            k_face_flux_fine<S><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, st>>>(
+                src_of<S>(F), F->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs,
+                R->pad, R->dx_f * R->dx_f * R->dx_f, R->reg_f);
+        } else {
+            k_reflux<S><<<dim3((unsigned)split_blocks(R->max_face), R->nfaces), SPLIT_THREADS, 0, st>>>(
+                src_of<S>(C), C->G, R->d_faces, R->nfaces, R->d_offs, R->reg_c, R->reg_f,
+                1.0 / (R->dx_c * R->dx_c * R->dx_c), R->d_flag);
+        }
+        AK_CUDA(cudaGetLastError());
+        return AK_OK;
+    });
+    if (r != AK_OK) return r;
+    if (op == 2) {
+        AK_CUDA(cudaMemcpyAsync(out, R->reg_c, sizeof(double) * R->reg_doubles, cudaMemcpyDeviceToHost, st));
+        AK_CUDA(cudaMemcpyAsync(out + R->reg_doubles, R->reg_f, sizeof(double) * R->reg_doubles,
+                                cudaMemcpyDeviceToHost, st));
+    }
+    int flag = 0;
+    AK_CUDA(cudaMemcpyAsync(&flag, R->d_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    AK_CUDA(cudaStreamSynchronize(st));
+    if (flag) return fail(AK_ERR_NONFINITE, "a transfer check failed (flag " + std::to_string(flag) + ")");
     return AK_OK;
 }
 

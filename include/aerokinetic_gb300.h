@@ -112,14 +112,17 @@ int ak_init_fields(ak_case *c, const double *rho, const double *u);
  * element, in lattice units, Mz about the normalised frame's origin. */
 int ak_step(ak_case *c, int32_t nsteps, double *loads);
 /* ak_step with loads that allocates no device memory, for callers that
- * cannot allocate (inside stream capture, on a fixed device-memory budget):
- * the per-block partial sums of the loads live in a static device array of
- * 131072 doubles (1 MiB, held by every GPU that loads the library).  No
- * counterpart in the reference.  The first call on a device looks up the
- * array's device address, so make that first call before any stream capture,
- * with the case's device current.  Cases whose wall links need more partial
- * sums than the array holds get AK_ERR_INVALID.  All calls share the array:
- * calls that overlap on the GPU (other cases on other streams) race. */
+ * cannot allocate once running (a host whose memory pool already holds the
+ * GPU's free memory, a fixed device budget, a plugin host that forbids
+ * allocation after start-up): the per-block partial sums of the loads live
+ * in a static device array of 131072 doubles (1 MiB, held by every GPU that
+ * loads the library).  No counterpart in the reference.  The first call on a
+ * device looks up the array's device address, with the case's device
+ * current.  Steps run eagerly (no graph replay).  Cases whose wall links
+ * need more partial sums than the array holds get AK_ERR_INVALID before
+ * anything is launched: a rejected call leaves the case unchanged.  All
+ * calls share the array: calls that overlap on the GPU (other cases on
+ * other streams) race. */
 int ak_step_loads_static(ak_case *c, int32_t nsteps, double *loads);
 int64_t ak_steps_done(const ak_case *c);
 /* Kernels the case has issued while stepping (for launch accounting). */
@@ -269,6 +272,24 @@ int ak_refined_integrals(ak_refined *r, double *out);
  * the transfer block (the box and three cells around it) alone and ms[2] the
  * fused pass.  No counterpart in the reference; it exists for measurement. */
 int ak_refined_step_timed(ak_refined *r, int32_t nsteps, double *ms);
+/* One interface kernel of the two-level step, run alone on the levels'
+ * current population copies, so that each can be compared with the
+ * reference's transfer algebra in isolation:
+ *   op 0  donors: moments of the coarse donor block (interface.py:257-263,
+ *         refinement.py:148-175), the 5-point prolongation (refinement.py:
+ *         78-105), the coarse -> fine stress rescale and the fine padding
+ *         band's populations (refinement.py:177-213), coarse-time fraction 0
+ *   op 1  restriction of the fine block onto the covered coarse cells
+ *         (refined_solver.py:183-188, refinement.py:108-114, 245-254)
+ *   op 2  face fluxes (interface.py:44-104) of the coarse copy and of the
+ *         fine copy: out[0, n/2) the coarse registers, out[n/2, n) the fine
+ *         ones (2 x 2 fine entries summed per coarse entry), n in *n_out;
+ *         out = NULL only reports n
+ *   op 3  reflux (interface.py:285-295) of the coarse copy from the
+ *         registers op 2 left.
+ * A failed positivity or Mach check returns AK_ERR_NONFINITE.  No
+ * counterpart in the reference; it exists for unit tests. */
+int ak_refined_probe(ak_refined *r, int32_t op, double *out, int64_t *n_out);
 /* The level's lattice (0 coarse, 1 fine block) for ak_get_pdf / ak_macros /
  * ak_get_wall_links; owned by the refined case.  When the fine box lies three
  * coarse cells inside the lattice, the coarse level holds post-collision
@@ -308,6 +329,20 @@ void *ak_batch_stream(const ak_batch *b);
 const char *ak_last_error(void);
 /* Library build identification, e.g. "aerokinetic_gb300 sm_103a". */
 const char *ak_version(void);
+/* Fused multiply-add throughput of the current device in TFLOP/s (two FLOPs
+ * per FMA), precision 0 = FP64, 1 = FP32: eight dependent FMA chains per
+ * thread over 8 blocks of 256 threads per SM, best of three timed launches
+ * (CUDA events).  The ceiling of the FP64-bound plain collision.  No
+ * counterpart in the reference; it exists for measurement. */
+int ak_fma_peak(int32_t precision, double *tflops);
+/* Algorithmic floating-point operations of one cell's collision in the form
+ * the storage type uses (AK_STORAGE_F64 / F16: the chimera form, F32: the
+ * deviation form), counted by evaluating the same collision template on a
+ * counting number type: counts[0] additions and subtractions, counts[1]
+ * multiplications, counts[2] divisions, counts[3] their sum (a fused
+ * multiply-add of the compiled kernel counts as one multiplication and one
+ * addition).  No counterpart in the reference; it exists for measurement. */
+int ak_collision_flops(int32_t storage, double *counts);
 
 #ifdef __cplusplus
 }

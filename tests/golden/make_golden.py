@@ -1,9 +1,8 @@
 """Regenerate the golden fixtures of tests/golden/ from the reference checkout.
 
-Run in a container that has the reference sources (read-only) at
-/root/reference:
+Run where a checkout of the reference sources is available, naming it:
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py --reference <path to the checkout>
 
 Two kinds of fixture are written:
 
@@ -14,7 +13,13 @@ Two kinds of fixture are written:
   (aerokinetic.geometry, aerokinetic.config) and calling them: plans,
   normalised polygons, solid flags, and Bouzidi fractions from the
   reference's own link callback (solver.py:100-122), driven on a stub index
-  list that holds every (fluid cell, direction) pair whose neighbour is solid.
+  list that holds every (fluid cell, direction) pair whose neighbour is solid;
+* two-level plans from the reference's RefinedPlan.create
+  (refined_solver.py:42-99) for the two-level benchmark cases (refined_plans.json);
+* unit vectors of the reference's level-transfer algebra on seeded inputs:
+  D3Q27Transfer.moments / populations / _rescale_stress,
+  prolong_cell_averages, restrict_cell_averages (refinement.py:78-254) and
+  StreamingFaceFlux (interface.py:44-104) (transfer.json).
 
 Nothing at test time reads the reference checkout.
 """
@@ -153,9 +158,116 @@ def geometry_fixture(ak, spec):
     }
 
 
+# Two-level benchmark cases, described by the parameters both sides build them
+# from: the headline case (coarse 512 x 384 x 8 at chord 32, AoA 8) and the
+# large two-element case (main element + 0.3c flap at 20 deg, chord 64).
+REFINED_PLAN_CASES = {
+    "two_level_512x384x8": dict(
+        flap=None, flow=dict(reynolds=30000, alpha_deg=8, lattice_speed=0.1 / np.sqrt(3)),
+        grid=dict(cells_per_chord=32, upstream_chords=5.0, downstream_chords=9.9938, transverse_chords=5.9056,
+                  span_chords=0.25, memory_limit_gib=64),
+        refinement=dict(upstream_chords=0.5, downstream_chords=1.0, transverse_chords=0.5)),
+    "two_element_large": dict(
+        flap=dict(m=0.0, p=0.0, thickness=0.12, flap_deg=20.0, n_side=161),
+        flow=dict(reynolds=1e5, alpha_deg=6.0, lattice_speed=0.1 / np.sqrt(3)),
+        grid=dict(cells_per_chord=64, upstream_chords=16.0, downstream_chords=34.0, transverse_chords=17.0,
+                  span_chords=0.5, memory_limit_gib=1000),
+        refinement=dict(upstream_chords=1.5, downstream_chords=4.0, transverse_chords=1.5)),
+}
+
+
+def refined_section(ak_geometry, spec):
+    """The case's section as reference Contours.  The reference has no flap
+    builder: the flapped polygon comes from this repository's
+    serve.flapped_section (the same function the engine's cases use) and is
+    handed to the reference as plain vertex arrays."""
+    if spec["flap"] is None:
+        return ak_geometry.Section((ak_geometry.naca4("0012", 161),))
+    sys.path.insert(0, str(HERE.parents[1]))
+    from aerokinetic_gb300.serve import flapped_section
+    mine = flapped_section(**spec["flap"])
+    elements = tuple(ak_geometry.Contour(np.array(e.xy), e.name) for e in mine.elements)
+    return ak_geometry.Section(elements, mine.chord, mine.moment_reference)
+
+
+def refined_plan_fixtures():
+    """RefinedPlan.create of the reference (refined_solver.py:42-99) for the
+    two-level benchmark cases."""
+    from aerokinetic import geometry as G
+    from aerokinetic.config import Flow, Grid
+    from aerokinetic.project import Project
+    from aerokinetic.refined_solver import RefinedPlan, RefinementSettings
+    out = {}
+    for name, spec in REFINED_PLAN_CASES.items():
+        project = Project(refined_section(G, spec), Flow(**spec["flow"]), Grid(**spec["grid"]))
+        plan = RefinedPlan.create(project, RefinementSettings(**spec["refinement"]))
+        level = lambda L: {"dx": L.dx, "dt": L.dt, "tau_shear": L.tau_shear, "tau_bulk": L.tau_bulk}
+        out[name] = {"spec": spec, "shape": list(plan.shape), "origin": list(plan.origin),
+                     "box_lower": list(plan.box.lower), "box_upper": list(plan.box.upper),
+                     "coarse_level": level(plan.coarse_level), "fine_level": level(plan.fine_level),
+                     "span": plan.span,
+                     "minimum_wall_interface_distance_coarse_cells":
+                         plan.minimum_wall_interface_distance_coarse_cells}
+    return out
+
+
+def transfer_inputs(rng, shape):
+    """Seeded pre-collision populations near a slow equilibrium: rho in
+    [0.98, 1.02], |u| < 0.05, stress perturbations ~1e-3 of the weights, so
+    the transfer's positivity and Mach checks pass."""
+    w = np.prod(np.where(np.array(D3Q27) == 0, 2 / 3, 1 / 6), axis=1)
+    c = np.array(D3Q27, dtype=float)
+    rho = 1 + 0.02 * (2 * rng.random(shape) - 1)
+    u = 0.05 / np.sqrt(3) * (2 * rng.random(shape + (3,)) - 1)
+    cu = u @ c.T
+    usq = np.sum(u * u, axis=-1)[..., None]
+    feq = rho[..., None] * w * (1 + 3 * cu + 4.5 * cu ** 2 - 1.5 * usq)
+    noise = 1e-3 * w * (2 * rng.random(shape + (27,)) - 1)
+    return feq + noise - w  # zero-centred
+
+
+def transfer_fixtures():
+    """The reference's transfer algebra (refinement.py:78-254,
+    interface.py:44-104) applied to seeded inputs; every array is stored in
+    full so the tests need only numpy."""
+    from aerokinetic.interface import StreamingFaceFlux
+    from aerokinetic.refinement import (AcousticLevel, D3Q27Transfer, prolong_cell_averages,
+                                        restrict_cell_averages)
+    rng = np.random.default_rng(20261204)
+    coarse = AcousticLevel(1 / 32, 0.1 / np.sqrt(3) / 32, 0.5 + 3 * 0.1 / np.sqrt(3) * 32 / 30000, 1.0)
+    t = D3Q27Transfer(D3Q27, coarse, zero_centered=True, pdf_stage="pre_collision")
+    cells = transfer_inputs(rng, (12,))
+    moments = t.moments(cells)
+    fields = moments.copy()
+    fields[:, 4:] += 1e-4 * (2 * rng.random((12, 6)) - 1)
+    block = transfer_inputs(rng, (6, 6, 5))
+    block_moments = t.moments(block)
+    fine = transfer_inputs(rng, (4, 6, 4))
+    lattice = transfer_inputs(rng, (5, 6, 4))
+    fluxes = []
+    for axis, index, ranges in ((0, 1, ((1, 4), (0, 4))), (1, 2, ((0, 5), (1, 3))), (2, 0, ((1, 4), (2, 5)))):
+        flux = StreamingFaceFlux((5, 6, 4), D3Q27, axis, index, ranges, periodic=True)
+        fluxes.append({"axis": axis, "index": index, "ranges": [list(r) for r in ranges],
+                       "flux": flux(lattice).tolist()})
+    return {
+        "stencil": D3Q27,
+        "coarse_level": {"dx": coarse.dx, "dt": coarse.dt, "tau_shear": coarse.tau_shear,
+                         "tau_bulk": coarse.tau_bulk},
+        "cells": cells.tolist(), "moments": moments.tolist(),
+        "fields": fields.tolist(), "populations": t.populations(fields).tolist(),
+        "rescale_to_fine": t._rescale_stress(fields, t.coarse, t.fine).tolist(),
+        "rescale_to_coarse": t._rescale_stress(fields, t.fine, t.coarse).tolist(),
+        "block": block.tolist(), "prolonged_moments": prolong_cell_averages(block_moments).tolist(),
+        "prolonged_in_time": t.prolong_in_time(block, block[::-1], 0.5).tolist(),
+        "fine": fine.tolist(), "restricted_moments": restrict_cell_averages(t.moments(fine)).tolist(),
+        "restricted": t.restrict(fine).tolist(),
+        "lattice": lattice.tolist(), "face_fluxes": fluxes,
+    }
+
+
 def main():
     parser = argparse.ArgumentParser()
-    parser.add_argument("--reference", default="/root/reference")
+    parser.add_argument("--reference", required=True, help="path of the reference checkout")
     args = parser.parse_args()
     ref = Path(args.reference)
     sys.path.insert(0, str(ref / "src"))
@@ -197,6 +309,8 @@ def main():
 
     geometry = {name: geometry_fixture(ak, spec) for name, spec in GEOMETRY_CASES.items()}
     (HERE / "geometry.json").write_text(json.dumps(geometry) + "\n")
+    (HERE / "refined_plans.json").write_text(json.dumps(refined_plan_fixtures()) + "\n")
+    (HERE / "transfer.json").write_text(json.dumps(transfer_fixtures()) + "\n")
     print("wrote", sorted(p.name for p in HERE.glob("*.json")))
 
 

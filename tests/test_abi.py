@@ -45,3 +45,20 @@ def test_invalid_description_is_rejected_without_a_device():
     assert b"nx" in lib.ak_last_error()
     with pytest.raises(ValueError):
         _native.check(code)
+
+
+def test_collision_flop_count_runs_on_the_host():
+    """ak_collision_flops evaluates the collision templates on a counting type
+    (host code, no device): the FP64 and FP16 storage forms share the chimera
+    collision, the FP32 form uses the deviation form."""
+    import numpy as np
+    lib = _native.load()
+    counts = {}
+    for storage in ("f64", "f32", "f16"):
+        c = np.zeros(4)
+        assert lib.ak_collision_flops(_native.STORAGE[storage], c.ctypes.data_as(ctypes.c_void_p)) == 0
+        assert c[3] == c[0] + c[1] + c[2] and c[2] >= 1
+        counts[storage] = c.tolist()
+    assert counts["f64"] == counts["f16"] == [236.0, 213.0, 1.0, 450.0]
+    assert counts["f32"][3] > counts["f64"][3]
+    assert lib.ak_collision_flops(_native.STORAGE["df64"], None) == _native.AK_ERR_INVALID
