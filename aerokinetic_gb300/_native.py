@@ -68,7 +68,8 @@ class CaseDesc(ctypes.Structure):
 class RefinedDesc(ctypes.Structure):
     _fields_ = [("coarse", CaseDesc), ("tau_shear", ctypes.c_double), ("tau_bulk", ctypes.c_double),
                 ("dt_coarse", ctypes.c_double), ("span", ctypes.c_double),
-                ("box_lower", ctypes.c_int32 * 3), ("box_upper", ctypes.c_int32 * 3)]
+                ("box_lower", ctypes.c_int32 * 3), ("box_upper", ctypes.c_int32 * 3),
+                ("fine_storage", ctypes.c_int32)]
 
 
 class CaseInfo(ctypes.Structure):
@@ -127,6 +128,7 @@ SIGNATURES = {
     "ak_refined_step_timed": ([_P, ctypes.c_int32, _P], ctypes.c_int),
     "ak_refined_level": ([_P, ctypes.c_int32], _P),
     "ak_refined_probe": ([_P, ctypes.c_int32, _P, _P], ctypes.c_int),
+    "ak_refined_states": ([_P, _P, _P], ctypes.c_int),
     "ak_fma_peak": ([ctypes.c_int32, _P], ctypes.c_int),
     "ak_collision_flops": ([ctypes.c_int32, _P], ctypes.c_int),
     "ak_last_error": ([], ctypes.c_char_p),

@@ -145,7 +145,7 @@ def save_refined_checkpoint(solver, path, context=None):
     metadata = {"format": FORMAT, "schema_version": SCHEMA, "kind": "refined",
                 "project": solver.project.as_dict(), "refinement": dict(solver.refinement.__dict__),
                 "case_fingerprint": solver.case_fingerprint, "steps": solver.steps, "fine_steps": solver.fine_steps,
-                "storage": solver.storage, "budget": solver.budget,
+                "storage": solver.storage, "fine_storage": solver.fine_storage, "budget": solver.budget,
                 "last_loads": solver.last_loads, "last_budget": solver.last_budget,
                 "initial_integrals": solver._initial_integrals, "wall_fallback_links": solver.wall_fallback_links,
                 "context": context or {}}
@@ -161,7 +161,8 @@ def restore_refined_checkpoint(solver_type, path, progress=None):
             raise ValueError("Invalid refined checkpoint clocks")
         project = Project.from_dict(meta["project"])
         refinement = RefinementSettings(**meta["refinement"])
-        solver = solver_type(project, refinement, progress=progress, storage=meta["storage"], budget=meta["budget"])
+        solver = solver_type(project, refinement, progress=progress, storage=meta["storage"], budget=meta["budget"],
+                             fine_storage=meta.get("fine_storage"))
         try:
             if solver.case_fingerprint != meta["case_fingerprint"]:
                 raise ValueError("Refined checkpoint case fingerprint differs")

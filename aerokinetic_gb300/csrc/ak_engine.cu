@@ -11,6 +11,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/aerokinetic_gb300.h"
@@ -102,6 +103,7 @@ struct ak_case {
     long long fluid_cells = 0;
     long long steps = 0;
     long long launches = 0;  // kernels issued by stepping since creation
+    long long pdf_writes = 0;  // population writes from outside the step (set_pdf, init)
     bool prepared = false;
     int device = 0;  // CUDA device current when the case was created
     // stationarity residuals: the owned region (interior coordinates, an
@@ -1036,6 +1038,7 @@ int ak_init_perturbed(ak_case *c, double amp, double phase_y, double phase_z, do
     AK_CUDA(cudaStreamSynchronize(c->stream));
     c->prepared = c->farfield == AK_FARFIELD_EXTERIOR;
     c->steps = 0;
+    ++c->pdf_writes;
     return AK_OK;
 }
 
@@ -1057,6 +1060,7 @@ int ak_init_fields(ak_case *c, const double *rho, const double *u) {
     AK_CUDA(cudaStreamSynchronize(c->stream));
     c->prepared = c->farfield == AK_FARFIELD_EXTERIOR;
     c->steps = 0;
+    ++c->pdf_writes;
     return AK_OK;
 }
 
@@ -1284,6 +1288,7 @@ int ak_set_pdf(ak_case *c, const double *pdf) {
         AK_CUDA(cudaGetLastError());
         return AK_OK;
     }));
+    ++c->pdf_writes;
     AK_CUDA(cudaStreamSynchronize(c->stream));
     return AK_OK;
 }
@@ -1568,6 +1573,13 @@ struct ak_refined {
     // lattice (the donor block does not wrap).
     bool fused = false;
     int4 xfer{0, 0, 0, 0};
+    // where the reference's pre-collision coarse state lives (fused form):
+    // 0 the other copy holds it (after set-up), 1 it is the other copy pulled
+    // (after a step: the fused pass read that copy, boundaries applied, and
+    // collided what it pulled), -1 unknown; valid while the coarse level's
+    // pdf_writes equals pre_writes
+    int pre_mode = -1;
+    long long pre_writes = 0;
     // the outer boundaries' branch inside the captured graphs (fused form,
     // transfer block at least three columns from every outer face): UBB,
     // outflow and the budget's outer flux run beside the transfer-block
@@ -1622,6 +1634,11 @@ struct ak_refined {
     double *outer_partials = nullptr, *outer_out = nullptr;  // outer_out: last step [4], running sum [4]
     double *cum_loads = nullptr;                              // wall loads summed over all steps [n * 5]
     double *stats_partials = nullptr, *stats_out = nullptr;
+    // fused form in an FP64-arithmetic storage: the coarse statistics of a
+    // budget step come from the fused pass itself (rows of its far and near
+    // launches, then the transfer block's band outside the box)
+    double *cstats = nullptr;
+    long long cstats_far = 0, cstats_near = 0;
 };
 
 namespace {
@@ -1711,38 +1728,51 @@ constexpr int STATS_BLOCKS = 4 * 152;
 // direction-split kernels: 32 cells per 256-thread block
 long long split_blocks(long long cells) { return (cells + SPLIT_CELLS - 1) / SPLIT_CELLS; }
 
+// dispatch on the storage pair of a two-level case: both levels in one form,
+// or the FP16 form's FP32 fine level (the walls' level)
+template <typename F>
+int with_levels(ak_refined *R, F &&f) {
+    const int c = R->coarse->storage, fs = R->fine->storage;
+    if (c == fs) return with_storage(R->coarse, [&](auto *tag) { return f(tag, tag); });
+    if (c == AK_STORAGE_F16 && fs == AK_STORAGE_F32) return f((__half *)nullptr, (float *)nullptr);
+    return fail(AK_ERR_INVALID, "unsupported pair of level storage forms");
+}
+#define AK_LEVEL_TYPES(a, b) using S = std::remove_pointer_t<decltype(a)>; using SF = std::remove_pointer_t<decltype(b)>
+
 // restriction of the fine block onto the covered coarse cells
-template <typename S>
+template <typename S, typename SF>
 void launch_restrict(ak_refined *R, const Rescale &f2c, cudaStream_t st) {
     const BoxSpec &B = R->B;
     const long long ring = ring_count(B.bx, B.by, 3, 3) * B.bz;
     const long long core = (long long)std::max(B.bx - 6, 0) * std::max(B.by - 6, 0) * B.bz;
     const long long nb = std::max(split_blocks(ring), blocks3(core));
-    k_restrict<S, S><<<dim3((unsigned)nb, 2), SPLIT_THREADS, 0, st>>>(src_of<S>(R->coarse), R->coarse->G,
-                                                                       src_of<S>(R->fine), R->fine->G, B, R->pad,
-                                                                       R->d_free, f2c, R->d_flag);
+    k_restrict<S, SF><<<dim3((unsigned)nb, 2), SPLIT_THREADS, 0, st>>>(src_of<S>(R->coarse), R->coarse->G,
+                                                                        src_of<SF>(R->fine), R->fine->G, B, R->pad,
+                                                                        R->d_free, f2c, R->d_flag);
 }
 
-template <typename S>
+template <typename S, typename SF>
 int refined_init(ak_refined *R, double amp, double phase_y, double phase_z, double lead_x, double lead_y) {
     ak_case *C = R->coarse, *F = R->fine;
     cudaStream_t st = C->stream;
-    for (ak_case *L : {C, F})
-        for (int k = 0; k < 2; ++k) {
-            k_fill<S><<<(unsigned)blocks3(L->G.qs), 256, 0, st>>>((S *)L->pdf[k], L->G, R->d_free);
-            AK_CUDA(cudaGetLastError());
-        }
     const double ky = 2 * M_PI / (C->ny * R->dx_c), kz = 2 * M_PI / R->span;
-    for (ak_case *L : {C, F}) {
+    // both copies of a level at the free stream, then the perturbed state
+    auto level = [&](ak_case *L, auto *tag) -> int {
+        using SL = std::remove_pointer_t<decltype(tag)>;
+        for (int k = 0; k < 2; ++k)
+            k_fill<SL><<<(unsigned)blocks3(L->G.qs), 256, 0, st>>>((SL *)L->pdf[k], L->G, R->d_free);
         const long long n = (long long)L->nx * L->ny * L->nz;
-        k_init_perturbed<S><<<(unsigned)blocks3(n), 256, 0, st>>>(src_of<S>(L), L->G, L->flags, R->speed, amp,
-                                                                   phase_y, phase_z, lead_x, lead_y, L->origin_x,
-                                                                   L->origin_y, L->dx, ky, kz);
+        k_init_perturbed<SL><<<(unsigned)blocks3(n), 256, 0, st>>>(src_of<SL>(L), L->G, L->flags, R->speed, amp,
+                                                                    phase_y, phase_z, lead_x, lead_y, L->origin_x,
+                                                                    L->origin_y, L->dx, ky, kz);
         AK_CUDA(cudaGetLastError());
-    }
+        return AK_OK;
+    };
+    AK_TRY(level(C, (S *)nullptr));
+    AK_TRY(level(F, (SF *)nullptr));
     const Rescale f2c{R->tau_s_c * R->dt_c / (R->tau_s_f * R->dt_f), R->tau_b_c * R->dt_c / (R->tau_b_f * R->dt_f)};
     AK_CUDA(cudaMemsetAsync(R->d_flag, 0, sizeof(int), st));
-    launch_restrict<S>(R, f2c, st);
+    launch_restrict<S, SF>(R, f2c, st);
     AK_CUDA(cudaGetLastError());
     // boundary data from the initial state, ghosts still holding the free
     // stream (refined_solver.py:224-262)
@@ -1752,8 +1782,14 @@ int refined_init(ak_refined *R, double amp, double phase_y, double phase_z, doub
         AK_CUDA(cudaGetLastError());
     }
     if (R->fused) {
-        // outside the transfer block the coarse level stores post-collision
+        // outside the transfer block the coarse level stores post-collision;
+        // the other copy keeps the pre-collision state until the first step
+        // writes it
         using T = typename Store<S>::T;
+        AK_CUDA(cudaMemcpyAsync(dst_of<S>(C), src_of<S>(C), sizeof(S) * (size_t)Q * C->G.qs,
+                                cudaMemcpyDeviceToDevice, st));
+        R->pre_mode = 0;
+        R->pre_writes = C->pdf_writes;
         k_collide<S><<<(unsigned)blocks_for((long long)C->nx * C->ny * C->nz, 128), 128, 0, st>>>(
             src_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s, (T)C->omega_b, make_int4(0, 0, 0, 0),
             R->xfer);
@@ -1773,7 +1809,34 @@ int refined_init(ak_refined *R, double amp, double phase_y, double phase_z, doub
 // Mass, momentum and validity statistics of the coarse cells outside the
 // fine box and the fine block's physical cells, into stats_out[2][NSTAT]
 // (refined_solver.py:291-299, 347-361).
+// the storage forms whose collision arithmetic is FP64-accurate: their fused
+// pass supplies the budget's coarse mass and momentum sums
 template <typename S>
+constexpr bool fused_stats_form() {
+    return std::is_same_v<S, double> || std::is_same_v<S, df2>;
+}
+
+// The budget statistics when the fused coarse pass has written its rows to
+// cstats: the cells of the transfer block outside the box (after reflux and
+// restriction), the reduction over every row, then the fine block.
+template <typename S, typename SF>
+int enqueue_fused_stats(ak_refined *R, cudaStream_t st) {
+    ak_case *C = R->coarse, *F = R->fine;
+    const BoxSpec &B = R->B;
+    const Region band{R->xfer.x - 1, R->xfer.y - 1, R->xfer.z - 1, R->xfer.w - 1, B.lo[0], B.hi[0], B.lo[1], B.hi[1]};
+    const Region rf{R->pad, F->nx - R->pad, R->pad, F->ny - R->pad, 0, 0, 0, 0};
+    const long long rows = R->cstats_far + R->cstats_near + STATS_BLOCKS;
+    k_region_stats<S><<<STATS_BLOCKS, 256, 0, st>>>(src_of<S>(C), C->G, C->flags, band,
+                                                     R->cstats + (R->cstats_far + R->cstats_near) * NSTAT);
+    k_region_final<<<1, REDUCE_THREADS, 0, st>>>(R->cstats, (int)rows, R->stats_out);
+    k_region_stats<SF><<<STATS_BLOCKS, 256, 0, st>>>(src_of<SF>(F), F->G, F->flags, rf, R->stats_partials);
+    k_region_final<<<1, REDUCE_THREADS, 0, st>>>(R->stats_partials, STATS_BLOCKS, R->stats_out + NSTAT);
+    C->launches += 4;
+    AK_CUDA(cudaGetLastError());
+    return AK_OK;
+}
+
+template <typename S, typename SF>
 int enqueue_region_stats(ak_refined *R, cudaStream_t st) {
     ak_case *C = R->coarse, *F = R->fine;
     const BoxSpec &B = R->B;
@@ -1781,16 +1844,17 @@ int enqueue_region_stats(ak_refined *R, cudaStream_t st) {
     const Region rf{R->pad, F->nx - R->pad, R->pad, F->ny - R->pad, 0, 0, 0, 0};
     k_region_stats<S><<<STATS_BLOCKS, 256, 0, st>>>(src_of<S>(C), C->G, C->flags, rc, R->stats_partials);
     k_region_final<<<1, REDUCE_THREADS, 0, st>>>(R->stats_partials, STATS_BLOCKS, R->stats_out);
-    k_region_stats<S><<<STATS_BLOCKS, 256, 0, st>>>(src_of<S>(F), F->G, F->flags, rf, R->stats_partials);
+    k_region_stats<SF><<<STATS_BLOCKS, 256, 0, st>>>(src_of<SF>(F), F->G, F->flags, rf, R->stats_partials);
     k_region_final<<<1, REDUCE_THREADS, 0, st>>>(R->stats_partials, STATS_BLOCKS, R->stats_out + NSTAT);
     C->launches += 4;
     AK_CUDA(cudaGetLastError());
     return AK_OK;
 }
 
-template <typename S>
+template <typename S, typename SF>
 int refined_step(ak_refined *R, bool fork = false) {
     using T = typename Store<S>::T;
+    using TF = typename Store<SF>::T;
     ak_case *C = R->coarse, *F = R->fine;
     cudaStream_t st = C->stream;
     const BoxSpec &B = R->B;
@@ -1804,6 +1868,10 @@ int refined_step(ak_refined *R, bool fork = false) {
     // fork mode, fused form, transfer block away from the outer faces: the
     // boundaries and the far coarse pass on their own branch
     const bool bnd = fork && R->fused && R->bnd_branch;
+    // a budget step of an FP64-arithmetic fused form takes its coarse
+    // statistics from the fused pass
+    bool fstats = false;
+    if constexpr (fused_stats_form<S>()) fstats = R->track_budget && R->step_stats && R->fused && R->cstats;
     const unsigned gf1 = (unsigned)blocks_for((long long)F->nx * F->ny * F->nz, 128);
     const Rescale c2f{R->tau_s_f * R->dt_f / (R->tau_s_c * R->dt_c), R->tau_b_f * R->dt_f / (R->tau_b_c * R->dt_c)};
     const Rescale f2c{R->tau_s_c * R->dt_c / (R->tau_s_f * R->dt_f), R->tau_b_c * R->dt_c / (R->tau_b_f * R->dt_f)};
@@ -1846,9 +1914,14 @@ int refined_step(ak_refined *R, bool fork = false) {
             AK_CUDA(cudaEventRecord(R->ev_bnd_in, st));
             AK_CUDA(cudaStreamWaitEvent(R->bnd, R->ev_bnd_in, 0));
             AK_TRY(outer_part(R->bnd));
-            k_stream_collide<S><<<gc1, 128, 0, R->bnd>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, C->shift_host,
-                                                          (T)C->omega_s, (T)C->omega_b, Sgs<T>{}, R->xfer,
-                                                          make_int4(0, 0, 0, 0), R->near);
+            if (fstats)
+                k_stream_collide<S, true><<<gc1, 128, 0, R->bnd>>>(
+                    src_of<S>(C), dst_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s, (T)C->omega_b,
+                    Sgs<T>{}, R->xfer, make_int4(0, 0, 0, 0), R->near, R->cstats);
+            else
+                k_stream_collide<S><<<gc1, 128, 0, R->bnd>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G,
+                                                              C->shift_host, (T)C->omega_s, (T)C->omega_b, Sgs<T>{},
+                                                              R->xfer, make_int4(0, 0, 0, 0), R->near);
             AK_CUDA(cudaEventRecord(R->ev_bnd_out, R->bnd));
         }
         mark(C);
@@ -1870,11 +1943,23 @@ int refined_step(ak_refined *R, bool fork = false) {
             R->dx_c * R->dx_c * R->dx_c, R->reg_c);
         if (!bnd) AK_TRY(outer_part(st));
         mark(C);
-        if (bnd)
+        if (bnd && fstats)
+            k_stream_collide<S, true><<<gn1, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G,
+                                                            C->shift_host, (T)C->omega_s, (T)C->omega_b, Sgs<T>{},
+                                                            R->xfer, R->near, make_int4(0, 0, 0, 0),
+                                                            R->cstats + R->cstats_far * NSTAT);
+        else if (bnd)
             // the cells of near; the rest runs on the boundaries' branch
             k_stream_collide<S><<<gn1, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, C->shift_host,
                                                       (T)C->omega_s, (T)C->omega_b, Sgs<T>{}, R->xfer, R->near);
-        else if (R->fused)
+        else if (R->fused && fstats) {
+            // one launch covers every row of the far part; the near rows stay empty
+            AK_CUDA(cudaMemsetAsync(R->cstats + R->cstats_far * NSTAT, 0, sizeof(double) * R->cstats_near * NSTAT, st));
+            k_stream_collide<S, true><<<gc1, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G,
+                                                            C->shift_host, (T)C->omega_s, (T)C->omega_b, Sgs<T>{},
+                                                            R->xfer, make_int4(0, 0, 0, 0), make_int4(0, 0, 0, 0),
+                                                            R->cstats);
+        } else if (R->fused)
             // streaming fused with the next step's collision, the transfer
             // block streamed only
             k_stream_collide<S><<<gc1, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, C->shift_host,
@@ -1895,28 +1980,28 @@ int refined_step(ak_refined *R, bool fork = false) {
         // half-way (1 - 1/2) old + 1/2 new (refined_solver.py:311-318)
         k_prolong_x<<<(unsigned)blocks3(nprox), 256, 0, s>>>(B, C->nz, R->pad, sub ? R->mom_half : R->mom_old,
                                                               R->pro_x);
-        k_donors<S><<<(unsigned)split_blocks(nband), SPLIT_THREADS, 0, s>>>(src_of<S>(F), F->G, C->nz, R->pro_x, B.dny,
-                                                                            c2f, R->pad, R->d_flag);
+        k_donors<SF><<<(unsigned)split_blocks(nband), SPLIT_THREADS, 0, s>>>(src_of<SF>(F), F->G, C->nz, R->pro_x,
+                                                                             B.dny, c2f, R->pad, R->d_flag);
         mark(C);
-        k_collide<S><<<gf1, 128, 0, s>>>(src_of<S>(F), F->flags, F->G, F->shift_host, (T)F->omega_s,
-                                          (T)F->omega_b);
+        k_collide<SF><<<gf1, 128, 0, s>>>(src_of<SF>(F), F->flags, F->G, F->shift_host, (TF)F->omega_s,
+                                           (TF)F->omega_b);
         mark(C);
         cudaStream_t fs = flux_stream(s, 1 + sub);
         if (!fs) return fail(AK_ERR_CUDA, "face-flux branch could not be forked");
-        k_face_flux_fine<S><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, fs>>>(
-            src_of<S>(F), F->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs, R->pad,
+        k_face_flux_fine<SF><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, fs>>>(
+            src_of<SF>(F), F->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs, R->pad,
             R->dx_f * R->dx_f * R->dx_f, R->reg_f);
         if (fork && sub == 0) AK_CUDA(cudaEventRecord(R->ev_flux_f0, R->flux));
         if (nlinks) {
-            k_walls<S><<<(unsigned)nb, 256, 0, s>>>(src_of<S>(F), F->G, F->keys, F->wall_q, F->nkeys, 1,
-                                                    F->n_elements, F->ox, F->oy, F->partials);
+            k_walls<SF><<<(unsigned)nb, 256, 0, s>>>(src_of<SF>(F), F->G, F->keys, F->wall_q, F->nkeys, 1,
+                                                     F->n_elements, F->ox, F->oy, F->partials);
             k_sum_partials<<<5 * F->n_elements, 32, 0, s>>>(F->partials, (int)nb, 5 * F->n_elements,
                                                              R->d_loads + sub * 5 * F->n_elements);
         }
         mark(C);
         // the second fine step streams into the copy the first step's flux reads
         if (fork && sub == 1) AK_CUDA(cudaStreamWaitEvent(s, R->ev_flux_f0, 0));
-        k_stream<S><<<gf, 128, 0, s>>>(src_of<S>(F), dst_of<S>(F), F->flags, F->G, 1);
+        k_stream<SF><<<gf, 128, 0, s>>>(src_of<SF>(F), dst_of<SF>(F), F->flags, F->G, 1);
         mark(C);
         AK_CUDA(cudaGetLastError());
         F->cur = 1 - F->cur;
@@ -1957,7 +2042,7 @@ int refined_step(ak_refined *R, bool fork = false) {
     if (fork) {
         AK_CUDA(cudaEventRecord(R->ev_fork, st));
         AK_CUDA(cudaStreamWaitEvent(R->side, R->ev_fork, 0));
-        launch_restrict<S>(R, f2c, R->side);
+        launch_restrict<S, SF>(R, f2c, R->side);
         AK_CUDA(cudaEventRecord(R->ev_join, R->side));
     }
     k_reflux<S><<<dim3((unsigned)split_blocks(R->max_face), R->nfaces), SPLIT_THREADS, 0, st>>>(
@@ -1966,13 +2051,18 @@ int refined_step(ak_refined *R, bool fork = false) {
     if (fork)
         AK_CUDA(cudaStreamWaitEvent(st, R->ev_join, 0));
     else
-        launch_restrict<S>(R, f2c, st);
+        launch_restrict<S, SF>(R, f2c, st);
     AK_CUDA(cudaGetLastError());
     if (bnd) AK_CUDA(cudaStreamWaitEvent(st, R->ev_bnd_out, 0));
     // a tracked budget closes on the integrals of the state the step leaves
-    if (R->track_budget && R->step_stats) AK_TRY(enqueue_region_stats<S>(R, st));
+    if (fstats)
+        AK_TRY((enqueue_fused_stats<S, SF>(R, st)));
+    else if (R->track_budget && R->step_stats)
+        AK_TRY((enqueue_region_stats<S, SF>(R, st)));
     mark(C);  // step end
     C->launches += 6 + 7 * 2 + (C->n_ubb ? 1 : 0) + (C->n_out ? 1 : 0) + (nlinks ? 0 : -4) + 1 + (bnd ? 1 : 0);
+    R->pre_mode = 1;
+    R->pre_writes = C->pdf_writes;
     C->steps += 1;
     F->steps += 2;
     R->steps += 1;
@@ -1995,6 +2085,8 @@ int graph_priorities(ak_refined *R, cudaGraph_t g) {
     std::vector<cudaGraphNode_t> nodes(n);
     AK_CUDA(cudaGraphGetNodes(g, nodes.data(), &n));
     const void *pass = (const void *)k_stream_collide<S>;
+    const void *pass_stats = pass;
+    if constexpr (fused_stats_form<S>()) pass_stats = (const void *)k_stream_collide<S, true>;
     for (size_t k = 0; k < n; ++k) {
         cudaGraphNodeType type;
         AK_CUDA(cudaGraphNodeGetType(nodes[k], &type));
@@ -2002,7 +2094,7 @@ int graph_priorities(ak_refined *R, cudaGraph_t g) {
         cudaKernelNodeParams p{};
         AK_CUDA(cudaGraphKernelNodeGetParams(nodes[k], &p));
         cudaKernelNodeAttrValue v{};
-        v.priority = p.func == pass && p.gridDim.x == far_grid ? least : greatest;
+        v.priority = (p.func == pass || p.func == pass_stats) && p.gridDim.x == far_grid ? least : greatest;
         AK_CUDA(cudaGraphKernelNodeSetAttribute(nodes[k], cudaKernelNodeAttributePriority, &v));
     }
     return AK_OK;
@@ -2012,7 +2104,7 @@ int graph_priorities(ak_refined *R, cudaGraph_t g) {
 // captured once per buffer parity (the coarse copies swap every step, the
 // fine copies twice) and the host-side counters are advanced as the eager
 // step advances them.
-template <typename S>
+template <typename S, typename SF>
 int refined_step_graphed(ak_refined *R) {
     ak_case *C = R->coarse, *F = R->fine;
     const int slot = C->cur | (F->cur << 1) | (R->track_budget ? 4 : 0) | (R->step_stats ? 8 : 0);
@@ -2022,7 +2114,7 @@ int refined_step_graphed(ak_refined *R) {
         std::vector<cudaEvent_t> *timing = C->timing;
         C->timing = nullptr;
         AK_CUDA(cudaStreamBeginCapture(C->stream, cudaStreamCaptureModeThreadLocal));
-        const int r = refined_step<S>(R, true);
+        const int r = refined_step<S, SF>(R, true);
         cudaGraph_t g = nullptr;
         const cudaError_t e = cudaStreamEndCapture(C->stream, &g);
         C->timing = timing;
@@ -2055,6 +2147,8 @@ int refined_step_graphed(ak_refined *R) {
     }
     AK_CUDA(cudaGraphLaunch(R->graph[slot], C->stream));
     C->cur = 1 - C->cur;
+    R->pre_mode = 1;
+    R->pre_writes = C->pdf_writes;
     C->launches += R->launches_per_step;
     C->steps += 1;
     F->steps += 2;
@@ -2083,6 +2177,10 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
         return fail(AK_ERR_INVALID, "the refined box must fit strictly inside the external x/y domain");
     if (!(desc->tau_shear > 0.5) || !(desc->tau_bulk > 0.5) || !(desc->dt_coarse > 0) || !(desc->span > 0))
         return fail(AK_ERR_INVALID, "relaxation times must exceed 0.5 and dt, span be positive");
+    if (desc->fine_storage >= 0 && desc->fine_storage != cd.storage &&
+        !(cd.storage == AK_STORAGE_F16 && desc->fine_storage == AK_STORAGE_F32))
+        return fail(AK_ERR_INVALID, "the fine level shares the coarse storage form, or holds FP32 under an FP16 "
+                                    "coarse level");
     ak_refined *R = new ak_refined();
     R->dx_c = cd.dx;
     R->dt_c = desc->dt_coarse;
@@ -2119,6 +2217,7 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
     r = create_lattice(&coarse, AK_FARFIELD_LEGACY, false, &R->coarse);
     // fine block: two donor cells around the box in x and y, wraps everywhere
     ak_case_desc fine = cd;
+    fine.storage = desc->fine_storage >= 0 ? desc->fine_storage : cd.storage;
     fine.nx = 2 * B.bx + 2 * R->pad;
     fine.ny = 2 * B.by + 2 * R->pad;
     fine.nz = 2 * B.bz;
@@ -2217,6 +2316,14 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
         if (r == AK_OK) r = ralloc(R, &R->outer_out, 8);
         if (r == AK_OK) r = ralloc(R, &R->cum_loads, (size_t)5 * std::max(1, cd.n_elements));
         if (r == AK_OK) r = ralloc(R, &R->stats_partials, (size_t)STATS_BLOCKS * NSTAT);
+        if (r == AK_OK && R->fused) {
+            // rows of the fused pass's statistics: its far launch (a grid over
+            // the whole coarse lattice), its near launch, the band's blocks
+            const int4 nr = R->near;
+            R->cstats_far = blocks_for((long long)cd.nx * cd.ny * cd.nz, 128);
+            R->cstats_near = blocks_for((long long)(nr.y - nr.x) * (nr.w - nr.z) * cd.nz, 128);
+            r = ralloc(R, &R->cstats, (size_t)(R->cstats_far + R->cstats_near + STATS_BLOCKS) * NSTAT);
+        }
         if (r == AK_OK) r = ralloc(R, &R->stats_out, (size_t)2 * NSTAT);
         if (r == AK_OK && (cudaMemset(R->outer_out, 0, 8 * sizeof(double)) != cudaSuccess ||
                            cudaMemset(R->cum_loads, 0, 5 * std::max(1, cd.n_elements) * sizeof(double)) != cudaSuccess))
@@ -2271,8 +2378,9 @@ ak_case *ak_refined_level(ak_refined *R, int32_t level) {
 int ak_refined_init_perturbed(ak_refined *R, double amp, double phase_y, double phase_z, double lead_x,
                               double lead_y) {
     if (!R) return fail(AK_ERR_INVALID, "null case");
-    return with_storage(R->coarse, [&](auto *tag) {
-        return refined_init<std::remove_pointer_t<decltype(tag)>>(R, amp, phase_y, phase_z, lead_x, lead_y);
+    return with_levels(R, [&](auto *tc, auto *tf) {
+        AK_LEVEL_TYPES(tc, tf);
+        return refined_init<S, SF>(R, amp, phase_y, phase_z, lead_x, lead_y);
     });
 }
 
@@ -2288,10 +2396,13 @@ int ak_refined_step_budget(ak_refined *R, int32_t nsteps, double *loads, double 
     cudaStream_t st = R->coarse->stream;
     AK_CUDA(cudaMemsetAsync(R->d_flag, 0, sizeof(int), st));
     for (int s = 0; s < nsteps; ++s) {
-        // only the last step computes the integrals a caller asked for
-        R->step_stats = stats != nullptr && s == nsteps - 1;
-        const int r = with_storage(R->coarse, [&](auto *tag) {
-            return refined_step_graphed<std::remove_pointer_t<decltype(tag)>>(R);
+        // with stats every step closes its budget on the integrals of the
+        // state it leaves (the reference's step, refined_solver.py:311-343);
+        // the last step's are returned
+        R->step_stats = stats != nullptr;
+        const int r = with_levels(R, [&](auto *tc, auto *tf) {
+            AK_LEVEL_TYPES(tc, tf);
+            return refined_step_graphed<S, SF>(R);
         });
         R->step_stats = false;
         if (r != AK_OK) return r;
@@ -2355,7 +2466,10 @@ int ak_refined_integrals(ak_refined *R, double *out) {
     if (!R || !out) return fail(AK_ERR_INVALID, "a case and an output array are required");
     ak_case *C = R->coarse;
     cudaStream_t st = C->stream;
-    const int r = with_storage(C, [&](auto *tag) { return enqueue_region_stats<std::remove_pointer_t<decltype(tag)>>(R, st); });
+    const int r = with_levels(R, [&](auto *tc, auto *tf) {
+        AK_LEVEL_TYPES(tc, tf);
+        return enqueue_region_stats<S, SF>(R, st);
+    });
     if (r != AK_OK) return r;
     AK_CUDA(cudaMemcpyAsync(out, R->stats_out, 2 * NSTAT * sizeof(double), cudaMemcpyDeviceToHost, st));
     AK_CUDA(cudaStreamSynchronize(st));
@@ -2369,7 +2483,10 @@ int ak_refined_step_timed(ak_refined *R, int32_t nsteps, double *ms) {
     C->timing = &events;
     int r = AK_OK;
     for (int s = 0; s < nsteps && r == AK_OK; ++s)
-        r = with_storage(C, [&](auto *tag) { return refined_step<std::remove_pointer_t<decltype(tag)>>(R); });
+        r = with_levels(R, [&](auto *tc, auto *tf) {
+            AK_LEVEL_TYPES(tc, tf);
+            return refined_step<S, SF>(R);
+        });
     C->timing = nullptr;
     const cudaError_t e = cudaStreamSynchronize(C->stream);
     for (int k = 0; k < 6; ++k) ms[k] = 0.0;
@@ -2399,6 +2516,31 @@ int ak_refined_step_timed(ak_refined *R, int32_t nsteps, double *ms) {
     return AK_OK;
 }
 
+int ak_refined_states(ak_refined *R, double *coarse, double *fine) {
+    if (!R) return fail(AK_ERR_INVALID, "null case");
+    ak_case *C = R->coarse;
+    if (coarse && R->fused) {
+        if (R->pre_mode < 0 || C->pdf_writes != R->pre_writes)
+            return fail(AK_ERR_INVALID, "the pre-collision coarse state is known again after the next step (the "
+                                        "coarse populations were written from outside the step)");
+        const long long n = (long long)C->nx * C->ny * C->nz;
+        AK_TRY(ensure_staging(C, (size_t)n * Q));
+        AK_TRY(with_storage(C, [&](auto *tag) {
+            using S = std::remove_pointer_t<decltype(tag)>;
+            k_export_pre_collision<S><<<(unsigned)blocks_for(n, 256), 256, 0, C->stream>>>(
+                src_of<S>(C), dst_of<S>(C), C->G, R->xfer, R->pre_mode, C->staging);
+            AK_CUDA(cudaGetLastError());
+            return AK_OK;
+        }));
+        AK_CUDA(cudaMemcpyAsync(coarse, C->staging, n * Q * sizeof(double), cudaMemcpyDeviceToHost, C->stream));
+        AK_CUDA(cudaStreamSynchronize(C->stream));
+    } else if (coarse) {
+        AK_TRY(ak_get_pdf(C, coarse));
+    }
+    if (fine) AK_TRY(ak_get_pdf(R->fine, fine));
+    return AK_OK;
+}
+
 int ak_refined_probe(ak_refined *R, int32_t op, double *out, int64_t *n_out) {
     if (!R || op < 0 || op > 3) return fail(AK_ERR_INVALID, "a case and an operation 0..3 are required");
     if (n_out) *n_out = op == 2 ? 2 * R->reg_doubles : 0;
@@ -2408,8 +2550,8 @@ int ak_refined_probe(ak_refined *R, int32_t op, double *out, int64_t *n_out) {
     const BoxSpec &B = R->B;
     AK_CUDA(cudaStreamSynchronize(st));
     AK_CUDA(cudaMemsetAsync(R->d_flag, 0, sizeof(int), st));
-    const int r = with_storage(C, [&](auto *tag) -> int {
-        using S = std::remove_pointer_t<decltype(tag)>;
+    const int r = with_levels(R, [&](auto *tc, auto *tf) -> int {
+        AK_LEVEL_TYPES(tc, tf);
         if (op == 0) {
             const long long nring_block = ring_count(B.dnx, B.dny, DONOR_RING, DONOR_RING) * C->nz;
             const long long nprox = ring_count(F->nx, B.dny, R->pad, DONOR_RING) * C->nz;
@@ -2419,19 +2561,20 @@ int ak_refined_probe(ak_refined *R, int32_t op, double *out, int64_t *n_out) {
             k_block_moments<S><<<(unsigned)split_blocks(nring_block), SPLIT_THREADS, 0, st>>>(
                 src_of<S>(C), C->G, B, R->d_free, R->mom_old, nullptr, nullptr, R->d_flag);
             k_prolong_x<<<(unsigned)blocks3(nprox), 256, 0, st>>>(B, C->nz, R->pad, R->mom_old, R->pro_x);
-            k_donors<S><<<(unsigned)split_blocks(nband), SPLIT_THREADS, 0, st>>>(src_of<S>(F), F->G, C->nz, R->pro_x,
-                                                                                 B.dny, c2f, R->pad, R->d_flag);
+            k_donors<SF><<<(unsigned)split_blocks(nband), SPLIT_THREADS, 0, st>>>(src_of<SF>(F), F->G, C->nz,
+                                                                                  R->pro_x, B.dny, c2f, R->pad,
+                                                                                  R->d_flag);
         } else if (op == 1) {
             const Rescale f2c{R->tau_s_c * R->dt_c / (R->tau_s_f * R->dt_f),
                               R->tau_b_c * R->dt_c / (R->tau_b_f * R->dt_f)};
-            launch_restrict<S>(R, f2c, st);
+            launch_restrict<S, SF>(R, f2c, st);
         } else if (op == 2) {
             AK_CUDA(cudaMemsetAsync(R->reg_f, 0, sizeof(double) * R->reg_doubles, st));
             k_face_flux_coarse<S><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, st>>>(
                 src_of<S>(C), C->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs,
                 R->dx_c * R->dx_c * R->dx_c, R->reg_c);
-            k_face_flux_fine<S><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, st>>>(
-                src_of<S>(F), F->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs,
+            k_face_flux_fine<SF><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, st>>>(
+                src_of<SF>(F), F->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs,
                 R->pad, R->dx_f * R->dx_f * R->dx_f, R->reg_f);
         } else {
             k_reflux<S><<<dim3((unsigned)split_blocks(R->max_face), R->nfaces), SPLIT_THREADS, 0, st>>>(

@@ -73,16 +73,65 @@ __device__ __forceinline__ void store_g(S *pdf, const Grid &G, int q, int x, int
 __device__ __forceinline__ float shift_at(const Shift27 &s, int q) { return s.v[q]; }
 __device__ __forceinline__ float shift_at(const float *s, int q) { return __ldg(s + q); }
 
+// Validity and conservation statistics of a set of cells, in this order
+// (the layout the two-level budget reduces): max |u|^2, max |rho - 1|,
+// sum drho, sum j (3), cells, non-finite cells.
+constexpr int CELL_STATS = 8;
+__device__ __forceinline__ void add_cell_stats(double acc[CELL_STATS], double drho, double jx, double jy, double jz,
+                                               double u2) {
+    const double rho = 1.0 + drho;
+    if (!isfinite(rho) || !isfinite(u2)) {
+        acc[7] += 1.0;
+        return;
+    }
+    acc[0] = fmax(acc[0], u2);
+    acc[1] = fmax(acc[1], fabs(rho - 1.0));
+    acc[2] += drho;
+    acc[3] += jx;
+    acc[4] += jy;
+    acc[5] += jz;
+    acc[6] += 1.0;
+}
+
+// block sums of the per-thread statistics (the first two entries maxima) in a
+// fixed order; thread 0 writes out[row * CELL_STATS ...].  Every thread of
+// the block must call it.
+__device__ void block_cell_stats(double (&a)[CELL_STATS], double *out, long long row) {
+    __shared__ double red[32][CELL_STATS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a[0] = fmax(a[0], __shfl_down_sync(0xffffffffu, a[0], o));
+        a[1] = fmax(a[1], __shfl_down_sync(0xffffffffu, a[1], o));
+#pragma unroll
+        for (int k = 2; k < CELL_STATS; ++k) a[k] += __shfl_down_sync(0xffffffffu, a[k], o);
+    }
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < CELL_STATS; ++k) red[warp][k] = a[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        for (int w = 1; w < nw; ++w) {
+            red[0][0] = fmax(red[0][0], red[w][0]);
+            red[0][1] = fmax(red[0][1], red[w][1]);
+            for (int k = 2; k < CELL_STATS; ++k) red[0][k] += red[w][k];
+        }
+        for (int k = 0; k < CELL_STATS; ++k) out[row * CELL_STATS + k] = red[0][k];
+    }
+}
+
 // pull the 27 populations of interior cell (x, y, z) (padded x, y), collide,
 // store into dst if the column is fluid; stream_only: store the pulled values
-// as they are (bit copies, no collision)
+// as they are (bit copies, no collision); acc (optional): add the collided
+// cell's statistics (mass and momentum are those the collision conserves)
 template <typename S, typename Shift>
 __device__ __forceinline__ void stream_collide_cell(const S *__restrict__ src, S *__restrict__ dst,
                                                     const uint8_t *__restrict__ flags, const Grid &G,
                                                     const Shift &shift, typename Store<S>::T omega_s,
                                                     typename Store<S>::T omega_b, int x, int y, int z,
                                                     const Sgs<typename Store<S>::T> &sgs,
-                                                    bool stream_only = false) {
+                                                    bool stream_only = false, double *acc = nullptr) {
     using T = typename Store<S>::T;
     // the column flag only gates the stores, so the 27 loads issue at once
     const bool fluid = __ldg(flags + y * G.nxp + x) == FLAG_FLUID;
@@ -107,19 +156,24 @@ __device__ __forceinline__ void stream_collide_cell(const S *__restrict__ src, S
                    ? Store<S>::load(row[cz(q) + 1] + off, q, shift_at(shift, q))
                    : T(0);
     }
-    collide_stored<S>(g, omega_s, omega_b, sgs);
+    T mac[5];
+    collide_stored<S>(g, omega_s, omega_b, sgs, acc ? mac : nullptr);
     if (!fluid) return;
+    if (acc) add_cell_stats(acc, (double)mac[0], (double)mac[1], (double)mac[2], (double)mac[3], (double)mac[4]);
     const long long c = G.cell(x, y, z);
 #pragma unroll
     for (int q = 0; q < Q; ++q) Store<S>::store(dst + q * G.qs + c, q, g[q], shift_at(shift, q));
 }
 
-template <typename S>
+// STATS: every block also writes the statistics of the cells it collided
+// (not the streamed-only ones) to stats[blockIdx.x] (CELL_STATS each)
+template <typename S, bool STATS = false>
 __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
     k_stream_collide(const S *__restrict__ src, S *__restrict__ dst, const uint8_t *__restrict__ flags, Grid G,
                      Shift27 shift, typename Store<S>::T omega_s, typename Store<S>::T omega_b,
                      Sgs<typename Store<S>::T> sgs, int4 raw = make_int4(0, 0, 0, 0),
-                     int4 rect = make_int4(0, 0, 0, 0), int4 skip = make_int4(0, 0, 0, 0)) {
+                     int4 rect = make_int4(0, 0, 0, 0), int4 skip = make_int4(0, 0, 0, 0),
+                     double *__restrict__ stats = nullptr) {
     // one thread per cell of the padded columns x [rect.x, rect.y) by y
     // [rect.z, rect.w) (rect.y == 0: the whole interior), every z, x fastest,
     // numbered across rows: warps stay full whatever the width (the plain
@@ -130,15 +184,28 @@ __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
     const unsigned w = (unsigned)(rect.y - rect.x), h = (unsigned)(rect.w - rect.z);
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned nxy = w * h;
-    if (i >= nxy * (unsigned)G.nz) return;
-    const unsigned z = i / nxy, r = i - z * nxy;
-    const unsigned yr = r / w;
-    const int x = rect.x + (int)(r - yr * w), y = rect.z + (int)yr;
-    if (x >= skip.x && x < skip.y && y >= skip.z && y < skip.w) return;
-    // raw: the padded x [raw.x, raw.y) by y [raw.z, raw.w) columns are only
-    // streamed (they keep pre-collision populations)
-    const bool stream_only = x >= raw.x && x < raw.y && y >= raw.z && y < raw.w;
-    stream_collide_cell(src, dst, flags, G, shift, omega_s, omega_b, x, y, (int)z, sgs, stream_only);
+    double acc[CELL_STATS] = {0, 0, 0, 0, 0, 0, 0, 0};
+    bool active = i < nxy * (unsigned)G.nz;
+    int x = 0, y = 0, z = 0;
+    if (active) {
+        z = (int)(i / nxy);
+        const unsigned r = i - (unsigned)z * nxy;
+        const unsigned yr = r / w;
+        x = rect.x + (int)(r - yr * w);
+        y = rect.z + (int)yr;
+        active = !(x >= skip.x && x < skip.y && y >= skip.z && y < skip.w);
+    }
+    if constexpr (!STATS) {
+        if (!active) return;
+    }
+    if (active) {
+        // raw: the padded x [raw.x, raw.y) by y [raw.z, raw.w) columns are
+        // only streamed (they keep pre-collision populations)
+        const bool stream_only = x >= raw.x && x < raw.y && y >= raw.z && y < raw.w;
+        stream_collide_cell(src, dst, flags, G, shift, omega_s, omega_b, x, y, z, sgs, stream_only,
+                            STATS ? acc : nullptr);
+    }
+    if constexpr (STATS) block_cell_stats(acc, stats, blockIdx.x);
 }
 
 // ------------------------------------------------------------ walls

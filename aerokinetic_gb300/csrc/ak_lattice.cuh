@@ -152,6 +152,28 @@ template <>
 __host__ __device__ __forceinline__ df64 mul_pow2<df64>(df64 a, double s) {
     return df64(a.hi * (float)s, a.lo * (float)s);
 }
+// FP64 on the device: GB300 issues FP64 at 1/64 of its FP32 rate, and the
+// plain collision is bound by that pipe, so the exact scalings run on the
+// integer pipe instead: s = +-2^k adds k to the exponent field of the high
+// word (and flips the sign for s < 0).  Identical to a * s for every normal
+// a with a normal product and for +-0; a subnormal a (|a| < 2^-1022) is
+// returned unscaled.  s is a compile-time constant at every call site, so
+// the selection below folds away.
+template <>
+__host__ __device__ __forceinline__ double mul_pow2<double>(double a, double s) {
+#ifdef __CUDA_ARCH__
+    if (s == -1.0) return -a;  // a sign modifier on the consumer
+    const int k = (s == 0.5 || s == -0.5) ? -1 : ((s == 2.0 || s == -2.0) ? 1 : ((s == 4.0 || s == -4.0) ? 2 : 0));
+    if (k == 0) return a * s;
+    int hi = __double2hiint(a);
+    const int lo = __double2loint(a);
+    if (hi & 0x7ff00000) hi += k * (1 << 20);  // a normal a: scale; +-0 and subnormals keep their exponent
+    if (s < 0) hi ^= (int)0x80000000;
+    return __hiloint2double(hi, lo);
+#else
+    return a * s;
+#endif
+}
 
 // Smagorinsky subgrid model (sgs="smagorinsky", solver.py:74-77; Hou,
 // Sterling, Chen & Doolen 1996 in lattice units): with the non-equilibrium
@@ -176,8 +198,11 @@ __host__ __device__ __forceinline__ T smagorinsky_rate(const Sgs<T> &m, T rinv, 
     return T(R(2) / (m.tau0 + sqrt(m.c18 * norm + m.tau0 * m.tau0)));
 }
 
+// mac (optional): the cell's (drho, jx, jy, jz, |u|^2), which the collision
+// conserves (drho, j) or forms anyway; a null mac compiles away.
 template <typename T>
-__host__ __device__ __forceinline__ void collide(T g[Q], T omega_s, T omega_b, const Sgs<T> &sgs = Sgs<T>{}) {
+__host__ __device__ __forceinline__ void collide(T g[Q], T omega_s, T omega_b, const Sgs<T> &sgs = Sgs<T>{},
+                                                 T *mac = nullptr) {
     // raw moments of g up to second order through partial line sums
     T Z0[3][3], Z1[3][3], Z2[3][3];
 #pragma unroll
@@ -213,6 +238,13 @@ __host__ __device__ __forceinline__ void collide(T g[Q], T omega_s, T omega_b, c
     const T rho = T(1) + drho;
     const T rinv = T(1) / rho;
     const T ux = jx * rinv, uy = jy * rinv, uz = jz * rinv;
+    if (mac) {
+        mac[0] = drho;
+        mac[1] = jx;
+        mac[2] = jy;
+        mac[3] = jz;
+        mac[4] = ux * ux + uy * uy + uz * uz;
+    }
     // second-order central moments minus their rest value 1/3
     const T kdx = M200 - jx * ux, kdy = M020 - jy * uy, kdz = M002 - jz * uz;
     const T kxy = M110 - jx * uy, kxz = M101 - jx * uz, kyz = M011 - jy * uz;
@@ -275,7 +307,8 @@ __host__ __device__ __forceinline__ void collide(T g[Q], T omega_s, T omega_b, c
 // first along x for A, B, C of every c_y, then along z with rho folded into
 // the z-functions.  About 370 FP64 operations per cell.
 template <typename T>
-__host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b, const Sgs<T> &sgs = Sgs<T>{}) {
+__host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b, const Sgs<T> &sgs = Sgs<T>{},
+                                                      T *mac = nullptr) {
     T Z0[3][3], Z1[3][3], Z2[3][3];
 #pragma unroll
     for (int ix = 0; ix < 3; ++ix)
@@ -310,6 +343,13 @@ __host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b, 
     const T rho = T(1) + drho;
     const T rinv = T(1) / rho;
     const T ux = jx * rinv, uy = jy * rinv, uz = jz * rinv;
+    if (mac) {
+        mac[0] = drho;
+        mac[1] = jx;
+        mac[2] = jy;
+        mac[3] = jz;
+        mac[4] = ux * ux + uy * uy + uz * uz;
+    }
     // second-order central moments minus 1/3, relaxed
     const T kdx = M200 - jx * ux, kdy = M020 - jy * uy, kdz = M002 - jz * uz;
     const T third = T(1.0 / 3.0);
@@ -388,12 +428,13 @@ __host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b, 
 template <typename S>
 __host__ __device__ __forceinline__ void collide_stored(typename Store<S>::T g[Q], typename Store<S>::T omega_s,
                                                         typename Store<S>::T omega_b,
-                                                        const Sgs<typename Store<S>::T> &sgs = {}) {
+                                                        const Sgs<typename Store<S>::T> &sgs = {},
+                                                        typename Store<S>::T *mac = nullptr) {
     using T = typename Store<S>::T;
     if constexpr (sizeof(S) == sizeof(float))
-        collide<T>(g, omega_s, omega_b, sgs);
+        collide<T>(g, omega_s, omega_b, sgs, mac);
     else
-        collide_full<T>(g, T(1) - omega_s, omega_b, sgs);
+        collide_full<T>(g, T(1) - omega_s, omega_b, sgs, mac);
 }
 
 }  // namespace ak

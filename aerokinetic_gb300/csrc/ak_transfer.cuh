@@ -358,6 +358,33 @@ __global__ void k_stream(const S *__restrict__ src, S *__restrict__ dst, const u
     }
 }
 
+// The pre-collision coarse state of the fused form, (x, y, z, 27) doubles:
+// mode 1 (after a step) pulls every cell outside the transfer block (padded
+// columns x [xfer.x, xfer.y) by y [xfer.z, xfer.w)) from the other copy,
+// which the step's fused pass read with the outer boundaries applied, and
+// takes the transfer block's cells from the current copy; mode 0 (after
+// set-up) reads every cell of the other copy.
+template <typename S>
+__global__ void k_export_pre_collision(const S *__restrict__ cur, const S *__restrict__ other, Grid G, int4 xfer,
+                                       int mode, double *__restrict__ out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)G.nx * G.ny * G.nz) return;
+    const int z = (int)(i % G.nz);
+    const long long xy = i / G.nz;
+    const int y = (int)(xy % G.ny) + 1, x = (int)(xy / G.ny) + 1;
+    const bool block = x >= xfer.x && x < xfer.y && y >= xfer.z && y < xfer.w;
+    for (int q = 0; q < Q; ++q) {
+        double v;
+        if (mode == 0)
+            v = load_g(other, G, q, x, y, z);
+        else if (block)
+            v = load_g(cur, G, q, x, y, z);
+        else
+            v = load_g(other, G, q, x - cx(q), y - cy(q), G.wrapz(z - cz(q)));
+        out[i * Q + q] = v;
+    }
+}
+
 // every cell, ghosts included, set to the given zero-centred populations
 template <typename S>
 __global__ void k_fill(S *__restrict__ pdf, Grid G, const double *__restrict__ g27) {
@@ -866,7 +893,7 @@ __device__ __forceinline__ void mass_momentum(const S *__restrict__ cell, const 
     j[1] = sy[2] - sy[0];
     j[2] = jz;
 }
-constexpr int NSTAT = 8;
+constexpr int NSTAT = CELL_STATS;
 template <typename S>
 __global__ void __launch_bounds__(256)
     k_region_stats(const S *__restrict__ pdf, Grid G, const uint8_t *__restrict__ flags, Region R,

@@ -59,10 +59,19 @@ class RefinedSolver:
     budget=False skips the per-step integrals and outer-face fluxes."""
     pad = 2
 
-    def __init__(self, project, refinement=RefinementSettings(), progress=None, storage="f64", budget=True):
+    def __init__(self, project, refinement=RefinementSettings(), progress=None, storage="f64", budget=True,
+                 fine_storage=None):
         if storage not in _native.STORAGE:
             raise ValueError(f"storage must be one of {sorted(_native.STORAGE)}")
+        # the FP16 form keeps the fine level, which holds the walls, in FP32:
+        # the FP16 significand is spent on the far field's small departures
+        # from the free stream, while the wall region's populations keep FP32's
+        if fine_storage is None:
+            fine_storage = "f32" if storage == "f16" else storage
+        if fine_storage != storage and (storage, fine_storage) != ("f16", "f32"):
+            raise ValueError("fine_storage must equal storage, or be 'f32' (or 'f16') under storage='f16'")
         self.project, self.refinement, self.storage = project, refinement, storage
+        self.fine_storage = fine_storage
         self.budget = bool(budget)
         self.section, self.flow, self.grid = project.section, project.flow, project.grid
         self.plan = RefinedPlan.create(project, refinement)
@@ -92,7 +101,7 @@ class RefinedSolver:
         box = self.plan.box
         desc = _native.RefinedDesc(coarse, self.coarse_level.tau_shear, self.coarse_level.tau_bulk,
                                    self.coarse_level.dt, self.plan.span, (ctypes.c_int32 * 3)(*box.lower),
-                                   (ctypes.c_int32 * 3)(*box.upper))
+                                   (ctypes.c_int32 * 3)(*box.upper), _native.STORAGE[self.fine_storage])
         handle = ctypes.c_void_p()
         check(self._lib.ak_refined_create(ctypes.byref(desc), ctypes.byref(handle)))
         self._handle = handle
@@ -284,8 +293,21 @@ class RefinedSolver:
         return post_collision_columns(self.plan)
 
     def states(self):
-        """Coarse populations (covered cells virtual; post-collision where
-        coarse_post_collision() is set) and the physical fine block, (x, y, z, 27)."""
+        """Pre-collision populations of the coarse lattice (covered cells
+        virtual) and of the physical fine block, (x, y, z, 27) each, as the
+        reference's states() returns them (interface.py:354-358).  Where the
+        engine holds the coarse level post-collision (coarse_post_collision())
+        the pre-collision state is rebuilt from the copy the last step read."""
+        nx, ny, nz = self.plan.shape
+        coarse = np.empty((nx, ny, nz, 27))
+        fx, fy, fz = self.fine_shape
+        padded = np.empty((fx + 2 * self.pad, fy + 2 * self.pad, fz, 27))
+        check(self._lib.ak_refined_states(self._handle, _ptr(coarse), _ptr(padded)))
+        return coarse, padded[self.pad:-self.pad, self.pad:-self.pad]
+
+    def held_states(self):
+        """The populations as the engine holds them (post-collision in the
+        coarse_post_collision() columns), the representation checkpoints store."""
         nx, ny, nz = self.plan.shape
         coarse = np.empty((nx, ny, nz, 27))
         check(self._lib.ak_get_pdf(self._coarse, _ptr(coarse)))
@@ -456,7 +478,8 @@ class RefinedSolver:
                         "coefficient_convention": "Cl up; Cd downstream; Cm nose-up about the chosen reference; area=c*periodic_span",
                         "force_time": "average of both fine momentum-transfer intervals; timestamp at coarse interval midpoint",
                         "experimental_validation": "not_performed", "resume_supported": True,
-                        "storage": self.storage, "reference_chord_input_units": self.section.chord,
+                        "storage": self.storage, "fine_storage": self.fine_storage,
+                        "reference_chord_input_units": self.section.chord,
                         "moment_reference_input_units": self.section.moment_reference}
             write_json(output / "project.json", refined_project_dict(self.project, self.refinement))
             with history.open("w", newline="", encoding="utf-8") as handle:

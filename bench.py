@@ -7,7 +7,7 @@ x in [-0.5c, 2c], y in [-0.6c, 0.6c] around the section: 160 x 76 x 16 fine
 cells.  Legacy outer boundary (the reference's refined solver accepts no
 other), FP64 (the reference's dtype).  MLUPS counts coarse cells + 2 x fine
 cells per coarse step, as the reference does for two-level runs.  Inputs are
-larger than L2 (2 x 686 MB of coarse populations).
+larger than L2 (2 x 340 MB of coarse populations).
 
 Also reported: the reduced-precision forms (FP32 arithmetic with FP32 or FP16
 shifted storage) of the same case, and the uniform 384 x 256 x 8 case with the
@@ -42,6 +42,16 @@ WORKLOAD = ("two-level NACA0012, coarse 512x384x8 (chord 32) + fine 160x76x16 (c
             "x in [-0.5c, 2c], y in [-0.6c, 0.6c], AoA 8, Re 3e4, Ma 0.1, legacy farfield")
 UNIFORM = "uniform NACA0012 384x256x8, chord 32, AoA 4, Re 3e4, Ma 0.1, characteristic farfield"
 BYTES_PER_CELL = {"f64": 27 * 2 * 8, "f32": 27 * 2 * 4, "f16": 27 * 2 * 2, "df64": 27 * 2 * 8}
+# coarse steps after which the reduced forms' coefficients are compared with
+# the FP64 form's (the start-up transient is over by then at chord 32)
+FORM_ERROR_STEPS = 2000
+# coarse steps of the end-to-end solve (set-up from the host description
+# included; the benchmark case itself is a 10000-step run)
+E2E_STEPS = 1000
+# DRAM bytes (read + write) per launch of the coarse k_stream_collide<double>
+# of the two-level case, from the ncu capture summarised in
+# profiles/collide_f64_refined_512x384x8.txt (same kernel and workload)
+TRAFFIC_BYTES_PER_LAUNCH = None
 
 
 def case_parts(farfield="characteristic_transport_v1", sgs="none"):
@@ -67,6 +77,22 @@ def refined_parts():
 def refined_cells(plan):
     fine = math.prod(2 * n for n in plan.box.shape)
     return math.prod(plan.shape) + 2 * fine
+
+
+def fma_peak(lib, precision):
+    """Measured FMA throughput of the device, TFLOP/s (0 FP64, 1 FP32)."""
+    from aerokinetic_gb300 import _native
+    out = ctypes.c_double()
+    _native.check(lib.ak_fma_peak(precision, ctypes.byref(out)))
+    return out.value
+
+
+def collision_flops(lib, storage):
+    """Algorithmic FLOPs of one cell's collision in the storage form's arithmetic."""
+    from aerokinetic_gb300 import _native
+    counts = np.zeros(4)
+    _native.check(lib.ak_collision_flops(_native.STORAGE[storage], counts.ctypes.data_as(ctypes.c_void_p)))
+    return float(counts[3])
 
 
 def peaks():
@@ -169,11 +195,13 @@ def oracle_refined(threads):
 
 
 def oracle_run(case, steps, budget_s):
-    """Up to `steps` oracle steps, stopping after budget_s."""
+    """Up to `steps` oracle steps, stopping after budget_s; a two-level step
+    closes its mass and momentum budget as the reference's step does."""
+    step = getattr(case, "step_with_budget", case.step)
     done, start = 0, time.perf_counter()
     while done < steps:
         done += 1
-        case.step()
+        step()
         if time.perf_counter() - start >= budget_s:
             break
     return done, time.perf_counter() - start
@@ -188,8 +216,8 @@ def oracle_sample(budget_s=15.0, refined=True):
     steps, elapsed = oracle_run(case, 10**9, budget_s)
     what = "two-level" if refined else "uniform"
     return {"value": cells * steps / elapsed / 1e6, "unit": "MLUPS", "cores": cores, "kind": "port",
-            "sample": f"{steps} steps of the same {what} case on {cores} host threads (FP64 oracle), "
-                      f"{elapsed:.1f} s"}
+            "sample": f"{steps} steps of the same {what} case (budget closed every step) on {cores} host threads "
+                      f"(FP64 oracle), {elapsed:.1f} s"}
 
 
 def run_reference(args, rank, world):
@@ -200,13 +228,14 @@ def run_reference(args, rank, world):
     oracle_run(case, args.warmup, 30.0)
     steps, elapsed = oracle_run(case, args.steps, 120.0)
     value = cells * steps / elapsed / 1e6
-    sample = (f"{steps} of {args.steps} requested coarse steps of the two-level case on {cores} host threads "
-              f"(FP64 oracle), {elapsed:.1f} s, capped at 120 s")
+    sample = (f"{steps} of {args.steps} requested coarse steps of the two-level case, each closing its mass and "
+              f"momentum budget, on {cores} host threads (FP64 oracle), {elapsed:.1f} s, capped at 120 s")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "MLUPS", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "engine": "CPU oracle (restatement of the reference step)",
+                       "step": "loads and the mass/momentum budget every coarse step (the reference's step)",
                        "l2": "host run"},
             "cpu_baseline": {"value": value, "unit": "MLUPS", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -238,7 +267,8 @@ def flush_l2(buf, stream):
         buf.add_(1)
 
 
-def measure_form(storage, steps, warmup, flush, farfield="characteristic_transport_v1", sgs="none"):
+def measure_form(storage, steps, warmup, flush, farfield="characteristic_transport_v1", sgs="none",
+                 measure_static=False):
     """Per-step timing of the uniform case's stream-collide kernel in one storage form."""
     import torch
     from aerokinetic_gb300.solver import Solver
@@ -276,9 +306,21 @@ def measure_form(storage, steps, warmup, flush, farfield="characteristic_transpo
             raise RuntimeError(lib.ak_last_error())
         graph += start.elapsed_time(end)
     info = solver.info
+    out = {"cells": info["cells"], "fluid_cells": info["fluid_cells"], "bulk_ms": bulk / steps,
+           "eager_step_ms": total / steps, "step_ms": graph / steps, "outer_ms": outer / steps}
+    if measure_static:
+        # a sampled step through ak_step (graph replay, lazily allocated
+        # partial sums) and through ak_step_loads_static (eager, static scratch)
+        loads = np.zeros((len(solver.contours), 5))
+        ptr = loads.ctypes.data_as(ctypes.c_void_p)
+        handle = lib.ak_case_stream(solver._case)
+        k = max(5, min(steps, 20))
+        out["sampled_step_ms"] = sum(stream_ms(lib, handle, lambda: lib.ak_step(solver._case, 1, ptr))
+                                     for _ in range(k)) / k
+        out["static_loads_step_ms"] = sum(
+            stream_ms(lib, handle, lambda: lib.ak_step_loads_static(solver._case, 1, ptr)) for _ in range(k)) / k
     solver.close()
-    return {"cells": info["cells"], "fluid_cells": info["fluid_cells"], "bulk_ms": bulk / steps,
-            "eager_step_ms": total / steps, "step_ms": graph / steps, "outer_ms": outer / steps}
+    return out
 
 
 def batch_case_parts(i, base_seed=2026):
@@ -309,16 +351,27 @@ def stream_ms(lib, stream_handle, fn):
     return float(a.elapsed_time(b))
 
 
-def form_errors(project, refinement, steps=400):
-    """The two-level case's FP32 and FP16 storage forms against the FP64 form
-    after the same number of coarse steps from the same initial state: Cl, Cd,
-    Cm (relative, floor 0.05), mean density over the owned cells and the
-    velocity field's relative L2 over both levels."""
+# the reduced forms of the two-level case compared with the FP64 form:
+# (label, coarse storage, fine storage)
+REFINED_FORMS = (("df64", "df64", "df64"), ("f32", "f32", "f32"), ("f16", "f16", "f32"), ("f16_all", "f16", "f16"))
+
+
+def form_errors(project, refinement, steps=2000, every=10, early=400):
+    """The two-level case's reduced forms against the FP64 form from the same
+    initial state: Cl, Cd, Cm sampled every `every` coarse steps; errors
+    relative to the FP64 value (floor 0.05) at step `early` (before the wake
+    turns unsteady), at the last step, and of the means over the second half
+    (the unsteady phase, where single samples diverge chaotically); mean
+    density over the owned cells and the velocity field's relative L2 over
+    both levels at the last step."""
     from aerokinetic_gb300.refined import RefinedSolver
     runs = {}
-    for storage in ("f64", "df64", "f32", "f16"):
-        solver = RefinedSolver(project, refinement, storage=storage)
-        record = solver.advance(steps)
+    for label, storage, fine in (("f64", "f64", "f64"),) + REFINED_FORMS:
+        solver = RefinedSolver(project, refinement, storage=storage, fine_storage=fine, budget=False)
+        series = []
+        for _ in range(steps // every):
+            rec = solver.advance(every)
+            series.append([rec["cl"], rec["cd"], rec["cm"]])
         integrals = solver.conserved_integrals()
         volume = (solver.coarse_owned_cells * solver.coarse_level.dx ** 3
                   + solver.fine_fluid_cells * solver.fine_level.dx ** 3)
@@ -327,18 +380,76 @@ def form_errors(project, refinement, steps=400):
         owned = np.ones(rc.shape, bool)
         owned[box.lower[0]:box.upper[0], box.lower[1]:box.upper[1]] = False
         fluid = np.broadcast_to(~solver._fine_solid_xy()[:, :, None], rf.shape)
-        runs[storage] = (record, integrals["mass"] / volume, uc[owned], uf[fluid])
+        runs[label] = (np.array(series), integrals["mass"] / volume, uc[owned], uf[fluid])
         solver.close()
     ref = runs["f64"]
-    out = {"coarse_steps": steps}
-    for storage in ("df64", "f32", "f16"):
-        rec, mean_rho, uc, uf = runs[storage]
+    half = len(ref[0]) // 2
+    k_early = early // every - 1
+
+    def rel(a, b):
+        return {k: float(abs(a[i] - b[i]) / max(abs(b[i]), 0.05)) for i, k in enumerate(("cl", "cd", "cm"))}
+    out = {"coarse_steps": steps, "sample_every": every, "early_step": early,
+           "mean_window": [int((half + 1) * every), steps], "error_floor": 0.05}
+    for label, storage, fine in REFINED_FORMS:
+        series, mean_rho, uc, uf = runs[label]
         du = np.sum((uc - ref[2]) ** 2) + np.sum((uf - ref[3]) ** 2)
         norm = np.sum(ref[2] ** 2) + np.sum(ref[3] ** 2)
-        out[storage] = {**{k: abs(rec[k] - ref[0][k]) / max(abs(ref[0][k]), 0.05) for k in ("cl", "cd", "cm")},
-                        "mean_rho_abs": abs(mean_rho - ref[1]), "u_l2_rel": float(np.sqrt(du / norm))}
-    out["f64_values"] = {"cl": ref[0]["cl"], "cd": ref[0]["cd"], "cm": ref[0]["cm"], "mean_rho": ref[1]}
+        window = rel(series[half:].mean(axis=0), ref[0][half:].mean(axis=0))
+        out[label] = {"coarse_storage": storage, "fine_storage": fine,
+                      "at_early_step": rel(series[k_early], ref[0][k_early]), "at_last_step": rel(series[-1], ref[0][-1]),
+                      "window_mean": window, "max_window_mean": max(window.values()),
+                      "mean_rho_abs": abs(mean_rho - ref[1]), "u_l2_rel": float(np.sqrt(du / norm))}
+    out["f64_values"] = {"cl": ref[0][-1][0], "cd": ref[0][-1][1], "cm": ref[0][-1][2], "mean_rho": ref[1],
+                         "window_mean": dict(zip(("cl", "cd", "cm"), ref[0][half:].mean(axis=0).tolist()))}
     return out
+
+
+def coefficient_series(solver, steps, every):
+    """Cl, Cd, Cm of a uniform case every `every` steps."""
+    out = []
+    for _ in range(steps // every):
+        rec = solver.advance(every, sample_last=True)
+        out.append([rec["cl"], rec["cd"], rec["cm"]])
+    return np.array(out)
+
+
+def series_errors(low, ref, floor=0.05):
+    """Relative errors (floor) of the last sample and of the second half's mean."""
+    half = len(ref) // 2
+    names = ("cl", "cd", "cm")
+    last = {k: float(abs(low[-1][i] - ref[-1][i]) / max(abs(ref[-1][i]), floor)) for i, k in enumerate(names)}
+    lm, rm = low[half:].mean(axis=0), ref[half:].mean(axis=0)
+    window = {k: float(abs(lm[i] - rm[i]) / max(abs(rm[i]), floor)) for i, k in enumerate(names)}
+    return last, window
+
+
+def batch_errors(parts, storage="f16", steps=2000, every=20, per_chord=2):
+    """Cl/Cd/Cm of the batch's reduced form against the plain FP64 form on
+    `per_chord` cases of each chord: every case's bits in a batch equal the
+    same case stepped alone (tests/test_batch.py), so each is stepped alone
+    here in both forms."""
+    from aerokinetic_gb300.solver import Solver
+    chosen, seen = [], {}
+    for i, p in enumerate(parts):
+        chord = p[2].cells_per_chord
+        if seen.get(chord, 0) < per_chord:
+            seen[chord] = seen.get(chord, 0) + 1
+            chosen.append(i)
+    worst_last, worst_window, cases = {}, {}, []
+    for i in chosen:
+        series = {}
+        for form in (storage, "f64"):
+            solver = Solver(*parts[i], storage=form)
+            series[form] = coefficient_series(solver, steps, every)
+            solver.close()
+        last, window = series_errors(series[storage], series["f64"])
+        cases.append({"case": i, "chord": parts[i][2].cells_per_chord, "alpha_deg": parts[i][1].alpha_deg,
+                      "at_last_step": last, "window_mean": window})
+        for k in last:
+            worst_last[k] = max(worst_last.get(k, 0.0), last[k])
+            worst_window[k] = max(worst_window.get(k, 0.0), window[k])
+    return {"form": storage, "steps": steps, "sample_every": every, "error_floor": 0.05,
+            "max_at_last_step": worst_last, "max_window_mean": worst_window, "cases": cases}
 
 
 def run_batch(steps, n_cases=64, solve_steps=5000):
@@ -391,6 +502,8 @@ def run_batch(steps, n_cases=64, solve_steps=5000):
     out["plain_sequential"] = {"solves_per_hour": n_cases / total_s * 3600, "form": "f64, one case at a time",
                                "ms_per_step_by_chord": {str(c): v[0] for c, v in sorted(per_chord.items())}}
     out["speedup_f16_vs_plain"] = out["f16"]["solves_per_hour"] / out["plain_sequential"]["solves_per_hour"]
+    out["speedup_f32_vs_plain"] = out["f32"]["solves_per_hour"] / out["plain_sequential"]["solves_per_hour"]
+    out["error_vs_f64"] = {form: batch_errors(parts, form) for form in ("f16", "f32")}
     return out
 
 
@@ -411,9 +524,10 @@ def large_parts():
                                                             transverse_chords=1.5)
 
 
-def run_large(steps=8):
+def run_large(steps=8, error_steps=100):
     """The large two-element two-level case in the plain FP64 form and the FP16
-    storage form: graph-replayed coarse steps timed by CUDA events."""
+    storage form: graph-replayed coarse steps timed by CUDA events; the FP16
+    form's Cl, Cd, Cm against the FP64 form's after error_steps coarse steps."""
     import torch
     from aerokinetic_gb300 import _native
     from aerokinetic_gb300.refined import RefinedSolver
@@ -421,6 +535,7 @@ def run_large(steps=8):
     out = {"workload": "two-element NACA0012 + 0.3c flap at 20 deg, chord 64/128, Re 1e5, AoA 6, span 32, "
                        "legacy farfield"}
     lib = _native.load()
+    coefficients = {}
     for storage in ("f64", "f16"):
         t0 = time.perf_counter()
         solver = RefinedSolver(project, refinement, storage=storage, budget=False)
@@ -437,15 +552,24 @@ def run_large(steps=8):
         _native.check(lib.ak_refined_step_timed(solver._handle, 2, groups.ctypes.data_as(ctypes.c_void_p)))
         # the coarse streaming fused with the collision plus the fine collisions
         collide_ms = (groups[2] + groups[3]) / 2
-        collide_bytes = (math.prod(solver.plan.shape) + 2 * fine_padded) * BYTES_PER_CELL[storage]
+        collide_bytes = (math.prod(solver.plan.shape) * BYTES_PER_CELL[storage]
+                         + 2 * fine_padded * BYTES_PER_CELL[solver.fine_storage])
         out.setdefault("coarse_shape", list(solver.plan.shape))
         out.setdefault("fine_shape", list(solver.fine_shape))
         out.setdefault("cell_updates_per_step", cells)
         out[storage] = {"mlups": cells * steps / (ms / 1e3) / 1e6, "ms_per_step": ms / steps,
                         "collide_achieved_gbs": collide_bytes / (collide_ms / 1e3) / 1e9,
-                        "setup_s": setup_s, "device_gib": solver.plan.estimated_memory_gib, "steps": steps}
+                        "setup_s": setup_s, "device_gib": solver.plan.estimated_memory_gib, "steps": steps,
+                        "fine_storage": solver.fine_storage}
+        done = lib.ak_refined_steps_done(solver._handle)
+        rec = solver.advance(error_steps - done) if error_steps > done else None
+        coefficients[storage] = rec
         solver.close()
         torch.cuda.synchronize()
+    ref, low = coefficients["f64"], coefficients["f16"]
+    if ref is not None and low is not None:
+        out["f16_error_vs_f64"] = {"coarse_steps": error_steps, "error_floor": 0.05,
+                                   **{k: abs(low[k] - ref[k]) / max(abs(ref[k]), 0.05) for k in ("cl", "cd", "cm")}}
     return out
 
 
@@ -498,9 +622,11 @@ def run_engine(args, rank, world, local_rank):
     lib = _native.load()
     project, refinement = refined_parts()
 
-    # ---- headline: the two-level case in FP64, K coarse steps in the timed region
-    # the step alone: the per-step mass/momentum budget (a diagnostic) is off
-    solver = RefinedSolver(project, refinement, storage="f64", budget=False)
+    # ---- headline: the two-level case in FP64, K coarse steps in the timed
+    # region, each the reference's whole step: the walls' loads, and the mass
+    # and momentum budget (outer-face flux, integrals of the state the step
+    # leaves) computed every step (refined_solver.py:311-343)
+    solver = RefinedSolver(project, refinement, storage="f64", budget=True)
     # timing group 2 is the coarse streaming fused with the collision
     assert solver.coarse_post_collision().any(), "the fine box must lie three coarse cells inside"
     plan = solver.plan
@@ -511,10 +637,13 @@ def run_engine(args, rank, world, local_rank):
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    # the timed region replays the captured step (ak_refined_step), timed by
-    # CUDA events on the case's stream
+    # the timed region replays the captured budget step (ak_refined_step_budget),
+    # timed by CUDA events on the case's stream
     stream = torch.cuda.ExternalStream(lib.ak_case_stream(solver._coarse))
-    _native.check(lib.ak_refined_step(solver._handle, max(3, args.warmup), None))
+    loads, outer, stats = np.zeros((len(solver.contours), 5)), np.zeros(8), np.zeros(16)
+    budget_args = [loads.ctypes.data_as(ctypes.c_void_p), outer.ctypes.data_as(ctypes.c_void_p),
+                   stats.ctypes.data_as(ctypes.c_void_p)]
+    _native.check(lib.ak_refined_step_budget(solver._handle, max(3, args.warmup), *budget_args))
     launches0 = lib.ak_kernel_launches(solver._coarse)
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local_rank) as clocks:
@@ -522,7 +651,7 @@ def run_engine(args, rank, world, local_rank):
         if dist:
             dist.barrier()
         start.record(stream)
-        _native.check(lib.ak_refined_step(solver._handle, args.steps, None))
+        _native.check(lib.ak_refined_step_budget(solver._handle, args.steps, *budget_args))
         end.record(stream)
         torch.cuda.synchronize()
         if dist:
@@ -543,20 +672,39 @@ def run_engine(args, rank, world, local_rank):
     fine_padded = math.prod(n for n in (2 * plan.box.shape[0] + 4, 2 * plan.box.shape[1] + 4, 2 * plan.box.shape[2]))
     coarse_cells = math.prod(plan.shape)
     solver.close()
+    # the same step without the budget (loads only), for the budget's cost
+    bare = RefinedSolver(project, refinement, storage="f64", budget=False)
+    _native.check(lib.ak_refined_step(bare._handle, max(3, args.warmup), None))
+    bare_ms = stream_ms(lib, lib.ak_case_stream(bare._coarse),
+                        lambda: _native.check(lib.ak_refined_step(bare._handle, max(args.steps, 20), None)))
+    bare_ms /= max(args.steps, 20)
+    bare.close()
     if rank != 0:
         return
     hbm, peak_kind = peaks()
-    # the collision launches of one coarse step, each population read and
-    # written once: the coarse streaming fused with the collision (outside the
-    # transfer block, which is streamed only and collided in its own small
-    # launch) and the two fine collisions
+    # the dominant kernel: the coarse k_stream_collide<double>, the coarse
+    # streaming fused with the next collision (every coarse cell read and
+    # written once; the transfer block's cells streamed only).  It is bound by
+    # GB300's FP64 pipe: its roofline is the measured FP64 FMA throughput,
+    # against the collision's algorithmic FLOPs per cell
+    fp64_peak = fma_peak(lib, 0)
+    fp32_peak = fma_peak(lib, 1)
+    flops_cell = collision_flops(lib, "f64")
+    xfer_cells = (plan.box.shape[0] + 6) * (plan.box.shape[1] + 6) * plan.shape[2]
+    kernel_ms = groups["coarse_stream_collide_ms"]
+    kernel_flops = (coarse_cells - xfer_cells) * flops_cell
+    kernel_bytes = coarse_cells * BYTES_PER_CELL["f64"]
+    achieved_tflops = kernel_flops / (kernel_ms / 1e3) / 1e12
+    achieved_gbs = kernel_bytes / (kernel_ms / 1e3) / 1e9
+    # the same for the collision launches of one coarse step (the fused coarse
+    # pass and the two fine collisions)
     collide_bytes = (coarse_cells + 2 * fine_padded) * BYTES_PER_CELL["f64"]
     collide_ms = groups["coarse_stream_collide_ms"] + groups["fine_collide_ms"]
     achieved = collide_bytes / (collide_ms / 1e3) / 1e9
 
     # ---- end to end through the public API: case set-up from the host
     # description, every coarse step returning its loads to the host
-    e2e_steps = max(32, min(args.steps, 500))
+    e2e_steps = E2E_STEPS
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     s = RefinedSolver(project, refinement, storage="f64")
@@ -569,8 +717,8 @@ def run_engine(args, rank, world, local_rank):
 
     # ---- reduced-precision forms of the two-level case
     forms = {}
-    for storage in ("df64", "f32", "f16"):
-        r = RefinedSolver(project, refinement, storage=storage, budget=False)
+    for label, storage, fine in REFINED_FORMS:
+        r = RefinedSolver(project, refinement, storage=storage, fine_storage=fine, budget=False)
         fst = torch.cuda.ExternalStream(lib.ak_case_stream(r._coarse))
         _native.check(lib.ak_refined_step(r._handle, max(3, args.warmup), None))
         k = min(args.steps, 400)
@@ -583,9 +731,10 @@ def run_engine(args, rank, world, local_rank):
         m = np.zeros(6)
         _native.check(lib.ak_refined_step_timed(r._handle, k, m.ctypes.data_as(ctypes.c_void_p)))
         r.close()
-        cb = (coarse_cells + 2 * fine_padded) * BYTES_PER_CELL[storage]
+        cb = coarse_cells * BYTES_PER_CELL[storage] + 2 * fine_padded * BYTES_PER_CELL[fine]
         cms = (m[2] + m[3]) / k
-        forms[storage] = {"mlups": cells / (step_ms / 1e3) / 1e6, "ms_per_step": step_ms,
+        forms[label] = {"coarse_storage": storage, "fine_storage": fine,
+                          "mlups": cells / (step_ms / 1e3) / 1e6, "ms_per_step": step_ms,
                           "collide_achieved_gbs": cb / (cms / 1e3) / 1e9,
                           "collide_frac_of_" + peak_kind: cb / (cms / 1e3) / 1e9 / hbm,
                           "groups_ms": {"coarse_transfer_block_collide": m[1] / k, "coarse_stream_collide": m[2] / k,
@@ -595,12 +744,16 @@ def run_engine(args, rank, world, local_rank):
     # ---- the uniform case (the reference's CPU-runnable configuration)
     uniform = {}
     for storage in ("f64", "df64", "f32", "f16"):
-        m = measure_form(storage, steps=min(args.steps, 100), warmup=args.warmup, flush=True)
+        m = measure_form(storage, steps=min(args.steps, 100), warmup=args.warmup, flush=True,
+                         measure_static=storage == "f64")
         bytes_launch = m["fluid_cells"] * BYTES_PER_CELL[storage]
         a = bytes_launch / (m["bulk_ms"] / 1e3) / 1e9
         uniform[storage] = {"mlups": m["cells"] / (m["step_ms"] / 1e3) / 1e6, "eager_step_ms": m["eager_step_ms"],
                             "kernel_mlups": m["cells"] / (m["bulk_ms"] / 1e3) / 1e6,
                             "stream_collide_ms": m["bulk_ms"], "achieved_gbs": a, "frac_of_" + peak_kind: a / hbm}
+        if storage == "f64":
+            uniform["f64"].update(sampled_step_ms=m["sampled_step_ms"],
+                                  static_loads_step_ms=m["static_loads_step_ms"])
     # the same case with the other outer boundaries and with the Smagorinsky
     # subgrid rate (FP64 and the FP32 form)
     for label, farfield, sgs in (("exterior", "exterior_regularized_fd_v1", "none"),
@@ -616,17 +769,11 @@ def run_engine(args, rank, world, local_rank):
                                              "stream_collide_ms": m["bulk_ms"], "outer_boundary_ms": m["outer_ms"],
                                              "achieved_gbs": a, "frac_of_" + peak_kind: a / hbm}
 
-    forms["error_vs_f64"] = form_errors(project, refinement, steps=min(args.steps, 400))
+    forms["error_vs_f64"] = form_errors(project, refinement, steps=FORM_ERROR_STEPS)
     batch = run_batch(steps=min(args.steps, 100))
     serving = run_serving()
     large = run_large()
 
-    traffic = None
-    summary = ROOT / "profiles" / "collide_f64_refined_512x384x8.txt"
-    if summary.exists():
-        for line in summary.read_text().splitlines():
-            if line.startswith("dram_bytes_per_launch:"):
-                traffic = float(line.split(":", 1)[1].split()[0])
     cpu = oracle_sample(budget_s=15.0, refined=True)
     line = {"metric": METRIC, "value": value, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
@@ -634,15 +781,25 @@ def run_engine(args, rank, world, local_rank):
             "config": {"workload": WORKLOAD, "coarse_cells": coarse_cells,
                        "fine_cells": math.prod(2 * n for n in plan.box.shape),
                        "cell_updates_per_step": cells, "storage": "f64 populations, two copies per level",
-                       "l2": "inputs larger than L2 (coarse 2 x 686 MB); uniform forms flushed between steps",
+                       "step": "loads and the mass/momentum budget every coarse step (the reference's step)",
+                       "l2": "inputs larger than L2 (coarse 2 x 340 MB); uniform forms flushed between steps",
                        "parallelism": f"replicas x{world}"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": "coarse k_stream_collide<double> (streaming fused with the collision) + two "
-                                   "fine k_collide<double> per coarse step",
-                         "bytes_per_launch": collide_bytes / 3, "kernel_ms": collide_ms / 3,
-                         "limit": "FP64 pipe (GB300 issues 2 FP64 instructions per clock per SM)"},
+            "roofline": {"bound": "fp64", "achieved": achieved_tflops, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": achieved_tflops / fp64_peak, "traffic": TRAFFIC_BYTES_PER_LAUNCH,
+                         "peak_source": "measured in this run (ak_fma_peak: FP64 FMA chains, 2 FLOPs per FMA)",
+                         "kernel": "coarse k_stream_collide<double> (streaming fused with the collision)",
+                         "flops_per_cell": flops_cell, "cells_collided_per_launch": coarse_cells - xfer_cells,
+                         "kernel_ms": kernel_ms, "bytes_per_launch": kernel_bytes,
+                         "hbm": {"achieved": achieved_gbs, "peak": hbm, "unit": "GB/s", "frac": achieved_gbs / hbm,
+                                 "peak_source": peak_kind},
+                         "collision_launches_per_step": {"bytes": collide_bytes, "ms": collide_ms,
+                                                         "achieved_gbs": achieved, "frac_of_hbm": achieved / hbm},
+                         "fp32_fma_peak_tflops": fp32_peak},
             "groups_ms": groups,
+            "budget": {"step_ms_with_budget": elapsed_ms / args.steps, "step_ms_without_budget": bare_ms,
+                       "cost_fraction": (elapsed_ms / args.steps) / bare_ms - 1.0,
+                       "includes": "outer-face flux and the integrals of the state each step leaves, every step; "
+                                   "the coarse integrals from the fused stream-collide pass"},
             "forms": forms,
             "uniform": {"workload": UNIFORM, **uniform},
             "cpu_baseline": cpu,

@@ -215,6 +215,8 @@ typedef struct {
     double dt_coarse;            /* coarse time step in convective units */
     double span;                 /* periodic span in chord units */
     int32_t box_lower[3], box_upper[3];  /* fine box in coarse cells; z spans the whole span */
+    int32_t fine_storage;        /* AK_STORAGE_* of the fine level (the walls' level): -1 = the coarse
+                                    level's; AK_STORAGE_F32 under an AK_STORAGE_F16 coarse level */
 } ak_refined_desc;
 
 /* RefinedSolver construction (refined_solver.py:116-162). */
@@ -234,8 +236,10 @@ int ak_refined_step(ak_refined *r, int32_t nsteps, double *loads);
 /* ak_refined_step that also returns, with one synchronisation, what the
  * budget of the last step needs (refined_solver.py:329-339): outer[8] as
  * ak_refined_outer_flux, stats[16] as ak_refined_integrals of the state the
- * step leaves (computed inside the step).  Needs ak_refined_track_budget on;
- * outer or stats may be NULL. */
+ * step leaves.  With stats every step computes these integrals, as the
+ * reference's step does; in the FP64-arithmetic forms the coarse level's
+ * come out of the fused stream-collide pass itself.  Needs
+ * ak_refined_track_budget on; outer or stats may be NULL. */
 int ak_refined_step_budget(ak_refined *r, int32_t nsteps, double *loads, double *outer, double *stats);
 int64_t ak_refined_steps_done(const ak_refined *r);
 /* With enable != 0, every following step also measures the inflow through
@@ -272,6 +276,15 @@ int ak_refined_integrals(ak_refined *r, double *out);
  * the transfer block (the box and three cells around it) alone and ms[2] the
  * fused pass.  No counterpart in the reference; it exists for measurement. */
 int ak_refined_step_timed(ak_refined *r, int32_t nsteps, double *ms);
+/* RefinedSolver.states() (interface.py:354-358): the pre-collision
+ * populations of both levels, coarse (nx, ny, nz, 27) and the padded fine
+ * block (2 bx + 4, 2 by + 4, 2 bz, 27), either output may be NULL.  Where the
+ * engine keeps the coarse level post-collision (the streaming fused with the
+ * next collision outside the box and three cells around it) the
+ * pre-collision state is rebuilt by pulling from the copy the last step read;
+ * after ak_set_pdf on the coarse level it is known again after the next
+ * step (AK_ERR_INVALID until then). */
+int ak_refined_states(ak_refined *r, double *coarse, double *fine);
 /* One interface kernel of the two-level step, run alone on the levels'
  * current population copies, so that each can be compared with the
  * reference's transfer algebra in isolation:

@@ -133,3 +133,16 @@ def test_post_collision_columns_follow_the_transfer_block(golden):
     assert mask.sum() == mask.size - (hi[0] - lo[0] + 6) * (hi[1] - lo[1] + 6)
     edge = SimpleNamespace(shape=plan.shape, box=SimpleNamespace(lower=(2, lo[1], lo[2]), upper=hi))
     assert not post_collision_columns(edge).any()
+
+
+def test_refined_fine_storage_choices_are_validated_before_any_device_work():
+    """storage='f16' keeps the walls' fine level in FP32 unless told
+    otherwise; any other mixture is refused up front."""
+    import pytest
+    from aerokinetic_gb300.refined import RefinedSolver
+    from aerokinetic_gb300.refined_plan import RefinementSettings
+    from aerokinetic_gb300 import Flow, Grid, Project, Section, naca0012
+    project = Project(Section((naca0012(41),)), Flow(), Grid(cells_per_chord=16, memory_limit_gib=1))
+    for storage, fine in (("f32", "f16"), ("f64", "f32"), ("f16", "f64")):
+        with pytest.raises(ValueError, match="fine_storage"):
+            RefinedSolver(project, RefinementSettings(), storage=storage, fine_storage=fine)

@@ -215,8 +215,9 @@ def test_failure_capture_guard_and_loads(golden):
 
 
 def test_full_size_uniform_case_matches_oracle(golden):
-    """384x256x8 characteristic-farfield case at lattice Mach 0.1 (the bench workload)."""
-    compare_run(geometry_project(golden["geometry"]["uniform_c1"]), steps=12, sample_every=4)
+    """384x256x8 characteristic-farfield case at lattice Mach 0.1 (the uniform
+    bench workload) over 64 steps, loads every 8."""
+    compare_run(geometry_project(golden["geometry"]["uniform_c1"]), steps=64, sample_every=8)
 
 
 def test_non_finite_state_is_reported(golden):
@@ -233,7 +234,7 @@ def test_non_finite_state_is_reported(golden):
         solver.close()
 
 
-@pytest.mark.parametrize("storage,inst_tol,mean_tol", [("f32", 5e-4, 5e-4), ("f16", 1e-2, 5e-3)])
+@pytest.mark.parametrize("storage,inst_tol,mean_tol", [("f32", 5e-4, 5e-4), ("f16", 5e-3, 5e-3)])
 def test_precision_forms_track_fp64(storage, inst_tol, mean_tol):
     """FP32 arithmetic with FP32 / FP16 shifted storage against the FP64 form on
     the impulsive start (steps 20..200, every 20): the largest instantaneous
@@ -284,29 +285,69 @@ def test_refined_levels_match_oracle(golden, storage):
     the plain form and the df64 form, at the plain form's tolerances."""
     solver, oracle = refined_pair(golden["histories"]["refined_startup"], storage=storage)
     try:
-        pad = oracle.pad
-        post = solver.coarse_post_collision()
-        assert post.any() and not post.all()
+        compare_refined(solver, oracle, steps=3)
+    finally:
+        solver.close()
 
-        def coarse_expected():
-            # outside the transfer block the engine's coarse level holds the
-            # oracle's state collided once more
-            ref = oracle.coarse.interior().copy()
-            ref[post] = O.collide(ref[post], oracle.coarse.omega_s, oracle.coarse.omega_b)
-            return ref
 
+def compare_refined(solver, oracle, steps, pdf_tol=2e-12, load_tol=2e-10):
+    """states() (the pre-collision populations of both levels, the reference's
+    contract) against the oracle's state on every coarse cell and every fine
+    fluid cell after each coarse step, the loads of each step, and the held
+    representation (post-collision in the fused columns) against the oracle's
+    state collided once more."""
+    post = solver.coarse_post_collision()
+    assert post.any() and not post.all()
+    fluid = (oracle.fine.flags[1:-1, 1:-1, 1:-1] == 0)[oracle.fine_slices]
+    coarse, fine = solver.states()
+    np.testing.assert_allclose(coarse, oracle.coarse.interior(), rtol=0, atol=1e-14)
+    np.testing.assert_allclose(fine, oracle.fine.interior()[oracle.fine_slices], rtol=0, atol=1e-14)
+    for s in range(1, steps + 1):
+        mine, theirs = solver.step(), oracle.step()
+        for k in ("cl", "cd", "cm"):
+            assert mine[k] == pytest.approx(theirs[k], abs=load_tol), (s, k)
         coarse, fine = solver.states()
-        np.testing.assert_allclose(coarse, coarse_expected(), rtol=0, atol=1e-14)
-        np.testing.assert_allclose(fine, oracle.fine.interior()[oracle.fine_slices], rtol=0, atol=1e-14)
-        for s in range(1, 4):
-            mine, theirs = solver.step(), oracle.step()
-            for k in ("cl", "cd", "cm"):
-                assert mine[k] == pytest.approx(theirs[k], abs=2e-10), (s, k)
-            coarse, fine = solver.states()
-            assert np.abs(coarse - coarse_expected()).max() <= 2e-12 * s
-            # solid cells hold no state the fluid reads (the engine leaves them unstreamed)
-            fluid = (oracle.fine.flags[1:-1, 1:-1, 1:-1] == 0)[oracle.fine_slices]
-            assert np.abs(fine - oracle.fine.interior()[oracle.fine_slices])[fluid].max() <= 2e-12 * s
+        assert np.abs(coarse - oracle.coarse.interior()).max() <= pdf_tol * s
+        # solid cells hold no state the fluid reads (the engine leaves them unstreamed)
+        assert np.abs(fine - oracle.fine.interior()[oracle.fine_slices])[fluid].max() <= pdf_tol * s
+    held, _ = solver.held_states()
+    expected = oracle.coarse.interior().copy()
+    expected[post] = O.collide(expected[post], oracle.coarse.omega_s, oracle.coarse.omega_b)
+    assert np.abs(held - expected).max() <= pdf_tol * steps
+
+
+def test_headline_two_level_case_matches_oracle():
+    """The benchmark's two-level case itself (coarse 512 x 384 x 8 at chord 32,
+    fine 160 x 76 x 16, AoA 8): states of both levels and loads against the
+    oracle for 3 coarse steps at the plain form's bars."""
+    import bench
+    from aerokinetic_gb300.refined import RefinedSolver
+    from aerokinetic_gb300.refined_plan import refined_project_dict
+    project, refinement = bench.refined_parts()
+    solver, oracle = refined_pair({"project": refined_project_dict(project, refinement)})
+    try:
+        assert tuple(solver.plan.shape) == (512, 384, 8)
+        compare_refined(solver, oracle, steps=3)
+    finally:
+        solver.close()
+
+
+def test_states_need_a_step_after_an_external_write(golden):
+    """After ak_set_pdf on the coarse level the pre-collision state is not
+    known until the next step; states() says so instead of returning the
+    held representation."""
+    solver, _ = refined_pair(golden["histories"]["refined_startup"])
+    try:
+        solver.step()
+        held, _ = solver.held_states()
+        from aerokinetic_gb300 import _native
+        import ctypes
+        _native.check(solver._lib.ak_set_pdf(solver._coarse, held.ctypes.data_as(ctypes.c_void_p)))
+        with pytest.raises(ValueError, match="next step"):
+            solver.states()
+        solver.step()
+        coarse, fine = solver.states()
+        assert np.isfinite(coarse).all() and np.isfinite(fine).all()
     finally:
         solver.close()
 
@@ -420,15 +461,17 @@ def test_refined_run_writes_history_frames_and_summary(golden, tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("storage,tol", [("f32", 1e-3), ("f16", 2e-2)])
+@pytest.mark.parametrize("storage,tol", [("f32", 5e-3), ("f16", 5e-3)])
 def test_refined_precision_forms_track_fp64(golden, storage, tol):
-    """The two-level case in the FP32-compute forms (FP32 or FP16 storage, FP32
-    transfer arithmetic) stays within the stated relative error of the FP64
-    form on Cl, Cd and Cm (floor 0.05) over 60 coarse steps."""
+    """The two-level case in the FP32-compute forms (FP32 storage; FP16
+    storage with the walls' fine level in FP32; FP32 transfer arithmetic)
+    stays within 0.5 % of the FP64 form on Cl, Cd and Cm (relative, floor
+    0.05) over 60 coarse steps."""
     from aerokinetic_gb300.refined import RefinedSolver
     from aerokinetic_gb300.refined_plan import load_refined_project
     project, refinement = load_refined_project(golden["histories"]["refined_startup"]["project"])
     plain, low = RefinedSolver(project, refinement), RefinedSolver(project, refinement, storage=storage)
+    assert low.fine_storage == "f32"
     try:
         for _ in range(6):
             a, b = plain.advance(10), low.advance(10)
