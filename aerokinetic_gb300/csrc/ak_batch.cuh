@@ -98,23 +98,34 @@ __global__ void k_batch_sum_partials(const BatchCase<S> *__restrict__ cases, dou
     if (lane == 0) loads[(long long)blockIdx.y * 5 * MAX_ELEMENTS + t] = s;
 }
 
-// fused pull-stream + collision over the packed block table; block chunk of
-// a case covers x in [bx * TB, bx * TB + TB) of row (y, z)
+// fused pull-stream + collision over the packed block table: block chunk of
+// a case covers its stream-collide items [chunk * TB, chunk * TB + TB) in
+// the single-case kernel's numbering (cells across rows, or cell pairs in
+// the pair forms), so a case's bits do not depend on the batch and no warp
+// is left part-empty at a row's end
 template <typename S, int TB>
-__global__ void __launch_bounds__(TB, Store<S>::MIN_BLOCKS * 128 / TB)
+__global__ void __launch_bounds__(TB, stream_collide_min_blocks<S>() * 128 / TB)
     k_batch_bulk(const BatchCase<S> *__restrict__ cases, const WorkItem *__restrict__ work, long long n_work,
                  int parity) {
     for (long long e = blockIdx.x; e < n_work; e += gridDim.x) {
         const WorkItem w = work[e];
         const BatchCase<S> &c = cases[w.c];
         const Grid G = c.G;
-        const int nbx = (G.nx + TB - 1) / TB;
-        const int bx = w.chunk % nbx, r = w.chunk / nbx;
-        const int y = r % G.ny + 1, z = r / G.ny;
-        const int x = bx * TB + threadIdx.x + 1;
-        if (x <= G.nx)
-            stream_collide_cell(c.pdf[c.cur0 ^ parity], c.pdf[c.cur0 ^ parity ^ 1], c.flags, G, G.shift, c.omega_s,
-                                c.omega_b, x, y, z, c.sgs);
+        const long long i = (long long)w.chunk * TB + threadIdx.x;
+        const S *src = c.pdf[c.cur0 ^ parity];
+        S *dst = c.pdf[c.cur0 ^ parity ^ 1];
+        if constexpr (pair_form<S>()) {
+            const int4 none = make_int4(0, 0, 0, 0);
+            stream_collide_pair_item(src, dst, c.flags, G, G.shift, c.omega_s, c.omega_b, c.sgs, none,
+                                     make_int4(1, G.nx + 1, 1, G.ny + 1), none, i);
+        } else {
+            const long long nxy = (long long)G.nx * G.ny;
+            if (i >= nxy * G.nz) continue;
+            const int z = (int)(i / nxy);
+            const long long r = i - (long long)z * nxy;
+            const int y = (int)(r / G.nx) + 1, x = (int)(r - (long long)(y - 1) * G.nx) + 1;
+            stream_collide_cell(src, dst, c.flags, G, G.shift, c.omega_s, c.omega_b, x, y, z, c.sgs);
+        }
     }
 }
 

@@ -587,7 +587,8 @@ int one_step(ak_case *c, bool sample, double *fixed_partials = nullptr, long lon
     }
     // bulk
     mark(c);
-    const unsigned grid = (unsigned)blocks_for((long long)c->nx * c->ny * c->nz, 128);
+    const unsigned grid =
+        (unsigned)blocks_for(stream_collide_items<S>(make_int4(0, 0, 0, 0), c->nx, c->ny, c->nz), 128);
     k_stream_collide<S><<<grid, 128, 0, c->stream>>>(src, dst_of<S>(c), c->flags, c->G, c->shift_host,
                                                      (T)c->omega_s, (T)c->omega_b, sgs_of<S>(c));
     AK_CUDA(cudaGetLastError());
@@ -717,7 +718,8 @@ int exterior_step(ak_case *c, double *fixed_partials, long long fixed_capacity, 
     AK_CUDA(cudaGetLastError());
     c->launches += 2;
     mark(c);
-    const unsigned grid = (unsigned)blocks_for((long long)c->nx * c->ny * c->nz, 128);
+    const unsigned grid =
+        (unsigned)blocks_for(stream_collide_items<S>(make_int4(0, 0, 0, 0), c->nx, c->ny, c->nz), 128);
     k_stream_collide<S><<<grid, 128, 0, c->stream>>>(src, dst, c->flags, c->G, c->shift_host, (T)c->omega_s,
                                                      (T)c->omega_b, Sgs<T>{});
     AK_CUDA(cudaGetLastError());
@@ -802,8 +804,8 @@ const char *ak_version(void) {
 }
 
 int ak_fma_peak(int32_t precision, double *tflops) {
-    if ((precision != 0 && precision != 1) || !tflops)
-        return fail(AK_ERR_INVALID, "precision 0 (FP64) or 1 (FP32) and an output are required");
+    if (precision < 0 || precision > 2 || !tflops)
+        return fail(AK_ERR_INVALID, "precision 0 (FP64), 1 (FP32) or 2 (packed FP32x2) and an output are required");
     int dev = 0, sms = 0;
     AK_CUDA(cudaGetDevice(&dev));
     AK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -823,8 +825,10 @@ int ak_fma_peak(int32_t precision, double *tflops) {
         cudaEventRecord(a, st);
         if (precision == 0)
             k_fma_peak<double><<<blocks, threads, 0, st>>>((double *)out, iters, 0.999999, 1e-6);
-        else
+        else if (precision == 1)
             k_fma_peak<float><<<blocks, threads, 0, st>>>((float *)out, iters, 0.999999f, 1e-6f);
+        else
+            k_fma2_peak<<<blocks, threads, 0, st>>>((float *)out, iters, 0.999999f, 1e-6f);
         cudaEventRecord(b, st);
         if (cudaEventSynchronize(b) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
             r = fail(AK_ERR_CUDA, "peak measurement kernel failed");
@@ -832,7 +836,7 @@ int ak_fma_peak(int32_t precision, double *tflops) {
         }
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, a, b);
-        const double flops = 2.0 * 8.0 * (double)iters * blocks * threads;
+        const double flops = (precision == 2 ? 4.0 : 2.0) * 8.0 * (double)iters * blocks * threads;
         if (rep > 0) best = std::max(best, flops / (ms * 1e-3) / 1e12);  // the first launch warms up
     }
     if (out) cudaFree(out);
@@ -1812,7 +1816,7 @@ int refined_init(ak_refined *R, double amp, double phase_y, double phase_z, doub
 // the storage forms whose collision arithmetic is FP64-accurate: their fused
 // pass supplies the budget's coarse mass and momentum sums
 template <typename S>
-constexpr bool fused_stats_form() {
+__host__ __device__ constexpr bool fused_stats_form() {
     return std::is_same_v<S, double> || std::is_same_v<S, df2>;
 }
 
@@ -1864,7 +1868,10 @@ int refined_step(ak_refined *R, bool fork = false) {
     // the collisions number their cells across rows (1-D grids)
     const unsigned gc1 = (unsigned)blocks_for((long long)C->nx * C->ny * C->nz, 128);
     const unsigned gx1 = (unsigned)blocks_for((long long)(R->xfer.y - R->xfer.x) * (R->xfer.w - R->xfer.z) * C->nz, 128);
-    const unsigned gn1 = (unsigned)blocks_for((long long)(R->near.y - R->near.x) * (R->near.w - R->near.z) * C->nz, 128);
+    // the stream-collide's grids (cells, or cell pairs in the pair forms):
+    // the whole lattice and the near part
+    const unsigned gsc = (unsigned)blocks_for(stream_collide_items<S>(make_int4(0, 0, 0, 0), C->nx, C->ny, C->nz), 128);
+    const unsigned gsn = (unsigned)blocks_for(stream_collide_items<S>(R->near, C->nx, C->ny, C->nz), 128);
     // fork mode, fused form, transfer block away from the outer faces: the
     // boundaries and the far coarse pass on their own branch
     const bool bnd = fork && R->fused && R->bnd_branch;
@@ -1915,11 +1922,11 @@ int refined_step(ak_refined *R, bool fork = false) {
             AK_CUDA(cudaStreamWaitEvent(R->bnd, R->ev_bnd_in, 0));
             AK_TRY(outer_part(R->bnd));
             if (fstats)
-                k_stream_collide<S, true><<<gc1, 128, 0, R->bnd>>>(
+                k_stream_collide<S, true><<<gsc, 128, 0, R->bnd>>>(
                     src_of<S>(C), dst_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s, (T)C->omega_b,
                     Sgs<T>{}, R->xfer, make_int4(0, 0, 0, 0), R->near, R->cstats);
             else
-                k_stream_collide<S><<<gc1, 128, 0, R->bnd>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G,
+                k_stream_collide<S><<<gsc, 128, 0, R->bnd>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G,
                                                               C->shift_host, (T)C->omega_s, (T)C->omega_b, Sgs<T>{},
                                                               R->xfer, make_int4(0, 0, 0, 0), R->near);
             AK_CUDA(cudaEventRecord(R->ev_bnd_out, R->bnd));
@@ -1944,25 +1951,25 @@ int refined_step(ak_refined *R, bool fork = false) {
         if (!bnd) AK_TRY(outer_part(st));
         mark(C);
         if (bnd && fstats)
-            k_stream_collide<S, true><<<gn1, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G,
+            k_stream_collide<S, true><<<gsn, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G,
                                                             C->shift_host, (T)C->omega_s, (T)C->omega_b, Sgs<T>{},
                                                             R->xfer, R->near, make_int4(0, 0, 0, 0),
                                                             R->cstats + R->cstats_far * NSTAT);
         else if (bnd)
             // the cells of near; the rest runs on the boundaries' branch
-            k_stream_collide<S><<<gn1, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, C->shift_host,
+            k_stream_collide<S><<<gsn, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, C->shift_host,
                                                       (T)C->omega_s, (T)C->omega_b, Sgs<T>{}, R->xfer, R->near);
         else if (R->fused && fstats) {
             // one launch covers every row of the far part; the near rows stay empty
             AK_CUDA(cudaMemsetAsync(R->cstats + R->cstats_far * NSTAT, 0, sizeof(double) * R->cstats_near * NSTAT, st));
-            k_stream_collide<S, true><<<gc1, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G,
+            k_stream_collide<S, true><<<gsc, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G,
                                                             C->shift_host, (T)C->omega_s, (T)C->omega_b, Sgs<T>{},
                                                             R->xfer, make_int4(0, 0, 0, 0), make_int4(0, 0, 0, 0),
                                                             R->cstats);
         } else if (R->fused)
             // streaming fused with the next step's collision, the transfer
             // block streamed only
-            k_stream_collide<S><<<gc1, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, C->shift_host,
+            k_stream_collide<S><<<gsc, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, C->shift_host,
                                                       (T)C->omega_s, (T)C->omega_b, Sgs<T>{}, R->xfer);
         else
             k_stream<S><<<gc, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, 0);
@@ -2077,7 +2084,8 @@ int refined_step(ak_refined *R, bool fork = false) {
 template <typename S>
 int graph_priorities(ak_refined *R, cudaGraph_t g) {
     ak_case *C = R->coarse;
-    const unsigned far_grid = (unsigned)blocks_for((long long)C->nx * C->ny * C->nz, 128);
+    const unsigned far_grid =
+        (unsigned)blocks_for(stream_collide_items<S>(make_int4(0, 0, 0, 0), C->nx, C->ny, C->nz), 128);
     int least = 0, greatest = 0;
     AK_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
     size_t n = 0;
@@ -2668,7 +2676,13 @@ std::vector<WorkItem> chunk_table(const std::vector<long long> &items) {
 // the stream-collide blocks of every case for block width tb
 std::vector<WorkItem> bulk_table(const ak_batch *B, int tb, int order) {
     std::vector<long long> count;
-    for (const ak_case *c : B->cases) count.push_back(blocks_for(c->nx, tb) * c->ny * c->nz);
+    // the single-case kernel's items (cells, or cell pairs in the pair forms)
+    for (const ak_case *c : B->cases) {
+        const bool pair = c->storage == AK_STORAGE_F32 || c->storage == AK_STORAGE_F16;
+        const long long items = pair ? stream_collide_items<float>(make_int4(0, 0, 0, 0), c->nx, c->ny, c->nz)
+                                     : stream_collide_items<double>(make_int4(0, 0, 0, 0), c->nx, c->ny, c->nz);
+        count.push_back(blocks_for(items, tb));
+    }
     std::vector<WorkItem> out;
     if (order == 0) {
         for (size_t c = 0; c < count.size(); ++c)

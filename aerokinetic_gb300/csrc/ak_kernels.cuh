@@ -18,6 +18,8 @@
 //   outer boundary kernels -> wall kernel (Bouzidi into solid cells, loads)
 //   -> stream_collide (pull from A, collide, write B) -> swap A/B.
 #pragma once
+#include <type_traits>
+
 #include "ak_lattice.cuh"
 
 namespace ak {
@@ -165,10 +167,146 @@ __device__ __forceinline__ void stream_collide_cell(const S *__restrict__ src, S
     for (int q = 0; q < Q; ++q) Store<S>::store(dst + q * G.qs + c, q, g[q], shift_at(shift, q));
 }
 
+// ------------------------------------------------------------ cell pairs
+// The FP32-compute storage forms advance two x-adjacent cells (xe, xe + 1),
+// xe even in padded coordinates, per thread: the collision of both runs as
+// one stream of packed FP32x2 instructions (ak_f32x2.cuh), the populations
+// that stay in their column (c_x = 0) are read as one aligned 4- or 8-byte
+// pair, and both cells' stores go out as pairs.  Rows, planes and the
+// population stride are even, so xe even keeps every pair aligned.
+template <typename S>
+__host__ __device__ constexpr bool pair_form() {
+    return std::is_same_v<S, float> || std::is_same_v<S, __half>;
+}
+// the pair of values at p, p + 1 as FP32 (p at an even element)
+__device__ __forceinline__ float2 load_pair(const float *p) { return __ldg(reinterpret_cast<const float2 *>(p)); }
+__device__ __forceinline__ float2 load_pair(const __half *p) {
+    return __half22float2(__ldg(reinterpret_cast<const __half2 *>(p)));
+}
+__device__ __forceinline__ float load_one(const float *p) { return __ldg(p); }
+__device__ __forceinline__ float load_one(const __half *p) { return __half2float(__ldg(p)); }
+__device__ __forceinline__ void store_pair(float *p, float2 v) { *reinterpret_cast<float2 *>(p) = v; }
+__device__ __forceinline__ void store_pair(__half *p, float2 v) {
+    *reinterpret_cast<__half2 *>(p) = __float22half2_rn(v);
+}
+__device__ __forceinline__ void store_one(float *p, float v) { *p = v; }
+__device__ __forceinline__ void store_one(__half *p, float v) { *p = __float2half_rn(v); }
+
+// Cells xe + k of row (y, z), k = 0, 1: live[k] the cell belongs to the
+// launch (only a live cell's pulls are read), only[k] it is streamed
+// without collision (then both cells take the one-cell path).  Each lane
+// rounds as the one-cell path's FP32 operations do, except that the
+// collision's multiply-add contractions are this code's own.
+template <typename S, typename Shift>
+__device__ __forceinline__ void stream_collide_pair(const S *__restrict__ src, S *__restrict__ dst,
+                                                    const uint8_t *__restrict__ flags, const Grid &G,
+                                                    const Shift &shift, float omega_s, float omega_b, int xe, int y,
+                                                    int z, bool live0, bool live1, bool only0, bool only1,
+                                                    const Sgs<F2> &sgs) {
+    if (only0 || only1) {
+        const Sgs<float> one{sgs.tau0, sgs.c18};
+        if (live0) stream_collide_cell(src, dst, flags, G, shift, omega_s, omega_b, xe, y, z, one, only0);
+        if (live1) stream_collide_cell(src, dst, flags, G, shift, omega_s, omega_b, xe + 1, y, z, one, only1);
+        return;
+    }
+    const bool store0 = live0 && __ldg(flags + y * G.nxp + xe) == FLAG_FLUID;
+    const bool store1 = live1 && __ldg(flags + y * G.nxp + xe + 1) == FLAG_FLUID;
+    const S *row[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) row[c] = src + (long long)G.wrapz(z - (c - 1)) * G.plane + (long long)y * G.sx + xe;
+    F2 g[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const S *p = row[cz(q) + 1] + ((long long)q * G.qs - (long long)cy(q) * G.sx);
+        float2 v;
+        if (cx(q) == 0) {
+            v = load_pair(p);
+        } else {
+            v.x = live0 ? load_one(p - cx(q)) : 0.0f;
+            v.y = live1 ? load_one(p + 1 - cx(q)) : 0.0f;
+        }
+        if constexpr (std::is_same_v<S, __half>) {
+            const float w = (float)weight(q), a = shift_at(shift, q);
+            v = f2_fma(v, make_float2(w, w), make_float2(a, a));
+        }
+        g[q] = F2(v);
+    }
+    if constexpr (sizeof(S) == sizeof(float))
+        collide<F2>(g, F2(omega_s), F2(omega_b), sgs);
+    else
+        collide_full<F2>(g, F2(1.0f - omega_s), F2(omega_b), sgs);
+    if (!store0 && !store1) return;
+    const long long c = G.cell(xe, y, z);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        float2 v = g[q].v;
+        if constexpr (std::is_same_v<S, __half>) {
+            const float a = shift_at(shift, q), inv = (float)(1.0 / weight(q));
+            v = f2_mul(f2_add(v, make_float2(-a, -a)), make_float2(inv, inv));
+        }
+        S *p = dst + q * G.qs + c;
+        if (store0 && store1) {
+            store_pair(p, v);
+        } else {
+            if (store0) store_one(p, v.x);
+            if (store1) store_one(p + 1, v.y);
+        }
+    }
+}
+
+// item i of a pair-form launch over the padded columns rect (rect.y != 0):
+// pairs (xe, xe + 1), xe even, covering the columns [rect.x, rect.y) of each
+// row, x fastest, then y, then z
+template <typename S, typename Shift>
+__device__ __forceinline__ void stream_collide_pair_item(const S *__restrict__ src, S *__restrict__ dst,
+                                                         const uint8_t *__restrict__ flags, const Grid &G,
+                                                         const Shift &shift, float omega_s, float omega_b,
+                                                         const Sgs<float> &sgs, int4 raw, int4 rect, int4 skip,
+                                                         long long i) {
+    const int xa = rect.x & ~1;
+    const long long wp = (((rect.y + 1) & ~1) - xa) / 2, h = rect.w - rect.z;
+    const long long nxy = wp * h;
+    if (i >= nxy * G.nz) return;
+    const int z = (int)(i / nxy);
+    const long long r = i - (long long)z * nxy;
+    const long long yr = r / wp;
+    const int xe = xa + 2 * (int)(r - yr * wp), y = rect.z + (int)yr;
+    bool live[2], only[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const int x = xe + k;
+        live[k] = x >= rect.x && x < rect.y && !(x >= skip.x && x < skip.y && y >= skip.z && y < skip.w);
+        only[k] = live[k] && x >= raw.x && x < raw.y && y >= raw.z && y < raw.w;
+    }
+    if (!live[0] && !live[1]) return;
+    Sgs<F2> s2;
+    s2.tau0 = sgs.tau0;
+    s2.c18 = sgs.c18;
+    stream_collide_pair(src, dst, flags, G, shift, omega_s, omega_b, xe, y, z, live[0], live[1], only[0], only[1],
+                        s2);
+}
+
+// items of one stream-collide launch over the padded columns rect (rect.y ==
+// 0: the interior): cells, or cell pairs (xe even) for the pair forms
+template <typename S>
+__host__ __device__ __forceinline__ long long stream_collide_items(int4 rect, int nx, int ny, int nz) {
+    if (rect.y == 0) rect = make_int4(1, nx + 1, 1, ny + 1);
+    const long long h = rect.w - rect.z;
+    if constexpr (pair_form<S>()) return (long long)((((rect.y + 1) & ~1) - (rect.x & ~1)) / 2) * h * nz;
+    return (long long)(rect.y - rect.x) * h * nz;
+}
+
+// resident 128-thread blocks per SM the stream-collide is compiled for: the
+// pair forms hold two cells' populations per thread
+template <typename S>
+__host__ __device__ constexpr int stream_collide_min_blocks() {
+    return pair_form<S>() ? 4 : Store<S>::MIN_BLOCKS;
+}
+
 // STATS: every block also writes the statistics of the cells it collided
 // (not the streamed-only ones) to stats[blockIdx.x] (CELL_STATS each)
 template <typename S, bool STATS = false>
-__global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
+__global__ void __launch_bounds__(128, stream_collide_min_blocks<S>())
     k_stream_collide(const S *__restrict__ src, S *__restrict__ dst, const uint8_t *__restrict__ flags, Grid G,
                      Shift27 shift, typename Store<S>::T omega_s, typename Store<S>::T omega_b,
                      Sgs<typename Store<S>::T> sgs, int4 raw = make_int4(0, 0, 0, 0),
@@ -181,6 +319,11 @@ __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
     // costs as much as a full one); columns inside skip are left to another
     // launch
     if (rect.y == 0) rect = make_int4(1, G.nx + 1, 1, G.ny + 1);
+    if constexpr (pair_form<S>()) {
+        stream_collide_pair_item(src, dst, flags, G, shift, omega_s, omega_b, sgs, raw, rect, skip,
+                                 (long long)blockIdx.x * blockDim.x + threadIdx.x);
+        return;
+    }
     const unsigned w = (unsigned)(rect.y - rect.x), h = (unsigned)(rect.w - rect.z);
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned nxy = w * h;

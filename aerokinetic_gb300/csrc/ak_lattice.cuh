@@ -29,6 +29,7 @@
 #include <stdint.h>
 
 #include "ak_df64.cuh"
+#include "ak_f32x2.cuh"
 
 namespace ak {
 
@@ -184,6 +185,7 @@ __host__ __device__ __forceinline__ double mul_pow2<double>(double a, double s) 
 // double-float form evaluates the rate in FP64 (a few operations per cell).
 template <typename T> struct SgsReal { using type = T; };
 template <> struct SgsReal<df64> { using type = double; };
+template <> struct SgsReal<F2> { using type = float; };
 template <typename T>
 struct Sgs {
     typename SgsReal<T>::type tau0 = 0, c18 = 0;
@@ -200,6 +202,14 @@ __host__ __device__ __forceinline__ T smagorinsky_rate(const Sgs<T> &m, T rinv, 
 
 // mac (optional): the cell's (drho, jx, jy, jz, |u|^2), which the collision
 // conserves (drho, j) or forms anyway; a null mac compiles away.
+// the subgrid rate of a pair of cells, lane by lane in FP32
+__device__ __forceinline__ F2 smagorinsky_rate(const Sgs<F2> &m, F2 rinv, F2 pxx, F2 pyy, F2 pzz, F2 pxy, F2 pxz,
+                                               F2 pyz) {
+    const Sgs<float> s{m.tau0, m.c18};
+    return F2(make_float2(smagorinsky_rate<float>(s, rinv.v.x, pxx.v.x, pyy.v.x, pzz.v.x, pxy.v.x, pxz.v.x, pyz.v.x),
+                          smagorinsky_rate<float>(s, rinv.v.y, pxx.v.y, pyy.v.y, pzz.v.y, pxy.v.y, pxz.v.y, pyz.v.y)));
+}
+
 template <typename T>
 __host__ __device__ __forceinline__ void collide(T g[Q], T omega_s, T omega_b, const Sgs<T> &sgs = Sgs<T>{},
                                                  T *mac = nullptr) {

@@ -35,6 +35,23 @@ __global__ void __launch_bounds__(256) k_fma_peak(T *__restrict__ out, int iters
     if (s == T(-1)) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// the same chains in packed FP32x2 fused multiply-adds (two FMAs per
+// instruction and lane): eight float2 chains per thread
+__global__ void __launch_bounds__(256) k_fma2_peak(float *__restrict__ out, int iters, float a, float b) {
+    float2 x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = make_float2((threadIdx.x + k) * 1e-3f, (threadIdx.x + 2 * k) * 1e-3f);
+    const float2 a2 = make_float2(a, a), b2 = make_float2(b, b);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = f2_fma(x[k], a2, b2);
+    }
+    float s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += x[k].x + x[k].y;
+    if (s == -1.0f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 // Host number type that counts the arithmetic applied to it.
 struct Counted {
     double v = 0;

@@ -7,8 +7,12 @@ arrive and as device memory frees up, and retiring each case when its lift
 coefficient settles or its step limit is reached.  Scheduling happens only at
 chunk boundaries, every case is stepped by the same batched kernels whatever
 its neighbours, and its convergence test reads only its own samples, so a
-request's result is the same whether it ran alone or in any mix.
+request's result is the same whether it ran alone or in any mix.  An
+admitted request's case is built (plan, geometry, device set-up on its own
+stream) by a host worker thread while the GPU advances the running batch; it
+joins the batch at the next chunk boundary after it is ready.
 """
+from concurrent.futures import ThreadPoolExecutor, wait, FIRST_COMPLETED
 from dataclasses import dataclass, field
 import math
 import time
@@ -109,31 +113,42 @@ class Server:
                 raise MemoryError(f"request {r.name!r} alone exceeds the memory budget")
         order = sorted(range(len(requests)), key=lambda i: arrivals[i])
         pending = [(arrivals[i], requests[i]) for i in order]
-        resident, results = [], []
+        resident, results, building = [], [], []
         batch, used = None, 0
         peak_cases = peak_bytes = 0
         batch_steps = rebuilds = 0
         cell_updates = 0
+        pool = ThreadPoolExecutor(max_workers=1, thread_name_prefix="admission")
         start = self.clock()
         try:
-            while pending or resident:
+            while pending or resident or building:
                 now = self.clock() - start
                 changed = False
-                # admission in arrival order while the footprint fits
-                while pending and pending[0][0] <= now and len(resident) < self.max_cases:
+                # admission in arrival order while the footprint fits: the
+                # memory is reserved now, the case is built by the worker
+                while pending and pending[0][0] <= now and len(resident) + len(building) < self.max_cases:
                     arrival, request = pending[0]
                     need = self.footprint(request)
                     if used + need > self.budget:
                         break
                     pending.pop(0)
-                    solver = Solver(request.section, request.flow, request.grid, storage=self.storage)
-                    resident.append(_Live(request, solver, arrival, self.clock() - start, need))
+                    future = pool.submit(Solver, request.section, request.flow, request.grid, storage=self.storage)
+                    building.append((future, arrival, need, request))
                     used += need
+                if building and not resident:
+                    # nothing to step: wait for a case (or the next arrival)
+                    timeout = None if not pending else max(0.0, pending[0][0] - (self.clock() - start))
+                    wait([b[0] for b in building], timeout=timeout, return_when=FIRST_COMPLETED)
+                for item in [b for b in building if b[0].done()]:
+                    building.remove(item)
+                    future, arrival, need, request = item
+                    resident.append(_Live(request, future.result(), arrival, self.clock() - start, need))
                     changed = True
                 peak_cases = max(peak_cases, len(resident))
                 peak_bytes = max(peak_bytes, used)
                 if not resident:
-                    self.sleep(max(0.0, pending[0][0] - (self.clock() - start)))
+                    if not building and pending:
+                        self.sleep(max(0.0, pending[0][0] - (self.clock() - start)))
                     continue
                 if changed or batch is None:
                     if batch is not None:
@@ -173,6 +188,10 @@ class Server:
                             live.solver.close()
                     resident = keep
         finally:
+            pool.shutdown(wait=True)
+            for future, _, _, _ in building:
+                if future.done() and future.exception() is None:
+                    future.result().close()
             if batch is not None:
                 batch.close()
             for live in resident:

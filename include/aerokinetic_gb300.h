@@ -343,7 +343,8 @@ const char *ak_last_error(void);
 /* Library build identification, e.g. "aerokinetic_gb300 sm_103a". */
 const char *ak_version(void);
 /* Fused multiply-add throughput of the current device in TFLOP/s (two FLOPs
- * per FMA), precision 0 = FP64, 1 = FP32: eight dependent FMA chains per
+ * per FMA), precision 0 = FP64, 1 = FP32, 2 = packed FP32x2 (two FMAs per
+ * instruction and lane): eight dependent FMA chains per
  * thread over 8 blocks of 256 threads per SM, best of three timed launches
  * (CUDA events).  The ceiling of the FP64-bound plain collision.  No
  * counterpart in the reference; it exists for measurement. */
