@@ -1598,6 +1598,10 @@ struct ak_refined {
     int4 near{0, 0, 0, 0};
     cudaStream_t bnd = nullptr;
     cudaEvent_t ev_bnd_in = nullptr, ev_bnd_out = nullptr;
+    // the budget's outer-face flux beside the far pass: it reads the coarse
+    // copy (ghosts written by UBB and outflow), which the far pass only reads
+    cudaStream_t ostr = nullptr;
+    cudaEvent_t ev_outer_in = nullptr, ev_outer_out = nullptr;
     double dx_c = 0, dt_c = 0, dx_f = 0, dt_f = 0, span = 0, speed = 0;
     double tau_s_c = 0, tau_b_c = 0, tau_s_f = 0, tau_b_f = 0;
     double free_g[Q];
@@ -1641,7 +1645,7 @@ struct ak_refined {
     // fused form in an FP64-arithmetic storage: the coarse statistics of a
     // budget step come from the fused pass itself (rows of its far and near
     // launches, then the transfer block's band outside the box)
-    double *cstats = nullptr;
+    double *cstats = nullptr, *cstats_stage = nullptr;
     long long cstats_far = 0, cstats_near = 0;
 };
 
@@ -1673,6 +1677,9 @@ void refined_release(ak_refined *R) {
         if (e) cudaEventDestroy(e);
     if (R->flux) cudaStreamDestroy(R->flux);
     if (R->ev_bnd_in) cudaEventDestroy(R->ev_bnd_in);
+    if (R->ev_outer_in) cudaEventDestroy(R->ev_outer_in);
+    if (R->ev_outer_out) cudaEventDestroy(R->ev_outer_out);
+    if (R->ostr) cudaStreamDestroy(R->ostr);
     if (R->ev_bnd_out) cudaEventDestroy(R->ev_bnd_out);
     if (R->bnd) cudaStreamDestroy(R->bnd);
     if (R->coarse) {
@@ -1820,22 +1827,34 @@ __host__ __device__ constexpr bool fused_stats_form() {
     return std::is_same_v<S, double> || std::is_same_v<S, df2>;
 }
 
-// The budget statistics when the fused coarse pass has written its rows to
-// cstats: the cells of the transfer block outside the box (after reflux and
-// restriction), the reduction over every row, then the fine block.
-template <typename S, typename SF>
-int enqueue_fused_stats(ak_refined *R, cudaStream_t st) {
-    ak_case *C = R->coarse, *F = R->fine;
-    const BoxSpec &B = R->B;
-    const Region band{R->xfer.x - 1, R->xfer.y - 1, R->xfer.z - 1, R->xfer.w - 1, B.lo[0], B.hi[0], B.lo[1], B.hi[1]};
+// The fine block's budget statistics (stats_out[NSTAT..2 NSTAT)), on the
+// stream the restriction runs on: both only read the fine state.
+template <typename SF>
+int enqueue_fine_stats(ak_refined *R, cudaStream_t st) {
+    ak_case *F = R->fine;
     const Region rf{R->pad, F->nx - R->pad, R->pad, F->ny - R->pad, 0, 0, 0, 0};
-    const long long rows = R->cstats_far + R->cstats_near + STATS_BLOCKS;
-    k_region_stats<S><<<STATS_BLOCKS, 256, 0, st>>>(src_of<S>(C), C->G, C->flags, band,
-                                                     R->cstats + (R->cstats_far + R->cstats_near) * NSTAT);
-    k_region_final<<<1, REDUCE_THREADS, 0, st>>>(R->cstats, (int)rows, R->stats_out);
     k_region_stats<SF><<<STATS_BLOCKS, 256, 0, st>>>(src_of<SF>(F), F->G, F->flags, rf, R->stats_partials);
     k_region_final<<<1, REDUCE_THREADS, 0, st>>>(R->stats_partials, STATS_BLOCKS, R->stats_out + NSTAT);
-    C->launches += 4;
+    R->coarse->launches += 2;
+    AK_CUDA(cudaGetLastError());
+    return AK_OK;
+}
+
+// The coarse budget statistics when the fused coarse pass has written its
+// rows to cstats: the cells of the transfer block outside the box (after
+// reflux and restriction), then the reduction over every row in two stages.
+template <typename S>
+int enqueue_coarse_fused_stats(ak_refined *R, cudaStream_t st) {
+    ak_case *C = R->coarse;
+    const BoxSpec &B = R->B;
+    const Region band{R->xfer.x - 1, R->xfer.y - 1, R->xfer.z - 1, R->xfer.w - 1, B.lo[0], B.hi[0], B.lo[1], B.hi[1]};
+    const long long rows = R->cstats_far + R->cstats_near + STATS_BLOCKS;
+    const long long stage = blocks_for(rows, REDUCE_THREADS);
+    k_region_stats<S><<<STATS_BLOCKS, 256, 0, st>>>(src_of<S>(C), C->G, C->flags, band,
+                                                     R->cstats + (R->cstats_far + R->cstats_near) * NSTAT);
+    k_region_stage<<<(unsigned)stage, REDUCE_THREADS, 0, st>>>(R->cstats, rows, R->cstats_stage);
+    k_region_final<<<1, REDUCE_THREADS, 0, st>>>(R->cstats_stage, (int)stage, R->stats_out);
+    C->launches += 3;
     AK_CUDA(cudaGetLastError());
     return AK_OK;
 }
@@ -1898,6 +1917,8 @@ int refined_step(ak_refined *R, bool fork = false) {
     };
     // the outer boundaries of the coarse level on stream s: UBB, outflow and
     // the budget's flux through the outer faces
+    // in the boundaries' branch (bnd) the budget's flux forks onto its own
+    // stream, so that the far pass does not wait for it
     auto outer_part = [&](cudaStream_t s) -> int {
         if (C->n_ubb)
             k_ubb<S><<<(unsigned)blocks3(C->n_ubb_cells * C->nz), 256, 0, s>>>(src_of<S>(C), C->G, C->ubb_cells,
@@ -1906,10 +1927,17 @@ int refined_step(ak_refined *R, bool fork = false) {
             k_outflow<S><<<(unsigned)blocks3(C->n_out), 256, 0, s>>>(src_of<S>(C), C->G, C->outer(), C->sel_out,
                                                                      C->n_out, C->out_state, 1, 0, 0);
         if (R->track_budget) {
-            k_outer_flux<S><<<dim3((unsigned)R->outer_blocks, 4), 256, 0, s>>>(
+            cudaStream_t fs = s;
+            if (bnd) {
+                AK_CUDA(cudaEventRecord(R->ev_outer_in, s));
+                AK_CUDA(cudaStreamWaitEvent(R->ostr, R->ev_outer_in, 0));
+                fs = R->ostr;
+            }
+            k_outer_flux<S><<<dim3((unsigned)R->outer_blocks, 4), 256, 0, fs>>>(
                 src_of<S>(C), C->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_outer, 4, R->outer_partials);
-            k_outer_final<<<1, REDUCE_THREADS, 0, s>>>(R->outer_partials, R->d_outer, 4, R->outer_blocks,
-                                                      R->dx_c * R->dx_c * R->dx_c, R->outer_out);
+            k_outer_final<<<1, REDUCE_THREADS, 0, fs>>>(R->outer_partials, R->d_outer, 4, R->outer_blocks,
+                                                       R->dx_c * R->dx_c * R->dx_c, R->outer_out);
+            if (bnd) AK_CUDA(cudaEventRecord(R->ev_outer_out, fs));
             C->launches += 2;
         }
         AK_CUDA(cudaGetLastError());
@@ -2050,6 +2078,9 @@ int refined_step(ak_refined *R, bool fork = false) {
         AK_CUDA(cudaEventRecord(R->ev_fork, st));
         AK_CUDA(cudaStreamWaitEvent(R->side, R->ev_fork, 0));
         launch_restrict<S, SF>(R, f2c, R->side);
+        // the fine block's statistics beside the reflux (both levels' final
+        // states are complete: the fine one before the fork)
+        if (fstats) AK_TRY(enqueue_fine_stats<SF>(R, R->side));
         AK_CUDA(cudaEventRecord(R->ev_join, R->side));
     }
     k_reflux<S><<<dim3((unsigned)split_blocks(R->max_face), R->nfaces), SPLIT_THREADS, 0, st>>>(
@@ -2061,10 +2092,12 @@ int refined_step(ak_refined *R, bool fork = false) {
         launch_restrict<S, SF>(R, f2c, st);
     AK_CUDA(cudaGetLastError());
     if (bnd) AK_CUDA(cudaStreamWaitEvent(st, R->ev_bnd_out, 0));
+    if (bnd && R->track_budget) AK_CUDA(cudaStreamWaitEvent(st, R->ev_outer_out, 0));
     // a tracked budget closes on the integrals of the state the step leaves
-    if (fstats)
-        AK_TRY((enqueue_fused_stats<S, SF>(R, st)));
-    else if (R->track_budget && R->step_stats)
+    if (fstats) {
+        if (!fork) AK_TRY(enqueue_fine_stats<SF>(R, st));
+        AK_TRY(enqueue_coarse_fused_stats<S>(R, st));
+    } else if (R->track_budget && R->step_stats)
         AK_TRY((enqueue_region_stats<S, SF>(R, st)));
     mark(C);  // step end
     C->launches += 6 + 7 * 2 + (C->n_ubb ? 1 : 0) + (C->n_out ? 1 : 0) + (nlinks ? 0 : -4) + 1 + (bnd ? 1 : 0);
@@ -2330,7 +2363,9 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
             const int4 nr = R->near;
             R->cstats_far = blocks_for((long long)cd.nx * cd.ny * cd.nz, 128);
             R->cstats_near = blocks_for((long long)(nr.y - nr.x) * (nr.w - nr.z) * cd.nz, 128);
-            r = ralloc(R, &R->cstats, (size_t)(R->cstats_far + R->cstats_near + STATS_BLOCKS) * NSTAT);
+            const long long rows = R->cstats_far + R->cstats_near + STATS_BLOCKS;
+            r = ralloc(R, &R->cstats, (size_t)rows * NSTAT);
+            if (r == AK_OK) r = ralloc(R, &R->cstats_stage, (size_t)blocks_for(rows, REDUCE_THREADS) * NSTAT);
         }
         if (r == AK_OK) r = ralloc(R, &R->stats_out, (size_t)2 * NSTAT);
         if (r == AK_OK && (cudaMemset(R->outer_out, 0, 8 * sizeof(double)) != cudaSuccess ||
@@ -2348,7 +2383,10 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
                        cudaEventCreateWithFlags(&R->ev_flux_done, cudaEventDisableTiming) != cudaSuccess ||
                        cudaStreamCreateWithFlags(&R->bnd, cudaStreamNonBlocking) != cudaSuccess ||
                        cudaEventCreateWithFlags(&R->ev_bnd_in, cudaEventDisableTiming) != cudaSuccess ||
-                       cudaEventCreateWithFlags(&R->ev_bnd_out, cudaEventDisableTiming) != cudaSuccess))
+                       cudaEventCreateWithFlags(&R->ev_bnd_out, cudaEventDisableTiming) != cudaSuccess ||
+                       cudaStreamCreateWithFlags(&R->ostr, cudaStreamNonBlocking) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&R->ev_outer_in, cudaEventDisableTiming) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&R->ev_outer_out, cudaEventDisableTiming) != cudaSuccess))
         r = fail(AK_ERR_CUDA, "stream or event creation failed");
     if (r == AK_OK) r = ralloc(R, &R->d_flag, 1);
     if (r == AK_OK) r = ralloc(R, &R->d_loads, (size_t)2 * 5 * std::max(1, cd.n_elements));

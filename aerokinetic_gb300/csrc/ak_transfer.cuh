@@ -945,6 +945,18 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// first stage of a reduction of many statistics rows: block b reduces rows
+// [b REDUCE_THREADS, (b + 1) REDUCE_THREADS) into out[b], so that the final
+// block reduces one row per stage block (a fixed order either way)
+__global__ void __launch_bounds__(REDUCE_THREADS)
+    k_region_stage(const double *__restrict__ partials, long long nrows, double *__restrict__ out) {
+    const long long first = (long long)blockIdx.x * REDUCE_THREADS;
+    double a[NSTAT];
+    reduce_rows<NSTAT>(partials + first * NSTAT, min((long long)REDUCE_THREADS, nrows - first), 0x3u, a);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < NSTAT; ++k) out[(long long)blockIdx.x * NSTAT + k] = a[k];
+}
+
 __global__ void __launch_bounds__(REDUCE_THREADS)
     k_region_final(const double *__restrict__ partials, int nblocks, double *__restrict__ out) {
     double a[NSTAT];
