@@ -79,22 +79,6 @@ __device__ __forceinline__ float shift_at(const float *s, int q) { return __ldg(
 // (the layout the two-level budget reduces): max |u|^2, max |rho - 1|,
 // sum drho, sum j (3), cells, non-finite cells.
 constexpr int CELL_STATS = 8;
-__device__ __forceinline__ void add_cell_stats(double acc[CELL_STATS], double drho, double jx, double jy, double jz,
-                                               double u2) {
-    const double rho = 1.0 + drho;
-    if (!isfinite(rho) || !isfinite(u2)) {
-        acc[7] += 1.0;
-        return;
-    }
-    acc[0] = fmax(acc[0], u2);
-    acc[1] = fmax(acc[1], fabs(rho - 1.0));
-    acc[2] += drho;
-    acc[3] += jx;
-    acc[4] += jy;
-    acc[5] += jz;
-    acc[6] += 1.0;
-}
-
 // block sums of the per-thread statistics (the first two entries maxima) in a
 // fixed order; thread 0 writes out[row * CELL_STATS ...].  Every thread of
 // the block must call it.
@@ -123,6 +107,38 @@ __device__ void block_cell_stats(double (&a)[CELL_STATS], double *out, long long
     }
 }
 
+// The same statistics accumulated inside the FP64-bound fused pass, with as
+// little FP64-pipe work as possible: the four sums in FP64, the maxima of
+// the non-negative |u|^2 and |drho| as integer maxima of their bit patterns
+// (the order of non-negative doubles), the finiteness test on the exponent
+// bits and the cell counts as integers.
+struct FusedStats {
+    double drho = 0, jx = 0, jy = 0, jz = 0;
+    long long u2 = 0, dr = 0;  // bit patterns of the maxima
+    int cells = 0, bad = 0;
+};
+__device__ __forceinline__ bool finite_bits(double v) { return (__double2hiint(v) & 0x7ff00000) != 0x7ff00000; }
+__device__ __forceinline__ void add_fused_stats(FusedStats &a, double drho, double jx, double jy, double jz,
+                                                double u2) {
+    if (!finite_bits(drho) || !finite_bits(u2)) {
+        ++a.bad;
+        return;
+    }
+    a.drho += drho;
+    a.jx += jx;
+    a.jy += jy;
+    a.jz += jz;
+    a.u2 = max(a.u2, __double_as_longlong(u2));
+    a.dr = max(a.dr, __double_as_longlong(drho) & 0x7fffffffffffffffLL);
+    ++a.cells;
+}
+// the block's statistics row in the CELL_STATS layout (every thread calls it)
+__device__ void block_fused_stats(const FusedStats &s, double *out, long long row) {
+    double a[CELL_STATS] = {__longlong_as_double(s.u2), __longlong_as_double(s.dr), s.drho, s.jx, s.jy, s.jz,
+                            (double)s.cells, (double)s.bad};
+    block_cell_stats(a, out, row);
+}
+
 // pull the 27 populations of interior cell (x, y, z) (padded x, y), collide,
 // store into dst if the column is fluid; stream_only: store the pulled values
 // as they are (bit copies, no collision); acc (optional): add the collided
@@ -133,7 +149,7 @@ __device__ __forceinline__ void stream_collide_cell(const S *__restrict__ src, S
                                                     const Shift &shift, typename Store<S>::T omega_s,
                                                     typename Store<S>::T omega_b, int x, int y, int z,
                                                     const Sgs<typename Store<S>::T> &sgs,
-                                                    bool stream_only = false, double *acc = nullptr) {
+                                                    bool stream_only = false, FusedStats *acc = nullptr) {
     using T = typename Store<S>::T;
     // the column flag only gates the stores, so the 27 loads issue at once
     const bool fluid = __ldg(flags + y * G.nxp + x) == FLAG_FLUID;
@@ -161,7 +177,7 @@ __device__ __forceinline__ void stream_collide_cell(const S *__restrict__ src, S
     T mac[5];
     collide_stored<S>(g, omega_s, omega_b, sgs, acc ? mac : nullptr);
     if (!fluid) return;
-    if (acc) add_cell_stats(acc, (double)mac[0], (double)mac[1], (double)mac[2], (double)mac[3], (double)mac[4]);
+    if (acc) add_fused_stats(*acc, (double)mac[0], (double)mac[1], (double)mac[2], (double)mac[3], (double)mac[4]);
     const long long c = G.cell(x, y, z);
 #pragma unroll
     for (int q = 0; q < Q; ++q) Store<S>::store(dst + q * G.qs + c, q, g[q], shift_at(shift, q));
@@ -192,44 +208,76 @@ __device__ __forceinline__ void store_pair(__half *p, float2 v) {
 __device__ __forceinline__ void store_one(float *p, float v) { *p = v; }
 __device__ __forceinline__ void store_one(__half *p, float v) { *p = __float2half_rn(v); }
 
-// Cells xe + k of row (y, z), k = 0, 1: live[k] the cell belongs to the
-// launch (only a live cell's pulls are read), only[k] it is streamed
-// without collision (then both cells take the one-cell path).  Each lane
-// rounds as the one-cell path's FP32 operations do, except that the
-// collision's multiply-add contractions are this code's own.
-template <typename S, typename Shift>
-__device__ __forceinline__ void stream_collide_pair(const S *__restrict__ src, S *__restrict__ dst,
-                                                    const uint8_t *__restrict__ flags, const Grid &G,
-                                                    const Shift &shift, float omega_s, float omega_b, int xe, int y,
-                                                    int z, bool live0, bool live1, bool only0, bool only1,
-                                                    const Sgs<F2> &sgs) {
-    if (only0 || only1) {
-        const Sgs<float> one{sgs.tau0, sgs.c18};
-        if (live0) stream_collide_cell(src, dst, flags, G, shift, omega_s, omega_b, xe, y, z, one, only0);
-        if (live1) stream_collide_cell(src, dst, flags, G, shift, omega_s, omega_b, xe + 1, y, z, one, only1);
-        return;
-    }
-    const bool store0 = live0 && __ldg(flags + y * G.nxp + xe) == FLAG_FLUID;
-    const bool store1 = live1 && __ldg(flags + y * G.nxp + xe + 1) == FLAG_FLUID;
+// items of one stream-collide launch over the padded columns rect (rect.y ==
+// 0: the interior): cells, or cell pairs (xe even) for the pair forms
+template <typename S>
+__host__ __device__ __forceinline__ long long stream_collide_items(int4 rect, int nx, int ny, int nz) {
+    if (rect.y == 0) rect = make_int4(1, nx + 1, 1, ny + 1);
+    const long long h = rect.w - rect.z;
+    if constexpr (pair_form<S>()) return (long long)((((rect.y + 1) & ~1) - (rect.x & ~1)) / 2) * h * nz;
+    return (long long)(rect.y - rect.x) * h * nz;
+}
+
+// The 27 pulled populations of a cell pair as loaded: FP16 pairs packed in
+// one 32-bit word each (so that a thread can hold the next pair's while it
+// collides the current one), FP32 pairs as float2.
+template <typename S> struct PairRaw;
+template <> struct PairRaw<__half> { unsigned v[Q]; };
+template <> struct PairRaw<float> { float2 v[Q]; };
+
+// Cells xe + k of row (y, z), k = 0, 1, with live[k] set when the cell
+// belongs to the launch (only a live cell's pulls are read): the pulls of
+// both, the c_x = 0 ones as one aligned pair
+template <typename S>
+__device__ __forceinline__ void pair_load(const S *__restrict__ src, const Grid &G, int xe, int y, int z, bool live0,
+                                          bool live1, PairRaw<S> &raw) {
     const S *row[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) row[c] = src + (long long)G.wrapz(z - (c - 1)) * G.plane + (long long)y * G.sx + xe;
-    F2 g[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         const S *p = row[cz(q) + 1] + ((long long)q * G.qs - (long long)cy(q) * G.sx);
-        float2 v;
-        if (cx(q) == 0) {
-            v = load_pair(p);
-        } else {
-            v.x = live0 ? load_one(p - cx(q)) : 0.0f;
-            v.y = live1 ? load_one(p + 1 - cx(q)) : 0.0f;
-        }
         if constexpr (std::is_same_v<S, __half>) {
-            const float w = (float)weight(q), a = shift_at(shift, q);
-            v = f2_fma(v, make_float2(w, w), make_float2(a, a));
+            if (cx(q) == 0) {
+                raw.v[q] = __ldg(reinterpret_cast<const unsigned *>(p));
+            } else {
+                const unsigned lo = live0 ? __ldg(reinterpret_cast<const unsigned short *>(p - cx(q))) : 0u;
+                const unsigned hi = live1 ? __ldg(reinterpret_cast<const unsigned short *>(p + 1 - cx(q))) : 0u;
+                raw.v[q] = lo | (hi << 16);
+            }
+        } else {
+            if (cx(q) == 0) {
+                raw.v[q] = __ldg(reinterpret_cast<const float2 *>(p));
+            } else {
+                raw.v[q].x = live0 ? __ldg(p - cx(q)) : 0.0f;
+                raw.v[q].y = live1 ? __ldg(p + 1 - cx(q)) : 0.0f;
+            }
         }
-        g[q] = F2(v);
+    }
+}
+
+// The collision of both cells in packed FP32x2 and their stores (fluid
+// cells only; a pair of stores where both are).  Each lane rounds as the
+// one-cell path's FP32 operations do, except that the collision's
+// multiply-add contractions are this code's own.
+template <typename S, typename Shift>
+__device__ __forceinline__ void pair_collide_store(const PairRaw<S> &raw, S *__restrict__ dst,
+                                                   const uint8_t *__restrict__ flags, const Grid &G,
+                                                   const Shift &shift, float omega_s, float omega_b, int xe, int y,
+                                                   int z, bool live0, bool live1, const Sgs<F2> &sgs) {
+    const bool store0 = live0 && __ldg(flags + y * G.nxp + xe) == FLAG_FLUID;
+    const bool store1 = live1 && __ldg(flags + y * G.nxp + xe + 1) == FLAG_FLUID;
+    F2 g[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        if constexpr (std::is_same_v<S, __half>) {
+            __half2 h;
+            memcpy(&h, &raw.v[q], sizeof h);
+            const float w = (float)weight(q), a = shift_at(shift, q);
+            g[q] = F2(f2_fma(__half22float2(h), make_float2(w, w), make_float2(a, a)));
+        } else {
+            g[q] = F2(raw.v[q]);
+        }
     }
     if constexpr (sizeof(S) == sizeof(float))
         collide<F2>(g, F2(omega_s), F2(omega_b), sgs);
@@ -256,44 +304,115 @@ __device__ __forceinline__ void stream_collide_pair(const S *__restrict__ src, S
 
 // item i of a pair-form launch over the padded columns rect (rect.y != 0):
 // pairs (xe, xe + 1), xe even, covering the columns [rect.x, rect.y) of each
-// row, x fastest, then y, then z
+// row, x fastest, then y, then z.  False when i lies beyond the launch or
+// neither cell belongs to it.
+struct PairItem {
+    int xe, y, z;
+    bool live0, live1, only;  // only: a cell is streamed without collision
+};
+__device__ __forceinline__ bool pair_item(const Grid &G, int4 raw, int4 rect, int4 skip, long long i, PairItem &it) {
+    const int xa = rect.x & ~1;
+    const long long wp = (((rect.y + 1) & ~1) - xa) / 2, h = rect.w - rect.z;
+    const long long nxy = wp * h;
+    if (i >= nxy * G.nz) return false;
+    it.z = (int)(i / nxy);
+    const long long r = i - (long long)it.z * nxy;
+    const long long yr = r / wp;
+    it.xe = xa + 2 * (int)(r - yr * wp);
+    it.y = rect.z + (int)yr;
+    bool live[2], only = false;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const int x = it.xe + k;
+        live[k] = x >= rect.x && x < rect.y && !(x >= skip.x && x < skip.y && it.y >= skip.z && it.y < skip.w);
+        only |= live[k] && x >= raw.x && x < raw.y && it.y >= raw.z && it.y < raw.w;
+    }
+    it.live0 = live[0];
+    it.live1 = live[1];
+    it.only = only;
+    return live[0] || live[1];
+}
+
+// one pair without prefetch; a pair with a streamed-only cell takes the
+// one-cell path for both cells
+template <typename S, typename Shift>
+__device__ __forceinline__ void stream_collide_pair(const S *__restrict__ src, S *__restrict__ dst,
+                                                    const uint8_t *__restrict__ flags, const Grid &G,
+                                                    const Shift &shift, float omega_s, float omega_b,
+                                                    const Sgs<float> &sgs, int4 raw, const PairItem &it) {
+    if (it.only) {
+        for (int k = 0; k < 2; ++k) {
+            const int x = it.xe + k;
+            if (!(k ? it.live1 : it.live0)) continue;
+            const bool only = x >= raw.x && x < raw.y && it.y >= raw.z && it.y < raw.w;
+            stream_collide_cell(src, dst, flags, G, shift, omega_s, omega_b, x, it.y, it.z, sgs, only);
+        }
+        return;
+    }
+    Sgs<F2> s2;
+    s2.tau0 = sgs.tau0;
+    s2.c18 = sgs.c18;
+    PairRaw<S> r;
+    pair_load(src, G, it.xe, it.y, it.z, it.live0, it.live1, r);
+    pair_collide_store(r, dst, flags, G, shift, omega_s, omega_b, it.xe, it.y, it.z, it.live0, it.live1, s2);
+}
+
+// item i of a pair-form launch (one pair, no prefetch): the batch's body
 template <typename S, typename Shift>
 __device__ __forceinline__ void stream_collide_pair_item(const S *__restrict__ src, S *__restrict__ dst,
                                                          const uint8_t *__restrict__ flags, const Grid &G,
                                                          const Shift &shift, float omega_s, float omega_b,
                                                          const Sgs<float> &sgs, int4 raw, int4 rect, int4 skip,
                                                          long long i) {
-    const int xa = rect.x & ~1;
-    const long long wp = (((rect.y + 1) & ~1) - xa) / 2, h = rect.w - rect.z;
-    const long long nxy = wp * h;
-    if (i >= nxy * G.nz) return;
-    const int z = (int)(i / nxy);
-    const long long r = i - (long long)z * nxy;
-    const long long yr = r / wp;
-    const int xe = xa + 2 * (int)(r - yr * wp), y = rect.z + (int)yr;
-    bool live[2], only[2];
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        const int x = xe + k;
-        live[k] = x >= rect.x && x < rect.y && !(x >= skip.x && x < skip.y && y >= skip.z && y < skip.w);
-        only[k] = live[k] && x >= raw.x && x < raw.y && y >= raw.z && y < raw.w;
-    }
-    if (!live[0] && !live[1]) return;
-    Sgs<F2> s2;
-    s2.tau0 = sgs.tau0;
-    s2.c18 = sgs.c18;
-    stream_collide_pair(src, dst, flags, G, shift, omega_s, omega_b, xe, y, z, live[0], live[1], only[0], only[1],
-                        s2);
+    PairItem it;
+    if (!pair_item(G, raw, rect, skip, i, it)) return;
+    stream_collide_pair(src, dst, flags, G, shift, omega_s, omega_b, sgs, raw, it);
 }
 
-// items of one stream-collide launch over the padded columns rect (rect.y ==
-// 0: the interior): cells, or cell pairs (xe even) for the pair forms
-template <typename S>
-__host__ __device__ __forceinline__ long long stream_collide_items(int4 rect, int nx, int ny, int nz) {
-    if (rect.y == 0) rect = make_int4(1, nx + 1, 1, ny + 1);
-    const long long h = rect.w - rect.z;
-    if constexpr (pair_form<S>()) return (long long)((((rect.y + 1) & ~1) - (rect.x & ~1)) / 2) * h * nz;
-    return (long long)(rect.y - rect.x) * h * nz;
+// A pair-form launch as a grid-stride loop over its items.  The FP16 form
+// loads the next item's pulls before it collides the current one (27
+// packed words), so that every thread keeps two pairs' loads in flight: the
+// kernel is bound by memory latency, not by issue.
+template <typename S, typename Shift>
+__device__ __forceinline__ void stream_collide_pairs(const S *__restrict__ src, S *__restrict__ dst,
+                                                     const uint8_t *__restrict__ flags, const Grid &G,
+                                                     const Shift &shift, float omega_s, float omega_b,
+                                                     const Sgs<float> &sgs, int4 raw, int4 rect, int4 skip) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if constexpr (std::is_same_v<S, __half>) {
+        Sgs<F2> s2;
+        s2.tau0 = sgs.tau0;
+        s2.c18 = sgs.c18;
+        PairItem it;
+        bool ok = pair_item(G, raw, rect, skip, i, it);
+        PairRaw<S> cur;
+        if (ok && !it.only) pair_load(src, G, it.xe, it.y, it.z, it.live0, it.live1, cur);
+        const long long n = stream_collide_items<S>(rect, G.nx, G.ny, G.nz);
+        for (; i < n; i += stride) {
+            PairItem nt;
+            const bool nok = pair_item(G, raw, rect, skip, i + stride, nt);
+            PairRaw<S> next;
+            if (nok && !nt.only) pair_load(src, G, nt.xe, nt.y, nt.z, nt.live0, nt.live1, next);
+            if (ok) {
+                if (it.only)
+                    stream_collide_pair(src, dst, flags, G, shift, omega_s, omega_b, sgs, raw, it);
+                else
+                    pair_collide_store(cur, dst, flags, G, shift, omega_s, omega_b, it.xe, it.y, it.z, it.live0,
+                                       it.live1, s2);
+            }
+            ok = nok;
+            it = nt;
+            cur = next;
+        }
+    } else {
+        const long long n = stream_collide_items<S>(rect, G.nx, G.ny, G.nz);
+        for (; i < n; i += stride) {
+            PairItem it;
+            if (pair_item(G, raw, rect, skip, i, it))
+                stream_collide_pair(src, dst, flags, G, shift, omega_s, omega_b, sgs, raw, it);
+        }
+    }
 }
 
 // resident 128-thread blocks per SM the stream-collide is compiled for: the
@@ -320,14 +439,13 @@ __global__ void __launch_bounds__(128, stream_collide_min_blocks<S>())
     // launch
     if (rect.y == 0) rect = make_int4(1, G.nx + 1, 1, G.ny + 1);
     if constexpr (pair_form<S>()) {
-        stream_collide_pair_item(src, dst, flags, G, shift, omega_s, omega_b, sgs, raw, rect, skip,
-                                 (long long)blockIdx.x * blockDim.x + threadIdx.x);
+        stream_collide_pairs(src, dst, flags, G, shift, omega_s, omega_b, sgs, raw, rect, skip);
         return;
     }
     const unsigned w = (unsigned)(rect.y - rect.x), h = (unsigned)(rect.w - rect.z);
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned nxy = w * h;
-    double acc[CELL_STATS] = {0, 0, 0, 0, 0, 0, 0, 0};
+    FusedStats acc;
     bool active = i < nxy * (unsigned)G.nz;
     int x = 0, y = 0, z = 0;
     if (active) {
@@ -346,9 +464,9 @@ __global__ void __launch_bounds__(128, stream_collide_min_blocks<S>())
         // only streamed (they keep pre-collision populations)
         const bool stream_only = x >= raw.x && x < raw.y && y >= raw.z && y < raw.w;
         stream_collide_cell(src, dst, flags, G, shift, omega_s, omega_b, x, y, z, sgs, stream_only,
-                            STATS ? acc : nullptr);
+                            STATS ? &acc : nullptr);
     }
-    if constexpr (STATS) block_cell_stats(acc, stats, blockIdx.x);
+    if constexpr (STATS) block_fused_stats(acc, stats, blockIdx.x);
 }
 
 // ------------------------------------------------------------ walls
