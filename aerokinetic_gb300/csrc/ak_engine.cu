@@ -52,17 +52,10 @@ long long blocks_for(long long n, int threads) { return (n + threads - 1) / thre
 
 namespace {
 // grid of a stream-collide launch of 128-thread blocks over rect: one block
-// per 128 items (cells, or cell pairs), or with persistent for the pair
-// forms a single wave of blocks (every SM's resident blocks) that strides
-// over the pairs, so that the FP16 form's prefetch has a next pair.  A launch
-// that must yield SM slots to other kernels as its blocks finish (the
-// two-level step's coarse pass) is not persistent.
+// per 128 items (cells, or cell pairs in the pair forms)
 template <typename S>
-unsigned stream_collide_grid(int4 rect, int nx, int ny, int nz, int sms, bool persistent) {
-    const long long full = blocks_for(stream_collide_items<S>(rect, nx, ny, nz), 128);
-    if constexpr (pair_form<S>())
-        if (persistent) return (unsigned)std::max(1LL, std::min(full, (long long)sms * stream_collide_min_blocks<S>()));
-    return (unsigned)full;
+unsigned stream_collide_grid(int4 rect, int nx, int ny, int nz) {
+    return (unsigned)blocks_for(stream_collide_items<S>(rect, nx, ny, nz), 128);
 }
 // fixed grid of the per-case reductions whose results must not depend on the device
 constexpr int STATS_BLOCKS_CASE = 4 * 152;
@@ -123,7 +116,6 @@ struct ak_case {
     long long pdf_writes = 0;  // population writes from outside the step (set_pdf, init)
     bool prepared = false;
     int device = 0;  // CUDA device current when the case was created
-    int sms = 152;   // its streaming multiprocessors
     // stationarity residuals: the owned region (interior coordinates, an
     // excluded rectangle) and the device snapshot of (rho, j / U) per cell
     int res_region[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -605,7 +597,7 @@ int one_step(ak_case *c, bool sample, double *fixed_partials = nullptr, long lon
     }
     // bulk
     mark(c);
-    const unsigned grid = stream_collide_grid<S>(make_int4(0, 0, 0, 0), c->nx, c->ny, c->nz, c->sms, true);
+    const unsigned grid = stream_collide_grid<S>(make_int4(0, 0, 0, 0), c->nx, c->ny, c->nz);
     k_stream_collide<S><<<grid, 128, 0, c->stream>>>(src, dst_of<S>(c), c->flags, c->G, c->shift_host,
                                                      (T)c->omega_s, (T)c->omega_b, sgs_of<S>(c));
     AK_CUDA(cudaGetLastError());
@@ -735,7 +727,7 @@ int exterior_step(ak_case *c, double *fixed_partials, long long fixed_capacity, 
     AK_CUDA(cudaGetLastError());
     c->launches += 2;
     mark(c);
-    const unsigned grid = stream_collide_grid<S>(make_int4(0, 0, 0, 0), c->nx, c->ny, c->nz, c->sms, true);
+    const unsigned grid = stream_collide_grid<S>(make_int4(0, 0, 0, 0), c->nx, c->ny, c->nz);
     k_stream_collide<S><<<grid, 128, 0, c->stream>>>(src, dst, c->flags, c->G, c->shift_host, (T)c->omega_s,
                                                      (T)c->omega_b, Sgs<T>{});
     AK_CUDA(cudaGetLastError());
@@ -958,8 +950,6 @@ int create_lattice(const ak_case_desc *desc, int farfield, bool periodic_xy, ak_
     }
     int r = AK_OK;
     if (cudaGetDevice(&c->device) != cudaSuccess) r = fail(AK_ERR_CUDA, "no current CUDA device");
-    if (r == AK_OK && cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess)
-        r = fail(AK_ERR_CUDA, "multiprocessor count query failed");
     if (r == AK_OK && cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         r = fail(AK_ERR_CUDA, "stream creation failed (no CUDA device?)");
     }
@@ -1907,8 +1897,8 @@ int refined_step(ak_refined *R, bool fork = false) {
     const unsigned gx1 = (unsigned)blocks_for((long long)(R->xfer.y - R->xfer.x) * (R->xfer.w - R->xfer.z) * C->nz, 128);
     // the stream-collide's grids (cells, or cell pairs in the pair forms):
     // the whole lattice and the near part
-    const unsigned gsc = stream_collide_grid<S>(make_int4(0, 0, 0, 0), C->nx, C->ny, C->nz, C->sms, false);
-    const unsigned gsn = stream_collide_grid<S>(R->near, C->nx, C->ny, C->nz, C->sms, false);
+    const unsigned gsc = stream_collide_grid<S>(make_int4(0, 0, 0, 0), C->nx, C->ny, C->nz);
+    const unsigned gsn = stream_collide_grid<S>(R->near, C->nx, C->ny, C->nz);
     // fork mode, fused form, transfer block away from the outer faces: the
     // boundaries and the far coarse pass on their own branch
     const bool bnd = fork && R->fused && R->bnd_branch;
@@ -2135,7 +2125,7 @@ int refined_step(ak_refined *R, bool fork = false) {
 template <typename S>
 int graph_priorities(ak_refined *R, cudaGraph_t g) {
     ak_case *C = R->coarse;
-    const unsigned far_grid = stream_collide_grid<S>(make_int4(0, 0, 0, 0), C->nx, C->ny, C->nz, C->sms, false);
+    const unsigned far_grid = stream_collide_grid<S>(make_int4(0, 0, 0, 0), C->nx, C->ny, C->nz);
     int least = 0, greatest = 0;
     AK_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
     size_t n = 0;

@@ -141,15 +141,17 @@ __device__ void block_fused_stats(const FusedStats &s, double *out, long long ro
 
 // pull the 27 populations of interior cell (x, y, z) (padded x, y), collide,
 // store into dst if the column is fluid; stream_only: store the pulled values
-// as they are (bit copies, no collision); acc (optional): add the collided
-// cell's statistics (mass and momentum are those the collision conserves)
+// as they are (bit copies, no collision); mac (optional): where the
+// collision writes the cell's (drho, j, |u|^2) as soon as it has them (a
+// shared-memory row, so that they hold no register through the rest of the
+// collision).  Returns true for a collided fluid cell.
 template <typename S, typename Shift>
-__device__ __forceinline__ void stream_collide_cell(const S *__restrict__ src, S *__restrict__ dst,
+__device__ __forceinline__ bool stream_collide_cell(const S *__restrict__ src, S *__restrict__ dst,
                                                     const uint8_t *__restrict__ flags, const Grid &G,
                                                     const Shift &shift, typename Store<S>::T omega_s,
                                                     typename Store<S>::T omega_b, int x, int y, int z,
                                                     const Sgs<typename Store<S>::T> &sgs,
-                                                    bool stream_only = false, FusedStats *acc = nullptr) {
+                                                    bool stream_only = false, typename Store<S>::T *mac = nullptr) {
     using T = typename Store<S>::T;
     // the column flag only gates the stores, so the 27 loads issue at once
     const bool fluid = __ldg(flags + y * G.nxp + x) == FLAG_FLUID;
@@ -159,12 +161,12 @@ __device__ __forceinline__ void stream_collide_cell(const S *__restrict__ src, S
 #pragma unroll
     for (int c = 0; c < 3; ++c) row[c] = src + (long long)G.wrapz(z - (c - 1)) * G.plane + (long long)y * G.sx + x;
     if (stream_only) {
-        if (!fluid) return;
+        if (!fluid) return false;
         const long long c = G.cell(x, y, z);
 #pragma unroll
         for (int q = 0; q < Q; ++q)
             dst[q * G.qs + c] = row[cz(q) + 1][(long long)q * G.qs - (long long)cy(q) * G.sx - cx(q)];
-        return;
+        return false;
     }
     T g[Q];
 #pragma unroll
@@ -174,13 +176,12 @@ __device__ __forceinline__ void stream_collide_cell(const S *__restrict__ src, S
                    ? Store<S>::load(row[cz(q) + 1] + off, q, shift_at(shift, q))
                    : T(0);
     }
-    T mac[5];
-    collide_stored<S>(g, omega_s, omega_b, sgs, acc ? mac : nullptr);
-    if (!fluid) return;
-    if (acc) add_fused_stats(*acc, (double)mac[0], (double)mac[1], (double)mac[2], (double)mac[3], (double)mac[4]);
+    collide_stored<S>(g, omega_s, omega_b, sgs, mac);
+    if (!fluid) return false;
     const long long c = G.cell(x, y, z);
 #pragma unroll
     for (int q = 0; q < Q; ++q) Store<S>::store(dst + q * G.qs + c, q, g[q], shift_at(shift, q));
+    return true;
 }
 
 // ------------------------------------------------------------ cell pairs
@@ -219,8 +220,7 @@ __host__ __device__ __forceinline__ long long stream_collide_items(int4 rect, in
 }
 
 // The 27 pulled populations of a cell pair as loaded: FP16 pairs packed in
-// one 32-bit word each (so that a thread can hold the next pair's while it
-// collides the current one), FP32 pairs as float2.
+// one 32-bit word each, FP32 pairs as float2.
 template <typename S> struct PairRaw;
 template <> struct PairRaw<__half> { unsigned v[Q]; };
 template <> struct PairRaw<float> { float2 v[Q]; };
@@ -369,52 +369,6 @@ __device__ __forceinline__ void stream_collide_pair_item(const S *__restrict__ s
     stream_collide_pair(src, dst, flags, G, shift, omega_s, omega_b, sgs, raw, it);
 }
 
-// A pair-form launch as a grid-stride loop over its items.  The FP16 form
-// loads the next item's pulls before it collides the current one (27
-// packed words), so that every thread keeps two pairs' loads in flight: the
-// kernel is bound by memory latency, not by issue.
-template <typename S, typename Shift>
-__device__ __forceinline__ void stream_collide_pairs(const S *__restrict__ src, S *__restrict__ dst,
-                                                     const uint8_t *__restrict__ flags, const Grid &G,
-                                                     const Shift &shift, float omega_s, float omega_b,
-                                                     const Sgs<float> &sgs, int4 raw, int4 rect, int4 skip) {
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if constexpr (std::is_same_v<S, __half>) {
-        Sgs<F2> s2;
-        s2.tau0 = sgs.tau0;
-        s2.c18 = sgs.c18;
-        PairItem it;
-        bool ok = pair_item(G, raw, rect, skip, i, it);
-        PairRaw<S> cur;
-        if (ok && !it.only) pair_load(src, G, it.xe, it.y, it.z, it.live0, it.live1, cur);
-        const long long n = stream_collide_items<S>(rect, G.nx, G.ny, G.nz);
-        for (; i < n; i += stride) {
-            PairItem nt;
-            const bool nok = pair_item(G, raw, rect, skip, i + stride, nt);
-            PairRaw<S> next;
-            if (nok && !nt.only) pair_load(src, G, nt.xe, nt.y, nt.z, nt.live0, nt.live1, next);
-            if (ok) {
-                if (it.only)
-                    stream_collide_pair(src, dst, flags, G, shift, omega_s, omega_b, sgs, raw, it);
-                else
-                    pair_collide_store(cur, dst, flags, G, shift, omega_s, omega_b, it.xe, it.y, it.z, it.live0,
-                                       it.live1, s2);
-            }
-            ok = nok;
-            it = nt;
-            cur = next;
-        }
-    } else {
-        const long long n = stream_collide_items<S>(rect, G.nx, G.ny, G.nz);
-        for (; i < n; i += stride) {
-            PairItem it;
-            if (pair_item(G, raw, rect, skip, i, it))
-                stream_collide_pair(src, dst, flags, G, shift, omega_s, omega_b, sgs, raw, it);
-        }
-    }
-}
-
 // resident 128-thread blocks per SM the stream-collide is compiled for: the
 // pair forms hold two cells' populations per thread
 template <typename S>
@@ -439,14 +393,16 @@ __global__ void __launch_bounds__(128, stream_collide_min_blocks<S>())
     // launch
     if (rect.y == 0) rect = make_int4(1, G.nx + 1, 1, G.ny + 1);
     if constexpr (pair_form<S>()) {
-        stream_collide_pairs(src, dst, flags, G, shift, omega_s, omega_b, sgs, raw, rect, skip);
+        stream_collide_pair_item(src, dst, flags, G, shift, omega_s, omega_b, sgs, raw, rect, skip,
+                                 (long long)blockIdx.x * blockDim.x + threadIdx.x);
         return;
     }
     const unsigned w = (unsigned)(rect.y - rect.x), h = (unsigned)(rect.w - rect.z);
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned nxy = w * h;
-    FusedStats acc;
-    bool active = i < nxy * (unsigned)G.nz;
+    using T = typename Store<S>::T;
+    __shared__ T mac[STATS ? 128 : 1][5];
+    bool active = i < nxy * (unsigned)G.nz, counted = false;
     int x = 0, y = 0, z = 0;
     if (active) {
         z = (int)(i / nxy);
@@ -463,10 +419,16 @@ __global__ void __launch_bounds__(128, stream_collide_min_blocks<S>())
         // raw: the padded x [raw.x, raw.y) by y [raw.z, raw.w) columns are
         // only streamed (they keep pre-collision populations)
         const bool stream_only = x >= raw.x && x < raw.y && y >= raw.z && y < raw.w;
-        stream_collide_cell(src, dst, flags, G, shift, omega_s, omega_b, x, y, z, sgs, stream_only,
-                            STATS ? &acc : nullptr);
+        counted = stream_collide_cell(src, dst, flags, G, shift, omega_s, omega_b, x, y, z, sgs, stream_only,
+                                      STATS ? mac[threadIdx.x] : nullptr);
     }
-    if constexpr (STATS) block_fused_stats(acc, stats, blockIdx.x);
+    if constexpr (STATS) {
+        FusedStats acc;
+        if (counted)
+            add_fused_stats(acc, (double)mac[threadIdx.x][0], (double)mac[threadIdx.x][1], (double)mac[threadIdx.x][2],
+                            (double)mac[threadIdx.x][3], (double)mac[threadIdx.x][4]);
+        block_fused_stats(acc, stats, blockIdx.x);
+    }
 }
 
 // ------------------------------------------------------------ walls
