@@ -2,8 +2,8 @@
 
 The reference runs one case per process (src/aerokinetic/cli.py:121-139); a
 polar sweep is many such runs.  Here a Batch borrows several Solver objects
-(uniform grid, characteristic farfield, one storage form) and steps them with
-one set of launches per step over packed work tables (include/
+(uniform grid, characteristic or legacy outer boundary, one storage form) and
+steps them with one set of launches per step over packed work tables (include/
 aerokinetic_gb300.h, ak_batch_*).  Every case computes the same bits as it
 would alone, so each Solver's state, diagnostics and frames stay valid.
 """

@@ -150,27 +150,30 @@ class Plan:
         tau = 0.5 + 3 * nu
         dt = flow.lattice_speed / n
         dt_s = None if flow.physical_speed is None else dt * flow.physical_chord_m / flow.physical_speed
-        notes = ["Uniform isotropic grid; no mesh refinement or wall model.",
-                 "Accuracy is unvalidated until grid/domain/span/Mach/statistical convergence and tunnel comparison.",
-                 "The initial spanwise perturbation is numerical seeding, not a specified tunnel turbulence spectrum."]
+        notes = ["One lattice spacing everywhere; walls by interpolated bounce-back, without a wall model "
+                 "(two-level refinement is a separate RefinedSolver case).",
+                 "The coefficients are lattice results: convergence in grid, domain, span, Mach number and averaging "
+                 "window, and agreement with experiment, are for the user to establish.",
+                 "The seeded spanwise perturbation only breaks the initial symmetry; it models no inflow turbulence."]
         if grid.farfield != "legacy":
             if min(grid.upstream_chords, grid.downstream_chords, grid.transverse_chords) * n < 2:
                 raise ValueError("Characteristic farfield needs at least two fluid cells between body bounds and exterior")
             if grid.farfield == EXTERIOR_FARFIELD:
                 if flow.sgs != "none":
                     raise ValueError("Exterior FD currently supports molecular viscosity with sgs=none only")
-                notes.append("Research exterior_regularized_fd_v1; physical shape unchanged, auxiliary ring of one "
-                             "cell in x and y; explicit exterior source. Uniform grids only; no validated airfoil "
-                             "accuracy or full viscous NSCBC.")
+                notes.append("exterior_regularized_fd_v1: the physical lattice keeps its shape; one auxiliary ring of "
+                             "cells in x and y is rebuilt every step from a predicted state, and the source this adds "
+                             "is reported. Uniform grids only; its airfoil accuracy is not established.")
             else:
-                notes.append("Experimental characteristic_transport_v1 farfield with linearized transverse "
-                             "transport; not full viscous NSCBC or validated airfoil accuracy.")
+                notes.append("characteristic_transport_v1: per-link Riemann invariants with a linearised transverse "
+                             "term, not a viscous characteristic boundary; its airfoil accuracy is not established.")
         if n < 256:
-            notes.append("Fewer than 256 cells/chord: use for development; do not assume a resolved boundary layer.")
+            notes.append("Below 256 cells per chord the boundary layer is not resolved; treat results as development runs.")
         if tau < 0.501:
-            notes.append("Relaxation time is close to 0.5; low-viscosity stability and resolution require special checks.")
+            notes.append("The relaxation time is within 1e-3 of 0.5: shear modes are barely damped, so watch the Mach "
+                         "and density guards and the resolution.")
         if flow.physical_speed is None:
-            notes.append("Physical chord unspecified; time is t*=t U/c only, with no invented dimensional seconds.")
+            notes.append("No physical chord given: time is reported as t* = t U / c only.")
         else:
             atm = flow.atmosphere
             mean_free_path = atm.dynamic_viscosity / atm.pressure_pa * math.sqrt(

@@ -3,9 +3,10 @@
 //
 // A batch holds a device array of per-case descriptors (BatchCase) and, for
 // every kernel of the uniform step, a packed work table of (case, chunk)
-// items: the characteristic farfield's ring macros and links, the Bouzidi
-// wall links and the fused stream-collide blocks.  A step is therefore four
-// launches (five when loads are sampled) whatever the number of cases, each
+// items: the characteristic farfield's ring macros and links, the legacy
+// boundary's UBB cells and outflow links, the Bouzidi wall links and the
+// fused stream-collide blocks.  A step is therefore four to six launches
+// (one more when loads are sampled) whatever the number of cases, each
 // kernel running the same per-item body as the single-case kernel
 // (ak_kernels.cuh) on the item's case, so a case computes the same bits alone
 // and in any mix.  The stream-collide launch is persistent: a fixed grid of
@@ -26,6 +27,13 @@ struct BatchCase {
     int cur0;  // copy holding the case's state at batch parity 0
     int n_elements;
     double ox, oy;
+    // legacy outer boundary (UBB cells, outflow links and their history)
+    const int *ubb_cells;
+    long long n_ubb_cells;
+    double speed;
+    const int *sel_out;
+    long long n_out;
+    double *out_state;
     // characteristic farfield
     OuterLinks L;
     FarfieldParams P;
@@ -69,6 +77,28 @@ __global__ void __launch_bounds__(256)
     const long long i = (long long)w.chunk * blockDim.x + threadIdx.x;
     if (i >= c.L.n) return;
     farfield_link(batch_src(c, parity), c.G, c.L, c.P, c.R, c.ff_in, c.ff_der, c.ff_clock, c.ff_lo, c.ff_hi, 0, i);
+}
+
+// legacy outer boundary: UBB (solver.py:131) then the ExtrapolationOutflow,
+// in the single-case step's order
+template <typename S>
+__global__ void __launch_bounds__(256)
+    k_batch_ubb(const BatchCase<S> *__restrict__ cases, const WorkItem *__restrict__ work, int parity) {
+    const WorkItem w = work[blockIdx.x];
+    const BatchCase<S> &c = cases[w.c];
+    const long long i = (long long)w.chunk * blockDim.x + threadIdx.x;
+    if (i >= c.n_ubb_cells * c.G.nz) return;
+    ubb_item(batch_src(c, parity), c.G, c.ubb_cells, c.n_ubb_cells, c.speed, 0.0, 0.0, i);
+}
+
+template <typename S>
+__global__ void __launch_bounds__(256)
+    k_batch_outflow(const BatchCase<S> *__restrict__ cases, const WorkItem *__restrict__ work, int parity) {
+    const WorkItem w = work[blockIdx.x];
+    const BatchCase<S> &c = cases[w.c];
+    const long long i = (long long)w.chunk * blockDim.x + threadIdx.x;
+    if (i >= c.n_out) return;
+    outflow_item(batch_src(c, parity), c.G, c.L, c.sel_out, c.out_state, 1, 0, 0, i);
 }
 
 template <typename S>

@@ -2367,9 +2367,10 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
         if (r == AK_OK && R->fused) {
             // rows of the fused pass's statistics: its far launch (a grid over
             // the whole coarse lattice), its near launch, the band's blocks
+            // one row per warp of the far and near launches
             const int4 nr = R->near;
-            R->cstats_far = blocks_for((long long)cd.nx * cd.ny * cd.nz, 128);
-            R->cstats_near = blocks_for((long long)(nr.y - nr.x) * (nr.w - nr.z) * cd.nz, 128);
+            R->cstats_far = 4 * blocks_for((long long)cd.nx * cd.ny * cd.nz, 128);
+            R->cstats_near = 4 * blocks_for((long long)(nr.y - nr.x) * (nr.w - nr.z) * cd.nz, 128);
             const long long rows = R->cstats_far + R->cstats_near + STATS_BLOCKS;
             r = ralloc(R, &R->cstats, (size_t)rows * NSTAT);
             if (r == AK_OK) r = ralloc(R, &R->cstats_stage, (size_t)blocks_for(rows, REDUCE_THREADS) * NSTAT);
@@ -2662,8 +2663,9 @@ struct ak_batch {
     int storage = 0, device = 0, sms = 0;
     cudaStream_t stream = nullptr;
     void *d_cases = nullptr;
-    WorkItem *w_ring = nullptr, *w_ff = nullptr, *w_walls = nullptr, *w_bulk = nullptr;
-    long long n_ring = 0, n_ff = 0, n_walls = 0, n_bulk = 0;
+    WorkItem *w_ring = nullptr, *w_ff = nullptr, *w_walls = nullptr, *w_bulk = nullptr, *w_ubb = nullptr,
+             *w_out = nullptr;
+    long long n_ring = 0, n_ff = 0, n_walls = 0, n_bulk = 0, n_ubb = 0, n_out = 0;
     double *loads = nullptr;  // [case][MAX_ELEMENTS * 5]
     int parity = 0;
     long long steps = 0, launches = 0;
@@ -2690,7 +2692,7 @@ void batch_release(ak_batch *B) {
     if (B->stream) cudaStreamSynchronize(B->stream);
     batch_drop_graphs(B);
     for (void *p : {(void *)B->d_cases, (void *)B->w_ring, (void *)B->w_ff, (void *)B->w_walls, (void *)B->w_bulk,
-                    (void *)B->loads})
+                    (void *)B->w_ubb, (void *)B->w_out, (void *)B->loads})
         if (p) cudaFree(p);
     if (B->ev_fork) cudaEventDestroy(B->ev_fork);
     if (B->ev_join) cudaEventDestroy(B->ev_join);
@@ -2785,6 +2787,14 @@ int batch_enqueue(ak_batch *B, int parity, bool sample, bool branch = false) {
         k_batch_farfield<S><<<(unsigned)B->n_ff, 256, 0, B->stream>>>(cases, B->w_ff, parity);
         AK_CUDA(cudaGetLastError());
     }
+    if (B->n_ubb) {
+        k_batch_ubb<S><<<(unsigned)B->n_ubb, 256, 0, B->stream>>>(cases, B->w_ubb, parity);
+        AK_CUDA(cudaGetLastError());
+    }
+    if (B->n_out) {
+        k_batch_outflow<S><<<(unsigned)B->n_out, 256, 0, B->stream>>>(cases, B->w_out, parity);
+        AK_CUDA(cudaGetLastError());
+    }
     if (B->n_walls) {
         k_batch_walls<S><<<(unsigned)B->n_walls, 256, 0, ws>>>(cases, B->w_walls, parity, sample ? 1 : 0);
         AK_CUDA(cudaGetLastError());
@@ -2803,13 +2813,14 @@ int batch_enqueue(ak_batch *B, int parity, bool sample, bool branch = false) {
 }
 
 long long batch_step_launches(const ak_batch *B, bool sample) {
-    return (B->n_ring ? 1 : 0) + (B->n_ff ? 1 : 0) + (B->n_walls ? 1 : 0) + (sample ? 1 : 0) + 1;
+    return (B->n_ring ? 1 : 0) + (B->n_ff ? 1 : 0) + (B->n_ubb ? 1 : 0) + (B->n_out ? 1 : 0) + (B->n_walls ? 1 : 0) +
+           (sample ? 1 : 0) + 1;
 }
 
 template <typename S>
 int batch_build(ak_batch *B) {
     std::vector<BatchCase<S>> host;
-    std::vector<long long> ring, ff, walls;
+    std::vector<long long> ring, ff, walls, ubb, outflow;
     for (size_t i = 0; i < B->cases.size(); ++i) {
         ak_case *c = B->cases[i];
         BatchCase<S> d{};
@@ -2824,6 +2835,12 @@ int batch_build(ak_batch *B) {
         d.n_elements = c->n_elements;
         d.ox = c->ox;
         d.oy = c->oy;
+        d.ubb_cells = c->ubb_cells;
+        d.n_ubb_cells = c->n_ubb_cells;
+        d.speed = c->speed;
+        d.sel_out = c->sel_out;
+        d.n_out = c->n_out;
+        d.out_state = c->out_state;
         d.L = c->outer();
         d.P = c->ff();
         d.R = c->ring();
@@ -2840,19 +2857,27 @@ int batch_build(ak_batch *B) {
         if (nlinks) AK_TRY(ensure_partials(c, d.wall_blocks * 5 * c->n_elements));
         d.partials = c->partials;
         host.push_back(d);
-        ring.push_back(c->ring_n * c->nz);
-        ff.push_back(c->nouter);
+        const bool legacy = c->farfield == AK_FARFIELD_LEGACY;
+        ring.push_back(legacy ? 0 : c->ring_n * c->nz);
+        ff.push_back(legacy ? 0 : c->nouter);
+        ubb.push_back(legacy ? c->n_ubb_cells * c->nz : 0);
+        outflow.push_back(legacy ? c->n_out : 0);
         walls.push_back(nlinks);
     }
     AK_CUDA(cudaMalloc(&B->d_cases, host.size() * sizeof(BatchCase<S>)));
     AK_CUDA(cudaMemcpy(B->d_cases, host.data(), host.size() * sizeof(BatchCase<S>), cudaMemcpyHostToDevice));
-    const std::vector<WorkItem> tr = chunk_table(ring), tf = chunk_table(ff), tw = chunk_table(walls);
+    const std::vector<WorkItem> tr = chunk_table(ring), tf = chunk_table(ff), tw = chunk_table(walls),
+                                tu = chunk_table(ubb), to = chunk_table(outflow);
     B->n_ring = (long long)tr.size();
     B->n_ff = (long long)tf.size();
     B->n_walls = (long long)tw.size();
+    B->n_ubb = (long long)tu.size();
+    B->n_out = (long long)to.size();
     AK_TRY(upload_work(&B->w_ring, tr));
     AK_TRY(upload_work(&B->w_ff, tf));
     AK_TRY(upload_work(&B->w_walls, tw));
+    AK_TRY(upload_work(&B->w_ubb, tu));
+    AK_TRY(upload_work(&B->w_out, to));
     const std::vector<WorkItem> tb = bulk_table(B, B->tb, B->order);
     B->n_bulk = (long long)tb.size();
     AK_TRY(upload_work(&B->w_bulk, tb));
@@ -2934,8 +2959,8 @@ int ak_batch_create(ak_case *const *cases, int32_t n, ak_batch **out) {
             r = fail(AK_ERR_INVALID, "null case in the batch");
         else if (i && (c->storage != cases[0]->storage || c->device != cases[0]->device))
             r = fail(AK_ERR_INVALID, "the cases of a batch share one storage form and one device");
-        else if (c->farfield != AK_FARFIELD_CHARACTERISTIC || c->periodic_xy)
-            r = fail(AK_ERR_INVALID, "batches hold uniform cases with the characteristic farfield");
+        else if ((c->farfield != AK_FARFIELD_CHARACTERISTIC && c->farfield != AK_FARFIELD_LEGACY) || c->periodic_xy)
+            r = fail(AK_ERR_INVALID, "batches hold uniform cases with the characteristic or the legacy outer boundary");
         else if (std::find(B->cases.begin(), B->cases.end(), c) != B->cases.end())
             r = fail(AK_ERR_INVALID, "a case appears twice in the batch");
         else
@@ -2955,7 +2980,25 @@ int ak_batch_create(ak_case *const *cases, int32_t n, ak_batch **out) {
     for (size_t i = 0; r == AK_OK && i < B->cases.size(); ++i) {
         ak_case *c = B->cases[i];
         if (!c->prepared)
-            r = with_storage(c, [&](auto *tag) { return prepare_boundaries<std::remove_pointer_t<decltype(tag)>>(c); });
+            r = with_storage(c, [&](auto *tag) {
+                using S = std::remove_pointer_t<decltype(tag)>;
+                if (c->farfield != AK_FARFIELD_LEGACY) return prepare_boundaries<S>(c);
+                // a legacy case that has not stepped: its outflow history is
+                // seeded as the first step seeds it, after the UBB (which the
+                // batch's first step applies again to the same state, writing
+                // the same values)
+                const int TB = 256;
+                if (c->n_ubb)
+                    k_ubb<S><<<(unsigned)blocks_for(c->n_ubb_cells * c->nz, TB), TB, 0, c->stream>>>(
+                        src_of<S>(c), c->G, c->ubb_cells, c->n_ubb_cells, c->speed, 0.0, 0.0);
+                if (c->n_out)
+                    k_outflow_prepare<S><<<(unsigned)blocks_for(c->n_out, TB), TB, 0, c->stream>>>(
+                        src_of<S>(c), c->G, c->outer(), c->sel_out, c->n_out, c->out_state, 1, 0, 0, 1.0, c->speed,
+                        0.0, 0.0);
+                AK_CUDA(cudaGetLastError());
+                c->prepared = true;
+                return AK_OK;
+            });
         if (r == AK_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) r = fail(AK_ERR_CUDA, "case sync failed");
         B->cur0.push_back(c->cur);
     }

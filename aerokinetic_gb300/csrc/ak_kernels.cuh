@@ -132,11 +132,31 @@ __device__ __forceinline__ void add_fused_stats(FusedStats &a, double drho, doub
     a.dr = max(a.dr, __double_as_longlong(drho) & 0x7fffffffffffffffLL);
     ++a.cells;
 }
-// the block's statistics row in the CELL_STATS layout (every thread calls it)
-__device__ void block_fused_stats(const FusedStats &s, double *out, long long row) {
-    double a[CELL_STATS] = {__longlong_as_double(s.u2), __longlong_as_double(s.dr), s.drho, s.jx, s.jy, s.jz,
-                            (double)s.cells, (double)s.bad};
-    block_cell_stats(a, out, row);
+// the warp's statistics row in the CELL_STATS layout (every lane calls it;
+// no block-wide barrier): shuffle sums in a fixed order, integer maxima
+__device__ __forceinline__ void warp_fused_stats(FusedStats s, double *out, long long row) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s.drho += __shfl_down_sync(0xffffffffu, s.drho, o);
+        s.jx += __shfl_down_sync(0xffffffffu, s.jx, o);
+        s.jy += __shfl_down_sync(0xffffffffu, s.jy, o);
+        s.jz += __shfl_down_sync(0xffffffffu, s.jz, o);
+        s.u2 = max(s.u2, __shfl_down_sync(0xffffffffu, s.u2, o));
+        s.dr = max(s.dr, __shfl_down_sync(0xffffffffu, s.dr, o));
+        s.cells += __shfl_down_sync(0xffffffffu, s.cells, o);
+        s.bad += __shfl_down_sync(0xffffffffu, s.bad, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        double *r = out + row * CELL_STATS;
+        r[0] = __longlong_as_double(s.u2);
+        r[1] = __longlong_as_double(s.dr);
+        r[2] = s.drho;
+        r[3] = s.jx;
+        r[4] = s.jy;
+        r[5] = s.jz;
+        r[6] = (double)s.cells;
+        r[7] = (double)s.bad;
+    }
 }
 
 // pull the 27 populations of interior cell (x, y, z) (padded x, y), collide,
@@ -376,8 +396,9 @@ __host__ __device__ constexpr int stream_collide_min_blocks() {
     return pair_form<S>() ? 4 : Store<S>::MIN_BLOCKS;
 }
 
-// STATS: every block also writes the statistics of the cells it collided
-// (not the streamed-only ones) to stats[blockIdx.x] (CELL_STATS each)
+// STATS: every warp also writes the statistics of the cells it collided
+// (not the streamed-only ones) to stats[blockIdx.x * 4 + warp] (CELL_STATS
+// each)
 template <typename S, bool STATS = false>
 __global__ void __launch_bounds__(128, stream_collide_min_blocks<S>())
     k_stream_collide(const S *__restrict__ src, S *__restrict__ dst, const uint8_t *__restrict__ flags, Grid G,
@@ -401,7 +422,7 @@ __global__ void __launch_bounds__(128, stream_collide_min_blocks<S>())
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned nxy = w * h;
     using T = typename Store<S>::T;
-    __shared__ T mac[STATS ? 128 : 1][5];
+    T mac[5];
     bool active = i < nxy * (unsigned)G.nz, counted = false;
     int x = 0, y = 0, z = 0;
     if (active) {
@@ -420,14 +441,12 @@ __global__ void __launch_bounds__(128, stream_collide_min_blocks<S>())
         // only streamed (they keep pre-collision populations)
         const bool stream_only = x >= raw.x && x < raw.y && y >= raw.z && y < raw.w;
         counted = stream_collide_cell(src, dst, flags, G, shift, omega_s, omega_b, x, y, z, sgs, stream_only,
-                                      STATS ? mac[threadIdx.x] : nullptr);
+                                      STATS ? mac : nullptr);
     }
     if constexpr (STATS) {
         FusedStats acc;
-        if (counted)
-            add_fused_stats(acc, (double)mac[threadIdx.x][0], (double)mac[threadIdx.x][1], (double)mac[threadIdx.x][2],
-                            (double)mac[threadIdx.x][3], (double)mac[threadIdx.x][4]);
-        block_fused_stats(acc, stats, blockIdx.x);
+        if (counted) add_fused_stats(acc, (double)mac[0], (double)mac[1], (double)mac[2], (double)mac[3], (double)mac[4]);
+        warp_fused_stats(acc, stats, (long long)blockIdx.x * 4 + (threadIdx.x >> 5));
     }
 }
 
@@ -566,10 +585,8 @@ struct OuterLinks {
 // padded y, cells[3 i + 2] = bit mask of the cell's UBB directions; the
 // density is summed once per cell, in direction order.
 template <typename S>
-__global__ void k_ubb(S *__restrict__ pdf, Grid G, const int *__restrict__ cells, long long ncells, double ux,
-                      double uy, double uz) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ncells * G.nz) return;
+__device__ __forceinline__ void ubb_item(S *__restrict__ pdf, const Grid &G, const int *__restrict__ cells,
+                                         long long ncells, double ux, double uy, double uz, long long i) {
     const int z = (int)(i / ncells);
     const long long c = i - (long long)z * ncells;
     const int x = cells[3 * c], y = cells[3 * c + 1], mask = cells[3 * c + 2];
@@ -587,16 +604,22 @@ __global__ void k_ubb(S *__restrict__ pdf, Grid G, const int *__restrict__ cells
         store_g(pdf, G, inv(d), x + cx(d), y + cy(d), G.wrapz(z + cz(d)), g[d] - term * rho);
     }
 }
+template <typename S>
+__global__ void k_ubb(S *__restrict__ pdf, Grid G, const int *__restrict__ cells, long long ncells, double ux,
+                      double uy, double uz) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ncells * G.nz) return;
+    ubb_item(pdf, G, cells, ncells, ux, uy, uz, i);
+}
 
 // ExtrapolationOutflow (Geier et al. 2015 eq. F.1, normal +x): first-order
 // upwind advection at c_s of the incoming population on the boundary cell.
 // state[2i] = neighbour value of the previous step, state[2i+1] = boundary
 // value of the previous step.
 template <typename S>
-__global__ void k_outflow(S *__restrict__ pdf, Grid G, OuterLinks L, const int *__restrict__ selected, long long n,
-                          double *__restrict__ state, int nx_, int ny_, int nz_) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__device__ __forceinline__ void outflow_item(S *__restrict__ pdf, const Grid &G, const OuterLinks &L,
+                                             const int *__restrict__ selected, double *__restrict__ state, int nx_,
+                                             int ny_, int nz_, long long i) {
     const int li = selected[i];
     const int x = L.x[li], y = L.y[li], z = L.z[li], d = L.d[li], di = inv(d);
     const double nb = load_g(pdf, G, di, x + cx(d) - nx_, y + cy(d) - ny_, G.wrapz(z + cz(d) - nz_));
@@ -604,6 +627,13 @@ __global__ void k_outflow(S *__restrict__ pdf, Grid G, OuterLinks L, const int *
     state[2 * i] = nb;
     state[2 * i + 1] = v;
     store_g(pdf, G, di, x + cx(d), y + cy(d), G.wrapz(z + cz(d)), v);
+}
+template <typename S>
+__global__ void k_outflow(S *__restrict__ pdf, Grid G, OuterLinks L, const int *__restrict__ selected, long long n,
+                          double *__restrict__ state, int nx_, int ny_, int nz_) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    outflow_item(pdf, G, L, selected, state, nx_, ny_, nz_, i);
 }
 
 // first application: neighbour value from the initial populations, boundary

@@ -232,12 +232,13 @@ def poisson_arrivals(rate_per_s, n, seed=0):
 
 
 def random_requests(n, seed=0, chord=(24, 96), span=(4, 32), steps=(1000, 20000), window=1000,
-                    flap_probability=0.5, cl_tolerance=1e-4, lattice_speed=0.1 / math.sqrt(3)):
+                    flap_probability=0.5, cl_tolerance=1e-4, lattice_speed=0.1 / math.sqrt(3),
+                    farfield="characteristic_transport_v1"):
     """Synthetic solve requests with the distributions of the serving workload:
     camber U[0, 0.04], camber position U[0.3, 0.5], thickness U[0.09, 0.15],
     optional 0.3c flap deflected U[0, 25] deg, chord cells in `chord`, span
     cells in `span`, AoA U[-4, 14] deg, Re log-uniform on [1e4, 1e5], step
-    limits in `steps` (multiples of window)."""
+    limits in `steps` (multiples of window), on the given outer boundary."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(n):
@@ -251,7 +252,7 @@ def random_requests(n, seed=0, chord=(24, 96), span=(4, 32), steps=(1000, 20000)
         flow = Flow(reynolds=float(10 ** rng.uniform(4, 5)), alpha_deg=float(rng.uniform(-4, 14)),
                     lattice_speed=lattice_speed, seed=int(rng.integers(0, 2**31 - 1)))
         grid = Grid(cells_per_chord=n_chord, upstream_chords=4.0, downstream_chords=7.0, transverse_chords=3.9,
-                    span_chords=n_span / n_chord, farfield="characteristic_transport_v1", memory_limit_gib=64)
+                    span_chords=n_span / n_chord, farfield=farfield, memory_limit_gib=64)
         limit = int(rng.integers(steps[0] // window, steps[1] // window + 1)) * window
         out.append(SolveRequest(section, flow, grid, max_steps=max(limit, window), window=window,
                                 cl_tolerance=cl_tolerance, name=f"request{i:04d}"))

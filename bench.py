@@ -573,13 +573,17 @@ def run_large(steps=8, error_steps=100):
     return out
 
 
-def run_serving(n_requests=16, rate_per_s=2.0, seed=7, budget_gib=120.0, chunk=500, error_budget_s=40.0):
+def run_serving(n_requests=16, rate_per_s=2.0, seed=7, budget_gib=120.0, chunk=500, error_budget_s=40.0,
+                farfield="legacy"):
     """Continuous batching of the serving workload as specified: NACA 4-digit
     sections (m U[0, 0.04], p U[0.3, 0.5], t U[0.09, 0.15]), half with a 0.3c
     flap deflected U[0, 25] deg, chord 24-96 cells, span 4-32 cells, AoA
     U[-4, 14] deg, Re log-U[1e4, 1e5], 1000-20000 steps or until Cl changes by
     less than 1e-4 over 1000 steps; Poisson arrivals, a fixed HBM budget,
-    FP32 compute and FP32 storage.  Against the plain FP64 form one request
+    FP32 compute and FP32 storage.  The outer boundary is the reference's
+    default (legacy UBB and outflow): on the characteristic farfield every
+    request that runs past ~5000 steps diverges, as the reference's own
+    characteristic-farfield record does (it failed at step 5192).  Against the plain FP64 form one request
     at a time: each request's set-up and per-step time measured in the plain
     form and scaled to the steps it was served; the served coefficients
     compared with full FP64 solves of the smallest requests (as many as fit
@@ -587,7 +591,7 @@ def run_serving(n_requests=16, rate_per_s=2.0, seed=7, budget_gib=120.0, chunk=5
     import torch
     from aerokinetic_gb300.serve import Server, poisson_arrivals, random_requests
     from aerokinetic_gb300.solver import Solver
-    requests = random_requests(n_requests, seed=seed)
+    requests = random_requests(n_requests, seed=seed, farfield=farfield)
     arrivals = poisson_arrivals(rate_per_s, n_requests, seed=seed)
     server = Server(memory_budget_gib=budget_gib, storage="f32", chunk=chunk)
     results = server.run(requests, arrivals)
@@ -626,7 +630,7 @@ def run_serving(n_requests=16, rate_per_s=2.0, seed=7, budget_gib=120.0, chunk=5
     stats.update({"workload": f"{n_requests} requests, Poisson arrivals at {rate_per_s}/s, NACA 4-digit m U[0, 0.04], "
                               "p U[0.3, 0.5], t U[0.09, 0.15], half with a 0.3c flap at U[0, 25] deg, chord 24-96 "
                               "cells, span 4-32 cells (plan minimum 8), AoA U[-4, 14], Re log-U[1e4, 1e5], "
-                              "1000-20000 steps or Cl settled to 1e-4 over 1000 steps",
+                              "1000-20000 steps or Cl settled to 1e-4 over 1000 steps, " + farfield + " outer boundary",
                   "memory_budget_gib": budget_gib, "chunk": chunk,
                   "statuses": {s_: sum(r.status == s_ for r in results) for s_ in ("converged", "step_limit",
                                                                                    "failed")},

@@ -313,13 +313,14 @@ ak_case *ak_refined_level(ak_refined *r, int32_t level);
 
 /* ---- batches of independent uniform cases --------------------------------
  * No reference counterpart: the reference runs one case per process.  A batch
- * borrows n uniform cases with the characteristic farfield (one storage form,
- * one device) and advances them together: per step one launch each for the
- * farfield ring macros, the farfield links and the Bouzidi walls of every
- * case, and one persistent stream-collide launch over a packed table of all
- * cases' blocks, replayed from CUDA graphs.  A case computes the same bits
- * alone (ak_step) and in a batch.  While a case belongs to a batch, step it
- * only through the batch; its state can be read with the per-case calls. */
+ * borrows n uniform cases with the characteristic farfield or the legacy
+ * outer boundary (one storage form, one device) and advances them together:
+ * per step one launch each for the farfield ring macros and links, the UBB
+ * cells and outflow links, and the Bouzidi walls of every case, and one
+ * persistent stream-collide launch over a packed table of all cases' blocks,
+ * replayed from CUDA graphs.  A case computes the same bits alone (ak_step)
+ * and in a batch.  While a case belongs to a batch, step it only through the
+ * batch; its state can be read with the per-case calls. */
 typedef struct ak_batch ak_batch;
 int ak_batch_create(ak_case *const *cases, int32_t n, ak_batch **out);
 int ak_batch_destroy(ak_batch *b);

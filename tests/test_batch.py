@@ -14,6 +14,8 @@ def _parts(chord, alpha, reynolds, seed, farfield="characteristic_transport_v1",
 
 
 CASES = [(16, 4.0, 2e4, 1), (24, -2.0, 5e4, 2), (16, 10.0, 1e4, 3), (20, 6.0, 3e4, 4)]
+# the same with two cases on the legacy outer boundary (UBB + outflow)
+MIXED_BOUNDARIES = [(16, 4.0, 2e4, 1, "legacy"), (24, -2.0, 5e4, 2), (16, 10.0, 1e4, 3, "legacy"), (20, 6.0, 3e4, 4)]
 
 
 def _solvers(storage, cases=CASES):
@@ -22,12 +24,14 @@ def _solvers(storage, cases=CASES):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("storage", ["f64", "f16"])
-def test_batch_matches_cases_stepped_alone(storage):
-    """Every case of a mixed-size batch ends bit-identical to the same case
-    stepped alone, and its sampled loads are the same numbers."""
+@pytest.mark.parametrize("storage,cases", [("f64", CASES), ("f16", CASES), ("f32", MIXED_BOUNDARIES),
+                                           ("f64", MIXED_BOUNDARIES)])
+def test_batch_matches_cases_stepped_alone(storage, cases):
+    """Every case of a mixed-size batch (characteristic and legacy outer
+    boundaries) ends bit-identical to the same case stepped alone, and its
+    sampled loads are the same numbers."""
     from aerokinetic_gb300.batch import Batch
-    alone, mixed = _solvers(storage), _solvers(storage)
+    alone, mixed = _solvers(storage, cases), _solvers(storage, cases)
     try:
         with Batch(mixed) as batch:
             for chunk in (7, 1, 12):
