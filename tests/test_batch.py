@@ -102,11 +102,11 @@ def test_batch_rejects_what_it_cannot_run():
     from aerokinetic_gb300 import _native
     from aerokinetic_gb300.batch import Batch
     from aerokinetic_gb300.solver import Solver
-    legacy = Solver(*_parts(16, 4.0, 2e4, 1, farfield="legacy"))
+    exterior = Solver(*_parts(16, 4.0, 2e4, 1, farfield="exterior_regularized_fd_v1"))
     a, b = _solvers("f64", CASES[:1])[0], _solvers("f32", CASES[1:2])[0]
     try:
-        with pytest.raises(ValueError, match="characteristic"):
-            Batch([legacy])
+        with pytest.raises(ValueError, match="outer boundary"):
+            Batch([exterior])
         with pytest.raises(ValueError, match="storage"):
             Batch([a, b])
         with pytest.raises(ValueError, match="twice"):
@@ -118,5 +118,5 @@ def test_batch_rejects_what_it_cannot_run():
                 batch.advance(1)
         assert isinstance(_native.load().ak_batch_launches(None), int)
     finally:
-        for s in (legacy, a, b):
+        for s in (exterior, a, b):
             s.close()
