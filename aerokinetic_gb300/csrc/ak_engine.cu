@@ -1627,6 +1627,7 @@ struct ak_refined {
     int nterms = 0;
     int *d_flag = nullptr;
     double *d_loads = nullptr;
+    unsigned *wall_done = nullptr;  // finished-block counters of the two fine steps' wall launches
     long long steps = 0;
     std::vector<void *> owned;  // device buffers the two-level case owns
     // one captured coarse step per (coarse, fine) buffer parity, replayed by
@@ -1650,6 +1651,7 @@ struct ak_refined {
     double *outer_partials = nullptr, *outer_out = nullptr;  // outer_out: last step [4], running sum [4]
     double *cum_loads = nullptr;                              // wall loads summed over all steps [n * 5]
     double *stats_partials = nullptr, *stats_out = nullptr;
+    double *fine_rows = nullptr, *fine_stage = nullptr;  // the fine block's budget sums
     // fused form in an FP64-arithmetic storage: the coarse statistics of a
     // budget step come from the fused pass itself (rows of its far and near
     // launches, then the transfer block's band outside the box)
@@ -1757,6 +1759,12 @@ int with_levels(ak_refined *R, F &&f) {
     return fail(AK_ERR_INVALID, "unsupported pair of level storage forms");
 }
 #define AK_LEVEL_TYPES(a, b) using S = std::remove_pointer_t<decltype(a)>; using SF = std::remove_pointer_t<decltype(b)>
+// a donor-moment buffer (allocated as doubles) in the transfer arithmetic
+// type of the coarse storage S (FP32 for the FP32-compute forms)
+template <typename S>
+typename Store<S>::A *moments_of(double *p) {
+    return reinterpret_cast<typename Store<S>::A *>(p);
+}
 
 // restriction of the fine block onto the covered coarse cells
 template <typename S, typename SF>
@@ -1835,36 +1843,61 @@ __host__ __device__ constexpr bool fused_stats_form() {
     return std::is_same_v<S, double> || std::is_same_v<S, df2>;
 }
 
-// The fine block's budget statistics (stats_out[NSTAT..2 NSTAT)), on the
-// stream the restriction runs on: both only read the fine state.
-template <typename SF>
-int enqueue_fine_stats(ak_refined *R, cudaStream_t st) {
-    ak_case *F = R->fine;
-    const Region rf{R->pad, F->nx - R->pad, R->pad, F->ny - R->pad, 0, 0, 0, 0};
-    k_region_stats<SF><<<STATS_BLOCKS, 256, 0, st>>>(src_of<SF>(F), F->G, F->flags, rf, R->stats_partials);
-    k_region_final<<<1, REDUCE_THREADS, 0, st>>>(R->stats_partials, STATS_BLOCKS, R->stats_out + NSTAT);
-    R->coarse->launches += 2;
+// reduction of rows of budget sums into out[NSTAT]: one block when they are
+// few, else a first stage into stage (blocks_for(nrows, REDUCE_THREADS) rows)
+int enqueue_rows_final(ak_refined *R, const double *rows, long long nrows, double *stage, double *out,
+                       cudaStream_t st) {
+    if (nrows <= 16 * REDUCE_THREADS) {
+        k_region_final<<<1, REDUCE_THREADS, 0, st>>>(rows, (int)nrows, out);
+        R->coarse->launches += 1;
+    } else {
+        const long long ns = blocks_for(nrows, REDUCE_THREADS);
+        k_region_stage<<<(unsigned)ns, REDUCE_THREADS, 0, st>>>(rows, nrows, stage);
+        k_region_final<<<1, REDUCE_THREADS, 0, st>>>(stage, (int)ns, out);
+        R->coarse->launches += 2;
+    }
     AK_CUDA(cudaGetLastError());
     return AK_OK;
 }
 
-// The coarse budget statistics when the fused coarse pass has written its
-// rows to cstats: the cells of the transfer block outside the box (after
-// reflux and restriction), then the reduction over every row in two stages.
+// the fine block's physical cells (interior coordinates of the padded block)
+Region fine_region(const ak_refined *R) {
+    const ak_case *F = R->fine;
+    return Region{R->pad, F->nx - R->pad, R->pad, F->ny - R->pad, 0, 0, 0, 0};
+}
+long long region_cells(const Region &g, int nz) { return (long long)(g.x1 - g.x0) * (g.y1 - g.y0) * nz; }
+
+// The fine block's budget sums (stats_out[NSTAT..2 NSTAT)), on the stream
+// the restriction runs on: both only read the fine state.
+template <typename SF>
+int enqueue_fine_stats(ak_refined *R, cudaStream_t st) {
+    ak_case *F = R->fine;
+    const Region rf = fine_region(R);
+    const long long rows = region_sum_rows(region_cells(rf, F->nz));
+    k_region_sums<SF><<<(unsigned)(rows / 8), 256, 0, st>>>(src_of<SF>(F), F->G, F->flags, rf, R->fine_rows);
+    R->coarse->launches += 1;
+    AK_CUDA(cudaGetLastError());
+    return enqueue_rows_final(R, R->fine_rows, rows, R->fine_stage, R->stats_out + NSTAT, st);
+}
+
+// The coarse budget sums when the fused coarse pass has written its rows to
+// cstats: the cells of the transfer block outside the box (after reflux and
+// restriction), then the reduction over every row.
+Region band_region(const ak_refined *R) {
+    const BoxSpec &B = R->B;
+    return Region{R->xfer.x - 1, R->xfer.y - 1, R->xfer.z - 1, R->xfer.w - 1, B.lo[0], B.hi[0], B.lo[1], B.hi[1]};
+}
 template <typename S>
 int enqueue_coarse_fused_stats(ak_refined *R, cudaStream_t st) {
     ak_case *C = R->coarse;
-    const BoxSpec &B = R->B;
-    const Region band{R->xfer.x - 1, R->xfer.y - 1, R->xfer.z - 1, R->xfer.w - 1, B.lo[0], B.hi[0], B.lo[1], B.hi[1]};
-    const long long rows = R->cstats_far + R->cstats_near + STATS_BLOCKS;
-    const long long stage = blocks_for(rows, REDUCE_THREADS);
-    k_region_stats<S><<<STATS_BLOCKS, 256, 0, st>>>(src_of<S>(C), C->G, C->flags, band,
-                                                     R->cstats + (R->cstats_far + R->cstats_near) * NSTAT);
-    k_region_stage<<<(unsigned)stage, REDUCE_THREADS, 0, st>>>(R->cstats, rows, R->cstats_stage);
-    k_region_final<<<1, REDUCE_THREADS, 0, st>>>(R->cstats_stage, (int)stage, R->stats_out);
-    C->launches += 3;
+    const Region band = band_region(R);
+    const long long band_rows = region_sum_rows(region_cells(band, C->nz));
+    k_region_sums<S><<<(unsigned)(band_rows / 8), 256, 0, st>>>(src_of<S>(C), C->G, C->flags, band,
+                                                                R->cstats + (R->cstats_far + R->cstats_near) * NSTAT);
+    C->launches += 1;
     AK_CUDA(cudaGetLastError());
-    return AK_OK;
+    return enqueue_rows_final(R, R->cstats, R->cstats_far + R->cstats_near + band_rows, R->cstats_stage,
+                              R->stats_out, st);
 }
 
 template <typename S, typename SF>
@@ -2013,21 +2046,52 @@ int refined_step(ak_refined *R, bool fork = false) {
         AK_CUDA(cudaGetLastError());
         C->cur = 1 - C->cur;
         k_block_moments<S><<<(unsigned)split_blocks(nring_block), SPLIT_THREADS, 0, st>>>(
-            src_of<S>(C), C->G, B, R->d_free, R->mom_new, R->mom_old, R->mom_half, R->d_flag);
+            src_of<S>(C), C->G, B, R->d_free, moments_of<S>(R->mom_new), moments_of<S>(R->mom_old), moments_of<S>(R->mom_half),
+            R->d_flag);
         AK_CUDA(cudaGetLastError());
         return AK_OK;
     };
+    // The fine steps, fused: the first fine step streams with the
+    // collision of the second over the physical block (the band's cells are
+    // overwritten by the second step's donors), and the second step collides
+    // only the band.  In the FP32 fine storage the donor kernel collides the
+    // band itself (its 32-cell blocks are cheap to collide in FP32; in the
+    // FP64-arithmetic forms one warp per block would serialise the FP64
+    // collision, and FP16 storage rounds the donors before the collision), in
+    // the others a band-only collision follows the donors.  The fine state
+    // between coarse steps stays pre-collision.
+    constexpr bool donors_collide = std::is_same_v<SF, float>;
+    const int4 fine_rect = make_int4(1 + R->pad, F->nx + 1 - R->pad, 1 + R->pad, F->ny + 1 - R->pad);
+    const unsigned gfr = stream_collide_grid<SF>(fine_rect, F->nx, F->ny, F->nz);
     // one fine step on stream s: donors, collide, face fluxes, walls, stream
     auto fine_part = [&](int sub, cudaStream_t s) -> int {
         // donor moments at the fine step's start: the old coarse state, then
         // half-way (1 - 1/2) old + 1/2 new (refined_solver.py:311-318)
-        k_prolong_x<<<(unsigned)blocks3(nprox), 256, 0, s>>>(B, C->nz, R->pad, sub ? R->mom_half : R->mom_old,
-                                                              R->pro_x);
-        k_donors<SF><<<(unsigned)split_blocks(nband), SPLIT_THREADS, 0, s>>>(src_of<SF>(F), F->G, C->nz, R->pro_x,
-                                                                             B.dny, c2f, R->pad, R->d_flag);
+        k_prolong_x<<<(unsigned)blocks3(nprox), 256, 0, s>>>(B, C->nz, R->pad,
+                                                              moments_of<S>(sub ? R->mom_half : R->mom_old),
+                                                              moments_of<S>(R->pro_x));
+        bool collided = false;
+        if constexpr (donors_collide) {
+            if (sub == 1) {
+                k_donors<SF, true><<<(unsigned)split_blocks(nband), SPLIT_THREADS, 0, s>>>(
+                    src_of<SF>(F), F->G, C->nz, moments_of<S>(R->pro_x), B.dny, c2f, R->pad, R->d_flag, F->flags,
+                    (TF)F->omega_s, (TF)F->omega_b);
+                collided = true;
+            }
+        }
+        if (!collided)
+            k_donors<SF><<<(unsigned)split_blocks(nband), SPLIT_THREADS, 0, s>>>(src_of<SF>(F), F->G, C->nz,
+                                                                                 moments_of<S>(R->pro_x), B.dny, c2f,
+                                                                                 R->pad, R->d_flag);
         mark(C);
-        k_collide<SF><<<gf1, 128, 0, s>>>(src_of<SF>(F), F->flags, F->G, F->shift_host, (TF)F->omega_s,
-                                           (TF)F->omega_b);
+        if (sub == 0)
+            k_collide<SF><<<gf1, 128, 0, s>>>(src_of<SF>(F), F->flags, F->G, F->shift_host, (TF)F->omega_s,
+                                               (TF)F->omega_b);
+        else if (!collided)
+            // the band alone: the physical block was collided by the first
+            // step's stream-collide
+            k_collide<SF><<<gf1, 128, 0, s>>>(src_of<SF>(F), F->flags, F->G, F->shift_host, (TF)F->omega_s,
+                                               (TF)F->omega_b, make_int4(0, 0, 0, 0), fine_rect);
         mark(C);
         cudaStream_t fs = flux_stream(s, 1 + sub);
         if (!fs) return fail(AK_ERR_CUDA, "face-flux branch could not be forked");
@@ -2035,16 +2099,22 @@ int refined_step(ak_refined *R, bool fork = false) {
             src_of<SF>(F), F->G, R->d_terms[0], R->d_terms[1], R->nterms, R->d_faces, R->nfaces, R->d_offs, R->pad,
             R->dx_f * R->dx_f * R->dx_f, R->reg_f);
         if (fork && sub == 0) AK_CUDA(cudaEventRecord(R->ev_flux_f0, R->flux));
-        if (nlinks) {
+        // the walls' last block sums the loads; the second fine step's also
+        // adds both steps' loads to the running sums
+        if (nlinks)
             k_walls<SF><<<(unsigned)nb, 256, 0, s>>>(src_of<SF>(F), F->G, F->keys, F->wall_q, F->nkeys, 1,
-                                                     F->n_elements, F->ox, F->oy, F->partials);
-            k_sum_partials<<<5 * F->n_elements, 32, 0, s>>>(F->partials, (int)nb, 5 * F->n_elements,
-                                                             R->d_loads + sub * 5 * F->n_elements);
-        }
+                                                     F->n_elements, F->ox, F->oy, F->partials, R->wall_done + sub,
+                                                     R->d_loads + sub * 5 * F->n_elements,
+                                                     sub ? R->cum_loads : nullptr, R->d_loads);
         mark(C);
         // the second fine step streams into the copy the first step's flux reads
         if (fork && sub == 1) AK_CUDA(cudaStreamWaitEvent(s, R->ev_flux_f0, 0));
-        k_stream<SF><<<gf, 128, 0, s>>>(src_of<SF>(F), dst_of<SF>(F), F->flags, F->G, 1);
+        if (sub == 0)
+            k_stream_collide<SF><<<gfr, 128, 0, s>>>(src_of<SF>(F), dst_of<SF>(F), F->flags, F->G, F->shift_host,
+                                                     (TF)F->omega_s, (TF)F->omega_b, Sgs<TF>{}, make_int4(0, 0, 0, 0),
+                                                     fine_rect);
+        else
+            k_stream<SF><<<gf, 128, 0, s>>>(src_of<SF>(F), dst_of<SF>(F), F->flags, F->G, 1);
         mark(C);
         AK_CUDA(cudaGetLastError());
         F->cur = 1 - F->cur;
@@ -2054,7 +2124,7 @@ int refined_step(ak_refined *R, bool fork = false) {
     mark(C);  // step start
     // donors before the coarse step
     k_block_moments<S><<<(unsigned)split_blocks(nring_block), SPLIT_THREADS, 0, st>>>(
-        src_of<S>(C), C->G, B, R->d_free, R->mom_old, nullptr, nullptr, R->d_flag);
+        src_of<S>(C), C->G, B, R->d_free, moments_of<S>(R->mom_old), nullptr, nullptr, R->d_flag);
     if (fork) {
         // the first fine step needs only the donors before the coarse step:
         // it runs on the side stream beside the coarse step (captured graphs)
@@ -2071,10 +2141,6 @@ int refined_step(ak_refined *R, bool fork = false) {
         AK_TRY(fine_part(0, st));
     }
     AK_TRY(fine_part(1, st));
-    if (nlinks) {
-        k_accumulate_loads<<<1, 128, 0, st>>>(R->d_loads, 5 * F->n_elements, R->cum_loads);
-        C->launches += 1;
-    }
     if (fork) {
         AK_CUDA(cudaEventRecord(R->ev_flux_done, R->flux));
         AK_CUDA(cudaStreamWaitEvent(st, R->ev_flux_done, 0));
@@ -2108,7 +2174,8 @@ int refined_step(ak_refined *R, bool fork = false) {
     } else if (R->track_budget && R->step_stats)
         AK_TRY((enqueue_region_stats<S, SF>(R, st)));
     mark(C);  // step end
-    C->launches += 6 + 7 * 2 + (C->n_ubb ? 1 : 0) + (C->n_out ? 1 : 0) + (nlinks ? 0 : -4) + 1 + (bnd ? 1 : 0);
+    C->launches += 6 + 6 * 2 - (donors_collide ? 1 : 0) + (C->n_ubb ? 1 : 0) + (C->n_out ? 1 : 0) + (nlinks ? 0 : -2) + 1 +
+                   (bnd ? 1 : 0);
     R->pre_mode = 1;
     R->pre_writes = C->pdf_writes;
     C->steps += 1;
@@ -2364,14 +2431,19 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
         if (r == AK_OK) r = ralloc(R, &R->outer_out, 8);
         if (r == AK_OK) r = ralloc(R, &R->cum_loads, (size_t)5 * std::max(1, cd.n_elements));
         if (r == AK_OK) r = ralloc(R, &R->stats_partials, (size_t)STATS_BLOCKS * NSTAT);
+        // rows of the fine block's budget sums
+        const long long frows = region_sum_rows(region_cells(fine_region(R), R->fine->nz));
+        if (r == AK_OK) r = ralloc(R, &R->fine_rows, (size_t)frows * NSTAT);
+        if (r == AK_OK) r = ralloc(R, &R->fine_stage, (size_t)blocks_for(frows, REDUCE_THREADS) * NSTAT);
         if (r == AK_OK && R->fused) {
-            // rows of the fused pass's statistics: its far launch (a grid over
-            // the whole coarse lattice), its near launch, the band's blocks
-            // one row per warp of the far and near launches
+            // rows of the fused pass's budget sums, one per warp: its far
+            // launch (a grid over the whole coarse lattice), its near launch,
+            // then the band's rows
             const int4 nr = R->near;
             R->cstats_far = 4 * blocks_for((long long)cd.nx * cd.ny * cd.nz, 128);
             R->cstats_near = 4 * blocks_for((long long)(nr.y - nr.x) * (nr.w - nr.z) * cd.nz, 128);
-            const long long rows = R->cstats_far + R->cstats_near + STATS_BLOCKS;
+            const long long rows =
+                R->cstats_far + R->cstats_near + region_sum_rows(region_cells(band_region(R), cd.nz));
             r = ralloc(R, &R->cstats, (size_t)rows * NSTAT);
             if (r == AK_OK) r = ralloc(R, &R->cstats_stage, (size_t)blocks_for(rows, REDUCE_THREADS) * NSTAT);
         }
@@ -2403,7 +2475,9 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
         const long long nb = blocks_for(F->nkeys * F->nz * 3, 256);
         r = ensure_partials(F, std::max<long long>(1, nb * 5 * F->n_elements));
     }
-    if (r == AK_OK && cudaMemset(R->d_loads, 0, sizeof(double) * 2 * 5 * std::max(1, cd.n_elements)) != cudaSuccess)
+    if (r == AK_OK) r = ralloc(R, &R->wall_done, 2);
+    if (r == AK_OK && (cudaMemset(R->d_loads, 0, sizeof(double) * 2 * 5 * std::max(1, cd.n_elements)) != cudaSuccess ||
+                       cudaMemset(R->wall_done, 0, 2 * sizeof(unsigned)) != cudaSuccess))
         r = fail(AK_ERR_CUDA, "memset failed");
     if (r == AK_OK && cudaDeviceSynchronize() != cudaSuccess) r = fail(AK_ERR_CUDA, "refined set-up failed");
     if (r != AK_OK) {
@@ -2613,10 +2687,11 @@ int ak_refined_probe(ak_refined *R, int32_t op, double *out, int64_t *n_out) {
             const Rescale c2f{R->tau_s_f * R->dt_f / (R->tau_s_c * R->dt_c),
                               R->tau_b_f * R->dt_f / (R->tau_b_c * R->dt_c)};
             k_block_moments<S><<<(unsigned)split_blocks(nring_block), SPLIT_THREADS, 0, st>>>(
-                src_of<S>(C), C->G, B, R->d_free, R->mom_old, nullptr, nullptr, R->d_flag);
-            k_prolong_x<<<(unsigned)blocks3(nprox), 256, 0, st>>>(B, C->nz, R->pad, R->mom_old, R->pro_x);
+                src_of<S>(C), C->G, B, R->d_free, moments_of<S>(R->mom_old), nullptr, nullptr, R->d_flag);
+            k_prolong_x<<<(unsigned)blocks3(nprox), 256, 0, st>>>(B, C->nz, R->pad, moments_of<S>(R->mom_old),
+                                                                   moments_of<S>(R->pro_x));
             k_donors<SF><<<(unsigned)split_blocks(nband), SPLIT_THREADS, 0, st>>>(src_of<SF>(F), F->G, C->nz,
-                                                                                  R->pro_x, B.dny, c2f, R->pad,
+                                                                                  moments_of<S>(R->pro_x), B.dny, c2f, R->pad,
                                                                                   R->d_flag);
         } else if (op == 1) {
             const Rescale f2c{R->tau_s_c * R->dt_c / (R->tau_s_f * R->dt_f),

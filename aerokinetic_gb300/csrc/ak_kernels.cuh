@@ -107,53 +107,98 @@ __device__ void block_cell_stats(double (&a)[CELL_STATS], double *out, long long
     }
 }
 
-// The same statistics accumulated inside the FP64-bound fused pass, with as
-// little FP64-pipe work as possible: the four sums in FP64, the maxima of
-// the non-negative |u|^2 and |drho| as integer maxima of their bit patterns
-// (the order of non-negative doubles), the finiteness test on the exponent
-// bits and the cell counts as integers.
-struct FusedStats {
-    double drho = 0, jx = 0, jy = 0, jz = 0;
-    long long u2 = 0, dr = 0;  // bit patterns of the maxima
-    int cells = 0, bad = 0;
-};
-__device__ __forceinline__ bool finite_bits(double v) { return (__double2hiint(v) & 0x7ff00000) != 0x7ff00000; }
-__device__ __forceinline__ void add_fused_stats(FusedStats &a, double drho, double jx, double jy, double jz,
-                                                double u2) {
-    if (!finite_bits(drho) || !finite_bits(u2)) {
-        ++a.bad;
-        return;
+// The budget's sums on the integer pipe.  A value v becomes the integer
+// round(v 2^FIX_BITS) (magnitude rounded half up, then the sign): integer
+// sums are exact, so a row's sum does not depend on the order of its cells,
+// and the FP64-bound passes spend no FP64 instruction on them (GB300 issues
+// an FP64 instruction per warp at 1/64 of the FP32 rate).  A value that is
+// not finite, or whose magnitude reaches 2^MAX_EXP, is refused.
+constexpr int FIX_BITS = 50;
+constexpr double FIX_UNIT = 1.0 / 1125899906842624.0;  // 2^-FIX_BITS
+// |result| < 2^(FIX_BITS + MAX_EXP)
+template <int MAX_EXP>
+__device__ __forceinline__ bool fixed_of(double v, long long &out) {
+    const long long b = __double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e == 0x7ff || e > 1022 + MAX_EXP) return false;
+    long long r = 0;
+    if (e != 0) {
+        const long long m = (b & 0x000fffffffffffffLL) | 0x0010000000000000LL;  // v = m 2^(e - 1075)
+        const int sh = e - 1075 + FIX_BITS;
+        if (sh >= 0)
+            r = m << sh;
+        else if (sh > -55)
+            r = (m + (1LL << (-sh - 1))) >> -sh;
     }
-    a.drho += drho;
-    a.jx += jx;
-    a.jy += jy;
-    a.jz += jz;
-    a.u2 = max(a.u2, __double_as_longlong(u2));
-    a.dr = max(a.dr, __double_as_longlong(drho) & 0x7fffffffffffffffLL);
-    ++a.cells;
+    out = b < 0 ? -r : r;
+    return true;
 }
-// the warp's statistics row in the CELL_STATS layout (every lane calls it;
-// no block-wide barrier): shuffle sums in a fixed order, integer maxima
-__device__ __forceinline__ void warp_fused_stats(FusedStats s, double *out, long long row) {
+template <int MAX_EXP>
+__device__ __forceinline__ bool fixed_of(float v, long long &out) {
+    const int b = __float_as_int(v);
+    const int e = (b >> 23) & 0xff;
+    if (e == 0xff || e > 126 + MAX_EXP) return false;
+    long long r = 0;
+    if (e != 0) {
+        const long long m = (b & 0x7fffff) | 0x800000;  // v = m 2^(e - 150)
+        const int sh = e - 150 + FIX_BITS;
+        if (sh >= 0)
+            r = m << sh;
+        else if (sh > -26)
+            r = (m + (1LL << (-sh - 1))) >> -sh;
+    }
+    out = b < 0 ? -r : r;
+    return true;
+}
+template <int MAX_EXP>
+__device__ __forceinline__ bool fixed_of(df64 v, long long &out) {
+    long long hi, lo;
+    if (!fixed_of<MAX_EXP>(v.hi, hi) || !fixed_of<MAX_EXP>(v.lo, lo)) return false;
+    out = hi + lo;
+    return true;
+}
+
+// The budget's row of a set of cells, in the CELL_STATS layout (the maxima,
+// which only the diagnostics use, are left 0): drho and j summed as fixed
+// point (each value below 256 in magnitude, so that 32 cells' sums stay
+// inside 64 bits), fluid cells and invalid cells counted.
+struct BudgetSums {
+    long long drho = 0, jx = 0, jy = 0, jz = 0;
+    int cells = 0, bad = 0;
+    template <typename T>
+    __device__ __forceinline__ void add_cell(T drho_, T jx_, T jy_, T jz_) {
+        long long a, b, c, d;
+        if (fixed_of<8>(drho_, a) && fixed_of<8>(jx_, b) && fixed_of<8>(jy_, c) && fixed_of<8>(jz_, d)) {
+            drho += a;
+            jx += b;
+            jy += c;
+            jz += d;
+            ++cells;
+        } else {
+            ++bad;
+        }
+    }
+};
+// the warp's row (every lane calls it; no block-wide barrier): integer
+// shuffle sums, converted to double once per warp
+__device__ __forceinline__ void warp_budget_row(BudgetSums s, double *out, long long row) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         s.drho += __shfl_down_sync(0xffffffffu, s.drho, o);
         s.jx += __shfl_down_sync(0xffffffffu, s.jx, o);
         s.jy += __shfl_down_sync(0xffffffffu, s.jy, o);
         s.jz += __shfl_down_sync(0xffffffffu, s.jz, o);
-        s.u2 = max(s.u2, __shfl_down_sync(0xffffffffu, s.u2, o));
-        s.dr = max(s.dr, __shfl_down_sync(0xffffffffu, s.dr, o));
         s.cells += __shfl_down_sync(0xffffffffu, s.cells, o);
         s.bad += __shfl_down_sync(0xffffffffu, s.bad, o);
     }
     if ((threadIdx.x & 31) == 0) {
         double *r = out + row * CELL_STATS;
-        r[0] = __longlong_as_double(s.u2);
-        r[1] = __longlong_as_double(s.dr);
-        r[2] = s.drho;
-        r[3] = s.jx;
-        r[4] = s.jy;
-        r[5] = s.jz;
+        r[0] = 0.0;
+        r[1] = 0.0;
+        r[2] = (double)s.drho * FIX_UNIT;
+        r[3] = (double)s.jx * FIX_UNIT;
+        r[4] = (double)s.jy * FIX_UNIT;
+        r[5] = (double)s.jz * FIX_UNIT;
         r[6] = (double)s.cells;
         r[7] = (double)s.bad;
     }
@@ -162,9 +207,8 @@ __device__ __forceinline__ void warp_fused_stats(FusedStats s, double *out, long
 // pull the 27 populations of interior cell (x, y, z) (padded x, y), collide,
 // store into dst if the column is fluid; stream_only: store the pulled values
 // as they are (bit copies, no collision); mac (optional): where the
-// collision writes the cell's (drho, j, |u|^2) as soon as it has them (a
-// shared-memory row, so that they hold no register through the rest of the
-// collision).  Returns true for a collided fluid cell.
+// collision writes the cell's drho and j.  Returns true for a collided fluid
+// cell.
 template <typename S, typename Shift>
 __device__ __forceinline__ bool stream_collide_cell(const S *__restrict__ src, S *__restrict__ dst,
                                                     const uint8_t *__restrict__ flags, const Grid &G,
@@ -390,10 +434,13 @@ __device__ __forceinline__ void stream_collide_pair_item(const S *__restrict__ s
 }
 
 // resident 128-thread blocks per SM the stream-collide is compiled for: the
-// pair forms hold two cells' populations per thread
+// pair forms hold two cells' populations per thread.  Measured on the
+// uniform 768 x 512 x 8 case (CUDA events, L2 flushed): the FP16 pairs reach
+// 0.54 / 0.58 / 0.60 / 0.51 of the HBM copy peak at 4 / 5 / 6 / 8 blocks
+// (96 / 95 / 80 / 64 registers), the FP32 pairs 0.87 / 0.81 / 0.63 at 4 / 5 / 6.
 template <typename S>
 __host__ __device__ constexpr int stream_collide_min_blocks() {
-    return pair_form<S>() ? 4 : Store<S>::MIN_BLOCKS;
+    return pair_form<S>() ? (std::is_same_v<S, __half> ? 6 : 4) : Store<S>::MIN_BLOCKS;
 }
 
 // STATS: every warp also writes the statistics of the cells it collided
@@ -422,7 +469,7 @@ __global__ void __launch_bounds__(128, stream_collide_min_blocks<S>())
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned nxy = w * h;
     using T = typename Store<S>::T;
-    T mac[5];
+    T mac[4];
     bool active = i < nxy * (unsigned)G.nz, counted = false;
     int x = 0, y = 0, z = 0;
     if (active) {
@@ -444,9 +491,9 @@ __global__ void __launch_bounds__(128, stream_collide_min_blocks<S>())
                                       STATS ? mac : nullptr);
     }
     if constexpr (STATS) {
-        FusedStats acc;
-        if (counted) add_fused_stats(acc, (double)mac[0], (double)mac[1], (double)mac[2], (double)mac[3], (double)mac[4]);
-        warp_fused_stats(acc, stats, (long long)blockIdx.x * 4 + (threadIdx.x >> 5));
+        BudgetSums acc;
+        if (counted) acc.add_cell(mac[0], mac[1], mac[2], mac[3]);
+        warp_budget_row(acc, stats, (long long)blockIdx.x * 4 + (threadIdx.x >> 5));
     }
 }
 
@@ -544,17 +591,51 @@ __device__ __forceinline__ void wall_block_sums(const double acc[5], int element
 // solver.py:217-243: F = sum c_d (g_out + g_in), Mz = sum rx Fy - ry Fx,
 // mass = sum g_in - g_out.  Partials: [element][block][5].
 constexpr int MAX_ELEMENTS = 8;
+
+// The last block of a sampled k_walls launch to finish sums the partials as
+// k_sum_partials does (the same order, so the same result) into
+// out[5 n_elements]; with cum it also adds first[t] + out[t] to cum[t] (the
+// running loads of a two-level step, first holding its first fine step's
+// loads), in the order of a two-level step's loads.  done counts the blocks that have
+// finished; the last one leaves it 0 for the next launch.
+__device__ void finish_wall_sums(const double *partials, int n_elements, unsigned *done, double *out, double *cum,
+                                 const double *first) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nv = 5 * n_elements, nb = gridDim.x;
+    for (int t = warp; t < nv; t += blockDim.x >> 5) {
+        const int e = t / 5, k = t - 5 * e;
+        double v = 0.0;
+        for (int b = lane; b < nb; b += 32) v += __ldcg(partials + ((long long)e * nb + b) * 5 + k);
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) {
+            out[t] = v;
+            if (cum) cum[t] += first[t] + v;
+        }
+    }
+    if (threadIdx.x == 0) *done = 0;
+}
+
+// done == nullptr: the partials are left for k_sum_partials
 template <typename S>
 __global__ void __launch_bounds__(256, 2) k_walls(S *__restrict__ pdf, Grid G, const WallKey *__restrict__ keys,
                                                const double *__restrict__ qs, long long nkeys, int sample,
                                                int n_elements, double ox, double oy,
-                                               double *__restrict__ partials) {
+                                               double *__restrict__ partials, unsigned *done = nullptr,
+                                               double *out = nullptr, double *cum = nullptr,
+                                               const double *first = nullptr) {
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     double acc[5] = {0, 0, 0, 0, 0};
     int element = -1;
     if (tid < nkeys * G.nz * 3) wall_link(pdf, G, keys, qs, tid, sample, ox, oy, acc, element);
     if (!sample) return;
     wall_block_sums(acc, element, n_elements, partials, blockIdx.x, gridDim.x);
+    if (done) finish_wall_sums(partials, n_elements, done, out, cum, first);
 }
 
 // partials laid out [element][block][5]; one warp per (element, component):

@@ -200,8 +200,8 @@ __host__ __device__ __forceinline__ T smagorinsky_rate(const Sgs<T> &m, T rinv, 
     return T(R(2) / (m.tau0 + sqrt(m.c18 * norm + m.tau0 * m.tau0)));
 }
 
-// mac (optional): the cell's (drho, jx, jy, jz, |u|^2), which the collision
-// conserves (drho, j) or forms anyway; a null mac compiles away.
+// mac (optional): the cell's (drho, jx, jy, jz), which the collision
+// conserves; a null mac compiles away.
 // the subgrid rate of a pair of cells, lane by lane in FP32
 __device__ __forceinline__ F2 smagorinsky_rate(const Sgs<F2> &m, F2 rinv, F2 pxx, F2 pyy, F2 pzz, F2 pxy, F2 pxz,
                                                F2 pyz) {
@@ -253,7 +253,6 @@ __host__ __device__ __forceinline__ void collide(T g[Q], T omega_s, T omega_b, c
         mac[1] = jx;
         mac[2] = jy;
         mac[3] = jz;
-        mac[4] = ux * ux + uy * uy + uz * uz;
     }
     // second-order central moments minus their rest value 1/3
     const T kdx = M200 - jx * ux, kdy = M020 - jy * uy, kdz = M002 - jz * uz;
@@ -358,7 +357,6 @@ __host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b, 
         mac[1] = jx;
         mac[2] = jy;
         mac[3] = jz;
-        mac[4] = ux * ux + uy * uy + uz * uz;
     }
     // second-order central moments minus 1/3, relaxed
     const T kdx = M200 - jx * ux, kdy = M020 - jy * uy, kdz = M002 - jz * uz;

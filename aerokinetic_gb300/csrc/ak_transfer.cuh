@@ -509,13 +509,14 @@ __device__ __forceinline__ bool in_core(const BoxSpec &B, int cxi, int cyi) {
 // free-stream populations.  Output out[k][z][y][x] (x fastest, n cells),
 // written on the ring of the block the prolongation reads (five cells wide);
 // with mix_from set, half also receives 0.5 mix_from + 0.5 out, the donor
-// moments half-way through the coarse step.
+// moments half-way through the coarse step.  Moments and their prolongation
+// are held in the transfer arithmetic type T of the storage form.
 constexpr int DONOR_RING = 5;
 template <typename S>
 __global__ void __launch_bounds__(SPLIT_THREADS)
     k_block_moments(const S *__restrict__ pdf, Grid G, BoxSpec B, const double *__restrict__ free_g,
-                    double *__restrict__ out, const double *__restrict__ mix_from, double *__restrict__ half,
-                    int *__restrict__ flag) {
+                    typename Store<S>::A *__restrict__ out, const typename Store<S>::A *__restrict__ mix_from,
+                    typename Store<S>::A *__restrict__ half, int *__restrict__ flag) {
     using T = typename Store<S>::A;
     __shared__ SplitShared<T> sh;
     const long long nring = ring_count(B.dnx, B.dny, DONOR_RING, DONOR_RING), nr = nring * G.nz;
@@ -555,22 +556,24 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
 #pragma unroll
     for (int k = 0; k < 10; ++k) {
         out[k * n + j] = m[k];
-        if (mix_from) half[k * n + j] = 0.5 * mix_from[k * n + j] + 0.5 * (double)m[k];
+        if (mix_from) half[k * n + j] = T(0.5) * mix_from[k * n + j] + T(0.5) * m[k];
     }
 }
 
 // Donors for the padding band of the fine block: the donor moments are
 // prolonged one axis at a time, as the reference does (refinement.py:78-105):
 // children = centre -+ [11/64 (a+1 - a-1) - 3/128 (a+2 - a-2)].
-__device__ __forceinline__ double prolong_child(double am2, double am1, double a0, double ap1, double ap2, int odd) {
-    const double offset = 11.0 / 64.0 * (ap1 - am1) - 3.0 / 128.0 * (ap2 - am2);
+template <typename T>
+__device__ __forceinline__ T prolong_child(T am2, T am1, T a0, T ap1, T ap2, int odd) {
+    const T offset = T(11.0 / 64.0) * (ap1 - am1) - T(3.0 / 128.0) * (ap2 - am2);
     return odd ? a0 + offset : a0 - offset;
 }
 
 // x pass: out[k][z][by][fx] (fx fastest, fx in [0, nfx = 2 (bx + 2))), on the
 // cells the y pass reads for the band: every fx of the five outer block rows
 // on each side, the band columns elsewhere
-__global__ void k_prolong_x(BoxSpec B, int nz, int pad, const double *__restrict__ m, double *__restrict__ out) {
+template <typename T>
+__global__ void k_prolong_x(BoxSpec B, int nz, int pad, const T *__restrict__ m, T *__restrict__ out) {
     const int nfx = 2 * (B.bx + 2);
     const long long nring = ring_count(nfx, B.dny, pad, DONOR_RING);
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -582,7 +585,7 @@ __global__ void k_prolong_x(BoxSpec B, int nz, int pad, const double *__restrict
     const long long row = (long long)z * B.dny + by, o = row * nfx + fx, base = row * B.dnx + (fx >> 1);
 #pragma unroll
     for (int k = 0; k < 10; ++k) {
-        const double *a = m + k * nblock + base;
+        const T *a = m + k * nblock + base;
         out[k * n + o] = prolong_child(a[0], a[1], a[2], a[3], a[4], fx & 1);
     }
 }
@@ -593,10 +596,16 @@ __global__ void k_prolong_x(BoxSpec B, int nz, int pad, const double *__restrict
 // z pass reads is first prolonged in y from the x pass's rows, so the y pass
 // needs no launch of its own (the same operations on the same values).  Warp
 // 0 rescales and prepares the fields, every warp writes its own directions.
-template <typename S>
+// COLLIDE: the populations go through shared memory instead, and warp 0
+// collides its 32 fluid cells (as k_collide would, on the values the storage
+// would hold) and stores the post-collision populations.  Forms whose stored
+// value is not the computed one (FP16) are not compiled with it.
+template <typename S, bool COLLIDE = false>
 __global__ void __launch_bounds__(SPLIT_THREADS)
-    k_donors(S *__restrict__ fine, Grid F, int nzc, const double *__restrict__ px, int dny, Rescale r, int pad,
-             int *__restrict__ flag) {
+    k_donors(S *__restrict__ fine, Grid F, int nzc, const typename Store<S>::A *__restrict__ px, int dny, Rescale r,
+             int pad, int *__restrict__ flag, const uint8_t *__restrict__ flags = nullptr,
+             typename Store<S>::T omega_s = 0, typename Store<S>::T omega_b = 0) {
+    static_assert(!COLLIDE || !std::is_same_v<S, __half>, "FP16 storage rounds the donors before the collision");
     using T = typename Store<S>::A;
     __shared__ SplitShared<T> sh;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -613,18 +622,18 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
     const long long nin = (long long)F.nx * dny * nzc, row0 = (long long)(fy >> 1) * F.nx + fx;
     const int pz = fz >> 1;
     for (int k = w; k < 10; k += SPLIT_WARPS) {
-        double a[5];
+        T a[5];
 #pragma unroll
         for (int j = 0; j < 5; ++j) {
             const int zz = ((pz + j - 2) % nzc + nzc) % nzc;
             if (valid) {
-                const double *b = px + k * nin + (long long)zz * dny * F.nx + row0;
+                const T *b = px + k * nin + (long long)zz * dny * F.nx + row0;
                 a[j] = prolong_child(b[0], b[F.nx], b[2 * F.nx], b[3 * F.nx], b[4 * F.nx], fy & 1);
             } else {
-                a[j] = k == 0 ? 1.0 : 0.0;
+                a[j] = k == 0 ? T(1) : T(0);
             }
         }
-        sh.field[0][k][lane] = T(prolong_child(a[0], a[1], a[2], a[3], a[4], fz & 1));
+        sh.field[0][k][lane] = prolong_child(a[0], a[1], a[2], a[3], a[4], fz & 1);
     }
     __syncthreads();
     if (w == 0) {
@@ -639,14 +648,36 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
     T m[10], fac[9];
     get_fields(sh, 1, m, fac);
     bool bad = false;
-    by_warp([&](auto wc) {
-        owned<decltype(wc)::value>([&](auto qc, int) {
-            constexpr int q = decltype(qc)::value;
-            const T g = population<q>(m, fac, bad);
-            if (valid) store_as<T>(fine, F, q, fx + 1, fy + 1, fz, g);
+    if constexpr (COLLIDE) {
+        __shared__ T pop[Q][SPLIT_CELLS];
+        by_warp([&](auto wc) {
+            owned<decltype(wc)::value>([&](auto qc, int) {
+                constexpr int q = decltype(qc)::value;
+                pop[q][lane] = population<q>(m, fac, bad);
+            });
         });
-    });
-    if (bad && valid) atomicOr(flag, XF_NEGATIVE);
+        if (bad && valid) atomicOr(flag, XF_NEGATIVE);
+        __syncthreads();
+        if (w != 0 || !valid) return;
+        using TS = typename Store<S>::T;
+        TS g[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) g[q] = TS(pop[q][lane]);
+        if (__ldg(flags + (fy + 1) * F.nxp + fx + 1) == FLAG_FLUID) collide_stored<S>(g, omega_s, omega_b);
+        const long long c = F.cell(fx + 1, fy + 1, fz);
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+            if (AK_CHECK(F, q, fx + 1, fy + 1, fz, 2)) Store<S>::store(fine + q * F.qs + c, q, g[q], F.shift[q]);
+    } else {
+        by_warp([&](auto wc) {
+            owned<decltype(wc)::value>([&](auto qc, int) {
+                constexpr int q = decltype(qc)::value;
+                const T g = population<q>(m, fac, bad);
+                if (valid) store_as<T>(fine, F, q, fx + 1, fy + 1, fz, g);
+            });
+        });
+        if (bad && valid) atomicOr(flag, XF_NEGATIVE);
+    }
 }
 
 // ------------------------------------------------------------ reflux, restriction
@@ -852,11 +883,6 @@ __global__ void __launch_bounds__(REDUCE_THREADS)
         }
 }
 
-// running sums of the wall loads over coarse steps: cum[k] += both fine steps
-__global__ void k_accumulate_loads(const double *__restrict__ loads, int n, double *__restrict__ cum) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) cum[t] += loads[t] + loads[n + t];
-}
 
 // Statistics of one level's region (refined_solver.py:291-299, 347-361):
 // fluid cells of [x0, x1) x [y0, y1) x all z (interior coordinates) outside
@@ -943,6 +969,66 @@ __global__ void __launch_bounds__(256)
         }
         for (int k = 0; k < NSTAT; ++k) partials[(long long)blockIdx.x * NSTAT + k] = red[0][k];
     }
+}
+
+// The budget's sums over the same region on the integer pipe: each fluid
+// cell's drho and j from its 27 populations as fixed point (FIX_BITS), four
+// cells per thread, one row per warp (CELL_STATS layout, maxima left 0).  A
+// population of magnitude 1 or more (no valid zero-centred population has
+// one) or a non-finite one makes the cell invalid; with that bound a row of
+// 128 cells stays inside 64 bits.  rows: region_sum_rows(cells) of them.
+constexpr int SUM_CELLS_PER_THREAD = 4;
+__host__ __device__ constexpr long long region_sum_rows(long long cells) {
+    return (cells + 256 * SUM_CELLS_PER_THREAD - 1) / (256 * SUM_CELLS_PER_THREAD) * 8;
+}
+template <typename S>
+__global__ void __launch_bounds__(256)
+    k_region_sums(const S *__restrict__ pdf, Grid G, const uint8_t *__restrict__ flags, Region R,
+                  double *__restrict__ rows) {
+    const int w = R.x1 - R.x0, h = R.y1 - R.y0;
+    const long long n = (long long)w * h * G.nz;
+    BudgetSums acc;
+#pragma unroll 1
+    for (int k = 0; k < SUM_CELLS_PER_THREAD; ++k) {
+        const long long i = ((long long)blockIdx.x * SUM_CELLS_PER_THREAD + k) * 256 + threadIdx.x;
+        if (i >= n) break;
+        const int z = (int)(i / ((long long)w * h));
+        const int r = (int)(i - (long long)z * w * h);
+        const int y = R.y0 + r / w, x = R.x0 + r % w;
+        if (x >= R.ex0 && x < R.ex1 && y >= R.ey0 && y < R.ey1) continue;
+        if (flags[(y + 1) * G.nxp + (x + 1)] != FLAG_FLUID) continue;
+        const S *cell = pdf + G.cell(x + 1, y + 1, z);
+        long long f[Q];
+        bool ok = true;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) ok &= fixed_of<0>(Store<S>::load(cell + q * G.qs, q, G.shift[q]), f[q]);
+        if (!ok) {
+            ++acc.bad;
+            continue;
+        }
+        // sums along z first, as mass_momentum does (exact in integers)
+        long long col[3][3], jz = 0;
+#pragma unroll
+        for (int ix = 0; ix < 3; ++ix)
+#pragma unroll
+            for (int iy = 0; iy < 3; ++iy) {
+                const long long a = f[qof(ix, iy, 0)], b = f[qof(ix, iy, 1)], c = f[qof(ix, iy, 2)];
+                col[ix][iy] = a + b + c;
+                jz += c - a;
+            }
+        long long sx[3], sy[3];
+#pragma unroll
+        for (int k2 = 0; k2 < 3; ++k2) {
+            sx[k2] = col[k2][0] + col[k2][1] + col[k2][2];
+            sy[k2] = col[0][k2] + col[1][k2] + col[2][k2];
+        }
+        acc.drho += sx[0] + sx[1] + sx[2];
+        acc.jx += sx[2] - sx[0];
+        acc.jy += sy[2] - sy[0];
+        acc.jz += jz;
+        ++acc.cells;
+    }
+    warp_budget_row(acc, rows, (long long)blockIdx.x * 8 + (threadIdx.x >> 5));
 }
 
 // first stage of a reduction of many statistics rows: block b reduces rows

@@ -48,10 +48,13 @@ FORM_ERROR_STEPS = 2000
 # coarse steps of the end-to-end solve (set-up from the host description
 # included; the benchmark case itself is a 10000-step run)
 E2E_STEPS = 1000
-# DRAM bytes (read + write) per launch of the coarse k_stream_collide<double>
-# of the two-level case, from the ncu capture summarised in
-# profiles/collide_f64_refined_512x384x8.txt (same kernel and workload)
-TRAFFIC_BYTES_PER_LAUNCH = None
+# DRAM bytes (read + write) of the coarse k_stream_collide<double> over one
+# coarse step of the two-level case, from the ncu capture summarised in
+# profiles/stream_collide_f64_refined_512x384x8.txt: the graphed step runs it
+# as a far launch (347383040 + 284257536 B) and a near launch (8960512 +
+# 8704 B); the eager step that kernel_ms times covers the same cells in one
+# launch.  The algorithmic figure is 1572864 cells x 432 B = 679477248 B.
+TRAFFIC_BYTES_PER_LAUNCH = 347383040 + 284257536 + 8960512 + 8704
 
 
 def case_parts(farfield="characteristic_transport_v1", sgs="none"):
@@ -72,6 +75,14 @@ def refined_parts():
                 transverse_chords=5.9056, span_chords=0.25, memory_limit_gib=64)
     refinement = RefinementSettings(upstream_chords=0.5, downstream_chords=1.0, transverse_chords=0.5)
     return Project(section, flow, grid), refinement
+
+
+def fine_passes(fine_storage):
+    """Passes over the fine block per coarse step, each reading and writing
+    every cell once: the first fine step's collision, its streaming fused
+    with the second step's collision, the second step's streaming (the band's
+    own collision in the second step is not counted)."""
+    return 3
 
 
 def refined_cells(plan):
@@ -550,10 +561,10 @@ def run_large(steps=8, error_steps=100):
                        lambda: _native.check(lib.ak_refined_step(solver._handle, steps, None)))
         groups = np.zeros(6)
         _native.check(lib.ak_refined_step_timed(solver._handle, 2, groups.ctypes.data_as(ctypes.c_void_p)))
-        # the coarse streaming fused with the collision plus the fine collisions
-        collide_ms = (groups[2] + groups[3]) / 2
+        # the coarse streaming fused with the collision plus the fine passes
+        collide_ms = (groups[2] + groups[3] + groups[4]) / 2
         collide_bytes = (math.prod(solver.plan.shape) * BYTES_PER_CELL[storage]
-                         + 2 * fine_padded * BYTES_PER_CELL[solver.fine_storage])
+                         + fine_passes(solver.fine_storage) * fine_padded * BYTES_PER_CELL[solver.fine_storage])
         out.setdefault("coarse_shape", list(solver.plan.shape))
         out.setdefault("fine_shape", list(solver.fine_shape))
         out.setdefault("cell_updates_per_step", cells)
@@ -731,9 +742,9 @@ def run_engine(args, rank, world, local_rank):
     achieved_tflops = kernel_flops / (kernel_ms / 1e3) / 1e12
     achieved_gbs = kernel_bytes / (kernel_ms / 1e3) / 1e9
     # the same for the collision launches of one coarse step (the fused coarse
-    # pass and the two fine collisions)
-    collide_bytes = (coarse_cells + 2 * fine_padded) * BYTES_PER_CELL["f64"]
-    collide_ms = groups["coarse_stream_collide_ms"] + groups["fine_collide_ms"]
+    # pass and the fine block's passes)
+    collide_bytes = (coarse_cells + fine_passes("f64") * fine_padded) * BYTES_PER_CELL["f64"]
+    collide_ms = groups["coarse_stream_collide_ms"] + groups["fine_collide_ms"] + groups["fine_stream_ms"]
     achieved = collide_bytes / (collide_ms / 1e3) / 1e9
 
     # ---- end to end through the public API: case set-up from the host
@@ -765,8 +776,9 @@ def run_engine(args, rank, world, local_rank):
         m = np.zeros(6)
         _native.check(lib.ak_refined_step_timed(r._handle, k, m.ctypes.data_as(ctypes.c_void_p)))
         r.close()
-        cb = coarse_cells * BYTES_PER_CELL[storage] + 2 * fine_padded * BYTES_PER_CELL[fine]
-        cms = (m[2] + m[3]) / k
+        # the coarse stream-collide and the fine block's passes
+        cb = coarse_cells * BYTES_PER_CELL[storage] + fine_passes(fine) * fine_padded * BYTES_PER_CELL[fine]
+        cms = (m[2] + m[3] + m[4]) / k
         forms[label] = {"coarse_storage": storage, "fine_storage": fine,
                           "mlups": cells / (step_ms / 1e3) / 1e6, "ms_per_step": step_ms,
                           "collide_achieved_gbs": cb / (cms / 1e3) / 1e9,

@@ -236,10 +236,13 @@ int ak_refined_step(ak_refined *r, int32_t nsteps, double *loads);
 /* ak_refined_step that also returns, with one synchronisation, what the
  * budget of the last step needs (refined_solver.py:329-339): outer[8] as
  * ak_refined_outer_flux, stats[16] as ak_refined_integrals of the state the
- * step leaves.  With stats every step computes these integrals, as the
- * reference's step does; in the FP64-arithmetic forms the coarse level's
- * come out of the fused stream-collide pass itself.  Needs
- * ak_refined_track_budget on; outer or stats may be NULL. */
+ * step leaves, but with the two maxima (diagnostics only) left 0.  With stats
+ * every step computes these integrals, as the reference's step does; in the
+ * FP64-arithmetic forms the coarse level's come out of the fused
+ * stream-collide pass itself.  The sums are exact fixed-point integer sums of
+ * each cell's values rounded to 2^-50 (a cell with a value of magnitude 256
+ * or more, or a population of magnitude 1 or more, counts as non-finite).
+ * Needs ak_refined_track_budget on; outer or stats may be NULL. */
 int ak_refined_step_budget(ak_refined *r, int32_t nsteps, double *loads, double *outer, double *stats);
 int64_t ak_refined_steps_done(const ak_refined *r);
 /* With enable != 0, every following step also measures the inflow through
