@@ -133,8 +133,15 @@ __global__ void k_batch_sum_partials(const BatchCase<S> *__restrict__ cases, dou
 // the single-case kernel's numbering (cells across rows, or cell pairs in
 // the pair forms), so a case's bits do not depend on the batch and no warp
 // is left part-empty at a row's end
+// resident 128-thread blocks per SM: the pair forms' body also holds the
+// case descriptor and the work loop, and spills at the single-case FP16
+// kernel's six blocks (80 registers), so every pair form keeps four
+template <typename S>
+__host__ __device__ constexpr int batch_bulk_min_blocks() {
+    return pair_form<S>() ? 4 : Store<S>::MIN_BLOCKS;
+}
 template <typename S, int TB>
-__global__ void __launch_bounds__(TB, stream_collide_min_blocks<S>() * 128 / TB)
+__global__ void __launch_bounds__(TB, batch_bulk_min_blocks<S>() * 128 / TB)
     k_batch_bulk(const BatchCase<S> *__restrict__ cases, const WorkItem *__restrict__ work, long long n_work,
                  int parity) {
     for (long long e = blockIdx.x; e < n_work; e += gridDim.x) {

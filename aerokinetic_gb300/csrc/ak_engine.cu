@@ -1887,8 +1887,9 @@ Region band_region(const ak_refined *R) {
     const BoxSpec &B = R->B;
     return Region{R->xfer.x - 1, R->xfer.y - 1, R->xfer.z - 1, R->xfer.w - 1, B.lo[0], B.hi[0], B.lo[1], B.hi[1]};
 }
+// the band's rows, as soon as its cells are final (after the reflux)
 template <typename S>
-int enqueue_coarse_fused_stats(ak_refined *R, cudaStream_t st) {
+int enqueue_band_sums(ak_refined *R, cudaStream_t st) {
     ak_case *C = R->coarse;
     const Region band = band_region(R);
     const long long band_rows = region_sum_rows(region_cells(band, C->nz));
@@ -1896,6 +1897,11 @@ int enqueue_coarse_fused_stats(ak_refined *R, cudaStream_t st) {
                                                                 R->cstats + (R->cstats_far + R->cstats_near) * NSTAT);
     C->launches += 1;
     AK_CUDA(cudaGetLastError());
+    return AK_OK;
+}
+// every coarse row into stats_out[0..NSTAT), once the fused pass has ended
+int enqueue_coarse_rows_final(ak_refined *R, cudaStream_t st) {
+    const long long band_rows = region_sum_rows(region_cells(band_region(R), R->coarse->nz));
     return enqueue_rows_final(R, R->cstats, R->cstats_far + R->cstats_near + band_rows, R->cstats_stage,
                               R->stats_out, st);
 }
@@ -2060,7 +2066,8 @@ int refined_step(ak_refined *R, bool fork = false) {
     // collision, and FP16 storage rounds the donors before the collision), in
     // the others a band-only collision follows the donors.  The fine state
     // between coarse steps stays pre-collision.
-    constexpr bool donors_collide = std::is_same_v<SF, float>;
+    constexpr bool fine_fused = true;
+    constexpr bool donors_collide = fine_fused && std::is_same_v<SF, float>;
     const int4 fine_rect = make_int4(1 + R->pad, F->nx + 1 - R->pad, 1 + R->pad, F->ny + 1 - R->pad);
     const unsigned gfr = stream_collide_grid<SF>(fine_rect, F->nx, F->ny, F->nz);
     // one fine step on stream s: donors, collide, face fluxes, walls, stream
@@ -2084,14 +2091,14 @@ int refined_step(ak_refined *R, bool fork = false) {
                                                                                  moments_of<S>(R->pro_x), B.dny, c2f,
                                                                                  R->pad, R->d_flag);
         mark(C);
-        if (sub == 0)
+        if (sub == 0 || !fine_fused)
             k_collide<SF><<<gf1, 128, 0, s>>>(src_of<SF>(F), F->flags, F->G, F->shift_host, (TF)F->omega_s,
                                                (TF)F->omega_b);
         else if (!collided)
             // the band alone: the physical block was collided by the first
             // step's stream-collide
-            k_collide<SF><<<gf1, 128, 0, s>>>(src_of<SF>(F), F->flags, F->G, F->shift_host, (TF)F->omega_s,
-                                               (TF)F->omega_b, make_int4(0, 0, 0, 0), fine_rect);
+            k_collide_band<SF><<<(unsigned)blocks_for(nband, 128), 128, 0, s>>>(
+                src_of<SF>(F), F->flags, F->G, F->shift_host, (TF)F->omega_s, (TF)F->omega_b, R->pad);
         mark(C);
         cudaStream_t fs = flux_stream(s, 1 + sub);
         if (!fs) return fail(AK_ERR_CUDA, "face-flux branch could not be forked");
@@ -2109,7 +2116,7 @@ int refined_step(ak_refined *R, bool fork = false) {
         mark(C);
         // the second fine step streams into the copy the first step's flux reads
         if (fork && sub == 1) AK_CUDA(cudaStreamWaitEvent(s, R->ev_flux_f0, 0));
-        if (sub == 0)
+        if (fine_fused && sub == 0)
             k_stream_collide<SF><<<gfr, 128, 0, s>>>(src_of<SF>(F), dst_of<SF>(F), F->flags, F->G, F->shift_host,
                                                      (TF)F->omega_s, (TF)F->omega_b, Sgs<TF>{}, make_int4(0, 0, 0, 0),
                                                      fine_rect);
@@ -2160,6 +2167,9 @@ int refined_step(ak_refined *R, bool fork = false) {
     k_reflux<S><<<dim3((unsigned)split_blocks(R->max_face), R->nfaces), SPLIT_THREADS, 0, st>>>(
         src_of<S>(C), C->G, R->d_faces, R->nfaces, R->d_offs, R->reg_c, R->reg_f,
         1.0 / (R->dx_c * R->dx_c * R->dx_c), R->d_flag);
+    // the transfer block's cells outside the box are final after the reflux
+    // (the restriction writes the box's): their sums run beside the far pass
+    if (fstats) AK_TRY(enqueue_band_sums<S>(R, st));
     if (fork)
         AK_CUDA(cudaStreamWaitEvent(st, R->ev_join, 0));
     else
@@ -2170,7 +2180,7 @@ int refined_step(ak_refined *R, bool fork = false) {
     // a tracked budget closes on the integrals of the state the step leaves
     if (fstats) {
         if (!fork) AK_TRY(enqueue_fine_stats<SF>(R, st));
-        AK_TRY(enqueue_coarse_fused_stats<S>(R, st));
+        AK_TRY(enqueue_coarse_rows_final(R, st));
     } else if (R->track_budget && R->step_stats)
         AK_TRY((enqueue_region_stats<S, SF>(R, st)));
     mark(C);  // step end

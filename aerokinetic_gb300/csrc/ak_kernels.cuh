@@ -179,18 +179,26 @@ struct BudgetSums {
         }
     }
 };
-// the warp's row (every lane calls it; no block-wide barrier): integer
-// shuffle sums, converted to double once per warp
+// the warp's sum of a 64-bit value whose 32-lane sum fits in 64 bits, by
+// three warp-reduce instructions: v = p2 2^54 + p1 2^27 + p0 with p0, p1 in
+// [0, 2^27) (32 of them sum below 2^32) and p2 = v >> 54; the parts' sums
+// are recombined modulo 2^64, which is exact when the sum fits
+__device__ __forceinline__ long long warp_sum_fixed(long long v) {
+    const unsigned long long u = (unsigned long long)v;
+    const unsigned s0 = __reduce_add_sync(0xffffffffu, (unsigned)(u & 0x7ffffffULL));
+    const unsigned s1 = __reduce_add_sync(0xffffffffu, (unsigned)((u >> 27) & 0x7ffffffULL));
+    const int s2 = __reduce_add_sync(0xffffffffu, (int)(v >> 54));
+    return (long long)(((unsigned long long)(long long)s2 << 54) + ((unsigned long long)s1 << 27) + s0);
+}
+// the warp's row (every lane calls it; no block-wide barrier): integer warp
+// sums, converted to double once per warp
 __device__ __forceinline__ void warp_budget_row(BudgetSums s, double *out, long long row) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        s.drho += __shfl_down_sync(0xffffffffu, s.drho, o);
-        s.jx += __shfl_down_sync(0xffffffffu, s.jx, o);
-        s.jy += __shfl_down_sync(0xffffffffu, s.jy, o);
-        s.jz += __shfl_down_sync(0xffffffffu, s.jz, o);
-        s.cells += __shfl_down_sync(0xffffffffu, s.cells, o);
-        s.bad += __shfl_down_sync(0xffffffffu, s.bad, o);
-    }
+    s.drho = warp_sum_fixed(s.drho);
+    s.jx = warp_sum_fixed(s.jx);
+    s.jy = warp_sum_fixed(s.jy);
+    s.jz = warp_sum_fixed(s.jz);
+    s.cells = __reduce_add_sync(0xffffffffu, s.cells);
+    s.bad = __reduce_add_sync(0xffffffffu, s.bad);
     if ((threadIdx.x & 31) == 0) {
         double *r = out + row * CELL_STATS;
         r[0] = 0.0;

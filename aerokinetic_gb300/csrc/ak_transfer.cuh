@@ -328,6 +328,30 @@ __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
     for (int q = 0; q < Q; ++q) Store<S>::store(pdf + q * G.qs + c, q, g[q], shift.v[q]);
 }
 
+// the collision of the cells of the padding band (pad cells around the
+// physical block in x and y, every z) alone, numbered around the ring so
+// that every lane of a warp holds a band cell
+template <typename S>
+__global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
+    k_collide_band(S *__restrict__ pdf, const uint8_t *__restrict__ flags, Grid G, Shift27 shift,
+                   typename Store<S>::T omega_s, typename Store<S>::T omega_b, int pad) {
+    using T = typename Store<S>::T;
+    const long long nring = ring_count(G.nx, G.ny, pad, pad);
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nring * G.nz) return;
+    const int z = (int)(i / nring);
+    int x, y;
+    ring_cell(i - z * nring, G.nx, G.ny, pad, pad, x, y);
+    if (__ldg(flags + (y + 1) * G.nxp + x + 1) != FLAG_FLUID) return;
+    const long long c = G.cell(x + 1, y + 1, z);
+    T g[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) g[q] = Store<S>::load(pdf + q * G.qs + c, q, shift.v[q]);
+    collide_stored<S>(g, omega_s, omega_b);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) Store<S>::store(pdf + q * G.qs + c, q, g[q], shift.v[q]);
+}
+
 // pull streaming of the stored values (bit copies); x and y wrap when periodic
 template <typename S>
 __global__ void k_stream(const S *__restrict__ src, S *__restrict__ dst, const uint8_t *__restrict__ flags, Grid G,
@@ -972,12 +996,14 @@ __global__ void __launch_bounds__(256)
 }
 
 // The budget's sums over the same region on the integer pipe: each fluid
-// cell's drho and j from its 27 populations as fixed point (FIX_BITS), four
-// cells per thread, one row per warp (CELL_STATS layout, maxima left 0).  A
-// population of magnitude 1 or more (no valid zero-centred population has
-// one) or a non-finite one makes the cell invalid; with that bound a row of
-// 128 cells stays inside 64 bits.  rows: region_sum_rows(cells) of them.
-constexpr int SUM_CELLS_PER_THREAD = 4;
+// cell's drho and j from its 27 populations as fixed point (FIX_BITS), one
+// cell per thread (the kernel is bound by load latency: a thread looping
+// over four cells took four times as long), one row per warp (CELL_STATS
+// layout, maxima left 0).  A population of magnitude 1 or more (no valid
+// zero-centred population has one) or a non-finite one makes the cell
+// invalid; with that bound a row of 32 cells stays inside 64 bits.  rows:
+// region_sum_rows(cells) of them.
+constexpr int SUM_CELLS_PER_THREAD = 1;
 __host__ __device__ constexpr long long region_sum_rows(long long cells) {
     return (cells + 256 * SUM_CELLS_PER_THREAD - 1) / (256 * SUM_CELLS_PER_THREAD) * 8;
 }
