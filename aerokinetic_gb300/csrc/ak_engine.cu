@@ -1651,11 +1651,13 @@ struct ak_refined {
     double *outer_partials = nullptr, *outer_out = nullptr;  // outer_out: last step [4], running sum [4]
     double *cum_loads = nullptr;                              // wall loads summed over all steps [n * 5]
     double *stats_partials = nullptr, *stats_out = nullptr;
-    double *fine_rows = nullptr, *fine_stage = nullptr;  // the fine block's budget sums
+    long long *fine_rows = nullptr;  // the fine block's budget rows
+    double *fine_stage = nullptr;
     // fused form in an FP64-arithmetic storage: the coarse statistics of a
     // budget step come from the fused pass itself (rows of its far and near
     // launches, then the transfer block's band outside the box)
-    double *cstats = nullptr, *cstats_stage = nullptr;
+    long long *cstats = nullptr;  // budget rows (warp_budget_row)
+    double *cstats_stage = nullptr;
     long long cstats_far = 0, cstats_near = 0;
 };
 
@@ -1843,16 +1845,16 @@ __host__ __device__ constexpr bool fused_stats_form() {
     return std::is_same_v<S, double> || std::is_same_v<S, df2>;
 }
 
-// reduction of rows of budget sums into out[NSTAT]: one block when they are
-// few, else a first stage into stage (blocks_for(nrows, REDUCE_THREADS) rows)
-int enqueue_rows_final(ak_refined *R, const double *rows, long long nrows, double *stage, double *out,
+// reduction of budget rows into out[NSTAT]: one block when they are few,
+// else a first stage into stage (blocks_for(nrows, REDUCE_THREADS) rows)
+int enqueue_rows_final(ak_refined *R, const long long *rows, long long nrows, double *stage, double *out,
                        cudaStream_t st) {
     if (nrows <= 16 * REDUCE_THREADS) {
-        k_region_final<<<1, REDUCE_THREADS, 0, st>>>(rows, (int)nrows, out);
+        k_budget_final<<<1, REDUCE_THREADS, 0, st>>>(rows, nrows, out);
         R->coarse->launches += 1;
     } else {
         const long long ns = blocks_for(nrows, REDUCE_THREADS);
-        k_region_stage<<<(unsigned)ns, REDUCE_THREADS, 0, st>>>(rows, nrows, stage);
+        k_budget_stage<<<(unsigned)ns, REDUCE_THREADS, 0, st>>>(rows, nrows, stage);
         k_region_final<<<1, REDUCE_THREADS, 0, st>>>(stage, (int)ns, out);
         R->coarse->launches += 2;
     }
@@ -2036,7 +2038,7 @@ int refined_step(ak_refined *R, bool fork = false) {
                                                       (T)C->omega_s, (T)C->omega_b, Sgs<T>{}, R->xfer, R->near);
         else if (R->fused && fstats) {
             // one launch covers every row of the far part; the near rows stay empty
-            AK_CUDA(cudaMemsetAsync(R->cstats + R->cstats_far * NSTAT, 0, sizeof(double) * R->cstats_near * NSTAT, st));
+            AK_CUDA(cudaMemsetAsync(R->cstats + R->cstats_far * NSTAT, 0, sizeof(long long) * R->cstats_near * NSTAT, st));
             k_stream_collide<S, true><<<gsc, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G,
                                                             C->shift_host, (T)C->omega_s, (T)C->omega_b, Sgs<T>{},
                                                             R->xfer, make_int4(0, 0, 0, 0), make_int4(0, 0, 0, 0),

@@ -191,8 +191,13 @@ __device__ __forceinline__ long long warp_sum_fixed(long long v) {
     return (long long)(((unsigned long long)(long long)s2 << 54) + ((unsigned long long)s1 << 27) + s0);
 }
 // the warp's row (every lane calls it; no block-wide barrier): integer warp
-// sums, converted to double once per warp
-__device__ __forceinline__ void warp_budget_row(BudgetSums s, double *out, long long row) {
+// sums, written as integers (drho, jx, jy, jz, fluid cells, invalid cells in
+// the first six of the row's CELL_STATS slots).  A conversion to double here
+// puts FP64 instructions at the end of every warp of an FP64-bound pass,
+// where they queue behind the collisions and hold the block: converting in
+// the warp made the two-level budget step 1.178 ms, converting in the
+// reduction 1.145 ms (bare step 1.113 ms); the reduction converts them
+__device__ __forceinline__ void warp_budget_row(BudgetSums s, long long *out, long long row) {
     s.drho = warp_sum_fixed(s.drho);
     s.jx = warp_sum_fixed(s.jx);
     s.jy = warp_sum_fixed(s.jy);
@@ -200,16 +205,23 @@ __device__ __forceinline__ void warp_budget_row(BudgetSums s, double *out, long 
     s.cells = __reduce_add_sync(0xffffffffu, s.cells);
     s.bad = __reduce_add_sync(0xffffffffu, s.bad);
     if ((threadIdx.x & 31) == 0) {
-        double *r = out + row * CELL_STATS;
-        r[0] = 0.0;
-        r[1] = 0.0;
-        r[2] = (double)s.drho * FIX_UNIT;
-        r[3] = (double)s.jx * FIX_UNIT;
-        r[4] = (double)s.jy * FIX_UNIT;
-        r[5] = (double)s.jz * FIX_UNIT;
-        r[6] = (double)s.cells;
-        r[7] = (double)s.bad;
+        long long *r = out + row * CELL_STATS;
+        r[0] = s.drho;
+        r[1] = s.jx;
+        r[2] = s.jy;
+        r[3] = s.jz;
+        r[4] = s.cells;
+        r[5] = s.bad;
     }
+}
+// a budget row as the CELL_STATS doubles (maxima 0)
+__device__ __forceinline__ void budget_row_values(const long long *__restrict__ r, double (&v)[CELL_STATS]) {
+    v[0] = 0.0;
+    v[1] = 0.0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[2 + k] = (double)r[k] * FIX_UNIT;
+    v[6] = (double)r[4];
+    v[7] = (double)r[5];
 }
 
 // pull the 27 populations of interior cell (x, y, z) (padded x, y), collide,
@@ -310,12 +322,18 @@ __device__ __forceinline__ void pair_load(const S *__restrict__ src, const Grid 
     for (int q = 0; q < Q; ++q) {
         const S *p = row[cz(q) + 1] + ((long long)q * G.qs - (long long)cy(q) * G.sx);
         if constexpr (std::is_same_v<S, __half>) {
+            // p is at xe: every load is an aligned 32-bit word; a shifted
+            // pair (xe - cx, xe + 1 - cx) is the upper half of one word and
+            // the lower half of the next, put together by one byte permute
+            const unsigned *w = reinterpret_cast<const unsigned *>(p);
             if (cx(q) == 0) {
-                raw.v[q] = __ldg(reinterpret_cast<const unsigned *>(p));
+                raw.v[q] = __ldg(w);
+            } else if (cx(q) > 0) {
+                const unsigned left = live0 ? __ldg(w - 1) : 0u, own = live1 ? __ldg(w) : 0u;
+                raw.v[q] = __byte_perm(left, own, 0x5432);
             } else {
-                const unsigned lo = live0 ? __ldg(reinterpret_cast<const unsigned short *>(p - cx(q))) : 0u;
-                const unsigned hi = live1 ? __ldg(reinterpret_cast<const unsigned short *>(p + 1 - cx(q))) : 0u;
-                raw.v[q] = lo | (hi << 16);
+                const unsigned own = live0 ? __ldg(w) : 0u, right = live1 ? __ldg(w + 1) : 0u;
+                raw.v[q] = __byte_perm(own, right, 0x5432);
             }
         } else {
             if (cx(q) == 0) {
@@ -361,8 +379,8 @@ __device__ __forceinline__ void pair_collide_store(const PairRaw<S> &raw, S *__r
     for (int q = 0; q < Q; ++q) {
         float2 v = g[q].v;
         if constexpr (std::is_same_v<S, __half>) {
-            const float a = shift_at(shift, q), inv = (float)(1.0 / weight(q));
-            v = f2_mul(f2_add(v, make_float2(-a, -a)), make_float2(inv, inv));
+            const float a = shift_at(shift, q), inv = (float)(1.0 / weight(q)), b = -a * inv;
+            v = f2_fma(v, make_float2(inv, inv), make_float2(b, b));
         }
         S *p = dst + q * G.qs + c;
         if (store0 && store1) {
@@ -451,16 +469,16 @@ __host__ __device__ constexpr int stream_collide_min_blocks() {
     return pair_form<S>() ? (std::is_same_v<S, __half> ? 6 : 4) : Store<S>::MIN_BLOCKS;
 }
 
-// STATS: every warp also writes the statistics of the cells it collided
-// (not the streamed-only ones) to stats[blockIdx.x * 4 + warp] (CELL_STATS
-// each)
+// STATS: every warp also writes the budget row (warp_budget_row) of the
+// cells it collided (not the streamed-only ones) to row blockIdx.x * 4 + warp
+// of stats
 template <typename S, bool STATS = false>
 __global__ void __launch_bounds__(128, stream_collide_min_blocks<S>())
     k_stream_collide(const S *__restrict__ src, S *__restrict__ dst, const uint8_t *__restrict__ flags, Grid G,
                      Shift27 shift, typename Store<S>::T omega_s, typename Store<S>::T omega_b,
                      Sgs<typename Store<S>::T> sgs, int4 raw = make_int4(0, 0, 0, 0),
                      int4 rect = make_int4(0, 0, 0, 0), int4 skip = make_int4(0, 0, 0, 0),
-                     double *__restrict__ stats = nullptr) {
+                     long long *__restrict__ stats = nullptr) {
     // one thread per cell of the padded columns x [rect.x, rect.y) by y
     // [rect.z, rect.w) (rect.y == 0: the whole interior), every z, x fastest,
     // numbered across rows: warps stay full whatever the width (the plain
@@ -1189,9 +1207,12 @@ __global__ void __launch_bounds__(256) k_diagnostics(const S *__restrict__ pdf, 
 // fixed strided accumulation, then a fixed shared-memory tree, so the result
 // does not depend on scheduling.  Thread 0 returns the reduced row.
 constexpr int REDUCE_THREADS = 256;
+// the block's fixed-order tree over every thread's acc (maxima where
+// max_mask has the bit, sums elsewhere); the result in every thread's acc
+template <int NV>
+__device__ void reduce_block(unsigned max_mask, double (&acc)[NV]);
 template <int NV>
 __device__ void reduce_rows(const double *__restrict__ rows, long long nrows, unsigned max_mask, double (&acc)[NV]) {
-    __shared__ double red[NV][REDUCE_THREADS];
     const int t = threadIdx.x;
 #pragma unroll
     for (int k = 0; k < NV; ++k) acc[k] = ((max_mask >> k) & 1) ? -INFINITY : 0.0;
@@ -1201,6 +1222,12 @@ __device__ void reduce_rows(const double *__restrict__ rows, long long nrows, un
             const double v = rows[b * NV + k];
             acc[k] = ((max_mask >> k) & 1) ? fmax(acc[k], v) : acc[k] + v;
         }
+    reduce_block<NV>(max_mask, acc);
+}
+template <int NV>
+__device__ void reduce_block(unsigned max_mask, double (&acc)[NV]) {
+    __shared__ double red[NV][REDUCE_THREADS];
+    const int t = threadIdx.x;
 #pragma unroll
     for (int k = 0; k < NV; ++k) red[k][t] = acc[k];
     __syncthreads();

@@ -120,7 +120,8 @@ template <> struct Store<__half> {
         return fmaf(__half2float(__ldg(p)), (float)weight(q), shift);
     }
     __device__ static __forceinline__ void store(__half *p, int q, float v, float shift) {
-        *p = __float2half_rn((v - shift) * (float)(1.0 / weight(q)));
+        const float inv = (float)(1.0 / weight(q));
+        *p = __float2half_rn(fmaf(v, inv, -shift * inv));
     }
 };
 // df64 form: FP64-sized storage as (hi, lo) float pairs, the collision in

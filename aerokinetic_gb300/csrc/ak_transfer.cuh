@@ -1010,7 +1010,7 @@ __host__ __device__ constexpr long long region_sum_rows(long long cells) {
 template <typename S>
 __global__ void __launch_bounds__(256)
     k_region_sums(const S *__restrict__ pdf, Grid G, const uint8_t *__restrict__ flags, Region R,
-                  double *__restrict__ rows) {
+                  long long *__restrict__ rows) {
     const int w = R.x1 - R.x0, h = R.y1 - R.y0;
     const long long n = (long long)w * h * G.nz;
     BudgetSums acc;
@@ -1073,6 +1073,35 @@ __global__ void __launch_bounds__(REDUCE_THREADS)
     k_region_final(const double *__restrict__ partials, int nblocks, double *__restrict__ out) {
     double a[NSTAT];
     reduce_rows<NSTAT>(partials, nblocks, 0x3u, a);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < NSTAT; ++k) out[k] = a[k];
+}
+
+// The budget's integer rows (warp_budget_row) into the CELL_STATS doubles:
+// each row converted once, then the fixed-order reduction of k_region_stage
+// (block b: rows [b REDUCE_THREADS, (b + 1) REDUCE_THREADS), one row each)
+// or of k_region_final (one block, every row)
+__global__ void __launch_bounds__(REDUCE_THREADS)
+    k_budget_stage(const long long *__restrict__ rows, long long nrows, double *__restrict__ out) {
+    const long long b = (long long)blockIdx.x * REDUCE_THREADS + threadIdx.x;
+    double a[NSTAT] = {-INFINITY, -INFINITY, 0, 0, 0, 0, 0, 0};
+    if (b < nrows) budget_row_values(rows + b * NSTAT, a);
+    reduce_block<NSTAT>(0x3u, a);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < NSTAT; ++k) out[(long long)blockIdx.x * NSTAT + k] = a[k];
+}
+__global__ void __launch_bounds__(REDUCE_THREADS)
+    k_budget_final(const long long *__restrict__ rows, long long nrows, double *__restrict__ out) {
+    double a[NSTAT] = {-INFINITY, -INFINITY, 0, 0, 0, 0, 0, 0};
+    for (long long b = threadIdx.x; b < nrows; b += REDUCE_THREADS) {
+        double v[NSTAT];
+        budget_row_values(rows + b * NSTAT, v);
+        a[0] = fmax(a[0], v[0]);
+        a[1] = fmax(a[1], v[1]);
+#pragma unroll
+        for (int k = 2; k < NSTAT; ++k) a[k] += v[k];
+    }
+    reduce_block<NSTAT>(0x3u, a);
     if (threadIdx.x == 0)
         for (int k = 0; k < NSTAT; ++k) out[k] = a[k];
 }
