@@ -135,10 +135,11 @@ __global__ void k_batch_sum_partials(const BatchCase<S> *__restrict__ cases, dou
 // is left part-empty at a row's end
 // resident 128-thread blocks per SM: the pair forms' body also holds the
 // case descriptor and the work loop, and spills at the single-case FP16
-// kernel's six blocks (80 registers), so every pair form keeps four
+// kernel's six blocks (80 registers); the FP16 form runs at five (96
+// registers, no spill), the FP32 form at four
 template <typename S>
 __host__ __device__ constexpr int batch_bulk_min_blocks() {
-    return pair_form<S>() ? 4 : Store<S>::MIN_BLOCKS;
+    return pair_form<S>() ? (std::is_same_v<S, __half> ? 5 : 4) : Store<S>::MIN_BLOCKS;
 }
 template <typename S, int TB>
 __global__ void __launch_bounds__(TB, batch_bulk_min_blocks<S>() * 128 / TB)

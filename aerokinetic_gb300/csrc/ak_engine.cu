@@ -1606,6 +1606,11 @@ struct ak_refined {
     int4 near{0, 0, 0, 0};
     cudaStream_t bnd = nullptr;
     cudaEvent_t ev_bnd_in = nullptr, ev_bnd_out = nullptr;
+    // two steps in one captured graph: the first leaves its far pass (and
+    // the budget's reduction of its rows) open on the boundaries' branch, and
+    // the second's near pass waits for it (ev_far_done); ev_band_done orders
+    // that reduction after the band's sums
+    cudaEvent_t ev_far_done = nullptr, ev_band_done = nullptr;
     // the budget's outer-face flux beside the far pass: it reads the coarse
     // copy (ghosts written by UBB and outflow), which the far pass only reads
     cudaStream_t ostr = nullptr;
@@ -1630,11 +1635,12 @@ struct ak_refined {
     unsigned *wall_done = nullptr;  // finished-block counters of the two fine steps' wall launches
     long long steps = 0;
     std::vector<void *> owned;  // device buffers the two-level case owns
-    // one captured coarse step per (coarse, fine) buffer parity, replayed by
-    // ak_refined_step; launches_per_step counts the kernels of one replay
-    cudaGraphExec_t graph[16] = {};  // (coarse copy, fine copy, budget, step integrals)
+    // one captured coarse step (or two) per (coarse, fine) buffer parity,
+    // replayed by ak_refined_step; graph_launches counts the kernels of one
+    // replay
+    cudaGraphExec_t graph[32] = {};  // (coarse copy, fine copy, budget, step integrals, two steps)
+    long long graph_launches[32] = {};
     bool step_stats = false;         // the step ends with the budget's integrals
-    long long launches_per_step = 0;
     cudaStream_t side = nullptr;  // the first fine step's stream inside the captured graphs
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // the face-flux registers' branch inside the captured graphs: the coarse
@@ -1693,6 +1699,8 @@ void refined_release(ak_refined *R) {
     if (R->ev_outer_out) cudaEventDestroy(R->ev_outer_out);
     if (R->ostr) cudaStreamDestroy(R->ostr);
     if (R->ev_bnd_out) cudaEventDestroy(R->ev_bnd_out);
+    if (R->ev_far_done) cudaEventDestroy(R->ev_far_done);
+    if (R->ev_band_done) cudaEventDestroy(R->ev_band_done);
     if (R->bnd) cudaStreamDestroy(R->bnd);
     if (R->coarse) {
         release(R->coarse);
@@ -1923,8 +1931,11 @@ int enqueue_region_stats(ak_refined *R, cudaStream_t st) {
     return AK_OK;
 }
 
+// after_open: the previous step of the same capture left its far pass open
+// (leave_open); this step's near pass waits for it.  Both need fork mode
+// with the boundaries' branch.
 template <typename S, typename SF>
-int refined_step(ak_refined *R, bool fork = false) {
+int refined_step(ak_refined *R, bool fork = false, bool after_open = false, bool leave_open = false) {
     using T = typename Store<S>::T;
     using TF = typename Store<SF>::T;
     ak_case *C = R->coarse, *F = R->fine;
@@ -2027,6 +2038,8 @@ int refined_step(ak_refined *R, bool fork = false) {
             R->dx_c * R->dx_c * R->dx_c, R->reg_c);
         if (!bnd) AK_TRY(outer_part(st));
         mark(C);
+        // the near cells pull from cells the previous step's far pass wrote
+        if (bnd && after_open) AK_CUDA(cudaStreamWaitEvent(st, R->ev_far_done, 0));
         if (bnd && fstats)
             k_stream_collide<S, true><<<gsn, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G,
                                                             C->shift_host, (T)C->omega_s, (T)C->omega_b, Sgs<T>{},
@@ -2177,14 +2190,25 @@ int refined_step(ak_refined *R, bool fork = false) {
     else
         launch_restrict<S, SF>(R, f2c, st);
     AK_CUDA(cudaGetLastError());
-    if (bnd) AK_CUDA(cudaStreamWaitEvent(st, R->ev_bnd_out, 0));
-    if (bnd && R->track_budget) AK_CUDA(cudaStreamWaitEvent(st, R->ev_outer_out, 0));
+    // leave_open: the far pass, the budget's outer flux and the reduction of
+    // the coarse rows stay on their branches; the next step of the capture
+    // joins them (its near pass waits for ev_far_done, its end for the rest)
+    const bool open = bnd && leave_open;
+    if (bnd && !open) AK_CUDA(cudaStreamWaitEvent(st, R->ev_bnd_out, 0));
+    if (bnd && R->track_budget && !open) AK_CUDA(cudaStreamWaitEvent(st, R->ev_outer_out, 0));
     // a tracked budget closes on the integrals of the state the step leaves
     if (fstats) {
         if (!fork) AK_TRY(enqueue_fine_stats<SF>(R, st));
-        AK_TRY(enqueue_coarse_rows_final(R, st));
+        if (open) {
+            AK_CUDA(cudaEventRecord(R->ev_band_done, st));
+            AK_CUDA(cudaStreamWaitEvent(R->bnd, R->ev_band_done, 0));
+            AK_TRY(enqueue_coarse_rows_final(R, R->bnd));
+        } else {
+            AK_TRY(enqueue_coarse_rows_final(R, st));
+        }
     } else if (R->track_budget && R->step_stats)
         AK_TRY((enqueue_region_stats<S, SF>(R, st)));
+    if (open) AK_CUDA(cudaEventRecord(R->ev_far_done, R->bnd));
     mark(C);  // step end
     C->launches += 6 + 6 * 2 - (donors_collide ? 1 : 0) + (C->n_ubb ? 1 : 0) + (C->n_out ? 1 : 0) + (nlinks ? 0 : -2) + 1 +
                    (bnd ? 1 : 0);
@@ -2227,25 +2251,34 @@ int graph_priorities(ak_refined *R, cudaGraph_t g) {
     return AK_OK;
 }
 
-// One coarse step replayed from a CUDA graph: the step's kernel sequence is
-// captured once per buffer parity (the coarse copies swap every step, the
-// fine copies twice) and the host-side counters are advanced as the eager
-// step advances them.
+// One coarse step, or two, replayed from a CUDA graph: the steps' kernel
+// sequence is captured once per buffer parity (the coarse copies swap every
+// step, the fine copies twice) and the host-side counters are advanced as the
+// eager step advances them.  Two steps in one graph (fused form with the
+// boundaries' branch) overlap the second step's first fine step, donor
+// moments and transfer-block collision with the first step's far pass.
 template <typename S, typename SF>
-int refined_step_graphed(ak_refined *R) {
+int refined_step_graphed(ak_refined *R, int nsteps) {
     ak_case *C = R->coarse, *F = R->fine;
-    const int slot = C->cur | (F->cur << 1) | (R->track_budget ? 4 : 0) | (R->step_stats ? 8 : 0);
+    const int slot = C->cur | (F->cur << 1) | (R->track_budget ? 4 : 0) | (R->step_stats ? 8 : 0) |
+                     (nsteps == 2 ? 16 : 0);
     if (!R->graph[slot]) {
         const int ccur = C->cur, fcur = F->cur;
         const long long cs = C->steps, fs = F->steps, rs = R->steps, cl = C->launches;
         std::vector<cudaEvent_t> *timing = C->timing;
         C->timing = nullptr;
         AK_CUDA(cudaStreamBeginCapture(C->stream, cudaStreamCaptureModeThreadLocal));
-        const int r = refined_step<S, SF>(R, true);
+        int r = AK_OK;
+        if (nsteps == 2) {
+            r = refined_step<S, SF>(R, true, false, true);
+            if (r == AK_OK) r = refined_step<S, SF>(R, true, true, false);
+        } else {
+            r = refined_step<S, SF>(R, true);
+        }
         cudaGraph_t g = nullptr;
         const cudaError_t e = cudaStreamEndCapture(C->stream, &g);
         C->timing = timing;
-        R->launches_per_step = C->launches - cl;
+        R->graph_launches[slot] = C->launches - cl;
         C->cur = ccur;
         F->cur = fcur;
         C->steps = cs;
@@ -2273,13 +2306,25 @@ int refined_step_graphed(ak_refined *R) {
         }
     }
     AK_CUDA(cudaGraphLaunch(R->graph[slot], C->stream));
-    C->cur = 1 - C->cur;
+    if (nsteps == 1) C->cur = 1 - C->cur;
     R->pre_mode = 1;
     R->pre_writes = C->pdf_writes;
-    C->launches += R->launches_per_step;
-    C->steps += 1;
-    F->steps += 2;
-    R->steps += 1;
+    C->launches += R->graph_launches[slot];
+    C->steps += nsteps;
+    F->steps += 2 * nsteps;
+    R->steps += nsteps;
+    return AK_OK;
+}
+
+// steps replayed two per graph where the form allows it
+template <typename S, typename SF>
+int refined_steps_graphed(ak_refined *R, int nsteps) {
+    const bool pairs = R->fused && R->bnd_branch;
+    for (int s = 0; s < nsteps;) {
+        const int k = pairs && nsteps - s >= 2 ? 2 : 1;
+        AK_TRY((refined_step_graphed<S, SF>(R, k)));
+        s += k;
+    }
     return AK_OK;
 }
 
@@ -2476,6 +2521,8 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
                        cudaStreamCreateWithFlags(&R->bnd, cudaStreamNonBlocking) != cudaSuccess ||
                        cudaEventCreateWithFlags(&R->ev_bnd_in, cudaEventDisableTiming) != cudaSuccess ||
                        cudaEventCreateWithFlags(&R->ev_bnd_out, cudaEventDisableTiming) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&R->ev_far_done, cudaEventDisableTiming) != cudaSuccess ||
+                       cudaEventCreateWithFlags(&R->ev_band_done, cudaEventDisableTiming) != cudaSuccess ||
                        cudaStreamCreateWithFlags(&R->ostr, cudaStreamNonBlocking) != cudaSuccess ||
                        cudaEventCreateWithFlags(&R->ev_outer_in, cudaEventDisableTiming) != cudaSuccess ||
                        cudaEventCreateWithFlags(&R->ev_outer_out, cudaEventDisableTiming) != cudaSuccess))
@@ -2535,14 +2582,14 @@ int ak_refined_step_budget(ak_refined *R, int32_t nsteps, double *loads, double 
         return fail(AK_ERR_INVALID, "the outer flux and the integrals of a step need budget tracking");
     cudaStream_t st = R->coarse->stream;
     AK_CUDA(cudaMemsetAsync(R->d_flag, 0, sizeof(int), st));
-    for (int s = 0; s < nsteps; ++s) {
+    {
         // with stats every step closes its budget on the integrals of the
         // state it leaves (the reference's step, refined_solver.py:311-343);
         // the last step's are returned
         R->step_stats = stats != nullptr;
         const int r = with_levels(R, [&](auto *tc, auto *tf) {
             AK_LEVEL_TYPES(tc, tf);
-            return refined_step_graphed<S, SF>(R);
+            return refined_steps_graphed<S, SF>(R, nsteps);
         });
         R->step_stats = false;
         if (r != AK_OK) return r;

@@ -389,6 +389,42 @@ def test_refined_graph_replay_matches_eager_steps(golden):
         eager.close()
 
 
+def test_refined_two_step_graphs_match_single_steps():
+    """Budget steps replayed two per graph (the second step's first fine step
+    and donor moments overlapping the first step's far pass) against the same
+    steps replayed one per graph and issued eagerly: states, loads, outer
+    flux and integrals agree bit for bit on the benchmark's two-level case."""
+    import ctypes
+    import bench
+    from aerokinetic_gb300 import _native
+    from aerokinetic_gb300.refined import RefinedSolver
+    project, refinement = bench.refined_parts()
+    pairs, single, eager = (RefinedSolver(project, refinement, storage="f64") for _ in range(3))
+    try:
+        lib = pairs._lib
+        n = len(pairs.contours)
+        out = {}
+        for name, solver in (("pairs", pairs), ("single", single)):
+            loads, outer, stats = np.zeros((n, 5)), np.zeros(8), np.zeros(16)
+            ptrs = [a.ctypes.data_as(ctypes.c_void_p) for a in (loads, outer, stats)]
+            if name == "pairs":
+                _native.check(lib.ak_refined_step_budget(solver._handle, 6, *ptrs))
+            else:
+                for _ in range(6):
+                    _native.check(lib.ak_refined_step_budget(solver._handle, 1, *ptrs))
+            out[name] = (loads, outer, stats)
+        ms = np.zeros(6)
+        _native.check(lib.ak_refined_step_timed(eager._handle, 6, ms.ctypes.data_as(ctypes.c_void_p)))
+        for a, b in zip(out["pairs"], out["single"]):
+            assert np.array_equal(a, b)
+        assert lib.ak_refined_steps_done(pairs._handle) == lib.ak_refined_steps_done(eager._handle) == 6
+        for a, b, c in zip(pairs.states(), single.states(), eager.states()):
+            assert np.array_equal(a, b) and np.array_equal(a, c)
+    finally:
+        for solver in (pairs, single, eager):
+            solver.close()
+
+
 def test_refined_budget_integrals_and_diagnostics_match_oracle(golden):
     """conserved_integrals, the per-step budget (last_budget) and diagnostics
     (refined_solver.py:291-361) against the oracle sampling the outer faces in
