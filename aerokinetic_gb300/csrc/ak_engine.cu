@@ -57,6 +57,42 @@ template <typename S>
 unsigned stream_collide_grid(int4 rect, int nx, int ny, int nz) {
     return (unsigned)blocks_for(stream_collide_items<S>(rect, nx, ny, nz), 128);
 }
+// A launch with programmatic stream serialization: it may be scheduled while
+// its predecessor on the stream drains (the launch latency of a chain of short
+// kernels overlaps their tails); the kernel itself waits (chain_wait) before
+// it touches memory.  Only kernels that start with chain_wait go through here.
+// With chained false it is an ordinary launch.  A chained kernel's blocks
+// can become resident while its predecessor still runs and then wait there,
+// holding SM slots that concurrent branches (the far coarse pass, the other
+// fine step) could use; the launch sites below are chained only where that
+// measured faster (CHAIN_* flags).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_chained(bool chained, void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st,
+                           Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = chained ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+// which launch sites are chained: the fine steps' kernels after their donor
+// moments' x pass (FINE), the x pass itself (PROLONG), the coarse
+// transfer-block collision, near pass and donor moments (COARSE), the
+// restriction, reflux and budget sums at the step's end (TAIL), the uniform
+// step's bulk pass (UNIFORM).  Measured on the two-level benchmark case,
+// graph-replayed ms per coarse step (FP32 / FP16 with FP32 walls / df64):
+// none 0.1744 / 0.1649 / 0.496; FINE 0.1633 / 0.1528 / 0.495; FINE + PROLONG
+// 0.1628 / 0.1527 / 0.495; + TAIL 0.1644 / 0.1539 / 0.494; all 0.1650 /
+// 0.1553 / 0.483.  The FP64 step (1.107 ms) and the uniform steps do not move.
+constexpr bool CHAIN_FINE = true, CHAIN_PROLONG = true, CHAIN_COARSE = false, CHAIN_TAIL = false,
+               CHAIN_UNIFORM = false;
+
 // fixed grid of the per-case reductions whose results must not depend on the device
 constexpr int STATS_BLOCKS_CASE = 4 * 152;
 
@@ -595,12 +631,13 @@ int one_step(ak_case *c, bool sample, double *fixed_partials = nullptr, long lon
         AK_CUDA(cudaEventRecord(c->ev_join, c->side));
         AK_CUDA(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
     }
-    // bulk
+    // bulk (scheduled while the boundary kernels drain; it waits for them)
     mark(c);
     const unsigned grid = stream_collide_grid<S>(make_int4(0, 0, 0, 0), c->nx, c->ny, c->nz);
-    k_stream_collide<S><<<grid, 128, 0, c->stream>>>(src, dst_of<S>(c), c->flags, c->G, c->shift_host,
-                                                     (T)c->omega_s, (T)c->omega_b, sgs_of<S>(c));
-    AK_CUDA(cudaGetLastError());
+    AK_CUDA(launch_chained(CHAIN_UNIFORM, k_stream_collide<S, false>, dim3(grid), dim3(128), c->stream, (const S *)src,
+                           dst_of<S>(c), (const uint8_t *)c->flags, c->G, c->shift_host, (T)c->omega_s,
+                           (T)c->omega_b, sgs_of<S>(c), make_int4(0, 0, 0, 0), make_int4(0, 0, 0, 0),
+                           make_int4(0, 0, 0, 0), (long long *)nullptr));
     ++c->launches;
     mark(c);
     c->cur = 1 - c->cur;
@@ -1778,14 +1815,14 @@ typename Store<S>::A *moments_of(double *p) {
 
 // restriction of the fine block onto the covered coarse cells
 template <typename S, typename SF>
-void launch_restrict(ak_refined *R, const Rescale &f2c, cudaStream_t st) {
+cudaError_t launch_restrict(ak_refined *R, const Rescale &f2c, cudaStream_t st) {
     const BoxSpec &B = R->B;
     const long long ring = ring_count(B.bx, B.by, 3, 3) * B.bz;
     const long long core = (long long)std::max(B.bx - 6, 0) * std::max(B.by - 6, 0) * B.bz;
     const long long nb = std::max(split_blocks(ring), blocks3(core));
-    k_restrict<S, SF><<<dim3((unsigned)nb, 2), SPLIT_THREADS, 0, st>>>(src_of<S>(R->coarse), R->coarse->G,
-                                                                        src_of<SF>(R->fine), R->fine->G, B, R->pad,
-                                                                        R->d_free, f2c, R->d_flag);
+    return launch_chained(CHAIN_TAIL, k_restrict<S, SF>, dim3((unsigned)nb, 2), dim3(SPLIT_THREADS), st, src_of<S>(R->coarse),
+                   R->coarse->G, (const SF *)src_of<SF>(R->fine), R->fine->G, B, R->pad, (const double *)R->d_free, f2c,
+                   R->d_flag);
 }
 
 template <typename S, typename SF>
@@ -1809,7 +1846,7 @@ int refined_init(ak_refined *R, double amp, double phase_y, double phase_z, doub
     AK_TRY(level(F, (SF *)nullptr));
     const Rescale f2c{R->tau_s_c * R->dt_c / (R->tau_s_f * R->dt_f), R->tau_b_c * R->dt_c / (R->tau_b_f * R->dt_f)};
     AK_CUDA(cudaMemsetAsync(R->d_flag, 0, sizeof(int), st));
-    launch_restrict<S, SF>(R, f2c, st);
+    AK_CUDA((launch_restrict<S, SF>(R, f2c, st)));
     AK_CUDA(cudaGetLastError());
     // boundary data from the initial state, ghosts still holding the free
     // stream (refined_solver.py:224-262)
@@ -1884,7 +1921,8 @@ int enqueue_fine_stats(ak_refined *R, cudaStream_t st) {
     ak_case *F = R->fine;
     const Region rf = fine_region(R);
     const long long rows = region_sum_rows(region_cells(rf, F->nz));
-    k_region_sums<SF><<<(unsigned)(rows / 8), 256, 0, st>>>(src_of<SF>(F), F->G, F->flags, rf, R->fine_rows);
+    AK_CUDA(launch_chained(CHAIN_TAIL, k_region_sums<SF>, dim3((unsigned)(rows / 8)), dim3(256), st, (const SF *)src_of<SF>(F),
+                           F->G, (const uint8_t *)F->flags, rf, R->fine_rows));
     R->coarse->launches += 1;
     AK_CUDA(cudaGetLastError());
     return enqueue_rows_final(R, R->fine_rows, rows, R->fine_stage, R->stats_out + NSTAT, st);
@@ -1903,8 +1941,9 @@ int enqueue_band_sums(ak_refined *R, cudaStream_t st) {
     ak_case *C = R->coarse;
     const Region band = band_region(R);
     const long long band_rows = region_sum_rows(region_cells(band, C->nz));
-    k_region_sums<S><<<(unsigned)(band_rows / 8), 256, 0, st>>>(src_of<S>(C), C->G, C->flags, band,
-                                                                R->cstats + (R->cstats_far + R->cstats_near) * NSTAT);
+    AK_CUDA(launch_chained(CHAIN_TAIL, k_region_sums<S>, dim3((unsigned)(band_rows / 8)), dim3(256), st, (const S *)src_of<S>(C),
+                           C->G, (const uint8_t *)C->flags, band,
+                           R->cstats + (R->cstats_far + R->cstats_near) * NSTAT));
     C->launches += 1;
     AK_CUDA(cudaGetLastError());
     return AK_OK;
@@ -2023,8 +2062,8 @@ int refined_step(ak_refined *R, bool fork = false, bool after_open = false, bool
         // fused: only the transfer block holds pre-collision populations (a
         // grid over its cells alone)
         if (R->fused)
-            k_collide<S><<<gx1, 128, 0, st>>>(src_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s,
-                                              (T)C->omega_b, R->xfer);
+            AK_CUDA(launch_chained(CHAIN_COARSE, k_collide<S>, dim3(gx1), dim3(128), st, src_of<S>(C), C->flags, C->G,
+                                   C->shift_host, (T)C->omega_s, (T)C->omega_b, R->xfer, make_int4(0, 0, 0, 0)));
         else
             k_collide<S><<<gc1, 128, 0, st>>>(src_of<S>(C), C->flags, C->G, C->shift_host, (T)C->omega_s,
                                               (T)C->omega_b);
@@ -2041,14 +2080,16 @@ int refined_step(ak_refined *R, bool fork = false, bool after_open = false, bool
         // the near cells pull from cells the previous step's far pass wrote
         if (bnd && after_open) AK_CUDA(cudaStreamWaitEvent(st, R->ev_far_done, 0));
         if (bnd && fstats)
-            k_stream_collide<S, true><<<gsn, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G,
-                                                            C->shift_host, (T)C->omega_s, (T)C->omega_b, Sgs<T>{},
-                                                            R->xfer, R->near, make_int4(0, 0, 0, 0),
-                                                            R->cstats + R->cstats_far * NSTAT);
+            AK_CUDA(launch_chained(CHAIN_COARSE, k_stream_collide<S, true>, dim3(gsn), dim3(128), st, (const S *)src_of<S>(C),
+                                   dst_of<S>(C), (const uint8_t *)C->flags, C->G, C->shift_host, (T)C->omega_s,
+                                   (T)C->omega_b, Sgs<T>{}, R->xfer, R->near, make_int4(0, 0, 0, 0),
+                                   R->cstats + R->cstats_far * NSTAT));
         else if (bnd)
             // the cells of near; the rest runs on the boundaries' branch
-            k_stream_collide<S><<<gsn, 128, 0, st>>>(src_of<S>(C), dst_of<S>(C), C->flags, C->G, C->shift_host,
-                                                      (T)C->omega_s, (T)C->omega_b, Sgs<T>{}, R->xfer, R->near);
+            AK_CUDA(launch_chained(CHAIN_COARSE, k_stream_collide<S, false>, dim3(gsn), dim3(128), st, (const S *)src_of<S>(C),
+                                   dst_of<S>(C), (const uint8_t *)C->flags, C->G, C->shift_host, (T)C->omega_s,
+                                   (T)C->omega_b, Sgs<T>{}, R->xfer, R->near, make_int4(0, 0, 0, 0),
+                                   (long long *)nullptr));
         else if (R->fused && fstats) {
             // one launch covers every row of the far part; the near rows stay empty
             AK_CUDA(cudaMemsetAsync(R->cstats + R->cstats_far * NSTAT, 0, sizeof(long long) * R->cstats_near * NSTAT, st));
@@ -2066,9 +2107,10 @@ int refined_step(ak_refined *R, bool fork = false, bool after_open = false, bool
         mark(C);
         AK_CUDA(cudaGetLastError());
         C->cur = 1 - C->cur;
-        k_block_moments<S><<<(unsigned)split_blocks(nring_block), SPLIT_THREADS, 0, st>>>(
-            src_of<S>(C), C->G, B, R->d_free, moments_of<S>(R->mom_new), moments_of<S>(R->mom_old), moments_of<S>(R->mom_half),
-            R->d_flag);
+        AK_CUDA(launch_chained(CHAIN_COARSE, k_block_moments<S>, dim3((unsigned)split_blocks(nring_block)), dim3(SPLIT_THREADS), st,
+                               (const S *)src_of<S>(C), C->G, B, (const double *)R->d_free, moments_of<S>(R->mom_new),
+                               (const typename Store<S>::A *)moments_of<S>(R->mom_old), moments_of<S>(R->mom_half),
+                               R->d_flag));
         AK_CUDA(cudaGetLastError());
         return AK_OK;
     };
@@ -2089,31 +2131,34 @@ int refined_step(ak_refined *R, bool fork = false, bool after_open = false, bool
     auto fine_part = [&](int sub, cudaStream_t s) -> int {
         // donor moments at the fine step's start: the old coarse state, then
         // half-way (1 - 1/2) old + 1/2 new (refined_solver.py:311-318)
-        k_prolong_x<<<(unsigned)blocks3(nprox), 256, 0, s>>>(B, C->nz, R->pad,
-                                                              moments_of<S>(sub ? R->mom_half : R->mom_old),
-                                                              moments_of<S>(R->pro_x));
+        AK_CUDA(launch_chained(CHAIN_PROLONG, k_prolong_x<typename Store<S>::A>, dim3((unsigned)blocks3(nprox)), dim3(256), s, B,
+                               C->nz, R->pad,
+                               (const typename Store<S>::A *)moments_of<S>(sub ? R->mom_half : R->mom_old),
+                               moments_of<S>(R->pro_x)));
         bool collided = false;
+        const dim3 gd((unsigned)split_blocks(nband)), bd(SPLIT_THREADS);
         if constexpr (donors_collide) {
             if (sub == 1) {
-                k_donors<SF, true><<<(unsigned)split_blocks(nband), SPLIT_THREADS, 0, s>>>(
-                    src_of<SF>(F), F->G, C->nz, moments_of<S>(R->pro_x), B.dny, c2f, R->pad, R->d_flag, F->flags,
-                    (TF)F->omega_s, (TF)F->omega_b);
+                AK_CUDA(launch_chained(CHAIN_FINE, k_donors<SF, true>, gd, bd, s, src_of<SF>(F), F->G, C->nz,
+                                       moments_of<S>(R->pro_x), B.dny, c2f, R->pad, R->d_flag, F->flags,
+                                       (TF)F->omega_s, (TF)F->omega_b));
                 collided = true;
             }
         }
         if (!collided)
-            k_donors<SF><<<(unsigned)split_blocks(nband), SPLIT_THREADS, 0, s>>>(src_of<SF>(F), F->G, C->nz,
-                                                                                 moments_of<S>(R->pro_x), B.dny, c2f,
-                                                                                 R->pad, R->d_flag);
+            AK_CUDA(launch_chained(CHAIN_FINE, k_donors<SF, false>, gd, bd, s, src_of<SF>(F), F->G, C->nz, moments_of<S>(R->pro_x),
+                                   B.dny, c2f, R->pad, R->d_flag, (const uint8_t *)nullptr, (TF)0, (TF)0));
         mark(C);
         if (sub == 0 || !fine_fused)
-            k_collide<SF><<<gf1, 128, 0, s>>>(src_of<SF>(F), F->flags, F->G, F->shift_host, (TF)F->omega_s,
-                                               (TF)F->omega_b);
+            AK_CUDA(launch_chained(CHAIN_FINE, k_collide<SF>, dim3(gf1), dim3(128), s, src_of<SF>(F), F->flags, F->G,
+                                   F->shift_host, (TF)F->omega_s, (TF)F->omega_b, make_int4(0, 0, 0, 0),
+                                   make_int4(0, 0, 0, 0)));
         else if (!collided)
             // the band alone: the physical block was collided by the first
             // step's stream-collide
-            k_collide_band<SF><<<(unsigned)blocks_for(nband, 128), 128, 0, s>>>(
-                src_of<SF>(F), F->flags, F->G, F->shift_host, (TF)F->omega_s, (TF)F->omega_b, R->pad);
+            AK_CUDA(launch_chained(CHAIN_FINE, k_collide_band<SF>, dim3((unsigned)blocks_for(nband, 128)), dim3(128), s,
+                                   src_of<SF>(F), F->flags, F->G, F->shift_host, (TF)F->omega_s, (TF)F->omega_b,
+                                   R->pad));
         mark(C);
         cudaStream_t fs = flux_stream(s, 1 + sub);
         if (!fs) return fail(AK_ERR_CUDA, "face-flux branch could not be forked");
@@ -2124,19 +2169,21 @@ int refined_step(ak_refined *R, bool fork = false, bool after_open = false, bool
         // the walls' last block sums the loads; the second fine step's also
         // adds both steps' loads to the running sums
         if (nlinks)
-            k_walls<SF><<<(unsigned)nb, 256, 0, s>>>(src_of<SF>(F), F->G, F->keys, F->wall_q, F->nkeys, 1,
-                                                     F->n_elements, F->ox, F->oy, F->partials, R->wall_done + sub,
-                                                     R->d_loads + sub * 5 * F->n_elements,
-                                                     sub ? R->cum_loads : nullptr, R->d_loads);
+            AK_CUDA(launch_chained(CHAIN_FINE, k_walls<SF>, dim3((unsigned)nb), dim3(256), s, src_of<SF>(F), F->G, F->keys,
+                                   F->wall_q, F->nkeys, 1, F->n_elements, F->ox, F->oy, F->partials,
+                                   R->wall_done + sub, R->d_loads + sub * 5 * F->n_elements,
+                                   sub ? R->cum_loads : (double *)nullptr, (const double *)R->d_loads));
         mark(C);
         // the second fine step streams into the copy the first step's flux reads
         if (fork && sub == 1) AK_CUDA(cudaStreamWaitEvent(s, R->ev_flux_f0, 0));
         if (fine_fused && sub == 0)
-            k_stream_collide<SF><<<gfr, 128, 0, s>>>(src_of<SF>(F), dst_of<SF>(F), F->flags, F->G, F->shift_host,
-                                                     (TF)F->omega_s, (TF)F->omega_b, Sgs<TF>{}, make_int4(0, 0, 0, 0),
-                                                     fine_rect);
+            AK_CUDA(launch_chained(CHAIN_FINE, k_stream_collide<SF, false>, dim3(gfr), dim3(128), s, (const SF *)src_of<SF>(F),
+                                   dst_of<SF>(F), (const uint8_t *)F->flags, F->G, F->shift_host, (TF)F->omega_s,
+                                   (TF)F->omega_b, Sgs<TF>{}, make_int4(0, 0, 0, 0), fine_rect,
+                                   make_int4(0, 0, 0, 0), (long long *)nullptr));
         else
-            k_stream<SF><<<gf, 128, 0, s>>>(src_of<SF>(F), dst_of<SF>(F), F->flags, F->G, 1);
+            AK_CUDA(launch_chained(CHAIN_FINE, k_stream<SF>, gf, dim3(128), s, (const SF *)src_of<SF>(F), dst_of<SF>(F),
+                                   (const uint8_t *)F->flags, F->G, 1));
         mark(C);
         AK_CUDA(cudaGetLastError());
         F->cur = 1 - F->cur;
@@ -2173,22 +2220,23 @@ int refined_step(ak_refined *R, bool fork = false, bool after_open = false, bool
     if (fork) {
         AK_CUDA(cudaEventRecord(R->ev_fork, st));
         AK_CUDA(cudaStreamWaitEvent(R->side, R->ev_fork, 0));
-        launch_restrict<S, SF>(R, f2c, R->side);
+        AK_CUDA((launch_restrict<S, SF>(R, f2c, R->side)));
         // the fine block's statistics beside the reflux (both levels' final
         // states are complete: the fine one before the fork)
         if (fstats) AK_TRY(enqueue_fine_stats<SF>(R, R->side));
         AK_CUDA(cudaEventRecord(R->ev_join, R->side));
     }
-    k_reflux<S><<<dim3((unsigned)split_blocks(R->max_face), R->nfaces), SPLIT_THREADS, 0, st>>>(
-        src_of<S>(C), C->G, R->d_faces, R->nfaces, R->d_offs, R->reg_c, R->reg_f,
-        1.0 / (R->dx_c * R->dx_c * R->dx_c), R->d_flag);
+    AK_CUDA(launch_chained(CHAIN_TAIL, k_reflux<S>, dim3((unsigned)split_blocks(R->max_face), R->nfaces), dim3(SPLIT_THREADS), st,
+                           src_of<S>(C), C->G, (const Face *)R->d_faces, R->nfaces, (const long long *)R->d_offs,
+                           (const double *)R->reg_c, (const double *)R->reg_f, 1.0 / (R->dx_c * R->dx_c * R->dx_c),
+                           R->d_flag));
     // the transfer block's cells outside the box are final after the reflux
     // (the restriction writes the box's): their sums run beside the far pass
     if (fstats) AK_TRY(enqueue_band_sums<S>(R, st));
     if (fork)
         AK_CUDA(cudaStreamWaitEvent(st, R->ev_join, 0));
     else
-        launch_restrict<S, SF>(R, f2c, st);
+        AK_CUDA((launch_restrict<S, SF>(R, f2c, st)));
     AK_CUDA(cudaGetLastError());
     // leave_open: the far pass, the budget's outer flux and the reduction of
     // the coarse rows stay on their branches; the next step of the capture
@@ -2755,7 +2803,7 @@ int ak_refined_probe(ak_refined *R, int32_t op, double *out, int64_t *n_out) {
         } else if (op == 1) {
             const Rescale f2c{R->tau_s_c * R->dt_c / (R->tau_s_f * R->dt_f),
                               R->tau_b_c * R->dt_c / (R->tau_b_f * R->dt_f)};
-            launch_restrict<S, SF>(R, f2c, st);
+            AK_CUDA((launch_restrict<S, SF>(R, f2c, st)));
         } else if (op == 2) {
             AK_CUDA(cudaMemsetAsync(R->reg_f, 0, sizeof(double) * R->reg_doubles, st));
             k_face_flux_coarse<S><<<dim3((unsigned)blocks3(32 * R->max_face), R->nfaces), 256, 0, st>>>(

@@ -58,6 +58,17 @@ __device__ __forceinline__ bool ak_in_range(const Grid &G, int q, int x, int y, 
 #define AK_CHECK(G, q, x, y, z, tag) true
 #endif
 
+// Kernels of the two-level step's chains may be launched with programmatic
+// stream serialization (launch_chained on the host): such a launch can be
+// scheduled while its predecessor on the stream drains, and waits here,
+// before it touches memory, until that predecessor has completed and its
+// writes are visible.  Launched the ordinary way, the wait returns at once.
+__device__ __forceinline__ void chain_wait() {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+}
+
 template <typename S>
 __device__ __forceinline__ double load_g(const S *pdf, const Grid &G, int q, int x, int y, int z) {
     if (!AK_CHECK(G, q, x, y, z, 1)) return 0.0;
@@ -479,6 +490,7 @@ __global__ void __launch_bounds__(128, stream_collide_min_blocks<S>())
                      Sgs<typename Store<S>::T> sgs, int4 raw = make_int4(0, 0, 0, 0),
                      int4 rect = make_int4(0, 0, 0, 0), int4 skip = make_int4(0, 0, 0, 0),
                      long long *__restrict__ stats = nullptr) {
+    chain_wait();
     // one thread per cell of the padded columns x [rect.x, rect.y) by y
     // [rect.z, rect.w) (rect.y == 0: the whole interior), every z, x fastest,
     // numbered across rows: warps stay full whatever the width (the plain
@@ -655,6 +667,7 @@ __global__ void __launch_bounds__(256, 2) k_walls(S *__restrict__ pdf, Grid G, c
                                                double *__restrict__ partials, unsigned *done = nullptr,
                                                double *out = nullptr, double *cum = nullptr,
                                                const double *first = nullptr) {
+    chain_wait();
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     double acc[5] = {0, 0, 0, 0, 0};
     int element = -1;

@@ -303,6 +303,7 @@ __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
     k_collide(S *__restrict__ pdf, const uint8_t *__restrict__ flags, Grid G, Shift27 shift,
               typename Store<S>::T omega_s, typename Store<S>::T omega_b,
               int4 rect = make_int4(0, 0, 0, 0), int4 skip = make_int4(0, 0, 0, 0)) {
+    chain_wait();
     using T = typename Store<S>::T;
     // one thread per cell of the padded columns x [rect.x, rect.y) by y
     // [rect.z, rect.w) (rect.y == 0: the whole interior), every z, x fastest,
@@ -335,6 +336,7 @@ template <typename S>
 __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
     k_collide_band(S *__restrict__ pdf, const uint8_t *__restrict__ flags, Grid G, Shift27 shift,
                    typename Store<S>::T omega_s, typename Store<S>::T omega_b, int pad) {
+    chain_wait();
     using T = typename Store<S>::T;
     const long long nring = ring_count(G.nx, G.ny, pad, pad);
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -356,6 +358,7 @@ __global__ void __launch_bounds__(128, Store<S>::MIN_BLOCKS)
 template <typename S>
 __global__ void k_stream(const S *__restrict__ src, S *__restrict__ dst, const uint8_t *__restrict__ flags, Grid G,
                          int periodic_xy) {
+    chain_wait();
     const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int y = blockIdx.y + 1;
     const int z = blockIdx.z;
@@ -541,6 +544,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
     k_block_moments(const S *__restrict__ pdf, Grid G, BoxSpec B, const double *__restrict__ free_g,
                     typename Store<S>::A *__restrict__ out, const typename Store<S>::A *__restrict__ mix_from,
                     typename Store<S>::A *__restrict__ half, int *__restrict__ flag) {
+    chain_wait();
     using T = typename Store<S>::A;
     __shared__ SplitShared<T> sh;
     const long long nring = ring_count(B.dnx, B.dny, DONOR_RING, DONOR_RING), nr = nring * G.nz;
@@ -598,6 +602,7 @@ __device__ __forceinline__ T prolong_child(T am2, T am1, T a0, T ap1, T ap2, int
 // on each side, the band columns elsewhere
 template <typename T>
 __global__ void k_prolong_x(BoxSpec B, int nz, int pad, const T *__restrict__ m, T *__restrict__ out) {
+    chain_wait();
     const int nfx = 2 * (B.bx + 2);
     const long long nring = ring_count(nfx, B.dny, pad, DONOR_RING);
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -630,6 +635,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
              int pad, int *__restrict__ flag, const uint8_t *__restrict__ flags = nullptr,
              typename Store<S>::T omega_s = 0, typename Store<S>::T omega_b = 0) {
     static_assert(!COLLIDE || !std::is_same_v<S, __half>, "FP16 storage rounds the donors before the collision");
+    chain_wait();
     using T = typename Store<S>::A;
     __shared__ SplitShared<T> sh;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -712,6 +718,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS)
     k_reflux(S *__restrict__ pdf, Grid G, const Face *__restrict__ faces, int nfaces,
              const long long *__restrict__ offsets, const double *__restrict__ reg_c,
              const double *__restrict__ reg_f, double inv_volume, int *__restrict__ flag) {
+    chain_wait();
     using T = typename Store<S>::A;
     __shared__ SplitShared<T> sh;
     const int f = blockIdx.y;
@@ -800,6 +807,7 @@ template <typename Sc, typename Sf>
 __global__ void __launch_bounds__(SPLIT_THREADS, 2)
     k_restrict(Sc *__restrict__ coarse, Grid G, const Sf *__restrict__ fine, Grid F, BoxSpec B, int pad,
                const double *__restrict__ free_g, Rescale r, int *__restrict__ flag) {
+    chain_wait();
     using T = typename Store<Sc>::A;
     __shared__ SplitShared<T> sh;
     if (blockIdx.y == 1) {
@@ -1011,6 +1019,7 @@ template <typename S>
 __global__ void __launch_bounds__(256)
     k_region_sums(const S *__restrict__ pdf, Grid G, const uint8_t *__restrict__ flags, Region R,
                   long long *__restrict__ rows) {
+    chain_wait();
     const int w = R.x1 - R.x0, h = R.y1 - R.y0;
     const long long n = (long long)w * h * G.nz;
     BudgetSums acc;
