@@ -1657,7 +1657,8 @@ struct ak_refined {
     double free_g[Q];
     double *d_free = nullptr;
     double *mom_old = nullptr, *mom_new = nullptr, *mom_half = nullptr;
-    double *pro_x = nullptr;  // donor moments after the x prolongation pass
+    double *pro_x = nullptr;  // donor moments after the x prolongation pass (first fine step)
+    double *pro_x2 = nullptr; // the same for the second fine step, made right after the coarse step
     Face faces[4];
     int nfaces = 0;
     long long offs[4] = {0, 0, 0, 0};
@@ -2111,6 +2112,11 @@ int refined_step(ak_refined *R, bool fork = false, bool after_open = false, bool
                                (const S *)src_of<S>(C), C->G, B, (const double *)R->d_free, moments_of<S>(R->mom_new),
                                (const typename Store<S>::A *)moments_of<S>(R->mom_old), moments_of<S>(R->mom_half),
                                R->d_flag));
+        // the second fine step's x pass, from the half-way donor moments: it
+        // needs nothing of the first fine step, so it runs before the join
+        AK_CUDA(launch_chained(CHAIN_PROLONG, k_prolong_x<typename Store<S>::A>, dim3((unsigned)blocks3(nprox)),
+                               dim3(256), st, B, C->nz, R->pad, (const typename Store<S>::A *)moments_of<S>(R->mom_half),
+                               moments_of<S>(R->pro_x2)));
         AK_CUDA(cudaGetLastError());
         return AK_OK;
     };
@@ -2131,22 +2137,24 @@ int refined_step(ak_refined *R, bool fork = false, bool after_open = false, bool
     auto fine_part = [&](int sub, cudaStream_t s) -> int {
         // donor moments at the fine step's start: the old coarse state, then
         // half-way (1 - 1/2) old + 1/2 new (refined_solver.py:311-318)
-        AK_CUDA(launch_chained(CHAIN_PROLONG, k_prolong_x<typename Store<S>::A>, dim3((unsigned)blocks3(nprox)), dim3(256), s, B,
-                               C->nz, R->pad,
-                               (const typename Store<S>::A *)moments_of<S>(sub ? R->mom_half : R->mom_old),
-                               moments_of<S>(R->pro_x)));
+        // (the second fine step's x pass ran at the end of the coarse step)
+        if (sub == 0)
+            AK_CUDA(launch_chained(CHAIN_PROLONG, k_prolong_x<typename Store<S>::A>, dim3((unsigned)blocks3(nprox)),
+                                   dim3(256), s, B, C->nz, R->pad,
+                                   (const typename Store<S>::A *)moments_of<S>(R->mom_old), moments_of<S>(R->pro_x)));
+        const typename Store<S>::A *px = moments_of<S>(sub ? R->pro_x2 : R->pro_x);
         bool collided = false;
         const dim3 gd((unsigned)split_blocks(nband)), bd(SPLIT_THREADS);
         if constexpr (donors_collide) {
             if (sub == 1) {
                 AK_CUDA(launch_chained(CHAIN_FINE, k_donors<SF, true>, gd, bd, s, src_of<SF>(F), F->G, C->nz,
-                                       moments_of<S>(R->pro_x), B.dny, c2f, R->pad, R->d_flag, F->flags,
+                                       px, B.dny, c2f, R->pad, R->d_flag, F->flags,
                                        (TF)F->omega_s, (TF)F->omega_b));
                 collided = true;
             }
         }
         if (!collided)
-            AK_CUDA(launch_chained(CHAIN_FINE, k_donors<SF, false>, gd, bd, s, src_of<SF>(F), F->G, C->nz, moments_of<S>(R->pro_x),
+            AK_CUDA(launch_chained(CHAIN_FINE, k_donors<SF, false>, gd, bd, s, src_of<SF>(F), F->G, C->nz, px,
                                    B.dny, c2f, R->pad, R->d_flag, (const uint8_t *)nullptr, (TF)0, (TF)0));
         mark(C);
         if (sub == 0 || !fine_fused)
@@ -2210,33 +2218,39 @@ int refined_step(ak_refined *R, bool fork = false, bool after_open = false, bool
         AK_TRY(fine_part(0, st));
     }
     AK_TRY(fine_part(1, st));
+    auto reflux = [&](cudaStream_t s) -> int {
+        AK_CUDA(launch_chained(CHAIN_TAIL, k_reflux<S>, dim3((unsigned)split_blocks(R->max_face), R->nfaces),
+                               dim3(SPLIT_THREADS), s, src_of<S>(C), C->G, (const Face *)R->d_faces, R->nfaces,
+                               (const long long *)R->d_offs, (const double *)R->reg_c, (const double *)R->reg_f,
+                               1.0 / (R->dx_c * R->dx_c * R->dx_c), R->d_flag));
+        // the transfer block's cells outside the box are final after the
+        // reflux (the restriction writes the box's): their budget sums
+        if (fstats) AK_TRY(enqueue_band_sums<S>(R, s));
+        return AK_OK;
+    };
     if (fork) {
+        // The reflux needs the face fluxes of both fine steps and the coarse
+        // cells just outside the box faces, which nothing reads after the
+        // donor moments that precede the second fine step: it runs on the
+        // face-flux branch right after the last flux, beside the second fine
+        // step's walls and streaming.  The restriction (box cells, disjoint)
+        // follows the fine streaming on the step's stream, the fine block's
+        // budget sums beside it.
+        AK_TRY(reflux(R->flux));
         AK_CUDA(cudaEventRecord(R->ev_flux_done, R->flux));
-        AK_CUDA(cudaStreamWaitEvent(st, R->ev_flux_done, 0));
-    }
-    // the restriction (coarse cells inside the box) and the reflux (coarse
-    // cells just outside its faces) write disjoint cells: in the graph the
-    // restriction runs on the side stream beside the reflux
-    if (fork) {
-        AK_CUDA(cudaEventRecord(R->ev_fork, st));
-        AK_CUDA(cudaStreamWaitEvent(R->side, R->ev_fork, 0));
-        AK_CUDA((launch_restrict<S, SF>(R, f2c, R->side)));
-        // the fine block's statistics beside the reflux (both levels' final
-        // states are complete: the fine one before the fork)
-        if (fstats) AK_TRY(enqueue_fine_stats<SF>(R, R->side));
-        AK_CUDA(cudaEventRecord(R->ev_join, R->side));
-    }
-    AK_CUDA(launch_chained(CHAIN_TAIL, k_reflux<S>, dim3((unsigned)split_blocks(R->max_face), R->nfaces), dim3(SPLIT_THREADS), st,
-                           src_of<S>(C), C->G, (const Face *)R->d_faces, R->nfaces, (const long long *)R->d_offs,
-                           (const double *)R->reg_c, (const double *)R->reg_f, 1.0 / (R->dx_c * R->dx_c * R->dx_c),
-                           R->d_flag));
-    // the transfer block's cells outside the box are final after the reflux
-    // (the restriction writes the box's): their sums run beside the far pass
-    if (fstats) AK_TRY(enqueue_band_sums<S>(R, st));
-    if (fork)
-        AK_CUDA(cudaStreamWaitEvent(st, R->ev_join, 0));
-    else
+        if (fstats) {
+            AK_CUDA(cudaEventRecord(R->ev_fork, st));
+            AK_CUDA(cudaStreamWaitEvent(R->side, R->ev_fork, 0));
+            AK_TRY(enqueue_fine_stats<SF>(R, R->side));
+            AK_CUDA(cudaEventRecord(R->ev_join, R->side));
+        }
         AK_CUDA((launch_restrict<S, SF>(R, f2c, st)));
+        if (fstats) AK_CUDA(cudaStreamWaitEvent(st, R->ev_join, 0));
+        AK_CUDA(cudaStreamWaitEvent(st, R->ev_flux_done, 0));
+    } else {
+        AK_TRY(reflux(st));
+        AK_CUDA((launch_restrict<S, SF>(R, f2c, st)));
+    }
     AK_CUDA(cudaGetLastError());
     // leave_open: the far pass, the budget's outer flux and the reduction of
     // the coarse rows stay on their branches; the next step of the capture
@@ -2475,6 +2489,7 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
     if (r == AK_OK) r = ralloc(R, &R->mom_new, (size_t)nblock * 10);
     if (r == AK_OK) r = ralloc(R, &R->mom_half, (size_t)nblock * 10);
     if (r == AK_OK) r = ralloc(R, &R->pro_x, (size_t)(2 * B.bx + 2 * R->pad) * B.dny * cd.nz * 10);
+    if (r == AK_OK) r = ralloc(R, &R->pro_x2, (size_t)(2 * B.bx + 2 * R->pad) * B.dny * cd.nz * 10);
     if (r == AK_OK) {
         R->nfaces = 0;
         long long off = 0;
