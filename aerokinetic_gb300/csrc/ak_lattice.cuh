@@ -309,27 +309,22 @@ __host__ __device__ __forceinline__ void collide(T g[Q], T omega_s, T omega_b, c
         }
 }
 
-// Plain FP64 form.  The same operator with the fewest double-precision
-// operations (the FP64 pipe bounds this kernel on GB300): populations f = g + w
-// are formed directly, and the three per-axis expansions are factored as
-// chimera passes that share their coefficients,
-//   X(+-) = E_X +- D_X,  X(0) = (1 - t) X_phi - 2u X_psi - X_chi,
-// first along x for A, B, C of every c_y, then along z with rho folded into
-// the z-functions.  About 370 FP64 operations per cell.
-template <typename T>
-__host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b, const Sgs<T> &sgs = Sgs<T>{},
-                                                      T *mac = nullptr) {
-    T Z0[3][3], Z1[3][3], Z2[3][3];
+// The ten moments the collision needs, m = (drho, jx, jy, jz, M200, M020,
+// M002, M110, M101, M011), from 27 values by the chimera sums along z, then
+// y, then x (66 additions).
+template <typename V>
+__host__ __device__ __forceinline__ void chimera_sums(const V f[Q], V m[10]) {
+    V Z0[3][3], Z1[3][3], Z2[3][3];
 #pragma unroll
     for (int ix = 0; ix < 3; ++ix)
 #pragma unroll
         for (int iy = 0; iy < 3; ++iy) {
-            const T a = g[qof(ix, iy, 0)], b = g[qof(ix, iy, 1)], c = g[qof(ix, iy, 2)];
+            const V a = f[qof(ix, iy, 0)], b = f[qof(ix, iy, 1)], c = f[qof(ix, iy, 2)];
             Z1[ix][iy] = c - a;
             Z2[ix][iy] = c + a;
             Z0[ix][iy] = Z2[ix][iy] + b;
         }
-    T Y00[3], Y01[3], Y02[3], Y10[3], Y11[3], Y20[3];
+    V Y00[3], Y01[3], Y02[3], Y10[3], Y11[3], Y20[3];
 #pragma unroll
     for (int ix = 0; ix < 3; ++ix) {
         Y01[ix] = Z0[ix][2] - Z0[ix][0];
@@ -339,16 +334,106 @@ __host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b, 
         Y10[ix] = Z1[ix][0] + Z1[ix][1] + Z1[ix][2];
         Y20[ix] = Z2[ix][0] + Z2[ix][1] + Z2[ix][2];
     }
-    const T M200 = Y00[2] + Y00[0];
-    const T drho = M200 + Y00[1];
-    const T jx = Y00[2] - Y00[0];
-    const T jy = Y01[0] + Y01[1] + Y01[2];
-    const T M110 = Y01[2] - Y01[0];
-    const T M020 = Y02[0] + Y02[1] + Y02[2];
-    const T jz = Y10[0] + Y10[1] + Y10[2];
-    const T M101 = Y10[2] - Y10[0];
-    const T M011 = Y11[0] + Y11[1] + Y11[2];
-    const T M002 = Y20[0] + Y20[1] + Y20[2];
+    m[4] = Y00[2] + Y00[0];
+    m[0] = m[4] + Y00[1];
+    m[1] = Y00[2] - Y00[0];
+    m[2] = Y01[0] + Y01[1] + Y01[2];
+    m[7] = Y01[2] - Y01[0];
+    m[5] = Y02[0] + Y02[1] + Y02[2];
+    m[3] = Y10[0] + Y10[1] + Y10[2];
+    m[8] = Y10[2] - Y10[0];
+    m[9] = Y11[0] + Y11[1] + Y11[2];
+    m[6] = Y20[0] + Y20[1] + Y20[2];
+}
+
+// The plain FP64 form's forward sums on the integer pipe.  GB300 issues
+// FP64 at 1/64 of its FP32 rate and the plain collision is bound by that
+// pipe, while its integer pipe idles; the 66 additions are exact on
+// integers, so each zero-centred population becomes round(g 2^52) (integer
+// instructions on its bit pattern), the sums run on 64-bit integers, and
+// each of the ten moments is rounded back to double once (integer
+// instructions again).  Each population is rounded to a multiple of 2^-52
+// (half a unit in the last place of a value near 1) instead of every partial
+// sum being rounded.  |g| < 64 keeps every sum inside 63 bits; a population
+// of magnitude 64 or more, or a non-finite one, belongs to a state that has
+// diverged (the density alone would be 64 times the reference) and makes
+// the moments NaN, as a non-finite population does in FP64 sums.
+namespace fixsum {
+constexpr int BITS = 52;
+__device__ __forceinline__ long long from_double(double v, bool &ok) {
+    const long long b = __double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7ff);  // v = m 2^(e - 1075)
+    ok &= e <= 1028;                          // |v| < 2^6
+    long long r = 0;
+    if (e != 0) {
+        const long long m = (b & 0x000fffffffffffffLL) | 0x0010000000000000LL;
+        const int sh = e - 1075 + BITS;
+        if (sh >= 0)
+            r = m << (sh < 5 ? sh : 5);
+        else if (sh > -54)
+            r = (m + (1LL << (-sh - 1))) >> -sh;  // magnitude rounded half up
+    }
+    return b < 0 ? -r : r;
+}
+// v 2^-52 as the nearest double (ties away from zero)
+__device__ __forceinline__ double to_double(long long v) {
+    if (v == 0) return 0.0;
+    const unsigned long long a = v < 0 ? 0ULL - (unsigned long long)v : (unsigned long long)v;
+    int top = 63 - __clzll((long long)a);  // a in [2^top, 2^(top + 1))
+    unsigned long long mant;
+    if (top <= 52) {
+        mant = a << (52 - top);
+    } else {
+        const int d = top - 52;
+        mant = (a >> d) + ((a >> (d - 1)) & 1ULL);
+        if (mant >> 53) {
+            mant >>= 1;
+            ++top;
+        }
+    }
+    // a 2^-52 = (mant 2^-52) 2^(top - 52): biased exponent top - 52 + 1023
+    const unsigned long long bits = ((unsigned long long)(top + 971) << 52) | (mant & 0x000fffffffffffffULL) |
+                                    (v < 0 ? 0x8000000000000000ULL : 0ULL);
+    return __longlong_as_double((long long)bits);
+}
+}  // namespace fixsum
+
+template <typename T>
+__host__ __device__ __forceinline__ void forward_moments(const T g[Q], T m[10]) {
+    chimera_sums<T>(g, m);
+}
+template <>
+__host__ __device__ __forceinline__ void forward_moments<double>(const double g[Q], double m[10]) {
+#ifdef __CUDA_ARCH__
+    long long f[Q], s[10];
+    bool ok = true;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) f[q] = fixsum::from_double(g[q], ok);
+    chimera_sums<long long>(f, s);
+#pragma unroll
+    for (int k = 0; k < 10; ++k) m[k] = ok ? fixsum::to_double(s[k]) : __longlong_as_double(0x7ff8000000000000LL);
+#else
+    chimera_sums<double>(g, m);
+#endif
+}
+
+// Plain FP64 form.  The same operator with the fewest double-precision
+// operations (the FP64 pipe bounds this kernel on GB300): populations f = g + w
+// are formed directly, and the three per-axis expansions are factored as
+// chimera passes that share their coefficients,
+//   X(+-) = E_X +- D_X,  X(0) = (1 - t) X_phi - 2u X_psi - X_chi,
+// first along x for A, B, C of every c_y, then along z with rho folded into
+// the z-functions.  The forward sums (66 of the 450 operations) run on the
+// integer pipe on the device (forward_moments<double>): ncu counted 277 FP64
+// instructions per cell with FP64 sums (156 FMA, 87 add, 34 multiply), and
+// the two-level coarse pass went from 0.776 to 0.586 ms with integer sums.
+template <typename T>
+__host__ __device__ __forceinline__ void collide_full(T g[Q], T om1, T omega_b, const Sgs<T> &sgs = Sgs<T>{},
+                                                      T *mac = nullptr) {
+    T mom[10];
+    forward_moments(g, mom);
+    const T drho = mom[0], jx = mom[1], jy = mom[2], jz = mom[3];
+    const T M200 = mom[4], M020 = mom[5], M002 = mom[6], M110 = mom[7], M101 = mom[8], M011 = mom[9];
 
     const T rho = T(1) + drho;
     const T rinv = T(1) / rho;

@@ -732,6 +732,10 @@ def run_engine(args, rank, world, local_rank):
     # GB300's FP64 pipe: its roofline is the measured FP64 FMA throughput,
     # against the collision's algorithmic FLOPs per cell
     fp64_peak = fma_peak(lib, 0)
+    # the collision's forward sums (the chimera additions that take the 27
+    # populations to their ten moments) run as exact integer additions on the
+    # device: of the algorithmic FLOPs per cell these never reach the FP64 pipe
+    forward_sums_per_cell = 66
     fp32_peak = fma_peak(lib, 1)
     fp32x2_peak = fma_peak(lib, 2)
     flops_cell = collision_flops(lib, "f64")
@@ -783,6 +787,9 @@ def run_engine(args, rank, world, local_rank):
                           "mlups": cells / (step_ms / 1e3) / 1e6, "ms_per_step": step_ms,
                           "collide_achieved_gbs": cb / (cms / 1e3) / 1e9,
                           "collide_frac_of_" + peak_kind: cb / (cms / 1e3) / 1e9 / hbm,
+                          # the same bytes over the whole replayed step
+                          "step_achieved_gbs": cb / (step_ms / 1e3) / 1e9,
+                          "step_frac_of_" + peak_kind: cb / (step_ms / 1e3) / 1e9 / hbm,
                           "groups_ms": {"coarse_transfer_block_collide": m[1] / k, "coarse_stream_collide": m[2] / k,
                                         "fine_collide": m[3] / k, "fine_stream": m[4] / k,
                                         "interface_and_boundaries": m[5] / k, "eager_step": m[0] / k}}
@@ -835,6 +842,9 @@ def run_engine(args, rank, world, local_rank):
                          "peak_source": "measured in this run (ak_fma_peak: FP64 FMA chains, 2 FLOPs per FMA)",
                          "kernel": "coarse k_stream_collide<double> (streaming fused with the collision)",
                          "flops_per_cell": flops_cell, "cells_collided_per_launch": coarse_cells - xfer_cells,
+                         "integer_pipe_flops_per_cell": forward_sums_per_cell,
+                         "frac_fp64_pipe": (flops_cell - forward_sums_per_cell) * (coarse_cells - xfer_cells)
+                                           / (kernel_ms / 1e3) / 1e12 / fp64_peak,
                          "kernel_ms": kernel_ms, "bytes_per_launch": kernel_bytes,
                          "hbm": {"achieved": achieved_gbs, "peak": hbm, "unit": "GB/s", "frac": achieved_gbs / hbm,
                                  "peak_source": peak_kind},
