@@ -1671,6 +1671,7 @@ struct ak_refined {
     int *d_flag = nullptr;
     double *d_loads = nullptr;
     unsigned *wall_done = nullptr;  // finished-block counters of the two fine steps' wall launches
+    unsigned *rows_done = nullptr;  // the same for the coarse and the fine budget rows' reductions
     long long steps = 0;
     std::vector<void *> owned;  // device buffers the two-level case owns
     // one captured coarse step (or two) per (coarse, fine) buffer parity,
@@ -1893,17 +1894,16 @@ __host__ __device__ constexpr bool fused_stats_form() {
 
 // reduction of budget rows into out[NSTAT]: one block when they are few,
 // else a first stage into stage (blocks_for(nrows, REDUCE_THREADS) rows)
-int enqueue_rows_final(ak_refined *R, const long long *rows, long long nrows, double *stage, double *out,
-                       cudaStream_t st) {
+int enqueue_rows_final(ak_refined *R, const long long *rows, long long nrows, double *stage, unsigned *done,
+                       double *out, cudaStream_t st) {
     if (nrows <= 16 * REDUCE_THREADS) {
         k_budget_final<<<1, REDUCE_THREADS, 0, st>>>(rows, nrows, out);
-        R->coarse->launches += 1;
     } else {
+        // one launch: its last block to finish reduces the stage
         const long long ns = blocks_for(nrows, REDUCE_THREADS);
-        k_budget_stage<<<(unsigned)ns, REDUCE_THREADS, 0, st>>>(rows, nrows, stage);
-        k_region_final<<<1, REDUCE_THREADS, 0, st>>>(stage, (int)ns, out);
-        R->coarse->launches += 2;
+        k_budget_stage<<<(unsigned)ns, REDUCE_THREADS, 0, st>>>(rows, nrows, stage, done, out);
     }
+    R->coarse->launches += 1;
     AK_CUDA(cudaGetLastError());
     return AK_OK;
 }
@@ -1926,7 +1926,7 @@ int enqueue_fine_stats(ak_refined *R, cudaStream_t st) {
                            F->G, (const uint8_t *)F->flags, rf, R->fine_rows));
     R->coarse->launches += 1;
     AK_CUDA(cudaGetLastError());
-    return enqueue_rows_final(R, R->fine_rows, rows, R->fine_stage, R->stats_out + NSTAT, st);
+    return enqueue_rows_final(R, R->fine_rows, rows, R->fine_stage, R->rows_done + 1, R->stats_out + NSTAT, st);
 }
 
 // The coarse budget sums when the fused coarse pass has written its rows to
@@ -1953,7 +1953,7 @@ int enqueue_band_sums(ak_refined *R, cudaStream_t st) {
 int enqueue_coarse_rows_final(ak_refined *R, cudaStream_t st) {
     const long long band_rows = region_sum_rows(region_cells(band_region(R), R->coarse->nz));
     return enqueue_rows_final(R, R->cstats, R->cstats_far + R->cstats_near + band_rows, R->cstats_stage,
-                              R->stats_out, st);
+                              R->rows_done, R->stats_out, st);
 }
 
 template <typename S, typename SF>
@@ -2598,8 +2598,10 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
         r = ensure_partials(F, std::max<long long>(1, nb * 5 * F->n_elements));
     }
     if (r == AK_OK) r = ralloc(R, &R->wall_done, 2);
+    if (r == AK_OK) r = ralloc(R, &R->rows_done, 2);
     if (r == AK_OK && (cudaMemset(R->d_loads, 0, sizeof(double) * 2 * 5 * std::max(1, cd.n_elements)) != cudaSuccess ||
-                       cudaMemset(R->wall_done, 0, 2 * sizeof(unsigned)) != cudaSuccess))
+                       cudaMemset(R->wall_done, 0, 2 * sizeof(unsigned)) != cudaSuccess ||
+                       cudaMemset(R->rows_done, 0, 2 * sizeof(unsigned)) != cudaSuccess))
         r = fail(AK_ERR_CUDA, "memset failed");
     if (r == AK_OK && cudaDeviceSynchronize() != cudaSuccess) r = fail(AK_ERR_CUDA, "refined set-up failed");
     if (r != AK_OK) {

@@ -1091,13 +1091,37 @@ __global__ void __launch_bounds__(REDUCE_THREADS)
 // (block b: rows [b REDUCE_THREADS, (b + 1) REDUCE_THREADS), one row each)
 // or of k_region_final (one block, every row)
 __global__ void __launch_bounds__(REDUCE_THREADS)
-    k_budget_stage(const long long *__restrict__ rows, long long nrows, double *__restrict__ out) {
+    k_budget_stage(const long long *__restrict__ rows, long long nrows, double *__restrict__ out,
+                   unsigned *__restrict__ done = nullptr, double *__restrict__ total = nullptr) {
     const long long b = (long long)blockIdx.x * REDUCE_THREADS + threadIdx.x;
     double a[NSTAT] = {-INFINITY, -INFINITY, 0, 0, 0, 0, 0, 0};
     if (b < nrows) budget_row_values(rows + b * NSTAT, a);
     reduce_block<NSTAT>(0x3u, a);
     if (threadIdx.x == 0)
         for (int k = 0; k < NSTAT; ++k) out[(long long)blockIdx.x * NSTAT + k] = a[k];
+    if (!done) return;
+    // done: the last block to finish reduces the stage rows into total[NSTAT]
+    // in k_region_final's order (same result), and leaves done at 0
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < NSTAT; ++k) a[k] = k < 2 ? -INFINITY : 0.0;
+    for (long long r = threadIdx.x; r < (long long)gridDim.x; r += REDUCE_THREADS)
+#pragma unroll
+        for (int k = 0; k < NSTAT; ++k) {
+            const double v = __ldcg(out + r * NSTAT + k);
+            a[k] = k < 2 ? fmax(a[k], v) : a[k] + v;
+        }
+    reduce_block<NSTAT>(0x3u, a);
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < NSTAT; ++k) total[k] = a[k];
+        *done = 0;
+    }
 }
 __global__ void __launch_bounds__(REDUCE_THREADS)
     k_budget_final(const long long *__restrict__ rows, long long nrows, double *__restrict__ out) {
