@@ -90,6 +90,10 @@ cudaError_t launch_chained(bool chained, void (*kernel)(KArgs...), dim3 grid, di
 // none 0.1744 / 0.1649 / 0.496; FINE 0.1633 / 0.1528 / 0.495; FINE + PROLONG
 // 0.1628 / 0.1527 / 0.495; + TAIL 0.1644 / 0.1539 / 0.494; all 0.1650 /
 // 0.1553 / 0.483.  The FP64 step (1.107 ms) and the uniform steps do not move.
+// coarse steps replayed per captured graph where the far pass runs on its own
+// branch (1, 2 or 4): consecutive steps of one graph overlap the next step's
+// start with the previous step's far pass
+constexpr int STEPS_PER_GRAPH = 4;
 constexpr bool CHAIN_FINE = true, CHAIN_PROLONG = true, CHAIN_COARSE = false, CHAIN_TAIL = false,
                CHAIN_UNIFORM = false;
 
@@ -1677,8 +1681,9 @@ struct ak_refined {
     // one captured coarse step (or two) per (coarse, fine) buffer parity,
     // replayed by ak_refined_step; graph_launches counts the kernels of one
     // replay
-    cudaGraphExec_t graph[32] = {};  // (coarse copy, fine copy, budget, step integrals, two steps)
-    long long graph_launches[32] = {};
+    // (coarse copy, fine copy, budget, step integrals) x (1, 2 or 4 steps)
+    cudaGraphExec_t graph[48] = {};
+    long long graph_launches[48] = {};
     bool step_stats = false;         // the step ends with the budget's integrals
     cudaStream_t side = nullptr;  // the first fine step's stream inside the captured graphs
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -2313,17 +2318,17 @@ int graph_priorities(ak_refined *R, cudaGraph_t g) {
     return AK_OK;
 }
 
-// One coarse step, or two, replayed from a CUDA graph: the steps' kernel
+// One coarse step, or several, replayed from a CUDA graph: the steps' kernel
 // sequence is captured once per buffer parity (the coarse copies swap every
 // step, the fine copies twice) and the host-side counters are advanced as the
-// eager step advances them.  Two steps in one graph (fused form with the
-// boundaries' branch) overlap the second step's first fine step, donor
-// moments and transfer-block collision with the first step's far pass.
+// eager step advances them.  Several steps in one graph (fused form with the
+// boundaries' branch) overlap each step's first fine step, donor moments and
+// transfer-block collision with the previous step's far pass.
 template <typename S, typename SF>
 int refined_step_graphed(ak_refined *R, int nsteps) {
     ak_case *C = R->coarse, *F = R->fine;
     const int slot = C->cur | (F->cur << 1) | (R->track_budget ? 4 : 0) | (R->step_stats ? 8 : 0) |
-                     (nsteps == 2 ? 16 : 0);
+                     (nsteps == 4 ? 32 : (nsteps == 2 ? 16 : 0));
     if (!R->graph[slot]) {
         const int ccur = C->cur, fcur = F->cur;
         const long long cs = C->steps, fs = F->steps, rs = R->steps, cl = C->launches;
@@ -2331,12 +2336,10 @@ int refined_step_graphed(ak_refined *R, int nsteps) {
         C->timing = nullptr;
         AK_CUDA(cudaStreamBeginCapture(C->stream, cudaStreamCaptureModeThreadLocal));
         int r = AK_OK;
-        if (nsteps == 2) {
-            r = refined_step<S, SF>(R, true, false, true);
-            if (r == AK_OK) r = refined_step<S, SF>(R, true, true, false);
-        } else {
-            r = refined_step<S, SF>(R, true);
-        }
+        // every step but the last leaves its far pass open, every step but
+        // the first waits for the previous one's
+        for (int k = 0; k < nsteps && r == AK_OK; ++k)
+            r = refined_step<S, SF>(R, true, k > 0, k + 1 < nsteps);
         cudaGraph_t g = nullptr;
         const cudaError_t e = cudaStreamEndCapture(C->stream, &g);
         C->timing = timing;
@@ -2368,7 +2371,7 @@ int refined_step_graphed(ak_refined *R, int nsteps) {
         }
     }
     AK_CUDA(cudaGraphLaunch(R->graph[slot], C->stream));
-    if (nsteps == 1) C->cur = 1 - C->cur;
+    if (nsteps % 2) C->cur = 1 - C->cur;
     R->pre_mode = 1;
     R->pre_writes = C->pdf_writes;
     C->launches += R->graph_launches[slot];
@@ -2383,7 +2386,7 @@ template <typename S, typename SF>
 int refined_steps_graphed(ak_refined *R, int nsteps) {
     const bool pairs = R->fused && R->bnd_branch;
     for (int s = 0; s < nsteps;) {
-        const int k = pairs && nsteps - s >= 2 ? 2 : 1;
+        const int k = !pairs ? 1 : (nsteps - s >= STEPS_PER_GRAPH ? STEPS_PER_GRAPH : (nsteps - s >= 2 ? 2 : 1));
         AK_TRY((refined_step_graphed<S, SF>(R, k)));
         s += k;
     }

@@ -231,9 +231,9 @@ int ak_refined_init_perturbed(ak_refined *r, double amp, double phase_y, double 
  * loads[n_elements * 5] = fine-lattice (Fx, Fy, Fz, Mz, mass) of the last
  * coarse step summed over its two fine steps (walls.py:68-95), Mz about the
  * normalised frame's origin in fine lattice units.  The steps' kernels are
- * captured once per buffer parity into CUDA graphs and replayed, two steps
- * per graph where the coarse pass runs on its own branch (the second step's
- * first fine step beside the first step's coarse pass). */
+ * captured once per buffer parity into CUDA graphs and replayed, up to four
+ * steps per graph where the coarse pass runs on its own branch (each step's
+ * first fine step beside the previous step's coarse pass). */
 int ak_refined_step(ak_refined *r, int32_t nsteps, double *loads);
 /* ak_refined_step that also returns, with one synchronisation, what the
  * budget of the last step needs (refined_solver.py:329-339): outer[8] as
