@@ -492,7 +492,10 @@ def run_batch(steps, n_cases=64, solve_steps=5000):
         out[storage] = {"ms_per_step": step_ms, "mlups": sum(cells) / (step_ms / 1e3) / 1e6,
                         "solves_per_hour": n_cases / (solve_steps * step_ms / 1e3) * 3600,
                         "launches_per_step": launches / steps, "schedule": schedule,
-                        "achieved_gbs": sum(cells) * BYTES_PER_CELL[storage] / (step_ms / 1e3) / 1e9}
+                        "achieved_gbs": sum(cells) * BYTES_PER_CELL[storage] / (step_ms / 1e3) / 1e9,
+                        # the batched stream-collide launch alone (the tuner's timing of it)
+                        "bulk_achieved_gbs": sum(cells) * BYTES_PER_CELL[storage] / (schedule["ms_per_launch"] / 1e3)
+                                             / 1e9}
     # plain form, one case at a time: per-step time of one case of each chord,
     # set-up time included once per case
     per_chord = {}
