@@ -90,33 +90,6 @@ __device__ __forceinline__ float shift_at(const float *s, int q) { return __ldg(
 // (the layout the two-level budget reduces): max |u|^2, max |rho - 1|,
 // sum drho, sum j (3), cells, non-finite cells.
 constexpr int CELL_STATS = 8;
-// block sums of the per-thread statistics (the first two entries maxima) in a
-// fixed order; thread 0 writes out[row * CELL_STATS ...].  Every thread of
-// the block must call it.
-__device__ void block_cell_stats(double (&a)[CELL_STATS], double *out, long long row) {
-    __shared__ double red[32][CELL_STATS];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        a[0] = fmax(a[0], __shfl_down_sync(0xffffffffu, a[0], o));
-        a[1] = fmax(a[1], __shfl_down_sync(0xffffffffu, a[1], o));
-#pragma unroll
-        for (int k = 2; k < CELL_STATS; ++k) a[k] += __shfl_down_sync(0xffffffffu, a[k], o);
-    }
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < CELL_STATS; ++k) red[warp][k] = a[k];
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const int nw = (blockDim.x + 31) >> 5;
-        for (int w = 1; w < nw; ++w) {
-            red[0][0] = fmax(red[0][0], red[w][0]);
-            red[0][1] = fmax(red[0][1], red[w][1]);
-            for (int k = 2; k < CELL_STATS; ++k) red[0][k] += red[w][k];
-        }
-        for (int k = 0; k < CELL_STATS; ++k) out[row * CELL_STATS + k] = red[0][k];
-    }
-}
 
 // The budget's sums on the integer pipe.  A value v becomes the integer
 // round(v 2^FIX_BITS) (magnitude rounded half up, then the sign): integer
