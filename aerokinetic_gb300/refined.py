@@ -83,6 +83,7 @@ class RefinedSolver:
         (progress or (lambda m: None))("Building the two-level case on the GPU")
         self._lib = _native.load()
         self._handle = None
+        self._step_buffers = None
         self._build()
         self.steps = 0
         self.last_loads = None
@@ -162,14 +163,17 @@ class RefinedSolver:
                 self._integrals = None
             before = self._integrals if self._integrals is not None else (
                 self.conserved_integrals() if self.budget else None)
-            raw = np.zeros((len(self.contours), 5))
-            flux = stats = None
+            # the step's output arrays and their pointers, made once and
+            # rewritten by every step (nothing below keeps a reference)
+            if self._step_buffers is None:
+                arrays = (np.zeros((len(self.contours), 5)), np.zeros(8), np.zeros(16))
+                self._step_buffers = arrays + tuple(_ptr(a) for a in arrays)
+            raw, flux, stats, praw, pflux, pstats = self._step_buffers
             if self.budget:
                 # the step returns its loads, outer-face flux and integrals at once
-                flux, stats = np.zeros(8), np.zeros(16)
-                check(self._lib.ak_refined_step_budget(self._handle, 1, _ptr(raw), _ptr(flux), _ptr(stats)))
+                check(self._lib.ak_refined_step_budget(self._handle, 1, praw, pflux, pstats))
             else:
-                check(self._lib.ak_refined_step(self._handle, 1, _ptr(raw)))
+                check(self._lib.ak_refined_step(self._handle, 1, praw))
             self.steps += 1
         except Exception:
             self.initialized = False
