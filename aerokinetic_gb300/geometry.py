@@ -224,10 +224,20 @@ class Section:
         return np.array([[np.cos(angle), -np.sin(angle)], [np.sin(angle), np.cos(angle)]])
 
     def normalized(self, alpha_deg):
-        """Chord-scaled contours about the moment reference; positive alpha raises the nose."""
-        rotation = self.rotation(alpha_deg)
-        return tuple(Contour(_rotate((e.xy - self.moment_reference) / self.chord, rotation), e.name)
-                     for e in self.elements)
+        """Chord-scaled contours about the moment reference; positive alpha raises the nose.
+        The result for an angle is computed once per section (the exact rotation
+        and the contours' own checks dominate a case's host-side set-up) and
+        shared by later calls; its contours are not to be modified."""
+        cache = self.__dict__.setdefault("_normalized", {})
+        key = float(alpha_deg)
+        if key not in cache:
+            rotation = self.rotation(alpha_deg)
+            contours = tuple(Contour(_rotate((e.xy - self.moment_reference) / self.chord, rotation), e.name)
+                             for e in self.elements)
+            for c in contours:
+                c.xy.flags.writeable = False
+            cache[key] = contours
+        return cache[key]
 
 
 def naca0012(n_side=161, closed_te=False):
