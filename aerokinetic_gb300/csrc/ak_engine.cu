@@ -1674,6 +1674,11 @@ struct ak_refined {
     int nterms = 0;
     int *d_flag = nullptr;
     double *d_loads = nullptr;
+    // the step's report in one device block, copied to the host at once:
+    // validity flag (an int in the first slot), both fine steps' loads,
+    // outer-face flux (outer_out), integrals (stats_out); a pinned copy
+    double *report = nullptr, *host_report = nullptr;
+    long long report_doubles = 0;
     unsigned *wall_done = nullptr;  // finished-block counters of the two fine steps' wall launches
     unsigned *rows_done = nullptr;  // the same for the coarse and the fine budget rows' reductions
     long long steps = 0;
@@ -1732,6 +1737,7 @@ void refined_release(ak_refined *R) {
             g = nullptr;
         }
     for (void *p : R->owned) cudaFree(p);
+    if (R->host_report) cudaFreeHost(R->host_report);
     if (R->ev_fork) cudaEventDestroy(R->ev_fork);
     if (R->ev_join) cudaEventDestroy(R->ev_join);
     if (R->side) cudaStreamDestroy(R->side);
@@ -2551,7 +2557,17 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
         if (r == AK_OK) r = cudaMemcpy(R->d_outer, R->outer, sizeof R->outer, cudaMemcpyHostToDevice) == cudaSuccess
                                 ? AK_OK : fail(AK_ERR_CUDA, "upload failed");
         if (r == AK_OK) r = ralloc(R, &R->outer_partials, (size_t)4 * R->outer_blocks * 4);
-        if (r == AK_OK) r = ralloc(R, &R->outer_out, 8);
+        const long long nl = 10LL * std::max(1, cd.n_elements);
+        R->report_doubles = 1 + nl + 8 + 2 * NSTAT;
+        if (r == AK_OK) r = ralloc(R, &R->report, (size_t)R->report_doubles);
+        if (r == AK_OK) {
+            R->d_flag = reinterpret_cast<int *>(R->report);
+            R->d_loads = R->report + 1;
+            R->outer_out = R->d_loads + nl;
+            R->stats_out = R->outer_out + 8;
+            if (cudaMallocHost((void **)&R->host_report, sizeof(double) * R->report_doubles) != cudaSuccess)
+                r = fail(AK_ERR_NOMEM, "pinned host allocation failed");
+        }
         if (r == AK_OK) r = ralloc(R, &R->cum_loads, (size_t)5 * std::max(1, cd.n_elements));
         if (r == AK_OK) r = ralloc(R, &R->stats_partials, (size_t)STATS_BLOCKS * NSTAT);
         // rows of the fine block's budget sums
@@ -2570,7 +2586,6 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
             r = ralloc(R, &R->cstats, (size_t)rows * NSTAT);
             if (r == AK_OK) r = ralloc(R, &R->cstats_stage, (size_t)blocks_for(rows, REDUCE_THREADS) * NSTAT);
         }
-        if (r == AK_OK) r = ralloc(R, &R->stats_out, (size_t)2 * NSTAT);
         if (r == AK_OK && (cudaMemset(R->outer_out, 0, 8 * sizeof(double)) != cudaSuccess ||
                            cudaMemset(R->cum_loads, 0, 5 * std::max(1, cd.n_elements) * sizeof(double)) != cudaSuccess))
             r = fail(AK_ERR_CUDA, "memset failed");
@@ -2593,8 +2608,6 @@ int ak_refined_create(const ak_refined_desc *desc, ak_refined **out) {
                        cudaEventCreateWithFlags(&R->ev_outer_in, cudaEventDisableTiming) != cudaSuccess ||
                        cudaEventCreateWithFlags(&R->ev_outer_out, cudaEventDisableTiming) != cudaSuccess))
         r = fail(AK_ERR_CUDA, "stream or event creation failed");
-    if (r == AK_OK) r = ralloc(R, &R->d_flag, 1);
-    if (r == AK_OK) r = ralloc(R, &R->d_loads, (size_t)2 * 5 * std::max(1, cd.n_elements));
     if (r == AK_OK) {
         ak_case *F = R->fine;
         const long long nb = blocks_for(F->nkeys * F->nz * 3, 256);
@@ -2662,14 +2675,16 @@ int ak_refined_step_budget(ak_refined *R, int32_t nsteps, double *loads, double 
         R->step_stats = false;
         if (r != AK_OK) return r;
     }
-    int flag = 0;
-    AK_CUDA(cudaMemcpyAsync(&flag, R->d_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
-    const int n = R->fine->n_elements;
-    std::vector<double> two((size_t)10 * std::max(1, n));
-    if (loads) AK_CUDA(cudaMemcpyAsync(two.data(), R->d_loads, sizeof(double) * 10 * n, cudaMemcpyDeviceToHost, st));
-    if (outer) AK_CUDA(cudaMemcpyAsync(outer, R->outer_out, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
-    if (stats) AK_CUDA(cudaMemcpyAsync(stats, R->stats_out, 2 * NSTAT * sizeof(double), cudaMemcpyDeviceToHost, st));
+    // flag, loads, outer flux and integrals in one copy from the report block
+    AK_CUDA(cudaMemcpyAsync(R->host_report, R->report, sizeof(double) * R->report_doubles, cudaMemcpyDeviceToHost,
+                            st));
     AK_CUDA(cudaStreamSynchronize(st));
+    int flag = 0;
+    std::memcpy(&flag, R->host_report, sizeof(int));
+    const int n = R->fine->n_elements;
+    const double *two = R->host_report + 1;
+    if (outer) std::memcpy(outer, R->host_report + (R->outer_out - R->report), 8 * sizeof(double));
+    if (stats) std::memcpy(stats, R->host_report + (R->stats_out - R->report), 2 * NSTAT * sizeof(double));
     if (flag) {
         std::string why = (flag & XF_NEGATIVE) ? "negative physical populations" :
                           (flag & XF_MACH) ? "local lattice Mach above 0.3" : "nonpositive density";
