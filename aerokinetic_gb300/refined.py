@@ -134,16 +134,18 @@ class RefinedSolver:
         self._integrals = self._initial_integrals = self.conserved_integrals()
 
     def _record(self, raw):
+        # element sums once, then scalar arithmetic in the same order as the
+        # array expressions (sum * volume * unit, ...): the same doubles
+        tot = raw.sum(axis=0).tolist()
         f = self.fine_level
         volume, unit = f.dx ** 3, f.lattice_velocity_unit
-        impulse = raw[:, :3].sum(axis=0) * volume * unit
-        moment = raw[:, 3].sum() * f.dx * volume * unit
+        dt = self.coarse_level.dt
+        moment = tot[3] * f.dx * volume * unit
         q_area = 0.5 * self.plan.span
-        force = impulse / self.coarse_level.dt
-        record = {"step": self.steps, "t_star": (self.steps - 0.5) * self.coarse_level.dt,
-                  "cl": float(force[1] / q_area), "cd": float(force[0] / q_area),
-                  "cm": float(-(moment / self.coarse_level.dt) / q_area),
-                  "wall_mass_exchange": float(raw[:, 4].sum() * volume)}
+        record = {"step": self.steps, "t_star": (self.steps - 0.5) * dt,
+                  "cl": (tot[1] * volume * unit / dt) / q_area, "cd": (tot[0] * volume * unit / dt) / q_area,
+                  "cm": -(moment / dt) / q_area,
+                  "wall_mass_exchange": tot[4] * volume}
         if self.plan.dt_seconds is not None:
             record["time_s"] = (self.steps - 0.5) * self.plan.dt_seconds
         return record
@@ -189,20 +191,24 @@ class RefinedSolver:
 
     def _close_budget(self, before, raw, flux, after):
         """refined_solver.py:329-339 from the engine's integrals and outer-face flux."""
+        # scalar arithmetic in the order of the array expressions it replaces
         f = self.fine_level
         self._integrals = after
         unit = f.lattice_velocity_unit
-        external = flux[:4].copy()
-        external[1:] *= unit
-        impulse = raw[:, :3].sum(axis=0) * f.dx ** 3 * unit
-        wall_mass = float(raw[:, 4].sum() * f.dx ** 3)
+        tot = raw.sum(axis=0).tolist()
+        ext = flux[:4].tolist()
+        external = [ext[0]] + [e * unit for e in ext[1:]]
+        dx3 = f.dx ** 3
+        impulse = [tot[k] * dx3 * unit for k in range(3)]
+        wall_mass = tot[4] * dx3
         mass_residual = after["mass"] - before["mass"] - external[0] - wall_mass
-        momentum_residual = np.array(after["momentum"]) - before["momentum"] - external[1:] + impulse
-        volume = self.coarse_owned_cells * self.coarse_level.dx ** 3 + self.fine_fluid_cells * f.dx ** 3
-        self.last_budget = {"mass_residual_per_volume": float(mass_residual / volume),
-                            "momentum_residual_per_volume": (momentum_residual / volume).tolist(),
-                            "wall_mass_exchange": wall_mass, "external_mass_in": float(external[0]),
-                            "wall_impulse": impulse.tolist(), "external_impulse_in": external[1:].tolist()}
+        momentum_residual = [after["momentum"][k] - before["momentum"][k] - external[1 + k] + impulse[k]
+                             for k in range(3)]
+        volume = self.coarse_owned_cells * self.coarse_level.dx ** 3 + self.fine_fluid_cells * dx3
+        self.last_budget = {"mass_residual_per_volume": mass_residual / volume,
+                            "momentum_residual_per_volume": [m / volume for m in momentum_residual],
+                            "wall_mass_exchange": wall_mass, "external_mass_in": external[0],
+                            "wall_impulse": impulse, "external_impulse_in": external[1:]}
 
     # ------------------------------------------------------------ integrals, validity
     def _stats(self):
