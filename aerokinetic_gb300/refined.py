@@ -222,14 +222,16 @@ class RefinedSolver:
         return self._integrals_of(*self._stats())
 
     def _integrals_of(self, coarse, fine):
-        mass, impulse = 0.0, np.zeros(3)
+        mass, impulse = 0.0, [0.0, 0.0, 0.0]
         for st, level in zip((coarse, fine), (self.coarse_level, self.fine_level)):
+            st = st.tolist()
             if st[7]:
                 return {"mass": float("nan"), "momentum": [float("nan")] * 3}
             volume = level.dx ** 3
             mass += (st[6] + st[2]) * volume
-            impulse += st[3:6] * volume * level.lattice_velocity_unit
-        return {"mass": float(mass), "momentum": impulse.tolist()}
+            unit = level.lattice_velocity_unit
+            impulse = [impulse[k] + st[3 + k] * volume * unit for k in range(3)]
+        return {"mass": mass, "momentum": impulse}
 
     @property
     def cumulative_wall_impulse(self):
