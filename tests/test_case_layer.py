@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from aerokinetic_gb300.config import Flow, Grid, Plan
-from aerokinetic_gb300.geometry import Contour, Section, naca4
+from aerokinetic_gb300.geometry import Contour, Section, naca0012, naca4
 from aerokinetic_gb300.project import Project
 
 O = pytest.importorskip("oracle.oracle")
@@ -146,3 +146,14 @@ def test_refined_fine_storage_choices_are_validated_before_any_device_work():
     for storage, fine in (("f32", "f16"), ("f64", "f32"), ("f16", "f64")):
         with pytest.raises(ValueError, match="fine_storage"):
             RefinedSolver(project, RefinementSettings(), storage=storage, fine_storage=fine)
+
+
+def test_normalized_contours_are_computed_once_and_read_only():
+    """Section.normalized returns the same contours for the same angle (the
+    plan and the solver both ask for them) and they cannot be modified."""
+    section = Section((naca0012(41),))
+    first = section.normalized(4.0)
+    assert section.normalized(4) is first
+    assert section.normalized(5.0) is not first
+    with pytest.raises(ValueError):
+        first[0].xy[0, 0] = 1.0

@@ -425,6 +425,34 @@ def test_refined_two_step_graphs_match_single_steps():
             solver.close()
 
 
+def test_budget_step_integrals_match_the_region_statistics():
+    """The budget step's integrals (exact fixed-point sums: the fused coarse
+    pass's warp rows, the transfer block's band and the fine block) against
+    the FP64 region statistics of the same state (ak_refined_integrals), on
+    the benchmark's two-level case after budget steps replayed several per
+    graph."""
+    import ctypes
+    import bench
+    from aerokinetic_gb300 import _native
+    from aerokinetic_gb300.refined import RefinedSolver
+    project, refinement = bench.refined_parts()
+    solver = RefinedSolver(project, refinement, storage="f64")
+    try:
+        lib = solver._lib
+        n = len(solver.contours)
+        loads, outer, stats = np.zeros((n, 5)), np.zeros(8), np.zeros(16)
+        ptrs = [a.ctypes.data_as(ctypes.c_void_p) for a in (loads, outer, stats)]
+        _native.check(lib.ak_refined_step_budget(solver._handle, 6, *ptrs))
+        ref = np.zeros(16)
+        _native.check(lib.ak_refined_integrals(solver._handle, ref.ctypes.data_as(ctypes.c_void_p)))
+        for lo in (0, 8):  # coarse cells outside the box, fine physical block
+            assert stats[lo + 6] == ref[lo + 6] > 0 and stats[lo + 7] == ref[lo + 7] == 0
+            assert stats[lo + 2] + stats[lo + 6] == pytest.approx(ref[lo + 2] + ref[lo + 6], rel=1e-15)
+            np.testing.assert_allclose(stats[lo + 3:lo + 6], ref[lo + 3:lo + 6], rtol=1e-12, atol=1e-11)
+    finally:
+        solver.close()
+
+
 def test_refined_budget_integrals_and_diagnostics_match_oracle(golden):
     """conserved_integrals, the per-step budget (last_budget) and diagnostics
     (refined_solver.py:291-361) against the oracle sampling the outer faces in
