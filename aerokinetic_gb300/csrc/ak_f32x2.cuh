@@ -24,12 +24,26 @@ namespace ak {
 __device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 f2_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 f2_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+// a - b as one packed subtraction (PTX sub.rn.f32x2): the same rounding as
+// a + (-b), without negating b first
+__device__ __forceinline__ float2 f2_sub(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %5};\n\t"
+        "sub.rn.f32x2 rd, ra, rb;\n\t"
+        "mov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
 #else
 __device__ __forceinline__ float2 f2_fma(float2 a, float2 b, float2 c) {
     return make_float2(__fmaf_rn(a.x, b.x, c.x), __fmaf_rn(a.y, b.y, c.y));
 }
 __device__ __forceinline__ float2 f2_add(float2 a, float2 b) { return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y)); }
 __device__ __forceinline__ float2 f2_mul(float2 a, float2 b) { return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)); }
+__device__ __forceinline__ float2 f2_sub(float2 a, float2 b) { return make_float2(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y)); }
 #endif
 
 struct F2 {
@@ -55,7 +69,7 @@ __device__ __forceinline__ P2 operator*(F2 a, P2 b) { return P2{a.v, F2(b).v}; }
 __device__ __forceinline__ P2 operator*(P2 a, P2 b) { return P2{F2(a).v, F2(b).v}; }
 
 __device__ __forceinline__ F2 operator+(F2 a, F2 b) { return F2(f2_add(a.v, b.v)); }
-__device__ __forceinline__ F2 operator-(F2 a, F2 b) { return F2(f2_add(a.v, neg2(b.v))); }
+__device__ __forceinline__ F2 operator-(F2 a, F2 b) { return F2(f2_sub(a.v, b.v)); }
 __device__ __forceinline__ F2 operator-(F2 a) { return F2(neg2(a.v)); }
 __device__ __forceinline__ P2 operator-(P2 p) { return P2{neg2(p.a), p.b}; }
 
