@@ -330,6 +330,17 @@ __device__ __forceinline__ void pair_load(const S *__restrict__ src, const Grid 
     }
 }
 
+// population q of both cells as stored: FP16 storage holds (f - w - shift) / w
+template <typename S, typename Shift>
+__device__ __forceinline__ float2 stored_pair(F2 g, const Shift &shift, int q) {
+    if constexpr (std::is_same_v<S, __half>) {
+        const float a = shift_at(shift, q), inv = (float)(1.0 / weight(q)), b = -a * inv;
+        return f2_fma(g.v, make_float2(inv, inv), make_float2(b, b));
+    } else {
+        return g.v;
+    }
+}
+
 // The collision of both cells in packed FP32x2 and their stores (fluid
 // cells only; a pair of stores where both are).  Each lane rounds as the
 // one-cell path's FP32 operations do, except that the collision's
@@ -358,20 +369,18 @@ __device__ __forceinline__ void pair_collide_store(const PairRaw<S> &raw, S *__r
     else
         collide_full<F2>(g, F2(1.0f - omega_s), F2(omega_b), sgs);
     if (!store0 && !store1) return;
-    const long long c = G.cell(xe, y, z);
+    S *const p = dst + G.cell(xe, y, z);
+    // one branch for the pair: both cells stored (all but boundary pairs),
+    // or each on its own
+    if (store0 && store1) {
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-        float2 v = g[q].v;
-        if constexpr (std::is_same_v<S, __half>) {
-            const float a = shift_at(shift, q), inv = (float)(1.0 / weight(q)), b = -a * inv;
-            v = f2_fma(v, make_float2(inv, inv), make_float2(b, b));
-        }
-        S *p = dst + q * G.qs + c;
-        if (store0 && store1) {
-            store_pair(p, v);
-        } else {
-            if (store0) store_one(p, v.x);
-            if (store1) store_one(p + 1, v.y);
+        for (int q = 0; q < Q; ++q) store_pair(p + q * G.qs, stored_pair<S>(g[q], shift, q));
+    } else {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const float2 v = stored_pair<S>(g[q], shift, q);
+            if (store0) store_one(p + q * G.qs, v.x);
+            if (store1) store_one(p + q * G.qs + 1, v.y);
         }
     }
 }
@@ -386,12 +395,20 @@ struct PairItem {
 };
 __device__ __forceinline__ bool pair_item(const Grid &G, int4 raw, int4 rect, int4 skip, long long i, PairItem &it) {
     const int xa = rect.x & ~1;
-    const long long wp = (((rect.y + 1) & ~1) - xa) / 2, h = rect.w - rect.z;
-    const long long nxy = wp * h;
-    if (i >= nxy * G.nz) return false;
-    it.z = (int)(i / nxy);
-    const long long r = i - (long long)it.z * nxy;
-    const long long yr = r / wp;
+    // a row holds at most 16384 pairs and a plane at most 2^30 (the case
+    // limits), so 32-bit divisions serve every index below 2^32
+    const unsigned wp = (unsigned)((((rect.y + 1) & ~1) - xa) / 2), nxy = wp * (unsigned)(rect.w - rect.z);
+    if (i >= (long long)nxy * G.nz) return false;
+    unsigned z, r;
+    if (i < (1LL << 32)) {
+        z = (unsigned)i / nxy;
+        r = (unsigned)i - z * nxy;
+    } else {
+        z = (unsigned)(i / nxy);
+        r = (unsigned)(i - (long long)z * nxy);
+    }
+    const unsigned yr = r / wp;
+    it.z = (int)z;
     it.xe = xa + 2 * (int)(r - yr * wp);
     it.y = rect.z + (int)yr;
     bool live[2], only = false;
