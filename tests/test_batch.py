@@ -25,7 +25,7 @@ def _solvers(storage, cases=CASES):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("storage,cases", [("f64", CASES), ("f16", CASES), ("f32", MIXED_BOUNDARIES),
-                                           ("f64", MIXED_BOUNDARIES)])
+                                           ("f64", MIXED_BOUNDARIES), ("f16", MIXED_BOUNDARIES)])
 def test_batch_matches_cases_stepped_alone(storage, cases):
     """Every case of a mixed-size batch (characteristic and legacy outer
     boundaries) ends bit-identical to the same case stepped alone, and its
