@@ -132,11 +132,14 @@ __global__ void k_batch_sum_partials(const BatchCase<S> *__restrict__ cases, dou
 // a case covers its stream-collide items [chunk * TB, chunk * TB + TB) in
 // the single-case kernel's numbering (cells across rows, or cell pairs in
 // the pair forms), so a case's bits do not depend on the batch and no warp
-// is left part-empty at a row's end
+// is left part-empty at a row's end.  The pair forms take one table entry
+// per block (the grid is the table): the state of a persistent loop over the
+// table, held across the collision, made the FP16 body spill at five
+// resident blocks; the other forms loop over the table on a persistent grid.
 // resident 128-thread blocks per SM: the pair forms' body also holds the
-// case descriptor and the work loop, and spills at the single-case FP16
-// kernel's six blocks (80 registers); the FP16 form runs at five (96
-// registers, no spill), the FP32 form at four
+// case descriptor, and spills at the single-case FP16 kernel's six blocks
+// (80 registers); the FP16 form runs at five (96 registers, no spill), the
+// FP32 form at four
 template <typename S>
 __host__ __device__ constexpr int batch_bulk_min_blocks() {
     return pair_form<S>() ? (std::is_same_v<S, __half> ? 5 : 4) : Store<S>::MIN_BLOCKS;
@@ -145,18 +148,23 @@ template <typename S, int TB>
 __global__ void __launch_bounds__(TB, batch_bulk_min_blocks<S>() * 128 / TB)
     k_batch_bulk(const BatchCase<S> *__restrict__ cases, const WorkItem *__restrict__ work, long long n_work,
                  int parity) {
-    for (long long e = blockIdx.x; e < n_work; e += gridDim.x) {
-        const WorkItem w = work[e];
+    if constexpr (pair_form<S>()) {
+        if ((long long)blockIdx.x >= n_work) return;
+        const WorkItem w = work[blockIdx.x];
         const BatchCase<S> &c = cases[w.c];
-        const Grid G = c.G;
-        const long long i = (long long)w.chunk * TB + threadIdx.x;
-        const S *src = c.pdf[c.cur0 ^ parity];
-        S *dst = c.pdf[c.cur0 ^ parity ^ 1];
-        if constexpr (pair_form<S>()) {
-            const int4 none = make_int4(0, 0, 0, 0);
-            stream_collide_pair_item(src, dst, c.flags, G, G.shift, c.omega_s, c.omega_b, c.sgs, none,
-                                     make_int4(1, G.nx + 1, 1, G.ny + 1), none, i);
-        } else {
+        const Grid &G = c.G;
+        const int4 none = make_int4(0, 0, 0, 0);
+        stream_collide_pair_item(c.pdf[c.cur0 ^ parity], c.pdf[c.cur0 ^ parity ^ 1], c.flags, G, G.shift,
+                                 c.omega_s, c.omega_b, c.sgs, none, make_int4(1, G.nx + 1, 1, G.ny + 1), none,
+                                 (long long)w.chunk * TB + threadIdx.x);
+    } else {
+        for (long long e = blockIdx.x; e < n_work; e += gridDim.x) {
+            const WorkItem w = work[e];
+            const BatchCase<S> &c = cases[w.c];
+            const Grid G = c.G;
+            const long long i = (long long)w.chunk * TB + threadIdx.x;
+            const S *src = c.pdf[c.cur0 ^ parity];
+            S *dst = c.pdf[c.cur0 ^ parity ^ 1];
             const long long nxy = (long long)G.nx * G.ny;
             if (i >= nxy * G.nz) continue;
             const int z = (int)(i / nxy);

@@ -2961,9 +2961,12 @@ std::vector<WorkItem> bulk_table(const ak_batch *B, int tb, int order) {
     return out;
 }
 
+// grid: the persistent grid of the looping forms; the pair forms launch one
+// block per table entry
 template <typename S>
 int bulk_launch(ak_batch *B, int tb, int grid, int parity) {
     const BatchCase<S> *cases = (const BatchCase<S> *)B->d_cases;
+    if constexpr (pair_form<S>()) grid = (int)std::max<long long>(1, B->n_bulk);
     switch (tb) {
     case 64: k_batch_bulk<S, 64><<<grid, 64, 0, B->stream>>>(cases, B->w_bulk, B->n_bulk, parity); break;
     case 128: k_batch_bulk<S, 128><<<grid, 128, 0, B->stream>>>(cases, B->w_bulk, B->n_bulk, parity); break;
@@ -3286,7 +3289,8 @@ int ak_batch_tune(ak_batch *B, int32_t trials, double *report) {
                 const std::vector<WorkItem> t = bulk_table(B, tb, order);
                 B->n_bulk = (long long)t.size();
                 r = upload_work(&B->w_bulk, t);
-                for (int per = 1; per <= occ && r == AK_OK; per *= 2) {
+                // the pair forms' grid is their table: one timing per width and order
+                for (int per = pair_form<S>() ? occ : 1; per <= occ && r == AK_OK; per *= 2) {
                     r = bulk_launch<S>(B, tb, per * B->sms, B->parity);  // warm
                     cudaEventRecord(a, B->stream);
                     for (int k = 0; k < trials && r == AK_OK; ++k) r = bulk_launch<S>(B, tb, per * B->sms, B->parity);

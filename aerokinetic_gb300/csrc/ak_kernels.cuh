@@ -352,6 +352,11 @@ __device__ __forceinline__ void pair_collide_store(const PairRaw<S> &raw, S *__r
                                                    int z, bool live0, bool live1, const Sgs<F2> &sgs) {
     const bool store0 = live0 && __ldg(flags + y * G.nxp + xe) == FLAG_FLUID;
     const bool store1 = live1 && __ldg(flags + y * G.nxp + xe + 1) == FLAG_FLUID;
+    // the store address and stride formed before the collision: two values
+    // held across it instead of the lattice geometry (the batch kernel reads
+    // that from its case descriptor, not from launch parameters)
+    S *const p = dst + G.cell(xe, y, z);
+    const long long qs = G.qs;
     F2 g[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -369,18 +374,17 @@ __device__ __forceinline__ void pair_collide_store(const PairRaw<S> &raw, S *__r
     else
         collide_full<F2>(g, F2(1.0f - omega_s), F2(omega_b), sgs);
     if (!store0 && !store1) return;
-    S *const p = dst + G.cell(xe, y, z);
     // one branch for the pair: both cells stored (all but boundary pairs),
     // or each on its own
     if (store0 && store1) {
 #pragma unroll
-        for (int q = 0; q < Q; ++q) store_pair(p + q * G.qs, stored_pair<S>(g[q], shift, q));
+        for (int q = 0; q < Q; ++q) store_pair(p + q * qs, stored_pair<S>(g[q], shift, q));
     } else {
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             const float2 v = stored_pair<S>(g[q], shift, q);
-            if (store0) store_one(p + q * G.qs, v.x);
-            if (store1) store_one(p + q * G.qs + 1, v.y);
+            if (store0) store_one(p + q * qs, v.x);
+            if (store1) store_one(p + q * qs + 1, v.y);
         }
     }
 }
