@@ -36,7 +36,8 @@ class Batch:
             self.tune(tune_trials)
 
     def tune(self, trials=3):
-        """Pick the stream-collide block width, persistent grid and table order."""
+        """Pick the stream-collide block width, persistent grid (FP64 and df64
+        forms) and table order."""
         report = np.zeros(5)
         check(self._lib.ak_batch_tune(self._handle, int(trials), report.ctypes.data_as(ctypes.c_void_p)))
         self.schedule = {"block_width": int(report[0]), "ctas_per_sm": int(report[1]),

@@ -322,8 +322,9 @@ ak_case *ak_refined_level(ak_refined *r, int32_t level);
  * outer boundary (one storage form, one device) and advances them together:
  * per step one launch each for the farfield ring macros and links, the UBB
  * cells and outflow links, and the Bouzidi walls of every case, and one
- * persistent stream-collide launch over a packed table of all cases' blocks,
- * replayed from CUDA graphs.  A case computes the same bits alone (ak_step)
+ * stream-collide launch over a packed table of all cases' blocks (one block
+ * per table entry in the FP32 and FP16 forms, a persistent grid looping over
+ * the table in the FP64 and df64 forms), replayed from CUDA graphs.  A case computes the same bits alone (ak_step)
  * and in a batch.  While a case belongs to a batch, step it only through the
  * batch; its state can be read with the per-case calls. */
 typedef struct ak_batch ak_batch;
@@ -334,8 +335,9 @@ int ak_batch_destroy(ak_batch *b);
  * as ak_step returns them. */
 int ak_batch_step(ak_batch *b, int32_t nsteps, double *loads);
 /* Times the stream-collide launch for every block width (64, 128, 256),
- * persistent grid size (1, 2, 4, ... CTAs per SM up to the occupancy limit)
- * and table order (case-major, interleaved), trials launches each, and keeps
+ * persistent grid size (1, 2, 4, ... CTAs per SM up to the occupancy limit;
+ * FP64 and df64 forms) and table order (case-major, interleaved), trials
+ * launches each, and keeps
  * the fastest.  The cases' state is unchanged.  report[5] = chosen width,
  * CTAs per SM, order, its ms per launch, the previous schedule's ms. */
 int ak_batch_tune(ak_batch *b, int32_t trials, double *report);
