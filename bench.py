@@ -334,6 +334,16 @@ def measure_form(storage, steps, warmup, flush, farfield="characteristic_transpo
     return out
 
 
+def measure_form_at(cells_per_chord, storage, **kw):
+    """measure_form on the uniform case at another resolution."""
+    global CELLS_PER_CHORD
+    keep, CELLS_PER_CHORD = CELLS_PER_CHORD, cells_per_chord
+    try:
+        return measure_form(storage, **kw)
+    finally:
+        CELLS_PER_CHORD = keep
+
+
 def batch_case_parts(i, base_seed=2026):
     """Case i of the polar-sweep batch: chord cells from {24, 32, 48, 64}, a
     12c x 8c domain with a periodic span of 4 cells (the plan's minimum of 8),
@@ -824,6 +834,15 @@ def run_engine(args, rank, world, local_rank):
                                              "kernel_mlups": m["cells"] / (m["bulk_ms"] / 1e3) / 1e6,
                                              "stream_collide_ms": m["bulk_ms"], "outer_boundary_ms": m["outer_ms"],
                                              "achieved_gbs": a, "frac_of_" + peak_kind: a / hbm}
+    # the pair kernels on the same case at chord 64, whose copies exceed the
+    # 129 MB L2 in both forms (170 MB per FP16 copy, 340 MB per FP32 copy)
+    uniform["chord64"] = {"workload": "uniform NACA0012 768x512x8, chord 64, otherwise as above"}
+    for storage in ("f32", "f16"):
+        m = measure_form_at(64, storage, steps=min(args.steps, 50), warmup=args.warmup, flush=True)
+        a = m["fluid_cells"] * BYTES_PER_CELL[storage] / (m["bulk_ms"] / 1e3) / 1e9
+        uniform["chord64"][storage] = {"kernel_mlups": m["cells"] / (m["bulk_ms"] / 1e3) / 1e6,
+                                       "stream_collide_ms": m["bulk_ms"], "achieved_gbs": a,
+                                       "frac_of_" + peak_kind: a / hbm}
 
     forms["error_vs_f64"] = form_errors(project, refinement, steps=FORM_ERROR_STEPS)
     batch = run_batch(steps=min(args.steps, 100))
