@@ -811,16 +811,25 @@ __global__ void __launch_bounds__(SPLIT_THREADS, 2)
     using T = typename Store<Sc>::A;
     __shared__ SplitShared<T> sh;
     if (blockIdx.y == 1) {
+        // the covered core takes the free-stream populations: converted to
+        // the storage form once per block (as store_g converts them), then
+        // copied to every core cell
+        __shared__ Sc free_s[Q];
         const int cx0 = B.bx - 6, cy0 = B.by - 6;
         if (cx0 <= 0 || cy0 <= 0) return;
+        if (threadIdx.x < Q)
+            Store<Sc>::store(&free_s[threadIdx.x], threadIdx.x, (typename Store<Sc>::T)free_g[threadIdx.x],
+                             G.shift[threadIdx.x]);
+        __syncthreads();
         const long long ncore = (long long)cx0 * cy0 * B.bz;
         const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
         if (i >= ncore) return;
         const int x = (int)(i % cx0);
         const long long rest = i / cx0;
         const int y = (int)(rest % cy0), z = (int)(rest / cy0);
-        for (int q = 0; q < Q; ++q)
-            store_g(coarse, G, q, B.lo[0] + 3 + x + 1, B.lo[1] + 3 + y + 1, B.lo[2] + z, free_g[q]);
+        Sc *const cell = coarse + G.cell(B.lo[0] + 3 + x + 1, B.lo[1] + 3 + y + 1, B.lo[2] + z);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) cell[q * G.qs] = free_s[q];
         return;
     }
     const long long nring = ring_count(B.bx, B.by, 3, 3), n = nring * B.bz;
